@@ -1,0 +1,164 @@
+/*
+ * la_gpu.h — C ABI of the GB300 (sm_103a) dense LU factor-and-solve library
+ * (liblagpu.so). It is the drop-in boundary for the LU path of the `la` crate
+ * (xasmx/rust-la 0.2.0): a Rust, C, C++ or Python host binds these symbols and
+ * keeps the crate's types and semantics on its side.
+ *
+ * Conventions shared by every entry point:
+ *  - Matrices are dense, row-major f64, exactly like Matrix<f64>'s Vec<f64>
+ *    (src/matrix/mod.rs:26-30). Host pointers are plain (pageable or pinned)
+ *    memory; *_device entry points take device pointers with a row pitch `ld`
+ *    in elements.
+ *  - The reference's `assert!` failures (a panic) come back as LA_BADSHAPE and
+ *    its `None` as LA_SINGULAR. Nothing is written to the outputs then.
+ *  - Host-pointer calls return when their results are in host memory. Device
+ *    calls are ordered on the context's stream; an LU handle is complete when
+ *    la_lu_new* returns (pivots, sign and the singular flag are read back).
+ *  - One context serves one host thread at a time (the reference is
+ *    single-threaded); use one context per thread for concurrency.
+ */
+#ifndef LA_GPU_H
+#define LA_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LA_ABI_VERSION 1
+
+typedef enum la_status {
+  LA_OK = 0,
+  LA_SINGULAR = 1,       /* reference returns None (exact zero on U's diagonal) */
+  LA_BADSHAPE = 2,       /* reference panics (failed assert! / index out of bounds) */
+  LA_INVALID = 3,        /* null handle/pointer, bad option value */
+  LA_NOMEM = 4,          /* device or pinned allocation failed */
+  LA_CUDA_ERROR = 5,     /* a CUDA runtime call failed; see la_ctx_last_error */
+  LA_TIMEOUT = 6,        /* a bounded device-side wait gave up; the context stays usable */
+  LA_NOT_CONVERGED = 7,  /* iterative refinement stalled (mixed-precision entry points) */
+  LA_UNSUPPORTED = 8     /* size or option outside what this build implements */
+} la_status;
+
+typedef struct la_context* la_ctx;
+typedef struct la_lu_handle* la_lu;
+
+/* ---- context ------------------------------------------------------------ */
+
+/* Creates a context on CUDA device `device` with its own non-blocking stream. */
+la_status la_ctx_create(int device, la_ctx* out);
+void la_ctx_destroy(la_ctx ctx);
+/* Orders all later work of this context on `stream` (a cudaStream_t); NULL
+ * restores the context's own stream. */
+la_status la_ctx_set_stream(la_ctx ctx, void* stream);
+void* la_ctx_get_stream(la_ctx ctx);
+la_status la_ctx_synchronize(la_ctx ctx);
+const char* la_status_string(la_status s);
+/* Message of the last LA_CUDA_ERROR / LA_TIMEOUT seen by this context. */
+const char* la_ctx_last_error(la_ctx ctx);
+int la_abi_version(void);
+
+/* Options (la_ctx_set_option). */
+typedef enum la_option {
+  /* LU arithmetic. LA_ARITH_FAST (default): blocked right-looking LU with
+   * fused multiply-add. LA_ARITH_EXACT: the same blocked kernels carry each
+   * element's partial sum separately and add terms in the reference's order
+   * without fusion, so LU factors, pivots, det and solve results are
+   * bit-identical to src/decomp/lu.rs (at about half the FP64 rate). Also
+   * selects the summation of la_matrix_mul (mod.rs:957-980 order when EXACT). */
+  LA_OPT_ARITH = 1,
+  /* Panel width of the blocked LU (16, 32 or 64). */
+  LA_OPT_PANEL_WIDTH = 2,
+  /* Upper bound on CTAs of the cooperative panel kernel (0 = all SMs). */
+  LA_OPT_PANEL_CTAS = 3,
+  /* 1: record per-phase device times of each LU (la_ctx_last_phase_ms). */
+  LA_OPT_PROFILE = 4
+} la_option;
+
+#define LA_ARITH_FAST 0
+#define LA_ARITH_EXACT 1
+
+la_status la_ctx_set_option(la_ctx ctx, int option, int64_t value);
+la_status la_ctx_get_option(la_ctx ctx, int option, int64_t* value);
+
+/* ---- LUDecomposition<f64> (src/decomp/lu.rs) ---------------------------- */
+
+/* LUDecomposition::new (lu.rs:104-168). Copies A (m x n, m,n > 0) to the
+ * device and factors it with partial pivoting. Never reports LA_SINGULAR
+ * (the reference's `new` always succeeds). */
+la_status la_lu_new(la_ctx ctx, const double* a, size_t m, size_t n, la_lu* out);
+/* Same, from device memory (row pitch lda >= n elements). */
+la_status la_lu_new_device(la_ctx ctx, const double* d_a, size_t lda, size_t m, size_t n,
+                           la_lu* out);
+void la_lu_free(la_lu lu);
+la_status la_lu_shape(la_lu lu, size_t* m, size_t* n);
+
+/* lu.rs:170-182. *out = 1 when non-singular. LA_BADSHAPE where the
+ * reference indexes past its data (m < n with no zero diagonal found first). */
+la_status la_lu_is_non_singular(la_lu lu, int* out);
+/* lu.rs:224-232: (+-1) * product of U's diagonal in ascending order.
+ * LA_BADSHAPE unless square. */
+la_status la_lu_det(la_lu lu, double* out);
+/* lu.rs:222 get_piv (a permutation: piv[i] = original row now at i) and the
+ * sign flag (lu.rs:99). Either pointer may be NULL. */
+la_status la_lu_get_piv(la_lu lu, uint64_t* piv, int* pospivsign);
+/* The packed m x n LU (lu.rs:98): unit-L below the diagonal, U on/above. */
+la_status la_lu_get_packed(la_lu lu, double* out);
+/* lu.rs:184-202: m x min(m,n). */
+la_status la_lu_get_l(la_lu lu, double* out);
+/* lu.rs:204-215: min(m,n) x n. */
+la_status la_lu_get_u(la_lu lu, double* out);
+/* lu.rs:217-220: m x m permutation matrix, row i = e_{piv[i]}. */
+la_status la_lu_get_p(la_lu lu, double* out);
+/* Device pointer and row pitch of the packed LU (valid while `lu` lives). */
+const double* la_lu_device_data(la_lu lu, size_t* ld);
+
+/* LUDecomposition::solve (lu.rs:237-278). B is brows x nrhs; X is m x nrhs.
+ * LA_BADSHAPE if brows != m, LA_SINGULAR if U has an exact zero diagonal. */
+la_status la_lu_solve(la_lu lu, const double* b, size_t brows, size_t nrhs, double* x);
+/* Same on device memory (pitches ldb, ldx >= nrhs). */
+la_status la_lu_solve_device(la_lu lu, const double* d_b, size_t ldb, size_t brows,
+                             size_t nrhs, double* d_x, size_t ldx);
+
+/* ---- Matrix<f64> methods that go through LU (src/matrix/mod.rs) ---------- */
+
+/* mod.rs:1025-1028: asserts square, LU, det. */
+la_status la_matrix_det(la_ctx ctx, const double* a, size_t m, size_t n, double* out);
+/* mod.rs:1030-1032: LUDecomposition::new(a).solve(b) (no square assert). */
+la_status la_matrix_solve(la_ctx ctx, const double* a, size_t m, size_t n, const double* b,
+                          size_t brows, size_t nrhs, double* x);
+/* mod.rs:1034-1037: asserts square, then LU.solve(Matrix::id(n, n)). */
+la_status la_matrix_inverse(la_ctx ctx, const double* a, size_t m, size_t n, double* out);
+/* mod.rs:1044-1047: asserts square, LU, is_non_singular. */
+la_status la_matrix_is_non_singular(la_ctx ctx, const double* a, size_t m, size_t n, int* out);
+
+/* ---- Matrix * Matrix (mod.rs:957-998, mmatrix.rs:82-98) ------------------ */
+
+/* C (m x n) = A (m x k) * B (brows x n). LA_BADSHAPE unless k == brows. */
+la_status la_matrix_mul(la_ctx ctx, const double* a, size_t m, size_t k, const double* b,
+                        size_t brows, size_t n, double* c);
+/* mmul: like la_matrix_mul into a caller buffer of dst_rows x dst_cols;
+ * LA_BADSHAPE unless dst is m x n (mmatrix.rs:83-85). */
+la_status la_matrix_mmul(la_ctx ctx, const double* a, size_t m, size_t k, const double* b,
+                         size_t brows, size_t n, double* dst, size_t dst_rows, size_t dst_cols);
+/* Device form: C = A * B with row pitches; stream-ordered, no sync. */
+la_status la_matrix_mul_device(la_ctx ctx, const double* d_a, size_t lda, const double* d_b,
+                               size_t ldb, double* d_c, size_t ldc, size_t m, size_t k, size_t n);
+
+/* ---- diagnostics ---------------------------------------------------------- */
+
+/* Measures this GPU's FP64 FMA issue rate (TFLOP/s) with a short all-SM
+ * register-resident loop; used as the roofline denominator for FP64 kernels. */
+la_status la_probe_fp64_peak(la_ctx ctx, double* tflops);
+/* Number of kernels this context launched since creation (for launch counts). */
+uint64_t la_ctx_kernel_launches(la_ctx ctx);
+/* Per-phase device time of the last LU factorization, in milliseconds
+ * (panel, row swaps, triangular update, trailing GEMM, other), measured with
+ * CUDA events when LA_OPT_PROFILE is set; zeros otherwise. */
+la_status la_ctx_last_phase_ms(la_ctx ctx, double* ms5);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LA_GPU_H */

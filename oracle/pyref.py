@@ -1,0 +1,73 @@
+"""ORACLE — test infrastructure only.
+
+An independent pure-Python restatement of src/decomp/lu.rs:104-168 (factor),
+:224-232 (det) and :237-278 (solve), and src/matrix/mod.rs:957-980 (Mul), written
+with plain Python floats (IEEE binary64, no fused multiply-add) and lists. It is
+slow and meant only for small matrices: it cross-checks the C restatement.
+"""
+
+
+def lu_factor(a):
+    m = len(a)
+    n = len(a[0])
+    lu = [float(v) for row in a for v in row]
+    piv = list(range(m))
+    pos = True
+    for j in range(n):
+        for i in range(m):
+            s = 0.0
+            for k in range(min(i, j)):
+                s = s + lu[i * n + k] * lu[k * n + j]
+            lu[i * n + j] = lu[i * n + j] - s
+        p = j
+        for i in range(j + 1, m):
+            if abs(lu[i * n + j]) > abs(lu[p * n + j]):
+                p = i
+        if p != j:
+            for k in range(n):
+                lu[p * n + k], lu[j * n + k] = lu[j * n + k], lu[p * n + k]
+            piv[p], piv[j] = piv[j], piv[p]
+            pos = not pos
+        if j < m and lu[j * n + j] != 0.0:
+            for i in range(j + 1, m):
+                lu[i * n + j] = lu[i * n + j] / lu[j * n + j]
+    return lu, piv, pos
+
+
+def det(lu, n, pos):
+    d = 1.0 if pos else -1.0
+    for j in range(n):
+        d = d * lu[j * n + j]
+    return d
+
+
+def solve(lu, m, n, piv, b, nx):
+    for j in range(n):
+        if lu[j * n + j] == 0.0:
+            return None
+    x = [b[piv[i] * nx + j] for i in range(m) for j in range(nx)]
+    for k in range(n):
+        for i in range(k + 1, n):
+            for j in range(nx):
+                x[i * nx + j] = x[i * nx + j] - x[k * nx + j] * lu[i * n + k]
+    for k in range(n - 1, -1, -1):
+        for j in range(nx):
+            x[k * nx + j] = x[k * nx + j] / lu[k * n + k]
+        for i in range(k):
+            for j in range(nx):
+                x[i * nx + j] = x[i * nx + j] - x[k * nx + j] * lu[i * n + k]
+    return x
+
+
+def matmul(a, b):
+    m, k, n = len(a), len(b), len(b[0])
+    out = []
+    for r in range(m):
+        row = []
+        for c in range(n):
+            res = 0.0
+            for idx in range(k):
+                res = res + a[r][idx] * b[idx][c]
+            row.append(res)
+        out.append(row)
+    return out

@@ -1,0 +1,228 @@
+// FP64 GEMM tiles for the blocked LU (trailing update, triangular-solve
+// updates) and for Matrix * Matrix.
+//
+// GB300 executes FP64 FMA at roughly 2 per clock per SM (about 1.2 TFLOP/s for
+// the chip), two orders of magnitude below its tensor rates, so these tiles are
+// bound by the FP64 pipe, not by memory: a 64x64 output tile with a 32-deep K
+// slab needs 32 KB of operands for 131k FMAs. The kernel therefore aims at
+// keeping every SM's FP64 pipe fed (several resident CTAs, register-blocked
+// 4x4 micro-tiles, cp.async double buffering) rather than at operand reuse.
+//
+// Each output element is accumulated by one thread in a fixed k order, which
+// gives the EXACT modes the reference's summation order: src/matrix/mod.rs:
+// 965-973 (Mul: res = res + a*b from zero, ascending idx) and src/decomp/lu.rs:
+// 124-126 (s = s + l*u, ascending k) and :260/:272 (x = x - x_k*l, per term).
+#include "la_internal.cuh"
+
+namespace {
+
+constexpr int BM = 64;
+constexpr int BK = 32;
+constexpr int THREADS = 256;
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, int src_bytes) {
+  unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem),
+               "r"(src_bytes));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;\n" ::); }
+
+// Loads one K slab: A rows [m0, m0+64) x k [k0, k0+32) and B k [k0, k0+32) x cols [n0, n0+BN).
+// Out-of-range 16-byte chunks are zero-filled (src size 0 or 8), never read.
+template <int BN>
+__device__ __forceinline__ void load_slab(double* As, double* Bs, const double* A, size_t lda,
+                                          const double* B, size_t ldb, int M, int N, int K,
+                                          int m0, int n0, int k0) {
+  const int tid = threadIdx.x;
+  // A: 64 rows x 32 k = 1024 chunks of 2 doubles, 4 per thread.
+#pragma unroll
+  for (int t = 0; t < (BM * BK / 2) / THREADS; t++) {
+    int chunk = tid + t * THREADS;
+    int r = chunk / (BK / 2);
+    int kc = (chunk % (BK / 2)) * 2;
+    int gr = m0 + r, gk = k0 + kc;
+    int bytes = 0;
+    const double* src = A;
+    if (gr < M && gk < K) {
+      bytes = (gk + 1 < K) ? 16 : 8;
+      src = A + (size_t)gr * lda + gk;
+    }
+    cp_async16(As + r * BK + kc, src, bytes);
+  }
+  // B: 32 k x BN cols.
+  constexpr int BCH = BK * BN / 2;
+#pragma unroll
+  for (int t = 0; t < (BCH + THREADS - 1) / THREADS; t++) {
+    int chunk = tid + t * THREADS;
+    if (chunk < BCH) {
+      int kr = chunk / (BN / 2);
+      int cc = (chunk % (BN / 2)) * 2;
+      int gk = k0 + kr, gc = n0 + cc;
+      int bytes = 0;
+      const double* src = B;
+      if (gk < K && gc < N) {
+        bytes = (gc + 1 < N) ? 16 : 8;
+        src = B + (size_t)gk * ldb + gc;
+      }
+      cp_async16(Bs + kr * BN + cc, src, bytes);
+    }
+  }
+}
+
+// 256 threads; thread (tx = tid % 16, ty = tid / 16) owns rows ty + 16*i (i < 4)
+// and cols tx + 16*j (j < BN/16) of the 64 x BN output tile.
+template <int MODE, int BN>
+__global__ void __launch_bounds__(THREADS)
+gemm_f64_kernel(int M, int N, int K, const double* __restrict__ A, size_t lda,
+                const double* __restrict__ B, size_t ldb, double* __restrict__ C, size_t ldc) {
+  constexpr int TN = BN / 16;
+  extern __shared__ __align__(16) double smem[];
+  double* As = smem;                 // [2][BM][BK]
+  double* Bs = smem + 2 * BM * BK;   // [2][BK][BN]
+
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+
+  double acc[4][TN];
+  constexpr bool ZERO = (MODE == GM_FMA_ZERO || MODE == GM_EXACT_ZERO);
+  constexpr bool DESC = (MODE == GM_EXACT_SUB_DESC || MODE == GM_FMA_SUB_DESC);
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < TN; j++) {
+      int r = m0 + ty + 16 * i, c = n0 + tx + 16 * j;
+      acc[i][j] = (!ZERO && r < M && c < N) ? C[(size_t)r * ldc + c] : 0.0;
+    }
+
+  const int nslab = (K + BK - 1) / BK;
+  // Slab order: ascending, or descending for back substitution.
+  auto slab_k0 = [&](int s) { return DESC ? (nslab - 1 - s) * BK : s * BK; };
+
+  load_slab<BN>(As, Bs, A, lda, B, ldb, M, N, K, m0, n0, slab_k0(0));
+  cp_async_commit();
+
+  for (int s = 0; s < nslab; s++) {
+    const int buf = s & 1;
+    if (s + 1 < nslab) {
+      load_slab<BN>(As + (buf ^ 1) * BM * BK, Bs + (buf ^ 1) * BK * BN, A, lda, B, ldb, M, N, K,
+                    m0, n0, slab_k0(s + 1));
+      cp_async_commit();
+      cp_async_wait_1();
+    } else {
+      cp_async_wait_all();
+    }
+    __syncthreads();
+    const double* as = As + buf * BM * BK;
+    const double* bs = Bs + buf * BK * BN;
+    const int k0 = slab_k0(s);
+    const int kn = min(BK, K - k0);
+    if (kn == BK) {
+#pragma unroll 8
+      for (int kk = 0; kk < BK; kk++) {
+        const int k = DESC ? (BK - 1 - kk) : kk;
+        double a[4], b[TN];
+#pragma unroll
+        for (int i = 0; i < 4; i++) a[i] = as[(ty + 16 * i) * BK + k];
+#pragma unroll
+        for (int j = 0; j < TN; j++) b[j] = bs[k * BN + tx + 16 * j];
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+          for (int j = 0; j < TN; j++) {
+            if (MODE == GM_FMA_SUB || MODE == GM_FMA_SUB_DESC)
+              acc[i][j] = fma(-a[i], b[j], acc[i][j]);
+            else if (MODE == GM_FMA_ZERO)
+              acc[i][j] = fma(a[i], b[j], acc[i][j]);
+            else if (MODE == GM_EXACT_ADD || MODE == GM_EXACT_ZERO)
+              acc[i][j] = __dadd_rn(acc[i][j], __dmul_rn(a[i], b[j]));
+            else
+              acc[i][j] = __dsub_rn(acc[i][j], __dmul_rn(a[i], b[j]));
+          }
+      }
+    } else {
+      // Ragged last slab: only the kn valid k are applied (no padded terms).
+      for (int kk = 0; kk < kn; kk++) {
+        const int k = DESC ? (kn - 1 - kk) : kk;
+        double a[4], b[TN];
+#pragma unroll
+        for (int i = 0; i < 4; i++) a[i] = as[(ty + 16 * i) * BK + k];
+#pragma unroll
+        for (int j = 0; j < TN; j++) b[j] = bs[k * BN + tx + 16 * j];
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+          for (int j = 0; j < TN; j++) {
+            if (MODE == GM_FMA_SUB || MODE == GM_FMA_SUB_DESC)
+              acc[i][j] = fma(-a[i], b[j], acc[i][j]);
+            else if (MODE == GM_FMA_ZERO)
+              acc[i][j] = fma(a[i], b[j], acc[i][j]);
+            else if (MODE == GM_EXACT_ADD || MODE == GM_EXACT_ZERO)
+              acc[i][j] = __dadd_rn(acc[i][j], __dmul_rn(a[i], b[j]));
+            else
+              acc[i][j] = __dsub_rn(acc[i][j], __dmul_rn(a[i], b[j]));
+          }
+      }
+    }
+    __syncthreads();
+  }
+
+  if (MODE == GM_EXACT_ZERO && K == 0) {
+    // Nothing accumulated: the reference's res stays 0.0.
+  }
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < TN; j++) {
+      int r = m0 + ty + 16 * i, c = n0 + tx + 16 * j;
+      if (r < M && c < N) C[(size_t)r * ldc + c] = acc[i][j];
+    }
+}
+
+template <int MODE, int BN>
+la_status launch_mode(la_ctx ctx, int M, int N, int K, const double* A, size_t lda,
+                      const double* B, size_t ldb, double* C, size_t ldc) {
+  const size_t smem = (size_t)2 * (BM * BK + BK * BN) * sizeof(double);
+  static bool configured = false;  // one attribute call per instantiation
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(gemm_f64_kernel<MODE, BN>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaFuncSetAttribute(gemm)");
+    configured = true;
+  }
+  dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
+  gemm_f64_kernel<MODE, BN><<<grid, THREADS, smem, ctx->stream>>>(M, N, K, A, lda, B, ldb, C,
+                                                                  ldc);
+  ctx->launches++;
+  return la_check_launch(ctx, "gemm_f64_kernel");
+}
+
+template <int BN>
+la_status launch_bn(la_ctx ctx, int mode, int M, int N, int K, const double* A, size_t lda,
+                    const double* B, size_t ldb, double* C, size_t ldc) {
+  switch (mode) {
+    case GM_FMA_SUB: return launch_mode<GM_FMA_SUB, BN>(ctx, M, N, K, A, lda, B, ldb, C, ldc);
+    case GM_FMA_ZERO: return launch_mode<GM_FMA_ZERO, BN>(ctx, M, N, K, A, lda, B, ldb, C, ldc);
+    case GM_EXACT_ADD: return launch_mode<GM_EXACT_ADD, BN>(ctx, M, N, K, A, lda, B, ldb, C, ldc);
+    case GM_EXACT_ZERO: return launch_mode<GM_EXACT_ZERO, BN>(ctx, M, N, K, A, lda, B, ldb, C, ldc);
+    case GM_EXACT_SUB: return launch_mode<GM_EXACT_SUB, BN>(ctx, M, N, K, A, lda, B, ldb, C, ldc);
+    case GM_EXACT_SUB_DESC:
+      return launch_mode<GM_EXACT_SUB_DESC, BN>(ctx, M, N, K, A, lda, B, ldb, C, ldc);
+    case GM_FMA_SUB_DESC:
+      return launch_mode<GM_FMA_SUB_DESC, BN>(ctx, M, N, K, A, lda, B, ldb, C, ldc);
+    default: return LA_INVALID;
+  }
+}
+
+}  // namespace
+
+// C (M x N, ldc) op= A (M x K, lda) * B (K x N, ldb); all row-major. Pointers
+// must be 16-byte aligned and pitches even (the library pads pitches to 4).
+la_status launch_gemm(la_ctx ctx, int mode, int M, int N, int K, const double* A, size_t lda,
+                      const double* B, size_t ldb, double* C, size_t ldc) {
+  if (M <= 0 || N <= 0) return LA_OK;
+  if (K <= 0 && mode != GM_FMA_ZERO && mode != GM_EXACT_ZERO) return LA_OK;
+  if (N <= 16) return launch_bn<16>(ctx, mode, M, N, K, A, lda, B, ldb, C, ldc);
+  return launch_bn<64>(ctx, mode, M, N, K, A, lda, B, ldb, C, ldc);
+}

@@ -1,0 +1,119 @@
+// Internal declarations shared by the liblagpu translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include "../../include/la_gpu.h"
+
+// Accumulation forms of the FP64 kernels.
+//  FAST : c = fma(-a, b, c)                      (blocked LU, in place)
+//  EXACT: the reference's order, no fusion:
+//         LU carry  s = s + a*b, value = x - s   (lu.rs:122-128)
+//         solve     x = x - a*b per term         (lu.rs:260, :272)
+enum GemmMode : int {
+  GM_FMA_SUB = 0,        // C = C - A*B   fused, ascending k
+  GM_FMA_ZERO = 1,       // C = A*B       fused, from zero
+  GM_EXACT_ADD = 2,      // C = C + a*b   unfused, ascending k (LU carry)
+  GM_EXACT_ZERO = 3,     // C = 0 + a*b   unfused, ascending k (Mul, mod.rs:965-973)
+  GM_EXACT_SUB = 4,      // C = C - a*b   unfused, ascending k (forward solve)
+  GM_EXACT_SUB_DESC = 5, // C = C - a*b   unfused, descending k (back solve)
+  GM_FMA_SUB_DESC = 6    // C = C - A*B   fused, descending k
+};
+
+// Device-side error codes written to la_context::d_err.
+enum DeviceErr : int {
+  DERR_NONE = 0,
+  DERR_PANEL_TIMEOUT = 1,
+  DERR_PANEL_CAPACITY = 2
+};
+
+struct la_context {
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  int sm_count = 0;
+  size_t smem_optin = 0;
+  int arith = LA_ARITH_FAST;
+  int panel_width = 64;
+  int panel_ctas = 0;
+  int profile = 0;
+  std::string last_error;
+  uint64_t launches = 0;
+  double phase_ms[5] = {0, 0, 0, 0, 0};
+
+  // Device scratch for the cooperative panel kernel and small results.
+  void* d_scratch = nullptr;
+  size_t scratch_bytes = 0;
+  int* d_err = nullptr;          // inside d_scratch
+  unsigned* d_bar = nullptr;     // barrier counters (one per panel)
+  size_t bar_count = 0;
+  double* d_cand_abs = nullptr;  // [2][MAX_PANEL_CTAS]
+  int* d_cand_pos = nullptr;     // [2][MAX_PANEL_CTAS]
+  double* d_cand_row = nullptr;  // [2][MAX_PANEL_CTAS][64]
+  double* d_diag_a = nullptr;    // [2][64]
+  double* d_diag_s = nullptr;    // [2][64]
+  int* d_swaps = nullptr;        // [1 + 2*128] composed row moves of one panel
+  double* d_small = nullptr;     // [8] small device results (det, flags)
+  void* h_pinned = nullptr;      // pinned host staging for small readbacks
+};
+
+struct la_lu_handle {
+  la_ctx ctx = nullptr;
+  size_t m = 0, n = 0, ld = 0;
+  double* d_lu = nullptr;
+  int* d_ipiv = nullptr;         // LAPACK-style swap list, absolute rows, length min(m,n)
+  uint64_t* d_piv = nullptr;     // permutation vector (lu.rs piv), length m
+  int pospivsign = 1;
+  int zero_diag = 0;             // an exact 0 on U's diagonal (j < min(m,n))
+  int arith = LA_ARITH_FAST;
+};
+
+constexpr int MAX_PANEL_CTAS = 1024;
+constexpr int MAX_PANEL_W = 64;
+
+// Host helpers (context.cu).
+la_status la_cuda_fail(la_ctx ctx, cudaError_t e, const char* what);
+la_status la_check_launch(la_ctx ctx, const char* what);
+la_status la_device_alloc(la_ctx ctx, void** p, size_t bytes);
+void la_device_free(la_ctx ctx, void* p);
+la_status la_sync_and_check(la_ctx ctx, const char* what);
+
+#define LA_TRY(expr)                       \
+  do {                                     \
+    la_status _s = (expr);                 \
+    if (_s != LA_OK) return _s;            \
+  } while (0)
+
+#define LA_CUDA(ctx, call)                                  \
+  do {                                                      \
+    cudaError_t _e = (call);                                \
+    if (_e != cudaSuccess) return la_cuda_fail(ctx, _e, #call); \
+  } while (0)
+
+// Kernel launchers (one per translation unit of kernels).
+la_status launch_gemm(la_ctx ctx, int mode, int M, int N, int K, const double* A, size_t lda,
+                      const double* B, size_t ldb, double* C, size_t ldc);
+la_status launch_panel(la_ctx ctx, bool exact, double* A, double* S, size_t ld, int m, int j0,
+                       int jb, int* d_ipiv, unsigned* bar_base);
+la_status launch_laswp(la_ctx ctx, bool exact, double* A, double* S, size_t ld, int n, int j0,
+                       int jb);
+la_status launch_trsm_rowpanel(la_ctx ctx, bool exact, double* A, double* S, size_t ld, int j0,
+                               int jb, int c_begin, int c_end);
+la_status launch_solve_diag_fwd(la_ctx ctx, bool exact, const double* LU, size_t ld, int k0,
+                                int kb, double* X, size_t ldx, int nrhs);
+la_status launch_solve_diag_bwd(la_ctx ctx, bool exact, const double* LU, size_t ld, int k0,
+                                int kb, double* X, size_t ldx, int nrhs);
+la_status launch_lu_finish(la_ctx ctx, la_lu h);
+la_status launch_permute_rows(la_ctx ctx, const uint64_t* d_piv, const double* B, size_t ldb,
+                              double* X, size_t ldx, int m, int nrhs);
+la_status launch_identity_permuted(la_ctx ctx, const uint64_t* d_piv, double* X, size_t ldx,
+                                   int m);
+la_status launch_det(la_ctx ctx, const double* LU, size_t ld, int n, int pospivsign,
+                     double* d_out);
+la_status launch_unpack(la_ctx ctx, int which, const double* LU, size_t ld, int m, int n,
+                        const uint64_t* d_piv, double* out);
+la_status launch_copy2d(la_ctx ctx, const double* src, size_t lds, double* dst, size_t ldd,
+                        int rows, int cols);

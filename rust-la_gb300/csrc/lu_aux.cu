@@ -1,0 +1,380 @@
+// Row swaps, triangular updates and the small kernels around the blocked LU.
+#include "la_internal.cuh"
+
+namespace {
+
+// ---- row swaps outside the panel (lu.rs:140-145 for the other columns) ----
+// Applies the composed moves of one panel (dest <- src) to columns
+// [c_begin, c_end) of one matrix. All sources are read into shared memory
+// before any destination is written, so the moves act as one permutation.
+constexpr int SW_COLS = 32;
+__global__ void __launch_bounds__(256)
+laswp_kernel(double* M0, double* M1, double* M2, size_t ld, int b0, int e0, int b1, int e1,
+             int b2, int e2, const int* __restrict__ swaps) {
+  __shared__ double tmp[2 * MAX_PANEL_W][SW_COLS];
+  const int cnt = swaps[0];
+  if (cnt == 0) return;
+  const int* dst = swaps + 1;
+  const int* src = swaps + 1 + 2 * MAX_PANEL_W;
+  // blockIdx.y selects the segment.
+  double* M;
+  int cb, ce;
+  if (blockIdx.y == 0) { M = M0; cb = b0; ce = e0; }
+  else if (blockIdx.y == 1) { M = M1; cb = b1; ce = e1; }
+  else { M = M2; cb = b2; ce = e2; }
+  if (M == nullptr) return;
+  const int c = cb + blockIdx.x * SW_COLS + (threadIdx.x % SW_COLS);
+  if (cb + (int)blockIdx.x * SW_COLS >= ce) return;
+  const int ty = threadIdx.x / SW_COLS;  // 0..7
+  const bool ok = c < ce;
+  for (int q = ty; q < cnt; q += 8)
+    if (ok) tmp[q][threadIdx.x % SW_COLS] = M[(size_t)src[q] * ld + c];
+  __syncthreads();
+  for (int q = ty; q < cnt; q += 8)
+    if (ok) M[(size_t)dst[q] * ld + c] = tmp[q][threadIdx.x % SW_COLS];
+}
+
+// ---- row-panel triangular update: U12 = L11^{-1} A12 ----------------------
+// Rows [j0, j0+jb), columns [c_begin, c_end), one 32-column strip per CTA.
+// Column sweep over k (one barrier per k): row k is finished, then every row
+// i > k of the block takes its k-th term, i.e. each element receives its terms
+// in ascending k, like lu.rs:124-128 (EXACT: s += l*u, u = a - s) or with FMA.
+constexpr int TR_COLS = 32;
+constexpr int LP = MAX_PANEL_W + 1;  // padded row of the triangular block in shared memory
+constexpr size_t TRSM_SMEM_FAST = (size_t)(MAX_PANEL_W * LP + MAX_PANEL_W * TR_COLS) * 8;
+constexpr size_t TRSM_SMEM_EXACT = TRSM_SMEM_FAST + (size_t)MAX_PANEL_W * TR_COLS * 8;
+constexpr size_t SOLVE_SMEM = (size_t)(MAX_PANEL_W * LP + MAX_PANEL_W * TR_COLS) * 8;
+
+template <bool EXACT>
+__global__ void __launch_bounds__(256)
+trsm_rowpanel_kernel(double* A, const double* S, size_t ld, int j0, int jb, int c_begin,
+                     int c_end) {
+  extern __shared__ __align__(16) double dsm[];
+  double(*L)[LP] = reinterpret_cast<double(*)[LP]>(dsm);
+  double(*xa)[TR_COLS] = reinterpret_cast<double(*)[TR_COLS]>(dsm + MAX_PANEL_W * LP);
+  double(*xs)[TR_COLS] =
+      reinterpret_cast<double(*)[TR_COLS]>(dsm + MAX_PANEL_W * LP + MAX_PANEL_W * TR_COLS);
+  const int tx = threadIdx.x % TR_COLS, ty = threadIdx.x / TR_COLS;  // ty 0..7
+  const int c = c_begin + blockIdx.x * TR_COLS + tx;
+  const bool ok = c < c_end;
+  for (int idx = threadIdx.x; idx < jb * jb; idx += 256) {
+    int i = idx / jb, k = idx % jb;
+    L[i][k] = A[(size_t)(j0 + i) * ld + j0 + k];
+  }
+  for (int i = ty; i < jb; i += 8) {
+    size_t off = (size_t)(j0 + i) * ld + c;
+    xa[i][tx] = ok ? A[off] : 0.0;
+    if (EXACT) xs[i][tx] = ok ? S[off] : 0.0;
+  }
+  __syncthreads();
+  for (int k = 0; k < jb; k++) {
+    if (EXACT && ty == (k & 7)) {
+      // Row k is complete (this thread applied all its earlier terms): u = a - s.
+      xa[k][tx] = __dsub_rn(xa[k][tx], xs[k][tx]);
+    }
+    __syncthreads();
+    const double uk = xa[k][tx];
+    for (int i = ty; i < jb; i += 8) {
+      if (i <= k) continue;
+      if (EXACT)
+        xs[i][tx] = __dadd_rn(xs[i][tx], __dmul_rn(L[i][k], uk));
+      else
+        xa[i][tx] = fma(-L[i][k], uk, xa[i][tx]);
+    }
+  }
+  __syncthreads();
+  if (ok)
+    for (int i = ty; i < jb; i += 8) A[(size_t)(j0 + i) * ld + c] = xa[i][tx];
+}
+
+// ---- diagonal blocks of LUDecomposition::solve (lu.rs:256-275) ------------
+// Forward, unit L: for k ascending, x_i = x_i - x_k * l_ik for i in (k, k0+kb).
+template <bool EXACT>
+__global__ void __launch_bounds__(256)
+solve_diag_fwd_kernel(const double* LU, size_t ld, int k0, int kb, double* X, size_t ldx,
+                      int nrhs) {
+  extern __shared__ __align__(16) double dsm[];
+  double(*L)[LP] = reinterpret_cast<double(*)[LP]>(dsm);
+  double(*x)[TR_COLS] = reinterpret_cast<double(*)[TR_COLS]>(dsm + MAX_PANEL_W * LP);
+  const int tx = threadIdx.x % TR_COLS, ty = threadIdx.x / TR_COLS;
+  const int c = blockIdx.x * TR_COLS + tx;
+  const bool ok = c < nrhs;
+  for (int idx = threadIdx.x; idx < kb * kb; idx += 256) {
+    int i = idx / kb, k = idx % kb;
+    L[i][k] = LU[(size_t)(k0 + i) * ld + k0 + k];
+  }
+  for (int i = ty; i < kb; i += 8) x[i][tx] = ok ? X[(size_t)(k0 + i) * ldx + c] : 0.0;
+  __syncthreads();
+  for (int k = 0; k < kb; k++) {
+    const double xk = x[k][tx];
+    for (int i = ty; i < kb; i += 8) {
+      if (i <= k) continue;
+      if (EXACT)
+        x[i][tx] = __dsub_rn(x[i][tx], __dmul_rn(xk, L[i][k]));
+      else
+        x[i][tx] = fma(-xk, L[i][k], x[i][tx]);
+    }
+    __syncthreads();
+  }
+  if (ok)
+    for (int i = ty; i < kb; i += 8) X[(size_t)(k0 + i) * ldx + c] = x[i][tx];
+}
+
+// Backward, U: for k descending, x_k = x_k / u_kk, then x_i = x_i - x_k * u_ik
+// for i in [k0, k).
+template <bool EXACT>
+__global__ void __launch_bounds__(256)
+solve_diag_bwd_kernel(const double* LU, size_t ld, int k0, int kb, double* X, size_t ldx,
+                      int nrhs) {
+  extern __shared__ __align__(16) double dsm[];
+  double(*U)[LP] = reinterpret_cast<double(*)[LP]>(dsm);
+  double(*x)[TR_COLS] = reinterpret_cast<double(*)[TR_COLS]>(dsm + MAX_PANEL_W * LP);
+  const int tx = threadIdx.x % TR_COLS, ty = threadIdx.x / TR_COLS;
+  const int c = blockIdx.x * TR_COLS + tx;
+  const bool ok = c < nrhs;
+  for (int idx = threadIdx.x; idx < kb * kb; idx += 256) {
+    int i = idx / kb, k = idx % kb;
+    U[i][k] = LU[(size_t)(k0 + i) * ld + k0 + k];
+  }
+  for (int i = ty; i < kb; i += 8) x[i][tx] = ok ? X[(size_t)(k0 + i) * ldx + c] : 0.0;
+  __syncthreads();
+  for (int k = kb - 1; k >= 0; k--) {
+    if (ty == (k & 7)) x[k][tx] = x[k][tx] / U[k][k];
+    __syncthreads();
+    const double xk = x[k][tx];
+    for (int i = ty; i < k; i += 8) {
+      if (EXACT)
+        x[i][tx] = __dsub_rn(x[i][tx], __dmul_rn(xk, U[i][k]));
+      else
+        x[i][tx] = fma(-xk, U[i][k], x[i][tx]);
+    }
+    __syncthreads();
+  }
+  if (ok)
+    for (int i = ty; i < kb; i += 8) X[(size_t)(k0 + i) * ldx + c] = x[i][tx];
+}
+
+// ---- after the factorization: permutation vector, sign, zero diagonal ------
+// The swap list (LAPACK ipiv form) is replayed in order on a permutation
+// vector (lu.rs:147-149), the sign flips once per real swap (lu.rs:151), and
+// U's diagonal is scanned for an exact zero (lu.rs:177).
+__global__ void lu_finish_kernel(const int* __restrict__ ipiv, uint64_t* piv, int m, int kmin,
+                                 const double* LU, size_t ld, int* flags) {
+  __shared__ int zero;
+  if (threadIdx.x == 0) zero = 0;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) piv[i] = (uint64_t)i;
+  __syncthreads();
+  for (int j = threadIdx.x; j < kmin; j += blockDim.x)
+    if (LU[(size_t)j * ld + j] == 0.0) atomicOr(&zero, 1);
+  if (threadIdx.x == 0) {
+    int pos = 1;
+    for (int j = 0; j < kmin; j++) {
+      int p = ipiv[j];
+      if (p != j) {
+        uint64_t t = piv[p];
+        piv[p] = piv[j];
+        piv[j] = t;
+        pos = !pos;
+      }
+    }
+    flags[0] = pos;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) flags[1] = zero;
+}
+
+// X = B(piv, :) (lu.rs:245-254).
+__global__ void permute_rows_kernel(const uint64_t* __restrict__ piv, const double* __restrict__ B,
+                                    size_t ldb, double* __restrict__ X, size_t ldx, int m,
+                                    int nrhs) {
+  size_t total = (size_t)m * nrhs;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(idx / nrhs), j = (int)(idx % nrhs);
+    X[(size_t)i * ldx + j] = B[(size_t)piv[i] * ldb + j];
+  }
+}
+
+// X = I(piv, :) for inverse (mod.rs:1036 solves against Matrix::id).
+__global__ void identity_permuted_kernel(const uint64_t* __restrict__ piv, double* X, size_t ldx,
+                                         int m) {
+  size_t total = (size_t)m * m;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(idx / m), j = (int)(idx % m);
+    X[(size_t)i * ldx + j] = (piv[i] == (uint64_t)j) ? 1.0 : 0.0;
+  }
+}
+
+// det (lu.rs:224-232): one thread multiplies U's diagonal in ascending order,
+// the reference's exact sequence of roundings.
+__global__ void det_kernel(const double* LU, size_t ld, int n, int pospivsign, double* out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double d = pospivsign ? 1.0 : -1.0;
+    for (int j = 0; j < n; j++) d = d * LU[(size_t)j * ld + j];
+    out[0] = d;
+  }
+}
+
+// get_l (which 0, lu.rs:184-202), get_u (1, :204-215), get_p (2, :217-220),
+// packed copy (3).
+__global__ void unpack_kernel(int which, const double* LU, size_t ld, int m, int n,
+                              const uint64_t* piv, double* out) {
+  const int kmin = m < n ? m : n;
+  int rows, cols;
+  if (which == 0) { rows = m; cols = kmin; }
+  else if (which == 1) { rows = kmin; cols = n; }
+  else if (which == 2) { rows = m; cols = m; }
+  else { rows = m; cols = n; }
+  size_t total = (size_t)rows * cols;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(idx / cols), j = (int)(idx % cols);
+    double v;
+    if (which == 0) v = i > j ? LU[(size_t)i * ld + j] : (i == j ? 1.0 : 0.0);
+    else if (which == 1) v = i <= j ? LU[(size_t)i * ld + j] : 0.0;
+    else if (which == 2) v = (piv[i] == (uint64_t)j) ? 1.0 : 0.0;
+    else v = LU[(size_t)i * ld + j];
+    out[idx] = v;
+  }
+}
+
+__global__ void copy2d_kernel(const double* __restrict__ src, size_t lds, double* __restrict__ dst,
+                              size_t ldd, int rows, int cols) {
+  size_t total = (size_t)rows * cols;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(idx / cols), j = (int)(idx % cols);
+    dst[(size_t)i * ldd + j] = src[(size_t)i * lds + j];
+  }
+}
+
+// Dynamic shared memory above 48 KB needs an opt-in per kernel.
+void configure_smem_attrs() {
+  static bool done = false;
+  if (done) return;
+  cudaFuncSetAttribute(trsm_rowpanel_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)TRSM_SMEM_EXACT);
+  cudaFuncSetAttribute(trsm_rowpanel_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)TRSM_SMEM_FAST);
+  cudaFuncSetAttribute(solve_diag_fwd_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)SOLVE_SMEM);
+  cudaFuncSetAttribute(solve_diag_fwd_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)SOLVE_SMEM);
+  cudaFuncSetAttribute(solve_diag_bwd_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)SOLVE_SMEM);
+  cudaFuncSetAttribute(solve_diag_bwd_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)SOLVE_SMEM);
+  done = true;
+}
+
+int grid_for(la_ctx ctx, size_t total) {
+  size_t g = (total + 255) / 256;
+  size_t cap = (size_t)ctx->sm_count * 8;
+  return (int)std::max<size_t>(1, std::min(g, cap));
+}
+
+}  // namespace
+
+la_status launch_laswp(la_ctx ctx, bool exact, double* A, double* S, size_t ld, int n, int j0,
+                       int jb) {
+  const int j1 = j0 + jb;
+  const int left = j0, right = n - j1;
+  const int gx = std::max((left + SW_COLS - 1) / SW_COLS, (right + SW_COLS - 1) / SW_COLS);
+  if (gx == 0) return LA_OK;
+  dim3 grid(gx, exact ? 3 : 2);
+  laswp_kernel<<<grid, 256, 0, ctx->stream>>>(A, A, exact ? S : nullptr, ld, 0, j0, j1, n, j1, n,
+                                              ctx->d_swaps);
+  ctx->launches++;
+  return la_check_launch(ctx, "laswp_kernel");
+}
+
+la_status launch_trsm_rowpanel(la_ctx ctx, bool exact, double* A, double* S, size_t ld, int j0,
+                               int jb, int c_begin, int c_end) {
+  if (c_end <= c_begin) return LA_OK;
+  dim3 grid((c_end - c_begin + TR_COLS - 1) / TR_COLS);
+  configure_smem_attrs();
+  if (exact)
+    trsm_rowpanel_kernel<true><<<grid, 256, TRSM_SMEM_EXACT, ctx->stream>>>(A, S, ld, j0, jb,
+                                                                            c_begin, c_end);
+  else
+    trsm_rowpanel_kernel<false><<<grid, 256, TRSM_SMEM_FAST, ctx->stream>>>(A, S, ld, j0, jb,
+                                                                            c_begin, c_end);
+  ctx->launches++;
+  return la_check_launch(ctx, "trsm_rowpanel_kernel");
+}
+
+la_status launch_solve_diag_fwd(la_ctx ctx, bool exact, const double* LU, size_t ld, int k0,
+                                int kb, double* X, size_t ldx, int nrhs) {
+  dim3 grid((nrhs + TR_COLS - 1) / TR_COLS);
+  configure_smem_attrs();
+  if (exact)
+    solve_diag_fwd_kernel<true><<<grid, 256, SOLVE_SMEM, ctx->stream>>>(LU, ld, k0, kb, X, ldx,
+                                                                          nrhs);
+  else
+    solve_diag_fwd_kernel<false><<<grid, 256, SOLVE_SMEM, ctx->stream>>>(LU, ld, k0, kb, X,
+                                                                           ldx, nrhs);
+  ctx->launches++;
+  return la_check_launch(ctx, "solve_diag_fwd_kernel");
+}
+
+la_status launch_solve_diag_bwd(la_ctx ctx, bool exact, const double* LU, size_t ld, int k0,
+                                int kb, double* X, size_t ldx, int nrhs) {
+  dim3 grid((nrhs + TR_COLS - 1) / TR_COLS);
+  configure_smem_attrs();
+  if (exact)
+    solve_diag_bwd_kernel<true><<<grid, 256, SOLVE_SMEM, ctx->stream>>>(LU, ld, k0, kb, X, ldx,
+                                                                          nrhs);
+  else
+    solve_diag_bwd_kernel<false><<<grid, 256, SOLVE_SMEM, ctx->stream>>>(LU, ld, k0, kb, X,
+                                                                           ldx, nrhs);
+  ctx->launches++;
+  return la_check_launch(ctx, "solve_diag_bwd_kernel");
+}
+
+la_status launch_lu_finish(la_ctx ctx, la_lu h) {
+  const int kmin = (int)std::min(h->m, h->n);
+  lu_finish_kernel<<<1, 1024, 0, ctx->stream>>>(h->d_ipiv, h->d_piv, (int)h->m, kmin, h->d_lu,
+                                                h->ld, reinterpret_cast<int*>(ctx->d_small));
+  ctx->launches++;
+  return la_check_launch(ctx, "lu_finish_kernel");
+}
+
+la_status launch_permute_rows(la_ctx ctx, const uint64_t* d_piv, const double* B, size_t ldb,
+                              double* X, size_t ldx, int m, int nrhs) {
+  permute_rows_kernel<<<grid_for(ctx, (size_t)m * nrhs), 256, 0, ctx->stream>>>(d_piv, B, ldb, X,
+                                                                               ldx, m, nrhs);
+  ctx->launches++;
+  return la_check_launch(ctx, "permute_rows_kernel");
+}
+
+la_status launch_identity_permuted(la_ctx ctx, const uint64_t* d_piv, double* X, size_t ldx,
+                                   int m) {
+  identity_permuted_kernel<<<grid_for(ctx, (size_t)m * m), 256, 0, ctx->stream>>>(d_piv, X, ldx,
+                                                                                  m);
+  ctx->launches++;
+  return la_check_launch(ctx, "identity_permuted_kernel");
+}
+
+la_status launch_det(la_ctx ctx, const double* LU, size_t ld, int n, int pospivsign,
+                     double* d_out) {
+  det_kernel<<<1, 32, 0, ctx->stream>>>(LU, ld, n, pospivsign, d_out);
+  ctx->launches++;
+  return la_check_launch(ctx, "det_kernel");
+}
+
+la_status launch_unpack(la_ctx ctx, int which, const double* LU, size_t ld, int m, int n,
+                        const uint64_t* d_piv, double* out) {
+  size_t total = (size_t)std::max(m, n) * std::max(m, n);
+  unpack_kernel<<<grid_for(ctx, total), 256, 0, ctx->stream>>>(which, LU, ld, m, n, d_piv, out);
+  ctx->launches++;
+  return la_check_launch(ctx, "unpack_kernel");
+}
+
+la_status launch_copy2d(la_ctx ctx, const double* src, size_t lds, double* dst, size_t ldd,
+                        int rows, int cols) {
+  copy2d_kernel<<<grid_for(ctx, (size_t)rows * cols), 256, 0, ctx->stream>>>(src, lds, dst, ldd,
+                                                                             rows, cols);
+  ctx->launches++;
+  return la_check_launch(ctx, "copy2d_kernel");
+}

@@ -1,0 +1,345 @@
+// Panel factorization of the blocked LU: columns [j0, j0+jb) over rows
+// [j0, m), with partial pivoting (src/decomp/lu.rs:116-161 restricted to the
+// panel's columns).
+//
+// The tall panel is spread over G co-resident CTAs (cooperative launch); each
+// CTA keeps its contiguous chunk of rows in shared memory for the whole panel,
+// so the only global traffic per column is one candidate row per CTA. Per
+// column j there is exactly one grid barrier:
+//   1. each CTA finds its local pivot candidate, first row of max |v| (the
+//      reference's strict '>' scan, lu.rs:132-137), and publishes the value,
+//      its row position and the full finished row; the owner of row j also
+//      publishes row j (it moves to the pivot's place, lu.rs:140-145);
+//   2. barrier;
+//   3. every CTA picks the same winner (max |v|, then lowest position), takes
+//      the pivot row as U's row j, swaps in place, scales its rows below j by
+//      the pivot (true division, skipped for a zero pivot, lu.rs:156-160) and
+//      applies the rank-1 update to the rest of the panel.
+// Candidate buffers are double-buffered by column parity, so a CTA that runs
+// ahead never overwrites data a slower CTA is still reading.
+//
+// EXACT keeps, per element, the original value a and the running sum s of
+// l_ik*u_kj (added in ascending k without fusion, lu.rs:124-126) and forms
+// v = a - s only when the column is reached (lu.rs:128); finished entries
+// carry s = 0 so v = a - 0 = a for them. FAST updates v in place with FMA.
+//
+// Every wait is bounded: a CTA that waits past the limit (or sees another CTA
+// give up) records DERR_PANEL_TIMEOUT and returns; the host reports LA_TIMEOUT.
+#include "la_internal.cuh"
+
+namespace {
+
+constexpr int PT = 256;  // threads per panel CTA
+constexpr unsigned long long WAIT_LIMIT_NS = 2000000000ull;  // 2 s
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ int ld_volatile_i32(const int* p) {
+  int v;
+  asm volatile("ld.volatile.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Grid barrier on a monotonically increasing counter. Returns false when the
+// wait gave up (this CTA timed out or another CTA reported an error).
+__device__ bool grid_barrier(unsigned* counter, unsigned target, int* err) {
+  __shared__ int ok;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    atomicAdd(counter, 1u);
+    int good = 1;
+    unsigned long long t0 = globaltimer_ns();
+    unsigned spins = 0;
+    while (ld_acquire_u32(counter) < target) {
+      if (ld_volatile_i32(err) != 0) { good = 0; break; }
+      if ((++spins & 63u) == 0 && globaltimer_ns() - t0 > WAIT_LIMIT_NS) {
+        atomicCAS(err, 0, (int)DERR_PANEL_TIMEOUT);
+        good = 0;
+        break;
+      }
+    }
+    __threadfence();
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// Ordering key of a pivot candidate. NaN never wins a strict '>' test, so a
+// NaN below the diagonal ranks lowest; a NaN on the diagonal row j is never
+// displaced, so it ranks highest (ties go to the lowest position, which is j).
+__device__ __forceinline__ double pivot_key(double v, int pos, int j) {
+  if (v != v) return pos == j ? __longlong_as_double(0x7ff0000000000000ll) : -1.0;
+  return fabs(v);
+}
+__device__ __forceinline__ bool better(double ka, int pa, double kb, int pb) {
+  // a beats b: larger key, or equal key and lower position; pb < 0 means empty.
+  if (pb < 0) return pa >= 0;
+  if (pa < 0) return false;
+  return ka > kb || (ka == kb && pa < pb);
+}
+
+struct PanelParams {
+  double* A;
+  double* S;
+  size_t ld;
+  int m, j0, jb, rpc, G;
+  int* ipiv;
+  unsigned* bar;
+  unsigned bar_base;  // counter value at kernel start (the counter only grows)
+  int* err;
+  double* cand_abs;
+  int* cand_pos;
+  double* cand_row;
+  double* diag_a;
+  double* diag_s;
+  int* swaps;  // [0] = count, then (dest, src) pairs of the composed row moves
+};
+
+template <bool EXACT>
+__global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
+  extern __shared__ __align__(16) double sm[];
+  constexpr int W = MAX_PANEL_W;
+  const int rpc = p.rpc;
+  double* va = sm;                              // [rpc][W]  value (FAST) / a (EXACT)
+  double* vs = EXACT ? sm + rpc * W : nullptr;  // [rpc][W]  running sum s (EXACT)
+  double* urow = sm + (EXACT ? 2 : 1) * rpc * W;  // [W] pivot row
+  double* lrow = urow + W;                        // [rpc] multipliers of this step
+  __shared__ double red_k[PT / 32];
+  __shared__ int red_p[PT / 32];
+  __shared__ int s_win_pos;
+  __shared__ int s_pivs[W];
+
+  const int g = blockIdx.x;
+  const int tid = threadIdx.x;
+  const int jb = p.jb;
+  const int row0 = p.j0 + g * rpc;                  // position of local row 0
+  const int nrows = max(0, min(rpc, p.m - row0));   // rows owned by this CTA
+
+  // Load the owned rows of the panel.
+  for (int idx = tid; idx < rpc * W; idx += PT) {
+    int r = idx / W, c = idx % W;
+    double a = 0.0, s = 0.0;
+    if (r < nrows && c < jb) {
+      size_t off = (size_t)(row0 + r) * p.ld + p.j0 + c;
+      a = p.A[off];
+      if (EXACT) s = p.S[off];
+    }
+    va[idx] = a;
+    if (EXACT) vs[idx] = s;
+  }
+  __syncthreads();
+
+  for (int c = 0; c < jb; c++) {
+    const int j = p.j0 + c;
+    const int par = c & 1;
+    // 1. local candidate over owned rows at positions >= j.
+    double bk = 0.0;
+    int bp = -1;
+    for (int r = tid; r < nrows; r += PT) {
+      int pos = row0 + r;
+      if (pos < j) continue;
+      double v = EXACT ? __dsub_rn(va[r * W + c], vs[r * W + c]) : va[r * W + c];
+      double k = pivot_key(v, pos, j);
+      if (better(k, pos, bk, bp)) { bk = k; bp = pos; }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      double ok = __shfl_down_sync(0xffffffffu, bk, off);
+      int op = __shfl_down_sync(0xffffffffu, bp, off);
+      if (better(ok, op, bk, bp)) { bk = ok; bp = op; }
+    }
+    if ((tid & 31) == 0) { red_k[tid >> 5] = bk; red_p[tid >> 5] = bp; }
+    __syncthreads();
+    if (tid == 0) {
+      for (int w = 1; w < PT / 32; w++)
+        if (better(red_k[w], red_p[w], bk, bp)) { bk = red_k[w]; bp = red_p[w]; }
+      p.cand_abs[par * MAX_PANEL_CTAS + g] = bk;
+      p.cand_pos[par * MAX_PANEL_CTAS + g] = bp;
+      red_p[0] = bp;
+    }
+    __syncthreads();
+    // 2. publish the candidate row (finished values) and, if owned, row j.
+    {
+      const int cp = red_p[0];
+      if (cp >= 0 && tid < W) {
+        int r = cp - row0;
+        double v = EXACT ? __dsub_rn(va[r * W + tid], vs[r * W + tid]) : va[r * W + tid];
+        p.cand_row[((size_t)par * MAX_PANEL_CTAS + g) * W + tid] = v;
+      }
+      if (j >= row0 && j < row0 + nrows && tid < W) {
+        int r = j - row0;
+        p.diag_a[par * W + tid] = va[r * W + tid];
+        if (EXACT) p.diag_s[par * W + tid] = vs[r * W + tid];
+      }
+    }
+    if (!grid_barrier(p.bar, p.bar_base + (unsigned)(p.G * (c + 1)), p.err)) return;
+
+    // 3. global winner (identical in every CTA).
+    if (tid < 32) {
+      double k = 0.0;
+      int ps = -1;
+      for (int q = tid; q < p.G; q += 32) {
+        double qk = __ldcg(p.cand_abs + par * MAX_PANEL_CTAS + q);
+        int qp = __ldcg(p.cand_pos + par * MAX_PANEL_CTAS + q);
+        if (better(qk, qp, k, ps)) { k = qk; ps = qp; }
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        double ok = __shfl_down_sync(0xffffffffu, k, off);
+        int op = __shfl_down_sync(0xffffffffu, ps, off);
+        if (better(ok, op, k, ps)) { k = ok; ps = op; }
+      }
+      if (tid == 0) {
+        // Find which CTA published the winner (owner of that position).
+        s_win_pos = ps;
+        s_pivs[c] = ps;
+        if (g == 0) p.ipiv[j] = ps;
+      }
+    }
+    __syncthreads();
+    const int piv = s_win_pos;
+    const int wg = (piv - p.j0) / rpc;  // CTA that owns the winning row
+    if (tid < W) urow[tid] = __ldcg(p.cand_row + ((size_t)par * MAX_PANEL_CTAS + wg) * W + tid);
+    __syncthreads();
+    // Swap: row j <- pivot row (finished), row piv <- old row j (raw storage).
+    if (tid < W) {
+      if (piv != j && piv >= row0 && piv < row0 + nrows) {
+        int r = piv - row0;
+        va[r * W + tid] = __ldcg(p.diag_a + par * W + tid);
+        if (EXACT) vs[r * W + tid] = __ldcg(p.diag_s + par * W + tid);
+      }
+      if (j >= row0 && j < row0 + nrows) {
+        int r = j - row0;
+        va[r * W + tid] = urow[tid];
+        if (EXACT) vs[r * W + tid] = 0.0;
+      }
+    }
+    __syncthreads();
+    // 4a. multipliers l_i = v_i / u_jj for owned rows below j.
+    const double d = urow[c];
+    for (int r = tid; r < nrows; r += PT) {
+      int pos = row0 + r;
+      if (pos <= j) continue;
+      double v = EXACT ? __dsub_rn(va[r * W + c], vs[r * W + c]) : va[r * W + c];
+      double l = (d != 0.0) ? v / d : v;
+      va[r * W + c] = l;
+      if (EXACT) vs[r * W + c] = 0.0;
+      lrow[r] = l;
+    }
+    __syncthreads();
+    // 4b. rank-1 update of the remaining panel columns.
+    const int ncols = jb - c - 1;
+    if (ncols > 0) {
+      const int first = max(0, j + 1 - row0);
+      const int cnt = nrows - first;
+      for (int idx = tid; idx < cnt * ncols; idx += PT) {
+        int r = first + idx / ncols;
+        int cc = c + 1 + idx % ncols;
+        double l = lrow[r];
+        if (EXACT)
+          vs[r * W + cc] = __dadd_rn(vs[r * W + cc], __dmul_rn(l, urow[cc]));
+        else
+          va[r * W + cc] = fma(-l, urow[cc], va[r * W + cc]);
+      }
+    }
+    __syncthreads();
+  }
+
+  // Write the finished panel back.
+  for (int idx = tid; idx < nrows * W; idx += PT) {
+    int r = idx / W, c = idx % W;
+    if (c < jb) {
+      double v = EXACT ? __dsub_rn(va[idx], vs[idx]) : va[idx];
+      p.A[(size_t)(row0 + r) * p.ld + p.j0 + c] = v;
+    }
+  }
+  // Compose this panel's swaps into a list of row moves (dest <- src) for the
+  // columns outside the panel (applied by the row-swap kernel).
+  if (g == 0 && tid == 0) {
+    int cnt = 0;
+    int* dst = p.swaps + 1;
+    int* src = p.swaps + 1 + 2 * W;
+    auto find_or_add = [&](int pos) {
+      for (int q = 0; q < cnt; q++)
+        if (dst[q] == pos) return q;
+      dst[cnt] = pos;
+      src[cnt] = pos;
+      return cnt++;
+    };
+    for (int c = 0; c < jb; c++) {
+      int a = find_or_add(p.j0 + c);
+      int b = find_or_add(s_pivs[c]);
+      int t = src[a];
+      src[a] = src[b];
+      src[b] = t;
+    }
+    // Keep only real moves.
+    int k = 0;
+    for (int q = 0; q < cnt; q++)
+      if (src[q] != dst[q]) { dst[k] = dst[q]; src[k] = src[q]; k++; }
+    p.swaps[0] = k;
+  }
+}
+
+}  // namespace
+
+la_status launch_panel(la_ctx ctx, bool exact, double* A, double* S, size_t ld, int m, int j0,
+                       int jb, int* d_ipiv, unsigned* bar_base) {
+  const int R = m - j0;
+  if (R <= 0 || jb <= 0) return LA_OK;
+  const int W = MAX_PANEL_W;
+  int maxG = ctx->panel_ctas > 0 ? std::min(ctx->panel_ctas, ctx->sm_count) : ctx->sm_count;
+  maxG = std::min(maxG, MAX_PANEL_CTAS);
+  // At least 32 rows per CTA: fewer CTAs keep the per-column barrier cheap.
+  int G = std::max(1, std::min(maxG, (R + 31) / 32));
+  int rpc = (R + G - 1) / G;
+  const size_t per_row = (size_t)W * sizeof(double) * (exact ? 2 : 1) + sizeof(double);
+  const size_t fixed = (size_t)W * sizeof(double);
+  size_t smem = fixed + per_row * rpc;
+  if (smem > ctx->smem_optin) return LA_UNSUPPORTED;
+  G = (R + rpc - 1) / rpc;
+
+  PanelParams p;
+  p.A = A;
+  p.S = S;
+  p.ld = ld;
+  p.m = m;
+  p.j0 = j0;
+  p.jb = jb;
+  p.rpc = rpc;
+  p.G = G;
+  p.ipiv = d_ipiv;
+  p.bar = ctx->d_bar;
+  p.bar_base = *bar_base;
+  p.err = ctx->d_err;
+  p.cand_abs = ctx->d_cand_abs;
+  p.cand_pos = ctx->d_cand_pos;
+  p.cand_row = ctx->d_cand_row;
+  p.diag_a = ctx->d_diag_a;
+  p.diag_s = ctx->d_diag_s;
+  p.swaps = ctx->d_swaps;
+
+  void* args[] = {&p};
+  const void* fn = exact ? (const void*)panel_kernel<true> : (const void*)panel_kernel<false>;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaFuncSetAttribute(panel)");
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, PT, smem);
+  if (e != cudaSuccess) return la_cuda_fail(ctx, e, "occupancy(panel)");
+  if (per_sm * ctx->sm_count < G) return LA_UNSUPPORTED;
+  e = cudaLaunchCooperativeKernel(fn, dim3(G), dim3(PT), args, smem, ctx->stream);
+  if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaLaunchCooperativeKernel(panel)");
+  ctx->launches++;
+  *bar_base += (unsigned)(G * jb);
+  return la_check_launch(ctx, "panel_kernel");
+}

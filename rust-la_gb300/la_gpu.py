@@ -1,0 +1,387 @@
+"""Python host mirror of the `la` crate's LU path over liblagpu.so (include/la_gpu.h).
+
+The names, argument meaning and failure behaviour follow the reference crate
+(xasmx/rust-la 0.2.0):
+
+  Matrix.new(rows, cols, data)        src/matrix/mod.rs:207-211 (asserts len and dims > 0)
+  Matrix.id(m, n)                     mod.rs:416-426
+  a * b, a.mmul(b, dst)               mod.rs:957-998, mmatrix.rs:82-98
+  a.det(), a.solve(b), a.inverse()    mod.rs:1025-1037
+  a.is_singular(), a.is_non_singular() mod.rs:1039-1047
+  LUDecomposition.new(a)              src/decomp/lu.rs:104-168
+  lu.solve(b) / det / is_singular / is_non_singular / get_l / get_u / get_p / get_piv
+                                      lu.rs:170-278
+
+A reference `assert!` panic raises `Panic`; a reference `None` is returned as
+`None`. All arithmetic runs in the CUDA library; there is no CPU path here, and
+importing this module fails loudly when liblagpu.so is missing.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "liblagpu.so")
+
+OK, SINGULAR, BADSHAPE, INVALID, NOMEM, CUDA_ERROR, TIMEOUT, NOT_CONVERGED, UNSUPPORTED = range(9)
+OPT_ARITH, OPT_PANEL_WIDTH, OPT_PANEL_CTAS, OPT_PROFILE = 1, 2, 3, 4
+ARITH_FAST, ARITH_EXACT = 0, 1
+
+
+class Panic(Exception):
+    """The reference would panic here (failed assert! or out-of-bounds index)."""
+
+
+class LaError(RuntimeError):
+    def __init__(self, status, msg=""):
+        self.status = status
+        super().__init__("liblagpu status %d%s" % (status, (": " + msg) if msg else ""))
+
+
+_lib = None
+
+# Every symbol declared in include/la_gpu.h, with its ctypes signature.
+_P, _S, _I, _D = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_double
+SIGNATURES = {
+    "la_abi_version": ([], _I),
+    "la_status_string": ([_I], ctypes.c_char_p),
+    "la_ctx_create": ([_I, _P], _I),
+    "la_ctx_destroy": ([_P], None),
+    "la_ctx_set_stream": ([_P, _P], _I),
+    "la_ctx_get_stream": ([_P], _P),
+    "la_ctx_synchronize": ([_P], _I),
+    "la_ctx_last_error": ([_P], ctypes.c_char_p),
+    "la_ctx_set_option": ([_P, _I, ctypes.c_int64], _I),
+    "la_ctx_get_option": ([_P, _I, _P], _I),
+    "la_ctx_kernel_launches": ([_P], ctypes.c_uint64),
+    "la_ctx_last_phase_ms": ([_P, _P], _I),
+    "la_probe_fp64_peak": ([_P, _P], _I),
+    "la_lu_new": ([_P, _P, _S, _S, _P], _I),
+    "la_lu_new_device": ([_P, _P, _S, _S, _S, _P], _I),
+    "la_lu_free": ([_P], None),
+    "la_lu_shape": ([_P, _P, _P], _I),
+    "la_lu_is_non_singular": ([_P, _P], _I),
+    "la_lu_det": ([_P, _P], _I),
+    "la_lu_get_piv": ([_P, _P, _P], _I),
+    "la_lu_get_packed": ([_P, _P], _I),
+    "la_lu_get_l": ([_P, _P], _I),
+    "la_lu_get_u": ([_P, _P], _I),
+    "la_lu_get_p": ([_P, _P], _I),
+    "la_lu_device_data": ([_P, _P], _P),
+    "la_lu_solve": ([_P, _P, _S, _S, _P], _I),
+    "la_lu_solve_device": ([_P, _P, _S, _S, _S, _P, _S], _I),
+    "la_matrix_det": ([_P, _P, _S, _S, _P], _I),
+    "la_matrix_solve": ([_P, _P, _S, _S, _P, _S, _S, _P], _I),
+    "la_matrix_inverse": ([_P, _P, _S, _S, _P], _I),
+    "la_matrix_is_non_singular": ([_P, _P, _S, _S, _P], _I),
+    "la_matrix_mul": ([_P, _P, _S, _S, _P, _S, _S, _P], _I),
+    "la_matrix_mmul": ([_P, _P, _S, _S, _P, _S, _S, _P, _S, _S], _I),
+    "la_matrix_mul_device": ([_P, _P, _S, _P, _S, _P, _S, _S, _S, _S], _I),
+}
+
+
+def lib():
+    """Loads liblagpu.so (built by rust-la_gb300/build.py). Raises if it is missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("liblagpu.so not built: run python rust-la_gb300/build.py")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (args, res) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Context:
+    """One la_ctx: a device, a stream and the library's device scratch."""
+
+    def __init__(self, device=0, arith=ARITH_FAST):
+        self.h = ctypes.c_void_p()
+        st = lib().la_ctx_create(device, ctypes.byref(self.h))
+        if st != OK:
+            raise LaError(st, "la_ctx_create")
+        self.set_option(OPT_ARITH, arith)
+
+    def close(self):
+        if self.h:
+            lib().la_ctx_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_option(self, opt, value):
+        st = lib().la_ctx_set_option(self.h, opt, int(value))
+        if st != OK:
+            raise LaError(st, "set_option")
+
+    def get_option(self, opt):
+        v = ctypes.c_int64()
+        st = lib().la_ctx_get_option(self.h, opt, ctypes.byref(v))
+        if st != OK:
+            raise LaError(st, "get_option")
+        return v.value
+
+    def set_stream(self, stream_handle):
+        st = lib().la_ctx_set_stream(self.h, ctypes.c_void_p(stream_handle))
+        if st != OK:
+            raise LaError(st, "set_stream")
+
+    def synchronize(self):
+        _check(self, lib().la_ctx_synchronize(self.h))
+
+    def last_error(self):
+        return lib().la_ctx_last_error(self.h).decode()
+
+    def kernel_launches(self):
+        return lib().la_ctx_kernel_launches(self.h)
+
+    def phase_ms(self):
+        out = (ctypes.c_double * 5)()
+        lib().la_ctx_last_phase_ms(self.h, out)
+        return list(out)
+
+    def fp64_peak_tflops(self):
+        v = ctypes.c_double()
+        _check(self, lib().la_probe_fp64_peak(self.h, ctypes.byref(v)))
+        return v.value
+
+
+_default = None
+
+
+def default_context():
+    global _default
+    if _default is None:
+        _default = Context()
+    return _default
+
+
+def _check(ctx, st, allow=(OK,)):
+    if st in allow:
+        return st
+    if st == BADSHAPE:
+        raise Panic("reference would panic (shape assertion)")
+    msg = ctx.last_error() if ctx is not None else ""
+    raise LaError(st, msg)
+
+
+class Matrix:
+    """Row-major f64 matrix, the mirror of Matrix<f64> (mod.rs:26-30)."""
+
+    __slots__ = ("data", "ctx")
+
+    def __init__(self, array, ctx=None):
+        a = np.ascontiguousarray(array, dtype=np.float64)
+        if a.ndim != 2 or a.shape[0] == 0 or a.shape[1] == 0:
+            raise Panic("Matrix::new requires rows > 0 and cols > 0")
+        self.data = a
+        self.ctx = ctx
+
+    @staticmethod
+    def new(rows, cols, data, ctx=None):
+        data = list(data) if not isinstance(data, np.ndarray) else data.ravel()
+        if rows * cols != len(data) or rows == 0 or cols == 0:
+            raise Panic("Matrix::new: len(data) != rows * cols or empty")
+        return Matrix(np.asarray(data, dtype=np.float64).reshape(rows, cols), ctx)
+
+    @staticmethod
+    def id(m, n, ctx=None):
+        return Matrix(np.eye(m, n), ctx)
+
+    def _c(self):
+        return self.ctx if self.ctx is not None else default_context()
+
+    def rows(self):
+        return self.data.shape[0]
+
+    def cols(self):
+        return self.data.shape[1]
+
+    def get_data(self):
+        return self.data.ravel()
+
+    def get(self, r, c):
+        if r >= self.rows() or c >= self.cols():
+            raise Panic("Matrix::get out of range")
+        return float(self.data[r, c])
+
+    def __eq__(self, other):
+        return (isinstance(other, Matrix) and self.data.shape == other.data.shape
+                and bool(np.all(self.data == other.data)))
+
+    def approx_eq(self, other):
+        """mod.rs:1141-1147 with approxeq.rs:34-47 (|a-b| < 1e-6 for every entry)."""
+        if self.data.shape != other.data.shape:
+            return False
+        return bool(np.all(np.abs(self.data - other.data) < 1e-6))
+
+    def __mul__(self, other):
+        ctx = self._c()
+        if self.cols() != other.rows():
+            raise Panic("Mul: self.cols() != m.rows() (mod.rs:961)")
+        out = np.empty((self.rows(), other.cols()))
+        _check(ctx, lib().la_matrix_mul(ctx.h, _ptr(self.data), self.rows(), self.cols(),
+                                        _ptr(other.data), other.rows(), other.cols(), _ptr(out)))
+        return Matrix(out, self.ctx)
+
+    def mmul(self, m, dst):
+        """mmatrix.rs:82-98: writes self * m into dst (asserts dims)."""
+        ctx = self._c()
+        st = lib().la_matrix_mmul(ctx.h, _ptr(self.data), self.rows(), self.cols(), _ptr(m.data),
+                                  m.rows(), m.cols(), _ptr(dst.data), dst.rows(), dst.cols())
+        _check(ctx, st)
+        return dst
+
+    def det(self):
+        ctx = self._c()
+        out = ctypes.c_double()
+        _check(ctx, lib().la_matrix_det(ctx.h, _ptr(self.data), self.rows(), self.cols(),
+                                        ctypes.byref(out)))
+        return out.value
+
+    def solve(self, b):
+        ctx = self._c()
+        x = np.empty((self.rows(), b.cols()))
+        st = lib().la_matrix_solve(ctx.h, _ptr(self.data), self.rows(), self.cols(), _ptr(b.data),
+                                   b.rows(), b.cols(), _ptr(x))
+        if _check(ctx, st, (OK, SINGULAR)) == SINGULAR:
+            return None
+        return Matrix(x, self.ctx)
+
+    def inverse(self):
+        ctx = self._c()
+        out = np.empty_like(self.data)
+        st = lib().la_matrix_inverse(ctx.h, _ptr(self.data), self.rows(), self.cols(), _ptr(out))
+        if _check(ctx, st, (OK, SINGULAR)) == SINGULAR:
+            return None
+        return Matrix(out, self.ctx)
+
+    def is_non_singular(self):
+        ctx = self._c()
+        out = ctypes.c_int()
+        _check(ctx, lib().la_matrix_is_non_singular(ctx.h, _ptr(self.data), self.rows(),
+                                                    self.cols(), ctypes.byref(out)))
+        return bool(out.value)
+
+    def is_singular(self):
+        return not self.is_non_singular()
+
+    def __repr__(self):
+        return "Matrix(%r)" % (self.data,)
+
+
+def m(rows):
+    """The m! macro (src/macros.rs:40-42): m([[1, 2], [3, 4]])."""
+    return Matrix(np.array(rows, dtype=np.float64))
+
+
+class LUDecomposition:
+    """Device-resident LU factors, the mirror of LUDecomposition<f64> (lu.rs:95-101)."""
+
+    def __init__(self, handle, ctx, m_, n_):
+        self.h = handle
+        self.ctx = ctx
+        self.m = m_
+        self.n = n_
+
+    @staticmethod
+    def new(a, ctx=None):
+        """lu.rs:104-168. `a` is a Matrix or a 2-D array."""
+        if not isinstance(a, Matrix):
+            a = Matrix(a, ctx)
+        ctx = ctx or a._c()
+        h = ctypes.c_void_p()
+        _check(ctx, lib().la_lu_new(ctx.h, _ptr(a.data), a.rows(), a.cols(), ctypes.byref(h)))
+        return LUDecomposition(h, ctx, a.rows(), a.cols())
+
+    @staticmethod
+    def new_device(ptr, lda, m_, n_, ctx):
+        h = ctypes.c_void_p()
+        _check(ctx, lib().la_lu_new_device(ctx.h, ctypes.c_void_p(ptr), lda, m_, n_,
+                                           ctypes.byref(h)))
+        return LUDecomposition(h, ctx, m_, n_)
+
+    def free(self):
+        if self.h:
+            lib().la_lu_free(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def is_non_singular(self):
+        out = ctypes.c_int()
+        _check(self.ctx, lib().la_lu_is_non_singular(self.h, ctypes.byref(out)))
+        return bool(out.value)
+
+    def is_singular(self):
+        return not self.is_non_singular()
+
+    def det(self):
+        out = ctypes.c_double()
+        _check(self.ctx, lib().la_lu_det(self.h, ctypes.byref(out)))
+        return out.value
+
+    def get_piv(self):
+        piv = np.empty(self.m, dtype=np.uint64)
+        _check(self.ctx, lib().la_lu_get_piv(self.h, _ptr(piv), None))
+        return piv
+
+    def pospivsign(self):
+        s = ctypes.c_int()
+        _check(self.ctx, lib().la_lu_get_piv(self.h, None, ctypes.byref(s)))
+        return bool(s.value)
+
+    def _get(self, fn, shape):
+        out = np.empty(shape)
+        _check(self.ctx, fn(self.h, _ptr(out)))
+        return Matrix(out, self.ctx)
+
+    def get_packed(self):
+        return self._get(lib().la_lu_get_packed, (self.m, self.n))
+
+    def get_l(self):
+        return self._get(lib().la_lu_get_l, (self.m, min(self.m, self.n)))
+
+    def get_u(self):
+        return self._get(lib().la_lu_get_u, (min(self.m, self.n), self.n))
+
+    def get_p(self):
+        return self._get(lib().la_lu_get_p, (self.m, self.m))
+
+    def solve(self, b):
+        """lu.rs:237-278: None if singular, Panic if b.rows() != m."""
+        if not isinstance(b, Matrix):
+            b = Matrix(np.asarray(b, dtype=np.float64).reshape(self.m, -1)
+                       if np.ndim(b) == 1 else b, self.ctx)
+        x = np.empty((self.m, b.cols()))
+        st = lib().la_lu_solve(self.h, _ptr(b.data), b.rows(), b.cols(), _ptr(x))
+        if _check(self.ctx, st, (OK, SINGULAR)) == SINGULAR:
+            return None
+        return Matrix(x, self.ctx)
+
+    def solve_device(self, b_ptr, ldb, brows, nrhs, x_ptr, ldx):
+        st = lib().la_lu_solve_device(self.h, ctypes.c_void_p(b_ptr), ldb, brows, nrhs,
+                                      ctypes.c_void_p(x_ptr), ldx)
+        return _check(self.ctx, st, (OK, SINGULAR))
+
+
+def matrix_mul_device(ctx, a_ptr, lda, b_ptr, ldb, c_ptr, ldc, m_, k, n):
+    st = lib().la_matrix_mul_device(ctx.h, ctypes.c_void_p(a_ptr), lda, ctypes.c_void_p(b_ptr),
+                                    ldb, ctypes.c_void_p(c_ptr), ldc, m_, k, n)
+    return _check(ctx, st)

@@ -1,0 +1,160 @@
+"""The oracle (a CPU restatement of src/decomp/lu.rs and mod.rs Mul) pinned
+against the reference crate's own known-answer tests, against an independent
+pure-Python restatement, and against the committed golden fixtures."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from oracle import pyref
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+KATS = json.load(open(os.path.join(HERE, "golden", "kats.json")))["kats"]
+EPS32 = float(np.finfo(np.float32).eps)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built(oracle_lib):
+    return oracle_lib
+
+
+def _a(k, key="a"):
+    return np.array(k[key], dtype=np.float64)
+
+
+@pytest.mark.parametrize("k", KATS, ids=lambda k: k["ref"] + ":" + k["kind"])
+def test_reference_kat(k):
+    kind = k["kind"]
+    a = _a(k)
+    if kind == "lu_reconstruct_exact":
+        f = oracle.lu_factor(a)
+        lhs = oracle.matmul(oracle.get_l(f), oracle.get_u(f))
+        rhs = oracle.matmul(oracle.get_p(f), a)
+        assert np.array_equal(lhs, rhs)
+    elif kind in ("solve_approx", "solve_exact"):
+        x = oracle.solve(oracle.lu_factor(a), _a(k, "b"))
+        if kind == "solve_exact":
+            assert np.array_equal(x, _a(k, "x"))
+        else:
+            assert np.all(np.abs(x - _a(k, "x")) < 1e-6)
+    elif kind == "solve_panic":
+        with pytest.raises(oracle.ReferencePanic):
+            oracle.solve(oracle.lu_factor(a), _a(k, "b"))
+    elif kind == "solve_none":
+        assert oracle.solve(oracle.lu_factor(a), _a(k, "b")) is None
+    elif kind == "is_singular":
+        assert (not oracle.is_non_singular(oracle.lu_factor(a))) == k["expect"]
+    elif kind in ("is_non_singular", "matrix_is_non_singular"):
+        assert oracle.is_non_singular(oracle.lu_factor(a)) == k["expect"]
+    elif kind == "matrix_is_singular":
+        assert (not oracle.matrix_is_non_singular(a)) == k["expect"]
+    elif kind == "matrix_is_singular_panic":
+        with pytest.raises(oracle.ReferencePanic):
+            oracle.matrix_is_non_singular(a)
+    elif kind == "lu_det_exact":
+        assert oracle.det(oracle.lu_factor(a)) == k["expect"]
+    elif kind == "lu_det_panic":
+        with pytest.raises(oracle.ReferencePanic):
+            oracle.det(oracle.lu_factor(a))
+    elif kind == "matrix_det_le":
+        assert oracle.matrix_det(a) - k["expect"] <= EPS32
+    elif kind == "matrix_det_panic":
+        with pytest.raises(oracle.ReferencePanic):
+            oracle.matrix_det(a)
+    elif kind == "inverse_approx":
+        assert np.all(np.abs(oracle.inverse(a) - _a(k, "expect")) < 1e-6)
+    elif kind == "inverse_panic":
+        with pytest.raises(oracle.ReferencePanic):
+            oracle.inverse(a)
+    elif kind == "inverse_none":
+        assert oracle.inverse(a) is None
+    elif kind in ("mul_exact", "mmul_exact"):
+        assert np.array_equal(oracle.matmul(a, _a(k, "b")), _a(k, "expect"))
+    elif kind == "mul_panic":
+        with pytest.raises(oracle.ReferencePanic):
+            oracle.matmul(a, _a(k, "b"))
+    elif kind == "mmul_panic":
+        b = _a(k, "b")
+        ok_shape = (a.shape[1] == b.shape[0] and list(k["dst_shape"]) == [a.shape[0], b.shape[1]])
+        assert not ok_shape  # mmatrix.rs:83-85 asserts would fire
+    else:
+        raise AssertionError("unknown kat kind " + kind)
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (2, 2), (3, 3), (7, 7), (12, 12), (9, 5), (5, 9), (20, 20)])
+@pytest.mark.parametrize("seed", [0, 1])
+def test_c_oracle_matches_python_restatement(shape, seed):
+    rng = np.random.default_rng(seed * 100 + shape[0])
+    a = rng.uniform(-1, 1, size=shape)
+    # sprinkle exact zeros and ties to exercise the pivot rule
+    a[rng.random(shape) < 0.1] = 0.0
+    f = oracle.lu_factor(a)
+    lu, piv, pos = pyref.lu_factor(a.tolist())
+    assert np.array_equal(f.lu.ravel(), np.array(lu))
+    assert f.piv.tolist() == piv
+    assert f.pospivsign == pos
+    if shape[0] == shape[1]:
+        assert oracle.det(f) == pyref.det(lu, shape[1], pos)
+        b = rng.uniform(-1, 1, size=(shape[0], 2))
+        x = oracle.solve(f, b)
+        xr = pyref.solve(lu, shape[0], shape[1], piv, b.ravel().tolist(), 2)
+        if xr is None:
+            assert x is None
+        else:
+            assert np.array_equal(x.ravel(), np.array(xr))
+    b2 = rng.uniform(-1, 1, size=(shape[1], 3))
+    assert np.array_equal(oracle.matmul(a, b2), np.array(pyref.matmul(a.tolist(), b2.tolist())))
+
+
+def test_pivot_rule_ties_and_nan():
+    # ties: first maximal |value| wins (strict '>', lu.rs:134)
+    a = np.array([[1.0, 2.0], [-1.0, 3.0]])
+    f = oracle.lu_factor(a)
+    assert f.piv.tolist() == [0, 1] and f.pospivsign
+    lu, piv, pos = pyref.lu_factor([[1.0, 2.0], [-1.0, 3.0]])
+    assert piv == [0, 1]
+    # NaN on the diagonal is never displaced; NaN below never wins
+    a = np.array([[np.nan, 1.0], [5.0, 2.0]])
+    assert oracle.lu_factor(a).piv.tolist() == [0, 1]
+    a = np.array([[1.0, 1.0], [np.nan, 2.0], [3.0, 0.0]])
+    assert oracle.lu_factor(a).piv.tolist() == [2, 1, 0]
+
+
+def test_partial_factorization_prefix_matches_full():
+    rng = np.random.default_rng(5)
+    a = rng.uniform(-1, 1, size=(40, 40))
+    full = oracle.lu_factor(a)
+    part = oracle.lu_factor(a, j_end=40)
+    assert np.array_equal(full.lu, part.lu)
+    mt = oracle.lu_factor(a, threads=4)
+    assert np.array_equal(full.lu, mt.lu) and np.array_equal(full.piv, mt.piv)
+    b = rng.uniform(-1, 1, size=(40, 3))
+    assert np.array_equal(oracle.solve(full, b), oracle.solve_mt(full, b, 3))
+    b2 = rng.uniform(-1, 1, size=(40, 7))
+    assert np.array_equal(oracle.matmul(a, b2), oracle.matmul(a, b2, threads=4))
+
+
+def test_golden_fixtures_reproduce():
+    g = np.load(os.path.join(HERE, "golden", "random_small.npz"))
+    names = sorted({k.rsplit("_", 1)[0] for k in g.files})
+    assert names
+    for name in names:
+        f = oracle.lu_factor(g[name + "_a"])
+        assert np.array_equal(f.lu, g[name + "_lu"]), name
+        assert np.array_equal(f.piv, g[name + "_piv"]), name
+        assert int(f.pospivsign) == int(g[name + "_sign"][0]), name
+        if name + "_det" in g.files:
+            assert oracle.det(f) == g[name + "_det"][0]
+            assert np.array_equal(oracle.solve(f, g[name + "_b"]), g[name + "_x"])
+
+
+def test_backward_error_small():
+    rng = np.random.default_rng(3)
+    a = rng.uniform(-1, 1, size=(50, 50))
+    b = rng.uniform(-1, 1, size=(50, 2))
+    x = oracle.solve(oracle.lu_factor(a), b)
+    eta = oracle.backward_error(a, x, b)
+    assert 0 <= eta < 1e-15
+    assert oracle.backward_error(a, x + 1e-3, b) > 1e-6
