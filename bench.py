@@ -1,0 +1,411 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 LU factor-and-solve path.
+
+Workload (one step): plain FP64 LU with partial pivoting of an n=8192 matrix
+A ~ iid N(0,1), then the solve of 16 right-hand sides B ~ iid N(0,1) (seed 2),
+through the library's C ABI. Throughput is reported in GFLOP/s with the nominal
+count 2/3 n^3 + 2 n^2 nrhs (factor + solve).
+
+  value : inputs resident in HBM (la_lu_new_device + la_lu_solve_device),
+          timed with CUDA events on the library's stream. The 512 MiB matrix is
+          larger than L2 (129 MB), so no flush is needed between steps.
+  e2e   : the public host-pointer API (la_lu_new + la_lu_solve) from pinned
+          host memory; the copy of A and B to the device and of X back are
+          inside the timed region.
+  roofline : the trailing-update FP64 GEMM (the dominant kernel), its
+          algorithmic flops over its device time (per-phase CUDA events inside
+          the library), against this GPU's FP64 FMA rate measured live.
+  cpu_baseline : the oracle (a single-threaded restatement of the reference's
+          left-looking LUDecomposition::new) timed on a bounded prefix of the
+          same factorization on this host.
+
+`--impl reference` times the reference's CPU algorithm (the oracle's
+multi-threaded form, bit-identical results) on the same workload instead.
+Multi-GPU runs are independent replicas (the single LU does not shard).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "rust-la_gb300"))
+sys.path.insert(0, ROOT)
+
+METRIC = "LU-solve GFLOP/s & solves/s at backward err ≤1e-14: mixed-IR vs plain FP64"
+WORKLOAD = "plain FP64 LU with partial pivoting + solve, n=8192, 16 RHS, A and B iid N(0,1)"
+
+
+def lu_solve_flops(n, nrhs):
+    return 2.0 / 3.0 * n ** 3 + 2.0 * n ** 2 * nrhs
+
+
+def trailing_gemm_flops(n, w):
+    """Algorithmic flops of all trailing-update GEMM launches of one LU (square n, panel w)."""
+    total = 0.0
+    launches = 0
+    for j0 in range(0, n, w):
+        j1 = min(n, j0 + w)
+        r = n - j1
+        if r > 0:
+            total += 2.0 * r * r * (j1 - j0)
+            launches += 1
+    return total, launches
+
+
+def prefix_flops(n, jend):
+    """Flops the left-looking reference loop executes for columns [0, jend) of a square n."""
+    j = np.arange(jend, dtype=np.float64)
+    # sum_i min(i, j) multiply-adds for column j, plus n-j-1 divisions
+    madd = j * (j - 1) / 2 + j * (n - j)
+    return float(np.sum(2 * madd + np.maximum(n - j - 1, 0)))
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def read_traffic_summary():
+    """Per-launch DRAM traffic of the trailing GEMM from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "gemm_f64_trailing_update_n4096.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_algorithmic_flop:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def pick_prefix(oracle, a, n, target_s, threads):
+    """Longest column prefix whose left-looking factorization takes about target_s."""
+    j_try = 128
+    t0 = time.perf_counter()
+    oracle.lu_factor(a, j_end=j_try, threads=threads)
+    rate = prefix_flops(n, j_try) / max(time.perf_counter() - t0, 1e-4)
+    budget = rate * target_s
+    lo, hi = j_try, n
+    while lo < hi:
+        mid = (lo + hi + 1) // 2
+        if prefix_flops(n, mid) <= budget:
+            lo = mid
+        else:
+            hi = mid - 1
+    return lo
+
+
+def cpu_baseline(a, n, nrhs, target_s=15.0, threads=1):
+    """Times the oracle on a bounded prefix of the same factorization."""
+    import oracle
+    oracle.build()
+    jend = pick_prefix(oracle, a, n, target_s, threads)
+    t0 = time.perf_counter()
+    oracle.lu_factor(a, j_end=jend, threads=threads)
+    dt = time.perf_counter() - t0
+    fl = prefix_flops(n, jend)
+    gf = fl / dt / 1e9
+    return {"value": gf, "unit": "GFLOP/s", "cores": threads, "kind": "port",
+            "sample": ("columns [0,%d) of the n=%d left-looking factorization (lu.rs:116-161 "
+                       "order), %.2e flops in %.1f s; a full LU+solve at this rate would take "
+                       "~%.0f s (extrapolated)" % (jend, n, fl, dt,
+                                                   lu_solve_flops(n, nrhs) / gf / 1e9)),
+            "seconds": dt}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+        dist_mod.init_process_group(backend="nccl")
+        dist = dist_mod
+    return world, rank, local, dist
+
+
+def run_reference(args):
+    # Rank 0 alone times the CPU reference; other ranks exit without work.
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    import oracle
+    oracle.build()
+    n, nrhs = args.n, args.nrhs
+    a = np.random.default_rng(2).standard_normal((n, n))
+    threads = os.cpu_count() or 1
+    # one step = a prefix of the factorization sized to about ref_step_seconds
+    jend = pick_prefix(oracle, a, n, args.ref_step_seconds, threads)
+    fl = prefix_flops(n, jend)
+    for _ in range(args.warmup):
+        oracle.lu_factor(a, j_end=jend, threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.lu_factor(a, j_end=jend, threads=threads)
+    el = time.perf_counter() - t0
+    gf = fl * args.steps / el / 1e9
+    sample = ("each step: columns [0,%d) of the n=%d left-looking factorization "
+              "(lu.rs:116-161 order) on %d threads, %.2e flops" % (jend, n, threads, fl))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": gf, "unit": "GFLOP/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic: A iid N(0,1), seed 2",
+        "config": {"workload": WORKLOAD, "n": n, "nrhs": nrhs,
+                   "l2": "CPU run; not applicable"},
+        "cpu_baseline": {"value": gf, "unit": "GFLOP/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": gf, "unit": "GFLOP/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+    world, rank, local, dist = dist_setup(args)
+    torch.cuda.set_device(local)
+    import la_gpu
+    la_gpu.lib()
+    n, nrhs, K, W = args.n, args.nrhs, args.steps, args.warmup
+    rng = np.random.default_rng(2)
+    a_np = rng.standard_normal((n, n))
+    b_np = rng.standard_normal((n, nrhs))
+    # pinned host copies for the end-to-end leg
+    ha = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
+    hb = torch.empty((n, nrhs), dtype=torch.float64, pin_memory=True)
+    hx = torch.empty((n, nrhs), dtype=torch.float64, pin_memory=True)
+    ha.numpy()[:] = a_np
+    hb.numpy()[:] = b_np
+    da = ha.to("cuda")
+    db = hb.to("cuda")
+    dx = torch.empty((n, nrhs), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+
+    ctx = la_gpu.Context(local, la_gpu.ARITH_EXACT if args.arith == "exact" else la_gpu.ARITH_FAST)
+    # A created (non-NULL) stream shared by the library and the timing events.
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    fp64_peak = ctx.fp64_peak_tflops()
+    panel_w = ctx.get_option(la_gpu.OPT_PANEL_WIDTH)
+
+    def step():
+        lu = la_gpu.LUDecomposition.new_device(da.data_ptr(), n, n, n, ctx)
+        lu.solve_device(db.data_ptr(), nrhs, n, nrhs, dx.data_ptr(), nrhs)
+        lu.free()
+
+    for _ in range(W):
+        step()
+    torch.cuda.synchronize()
+    ctx.set_option(la_gpu.OPT_PROFILE, 1)
+    phases = np.zeros(5)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = ctx.kernel_launches()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(K):
+        lu = la_gpu.LUDecomposition.new_device(da.data_ptr(), n, n, n, ctx)
+        phases += np.array(ctx.phase_ms())
+        lu.solve_device(db.data_ptr(), nrhs, n, nrhs, dx.data_ptr(), nrhs)
+        lu.free()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = ctx.kernel_launches() - launches0
+    clk = clocks.stop()
+    if dist:
+        dist.barrier()
+    ms = e0.elapsed_time(e1) / K
+    ctx.set_option(la_gpu.OPT_PROFILE, 0)
+    if dist:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    flops = lu_solve_flops(n, nrhs)
+    value = flops * world / (ms * 1e-3) / 1e9
+
+    eta = la_gpu.backward_error_device(ctx, da.data_ptr(), n, dx.data_ptr(), nrhs, db.data_ptr(),
+                                       nrhs, n, nrhs)
+
+    # roofline of the trailing-update GEMM
+    gflops_gemm, gemm_launches = trailing_gemm_flops(n, panel_w)
+    gemm_ms = phases[3] / K
+    achieved = gflops_gemm / (gemm_ms * 1e-3) / 1e12 if gemm_ms > 0 else None
+    tpf = read_traffic_summary()
+    roof = {
+        "bound": "tensor", "compute_pipe": "FP64 FMA (DFMA); GB300 has no faster FP64 path",
+        "kernel": "gemm_f64_kernel (trailing update A22 -= L21*U12)",
+        "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+        "frac": (achieved / fp64_peak) if achieved else None,
+        "peak_source": "FP64 FMA microbenchmark run live in this process (la_probe_fp64_peak); "
+                       "the driver's measured-peaks file has no FP64 figure",
+        "traffic": (tpf * gflops_gemm / gemm_launches) if tpf else None,
+        "traffic_unit": "bytes per launch (mean), scaled from the ncu capture at n=4096",
+        "algorithmic_flops_per_launch": gflops_gemm / gemm_launches,
+        "gemm_ms_per_step": gemm_ms,
+        "phase_ms_per_step": {"panel": phases[0] / K, "row_swaps": phases[1] / K,
+                              "row_panel_trsm": phases[2] / K, "trailing_gemm": phases[3] / K,
+                              "finish": phases[4] / K},
+    }
+
+    # end-to-end through the host-pointer API, copies included
+    def e2e_step():
+        lu = la_gpu.LUDecomposition.new(la_gpu.Matrix(ha.numpy(), ctx), ctx)
+        x = lu.solve(la_gpu.Matrix(hb.numpy(), ctx))
+        hx.numpy()[:] = x.data
+        lu.free()
+
+    for _ in range(max(1, W // 2)):
+        e2e_step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / K
+    if dist:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": flops * world / e2e_s / 1e9, "unit": "GFLOP/s",
+           "h2d_bytes_per_step": 8 * n * n + 8 * n * nrhs, "d2h_bytes_per_step": 8 * n * nrhs,
+           "ms_per_step": e2e_s * 1e3}
+
+    gemm = None
+    if not args.no_gemm:
+        db2 = torch.from_numpy(np.random.default_rng(3).standard_normal((n, n))).cuda()
+        dc = torch.empty((n, n), dtype=torch.float64, device="cuda")
+        la_gpu.matrix_mul_device(ctx, da.data_ptr(), n, db2.data_ptr(), n, dc.data_ptr(), n, n, n, n)
+        torch.cuda.synchronize()
+        g0 = torch.cuda.Event(enable_timing=True)
+        g1 = torch.cuda.Event(enable_timing=True)
+        reps = 2
+        g0.record(stream)
+        for _ in range(reps):
+            la_gpu.matrix_mul_device(ctx, da.data_ptr(), n, db2.data_ptr(), n, dc.data_ptr(), n,
+                                     n, n, n)
+        g1.record(stream)
+        torch.cuda.synchronize()
+        gms = g0.elapsed_time(g1) / reps
+        gemm = {"workload": "C = A*B, 8192^3 f64 (Matrix * Matrix)", "ms": gms,
+                "gflops": 2.0 * n ** 3 / (gms * 1e-3) / 1e9,
+                "frac_of_fp64_peak": 2.0 * n ** 3 / (gms * 1e-3) / 1e12 / fp64_peak}
+        del db2, dc
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(a_np, n, nrhs, target_s=args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world, "steps": K,
+            "warmup": W, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: A iid N(0,1) f64 n=8192 (seed 2), 16 RHS iid N(0,1)",
+            "config": {"workload": WORKLOAD, "n": n, "nrhs": nrhs, "arith": args.arith,
+                       "panel_width": panel_w, "parallelism": "replicas" if world > 1 else "1 GPU",
+                       "l2": "inputs larger than L2 (512 MiB matrix), no flush"},
+            "solves_per_s": world / (ms * 1e-3),
+            "backward_error": eta,
+            "gpu_launches": int(launches),
+            "roofline": roof,
+            "e2e": e2e,
+            "clocks": clk,
+            "cpu_baseline": cpu,
+            "gemm_8192": gemm,
+            "fp64_peak_tflops": fp64_peak,
+        }
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=8192)
+    ap.add_argument("--nrhs", type=int, default=16)
+    ap.add_argument("--arith", default="fast", choices=["fast", "exact"])
+    ap.add_argument("--no-gemm", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-step-seconds", type=float, default=8.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

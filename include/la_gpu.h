@@ -73,7 +73,10 @@ typedef enum la_option {
   /* Upper bound on CTAs of the cooperative panel kernel (0 = all SMs). */
   LA_OPT_PANEL_CTAS = 3,
   /* 1: record per-phase device times of each LU (la_ctx_last_phase_ms). */
-  LA_OPT_PROFILE = 4
+  LA_OPT_PROFILE = 4,
+  /* 1 (default): factor the next panel on a second stream while the rest of
+   * the trailing update runs; 0: strictly one phase after the other. */
+  LA_OPT_LOOKAHEAD = 5
 } la_option;
 
 #define LA_ARITH_FAST 0
@@ -145,6 +148,17 @@ la_status la_matrix_mmul(la_ctx ctx, const double* a, size_t m, size_t k, const 
 /* Device form: C = A * B with row pitches; stream-ordered, no sync. */
 la_status la_matrix_mul_device(la_ctx ctx, const double* d_a, size_t lda, const double* d_b,
                                size_t ldb, double* d_c, size_t ldc, size_t m, size_t k, size_t n);
+
+/* ---- accuracy check (no reference counterpart) --------------------------- */
+
+/* Normwise backward error of a computed solution X of A X = B (A n x n):
+ *   eta = max_j ||b_j - A x_j||_inf / (||A||_inf ||x_j||_inf + ||b_j||_inf),
+ * with the residual accumulated in compensated FP64 on the device. */
+la_status la_backward_error_device(la_ctx ctx, const double* d_a, size_t lda, const double* d_x,
+                                   size_t ldx, const double* d_b, size_t ldb, size_t n,
+                                   size_t nrhs, double* eta);
+la_status la_backward_error(la_ctx ctx, const double* a, const double* x, const double* b,
+                            size_t n, size_t nrhs, double* eta);
 
 /* ---- diagnostics ---------------------------------------------------------- */
 

@@ -111,6 +111,18 @@ la_status la_ctx_create(int device, la_ctx* out) {
   e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { la_status s = la_cuda_fail(ctx, e, "stream"); delete ctx; return s; }
   ctx->stream = ctx->own_stream;
+  {
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    e = cudaStreamCreateWithPriority(&ctx->side_stream, cudaStreamNonBlocking, hi);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      la_status s = la_cuda_fail(ctx, e, "side stream");
+      la_ctx_destroy(ctx);
+      return s;
+    }
+  }
   // Keep freed stream-ordered allocations cached in the device pool.
   cudaMemPool_t pool;
   if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
@@ -167,6 +179,11 @@ void la_ctx_destroy(la_ctx ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  if (ctx->side_stream) cudaStreamSynchronize(ctx->side_stream);
+  for (auto ev : ctx->event_pool) cudaEventDestroy(ev);
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+  if (ctx->side_stream) cudaStreamDestroy(ctx->side_stream);
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
   if (ctx->d_scratch) cudaFree(ctx->d_scratch);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -208,6 +225,9 @@ la_status la_ctx_set_option(la_ctx ctx, int option, int64_t value) {
     case LA_OPT_PROFILE:
       ctx->profile = value ? 1 : 0;
       return LA_OK;
+    case LA_OPT_LOOKAHEAD:
+      ctx->lookahead = value ? 1 : 0;
+      return LA_OK;
   }
   return LA_INVALID;
 }
@@ -219,6 +239,7 @@ la_status la_ctx_get_option(la_ctx ctx, int option, int64_t* value) {
     case LA_OPT_PANEL_WIDTH: *value = ctx->panel_width; return LA_OK;
     case LA_OPT_PANEL_CTAS: *value = ctx->panel_ctas; return LA_OK;
     case LA_OPT_PROFILE: *value = ctx->profile; return LA_OK;
+    case LA_OPT_LOOKAHEAD: *value = ctx->lookahead; return LA_OK;
   }
   return LA_INVALID;
 }

@@ -168,9 +168,6 @@ gemm_f64_kernel(int M, int N, int K, const double* __restrict__ A, size_t lda,
     __syncthreads();
   }
 
-  if (MODE == GM_EXACT_ZERO && K == 0) {
-    // Nothing accumulated: the reference's res stays 0.0.
-  }
 #pragma unroll
   for (int i = 0; i < 4; i++)
 #pragma unroll
@@ -180,14 +177,19 @@ gemm_f64_kernel(int M, int N, int K, const double* __restrict__ A, size_t lda,
     }
 }
 
+constexpr size_t GEMM_SMEM_CAP = 96 * 1024;
+
 template <int MODE, int BN>
 la_status launch_mode(la_ctx ctx, int M, int N, int K, const double* A, size_t lda,
-                      const double* B, size_t ldb, double* C, size_t ldc) {
-  const size_t smem = (size_t)2 * (BM * BK + BK * BN) * sizeof(double);
+                      const double* B, size_t ldb, double* C, size_t ldc, size_t min_smem) {
+  const size_t smem =
+      std::min(GEMM_SMEM_CAP,
+               std::max((size_t)2 * (BM * BK + BK * BN) * sizeof(double), min_smem));
   static bool configured = false;  // one attribute call per instantiation
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(gemm_f64_kernel<MODE, BN>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)GEMM_SMEM_CAP);
     if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaFuncSetAttribute(gemm)");
     configured = true;
   }
@@ -200,17 +202,17 @@ la_status launch_mode(la_ctx ctx, int M, int N, int K, const double* A, size_t l
 
 template <int BN>
 la_status launch_bn(la_ctx ctx, int mode, int M, int N, int K, const double* A, size_t lda,
-                    const double* B, size_t ldb, double* C, size_t ldc) {
+                    const double* B, size_t ldb, double* C, size_t ldc, size_t ms) {
   switch (mode) {
-    case GM_FMA_SUB: return launch_mode<GM_FMA_SUB, BN>(ctx, M, N, K, A, lda, B, ldb, C, ldc);
-    case GM_FMA_ZERO: return launch_mode<GM_FMA_ZERO, BN>(ctx, M, N, K, A, lda, B, ldb, C, ldc);
-    case GM_EXACT_ADD: return launch_mode<GM_EXACT_ADD, BN>(ctx, M, N, K, A, lda, B, ldb, C, ldc);
-    case GM_EXACT_ZERO: return launch_mode<GM_EXACT_ZERO, BN>(ctx, M, N, K, A, lda, B, ldb, C, ldc);
-    case GM_EXACT_SUB: return launch_mode<GM_EXACT_SUB, BN>(ctx, M, N, K, A, lda, B, ldb, C, ldc);
+    case GM_FMA_SUB: return launch_mode<GM_FMA_SUB, BN>(ctx, M, N, K, A, lda, B, ldb, C, ldc, ms);
+    case GM_FMA_ZERO: return launch_mode<GM_FMA_ZERO, BN>(ctx, M, N, K, A, lda, B, ldb, C, ldc, ms);
+    case GM_EXACT_ADD: return launch_mode<GM_EXACT_ADD, BN>(ctx, M, N, K, A, lda, B, ldb, C, ldc, ms);
+    case GM_EXACT_ZERO: return launch_mode<GM_EXACT_ZERO, BN>(ctx, M, N, K, A, lda, B, ldb, C, ldc, ms);
+    case GM_EXACT_SUB: return launch_mode<GM_EXACT_SUB, BN>(ctx, M, N, K, A, lda, B, ldb, C, ldc, ms);
     case GM_EXACT_SUB_DESC:
-      return launch_mode<GM_EXACT_SUB_DESC, BN>(ctx, M, N, K, A, lda, B, ldb, C, ldc);
+      return launch_mode<GM_EXACT_SUB_DESC, BN>(ctx, M, N, K, A, lda, B, ldb, C, ldc, ms);
     case GM_FMA_SUB_DESC:
-      return launch_mode<GM_FMA_SUB_DESC, BN>(ctx, M, N, K, A, lda, B, ldb, C, ldc);
+      return launch_mode<GM_FMA_SUB_DESC, BN>(ctx, M, N, K, A, lda, B, ldb, C, ldc, ms);
     default: return LA_INVALID;
   }
 }
@@ -220,9 +222,9 @@ la_status launch_bn(la_ctx ctx, int mode, int M, int N, int K, const double* A, 
 // C (M x N, ldc) op= A (M x K, lda) * B (K x N, ldb); all row-major. Pointers
 // must be 16-byte aligned and pitches even (the library pads pitches to 4).
 la_status launch_gemm(la_ctx ctx, int mode, int M, int N, int K, const double* A, size_t lda,
-                      const double* B, size_t ldb, double* C, size_t ldc) {
+                      const double* B, size_t ldb, double* C, size_t ldc, size_t min_smem) {
   if (M <= 0 || N <= 0) return LA_OK;
   if (K <= 0 && mode != GM_FMA_ZERO && mode != GM_EXACT_ZERO) return LA_OK;
-  if (N <= 16) return launch_bn<16>(ctx, mode, M, N, K, A, lda, B, ldb, C, ldc);
-  return launch_bn<64>(ctx, mode, M, N, K, A, lda, B, ldb, C, ldc);
+  if (N <= 16) return launch_bn<16>(ctx, mode, M, N, K, A, lda, B, ldb, C, ldc, min_smem);
+  return launch_bn<64>(ctx, mode, M, N, K, A, lda, B, ldb, C, ldc, min_smem);
 }

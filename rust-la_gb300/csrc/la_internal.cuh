@@ -2,9 +2,13 @@
 #pragma once
 
 #include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
 #include <cstddef>
 #include <cstdint>
 #include <string>
+#include <vector>
 
 #include "../../include/la_gpu.h"
 
@@ -34,6 +38,9 @@ struct la_context {
   int device = 0;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
+  cudaStream_t side_stream = nullptr;    // high priority: lookahead panels
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  int lookahead = 1;
   int sm_count = 0;
   size_t smem_optin = 0;
   int arith = LA_ARITH_FAST;
@@ -43,6 +50,7 @@ struct la_context {
   std::string last_error;
   uint64_t launches = 0;
   double phase_ms[5] = {0, 0, 0, 0, 0};
+  std::vector<cudaEvent_t> event_pool;  // reused by the per-phase timer
 
   // Device scratch for the cooperative panel kernel and small results.
   void* d_scratch = nullptr;
@@ -94,19 +102,19 @@ la_status la_sync_and_check(la_ctx ctx, const char* what);
   } while (0)
 
 // Kernel launchers (one per translation unit of kernels).
+// min_smem > 0 raises the GEMM's dynamic shared memory so fewer CTAs share an
+// SM (room for a concurrent panel CTA).
 la_status launch_gemm(la_ctx ctx, int mode, int M, int N, int K, const double* A, size_t lda,
-                      const double* B, size_t ldb, double* C, size_t ldc);
-la_status launch_panel(la_ctx ctx, bool exact, double* A, double* S, size_t ld, int m, int j0,
-                       int jb, int* d_ipiv, unsigned* bar_base);
+                      const double* B, size_t ldb, double* C, size_t ldc, size_t min_smem = 0);
+la_status launch_panel(la_ctx ctx, cudaStream_t stream, bool exact, double* A, double* S,
+                       size_t ld, int m, int j0, int jb, int* d_ipiv, unsigned* bar_base);
 la_status launch_laswp(la_ctx ctx, bool exact, double* A, double* S, size_t ld, int n, int j0,
                        int jb);
 la_status launch_trsm_rowpanel(la_ctx ctx, bool exact, double* A, double* S, size_t ld, int j0,
                                int jb, int c_begin, int c_end);
-la_status launch_solve_diag_fwd(la_ctx ctx, bool exact, const double* LU, size_t ld, int k0,
-                                int kb, double* X, size_t ldx, int nrhs);
-la_status launch_solve_diag_bwd(la_ctx ctx, bool exact, const double* LU, size_t ld, int k0,
-                                int kb, double* X, size_t ldx, int nrhs);
 la_status launch_lu_finish(la_ctx ctx, la_lu h);
+la_status launch_lu_solve(la_ctx ctx, bool exact, const double* LU, size_t ld, double* X,
+                          size_t ldx, int n, int nrhs);
 la_status launch_permute_rows(la_ctx ctx, const uint64_t* d_piv, const double* B, size_t ldb,
                               double* X, size_t ldx, int m, int nrhs);
 la_status launch_identity_permuted(la_ctx ctx, const uint64_t* d_piv, double* X, size_t ldx,

@@ -32,81 +32,131 @@ struct DevBuf {
   double* d() { return static_cast<double*>(p); }
 };
 
-// Phase timing for LA_OPT_PROFILE: events recorded between phases.
+// Phase timing for LA_OPT_PROFILE: a pair of events (from the context's pool)
+// around each phase instance on the stream it runs on; the per-category sums
+// are device time, so a panel overlapped with the trailing update is counted
+// in full in both categories.
 struct PhaseTimer {
   la_ctx ctx;
   bool on;
-  std::vector<cudaEvent_t> ev;
-  std::vector<int> cat;
-  PhaseTimer(la_ctx c) : ctx(c), on(c->profile != 0) {
-    if (on) mark(-1);
+  size_t used = 0;
+  struct Span { size_t b, e; int cat; };
+  std::vector<Span> spans;
+  explicit PhaseTimer(la_ctx c) : ctx(c), on(c->profile != 0) {}
+  size_t record(cudaStream_t s) {
+    if (used == ctx->event_pool.size()) {
+      cudaEvent_t e;
+      if (cudaEventCreate(&e) != cudaSuccess) { on = false; return 0; }
+      ctx->event_pool.push_back(e);
+    }
+    cudaEventRecord(ctx->event_pool[used], s);
+    return used++;
   }
-  void mark(int category) {
+  size_t begin(cudaStream_t s) { return on ? record(s) : 0; }
+  void end(cudaStream_t s, size_t b, int cat) {
     if (!on) return;
-    cudaEvent_t e;
-    if (cudaEventCreate(&e) != cudaSuccess) { on = false; return; }
-    cudaEventRecord(e, ctx->stream);
-    ev.push_back(e);
-    cat.push_back(category);
+    size_t e = record(s);
+    if (on) spans.push_back({b, e, cat});
   }
   void finish() {
     for (int i = 0; i < 5; i++) ctx->phase_ms[i] = 0;
     if (!on) return;
-    cudaEventSynchronize(ev.back());
-    for (size_t i = 1; i < ev.size(); i++) {
+    for (auto& sp : spans) {
+      cudaEventSynchronize(ctx->event_pool[sp.e]);
       float ms = 0;
-      cudaEventElapsedTime(&ms, ev[i - 1], ev[i]);
-      ctx->phase_ms[cat[i]] += ms;
+      cudaEventElapsedTime(&ms, ctx->event_pool[sp.b], ctx->event_pool[sp.e]);
+      ctx->phase_ms[sp.cat] += ms;
     }
-  }
-  ~PhaseTimer() {
-    for (auto e : ev) cudaEventDestroy(e);
   }
 };
 
 enum { PH_PANEL = 0, PH_SWAP = 1, PH_TRSM = 2, PH_GEMM = 3, PH_OTHER = 4 };
 
+// Shared memory that keeps trailing-update GEMM CTAs at two per SM, leaving an
+// SM room for one CTA of the concurrent panel kernel.
+constexpr size_t GEMM_SMEM_WITH_PANEL = 78 * 1024;
+
 // Factors h->d_lu in place.
+//
+// With lookahead (default), after panel p's row swaps and triangular update,
+// the columns of panel p+1 get their trailing update first; panel p+1 is then
+// factored on the high-priority side stream while the rest of panel p's
+// trailing update runs on the main stream. The two touch disjoint columns:
+// panel p+1 owns columns [j1, j2) of rows >= j1, the rest of the update writes
+// columns >= j2 and reads L21 (columns < j1) and U12 (rows < j1).
 la_status lu_factor(la_ctx ctx, la_lu h) {
   const bool exact = (h->arith == LA_ARITH_EXACT);
   const int m = (int)h->m, n = (int)h->n;
   const size_t ld = h->ld;
   const int kmin = std::min(m, n);
   const int W = ctx->panel_width;
+  const bool look = ctx->lookahead != 0;
+  cudaStream_t ms = ctx->stream, ss = ctx->side_stream;
   double* A = h->d_lu;
   DevBuf S(ctx);
   if (exact) {
     LA_TRY(S.alloc((size_t)m * ld * sizeof(double)));
-    LA_CUDA(ctx, cudaMemsetAsync(S.p, 0, (size_t)m * ld * sizeof(double), ctx->stream));
+    LA_CUDA(ctx, cudaMemsetAsync(S.p, 0, (size_t)m * ld * sizeof(double), ms));
   }
-  LA_CUDA(ctx, cudaMemsetAsync(ctx->d_bar, 0, sizeof(unsigned), ctx->stream));
+  LA_CUDA(ctx, cudaMemsetAsync(ctx->d_bar, 0, sizeof(unsigned), ms));
   unsigned bar_base = 0;
   PhaseTimer t(ctx);
+  const int gmode = exact ? GM_EXACT_ADD : GM_FMA_SUB;
+  auto trailing = [&](int j0, int jb, int c0, int c1, size_t min_smem) -> la_status {
+    // rows [j0+jb, m), columns [c0, c1)
+    const int j1 = j0 + jb;
+    if (j1 >= m || c1 <= c0) return LA_OK;
+    const double* L21 = A + (size_t)j1 * ld + j0;
+    const double* U12 = A + (size_t)j0 * ld + c0;
+    double* C = exact ? S.d() + (size_t)j1 * ld + c0 : A + (size_t)j1 * ld + c0;
+    size_t b = t.begin(ms);
+    la_status st = launch_gemm(ctx, gmode, m - j1, c1 - c0, jb, L21, ld, U12, ld, C, ld, min_smem);
+    t.end(ms, b, PH_GEMM);
+    return st;
+  };
+
+  {
+    size_t b = t.begin(ms);
+    LA_TRY(launch_panel(ctx, ms, exact, A, S.d(), ld, m, 0, std::min(W, kmin), h->d_ipiv,
+                        &bar_base));
+    t.end(ms, b, PH_PANEL);
+  }
   for (int j0 = 0; j0 < kmin; j0 += W) {
     const int jb = std::min(W, kmin - j0);
     const int j1 = j0 + jb;
-    LA_TRY(launch_panel(ctx, exact, A, S.d(), ld, m, j0, jb, h->d_ipiv, &bar_base));
-    t.mark(PH_PANEL);
+    size_t b = t.begin(ms);
     LA_TRY(launch_laswp(ctx, exact, A, S.d(), ld, n, j0, jb));
-    t.mark(PH_SWAP);
+    t.end(ms, b, PH_SWAP);
     if (j1 < n) {
+      b = t.begin(ms);
       LA_TRY(launch_trsm_rowpanel(ctx, exact, A, S.d(), ld, j0, jb, j1, n));
-      t.mark(PH_TRSM);
-      if (j1 < m) {
-        const double* L21 = A + (size_t)j1 * ld + j0;
-        const double* U12 = A + (size_t)j0 * ld + j1;
-        double* C = exact ? S.d() + (size_t)j1 * ld + j1 : A + (size_t)j1 * ld + j1;
-        LA_TRY(launch_gemm(ctx, exact ? GM_EXACT_ADD : GM_FMA_SUB, m - j1, n - j1, jb, L21, ld,
-                           U12, ld, C, ld));
-        t.mark(PH_GEMM);
-      }
+      t.end(ms, b, PH_TRSM);
+    }
+    if (j1 >= kmin) break;  // no next panel
+    const int jbn = std::min(W, kmin - j1);
+    if (look) {
+      LA_TRY(trailing(j0, jb, j1, j1 + jbn, 0));
+      LA_CUDA(ctx, cudaEventRecord(ctx->ev_fork, ms));
+      LA_CUDA(ctx, cudaStreamWaitEvent(ss, ctx->ev_fork, 0));
+      b = t.begin(ss);
+      LA_TRY(launch_panel(ctx, ss, exact, A, S.d(), ld, m, j1, jbn, h->d_ipiv, &bar_base));
+      t.end(ss, b, PH_PANEL);
+      LA_CUDA(ctx, cudaEventRecord(ctx->ev_join, ss));
+      LA_TRY(trailing(j0, jb, j1 + jbn, n, GEMM_SMEM_WITH_PANEL));
+      LA_CUDA(ctx, cudaStreamWaitEvent(ms, ctx->ev_join, 0));
+    } else {
+      LA_TRY(trailing(j0, jb, j1, n, 0));
+      b = t.begin(ms);
+      LA_TRY(launch_panel(ctx, ms, exact, A, S.d(), ld, m, j1, jbn, h->d_ipiv, &bar_base));
+      t.end(ms, b, PH_PANEL);
     }
   }
+  // m < n: the columns right of the last panel got their triangular update above.
+  size_t b = t.begin(ms);
   LA_TRY(launch_lu_finish(ctx, h));
   int* flags = static_cast<int*>(ctx->h_pinned);
-  LA_CUDA(ctx, cudaMemcpyAsync(flags, ctx->d_small, 2 * sizeof(int), cudaMemcpyDeviceToHost,
-                               ctx->stream));
-  t.mark(PH_OTHER);
+  LA_CUDA(ctx, cudaMemcpyAsync(flags, ctx->d_small, 2 * sizeof(int), cudaMemcpyDeviceToHost, ms));
+  t.end(ms, b, PH_OTHER);
   LA_TRY(la_sync_and_check(ctx, "lu factorization"));
   t.finish();
   h->pospivsign = flags[0];
@@ -148,35 +198,11 @@ la_status lu_non_singular(la_lu h, int* out) {
   return LA_OK;
 }
 
-// X (m x nrhs, pitch ldx, 16-byte aligned, even pitch) holds B(piv,:) on entry
-// and the solution on exit (lu.rs:256-275).
+// X (m x nrhs, pitch ldx) holds B(piv,:) on entry and the solution on exit
+// (lu.rs:256-275; the loops run over the first n rows).
 la_status lu_solve_inplace(la_ctx ctx, la_lu h, double* X, size_t ldx, int nrhs) {
-  const bool exact = (h->arith == LA_ARITH_EXACT);
-  const int n = (int)h->n;
-  const size_t ld = h->ld;
-  const double* LU = h->d_lu;
-  const int W = MAX_PANEL_W;
-  // Forward: unit L, ascending k (lu.rs:257-263).
-  for (int k0 = 0; k0 < n; k0 += W) {
-    const int kb = std::min(W, n - k0);
-    LA_TRY(launch_solve_diag_fwd(ctx, exact, LU, ld, k0, kb, X, ldx, nrhs));
-    const int r0 = k0 + kb;
-    if (r0 < n)
-      LA_TRY(launch_gemm(ctx, exact ? GM_EXACT_SUB : GM_FMA_SUB, n - r0, nrhs, kb,
-                         LU + (size_t)r0 * ld + k0, ld, X + (size_t)k0 * ldx, ldx,
-                         X + (size_t)r0 * ldx, ldx));
-  }
-  // Backward: U, descending k (lu.rs:266-275).
-  const int nblk = (n + W - 1) / W;
-  for (int b = nblk - 1; b >= 0; b--) {
-    const int k0 = b * W;
-    const int kb = std::min(W, n - k0);
-    LA_TRY(launch_solve_diag_bwd(ctx, exact, LU, ld, k0, kb, X, ldx, nrhs));
-    if (k0 > 0)
-      LA_TRY(launch_gemm(ctx, exact ? GM_EXACT_SUB_DESC : GM_FMA_SUB, k0, nrhs, kb,
-                         LU + k0, ld, X + (size_t)k0 * ldx, ldx, X, ldx));
-  }
-  return LA_OK;
+  return launch_lu_solve(ctx, h->arith == LA_ARITH_EXACT, h->d_lu, h->ld, X, ldx, (int)h->n,
+                         nrhs);
 }
 
 la_status check_ctx(la_ctx ctx) {

@@ -43,7 +43,6 @@ constexpr int TR_COLS = 32;
 constexpr int LP = MAX_PANEL_W + 1;  // padded row of the triangular block in shared memory
 constexpr size_t TRSM_SMEM_FAST = (size_t)(MAX_PANEL_W * LP + MAX_PANEL_W * TR_COLS) * 8;
 constexpr size_t TRSM_SMEM_EXACT = TRSM_SMEM_FAST + (size_t)MAX_PANEL_W * TR_COLS * 8;
-constexpr size_t SOLVE_SMEM = (size_t)(MAX_PANEL_W * LP + MAX_PANEL_W * TR_COLS) * 8;
 
 template <bool EXACT>
 __global__ void __launch_bounds__(256)
@@ -87,82 +86,21 @@ trsm_rowpanel_kernel(double* A, const double* S, size_t ld, int j0, int jb, int 
     for (int i = ty; i < jb; i += 8) A[(size_t)(j0 + i) * ld + c] = xa[i][tx];
 }
 
-// ---- diagonal blocks of LUDecomposition::solve (lu.rs:256-275) ------------
-// Forward, unit L: for k ascending, x_i = x_i - x_k * l_ik for i in (k, k0+kb).
-template <bool EXACT>
-__global__ void __launch_bounds__(256)
-solve_diag_fwd_kernel(const double* LU, size_t ld, int k0, int kb, double* X, size_t ldx,
-                      int nrhs) {
-  extern __shared__ __align__(16) double dsm[];
-  double(*L)[LP] = reinterpret_cast<double(*)[LP]>(dsm);
-  double(*x)[TR_COLS] = reinterpret_cast<double(*)[TR_COLS]>(dsm + MAX_PANEL_W * LP);
-  const int tx = threadIdx.x % TR_COLS, ty = threadIdx.x / TR_COLS;
-  const int c = blockIdx.x * TR_COLS + tx;
-  const bool ok = c < nrhs;
-  for (int idx = threadIdx.x; idx < kb * kb; idx += 256) {
-    int i = idx / kb, k = idx % kb;
-    L[i][k] = LU[(size_t)(k0 + i) * ld + k0 + k];
-  }
-  for (int i = ty; i < kb; i += 8) x[i][tx] = ok ? X[(size_t)(k0 + i) * ldx + c] : 0.0;
-  __syncthreads();
-  for (int k = 0; k < kb; k++) {
-    const double xk = x[k][tx];
-    for (int i = ty; i < kb; i += 8) {
-      if (i <= k) continue;
-      if (EXACT)
-        x[i][tx] = __dsub_rn(x[i][tx], __dmul_rn(xk, L[i][k]));
-      else
-        x[i][tx] = fma(-xk, L[i][k], x[i][tx]);
-    }
-    __syncthreads();
-  }
-  if (ok)
-    for (int i = ty; i < kb; i += 8) X[(size_t)(k0 + i) * ldx + c] = x[i][tx];
-}
-
-// Backward, U: for k descending, x_k = x_k / u_kk, then x_i = x_i - x_k * u_ik
-// for i in [k0, k).
-template <bool EXACT>
-__global__ void __launch_bounds__(256)
-solve_diag_bwd_kernel(const double* LU, size_t ld, int k0, int kb, double* X, size_t ldx,
-                      int nrhs) {
-  extern __shared__ __align__(16) double dsm[];
-  double(*U)[LP] = reinterpret_cast<double(*)[LP]>(dsm);
-  double(*x)[TR_COLS] = reinterpret_cast<double(*)[TR_COLS]>(dsm + MAX_PANEL_W * LP);
-  const int tx = threadIdx.x % TR_COLS, ty = threadIdx.x / TR_COLS;
-  const int c = blockIdx.x * TR_COLS + tx;
-  const bool ok = c < nrhs;
-  for (int idx = threadIdx.x; idx < kb * kb; idx += 256) {
-    int i = idx / kb, k = idx % kb;
-    U[i][k] = LU[(size_t)(k0 + i) * ld + k0 + k];
-  }
-  for (int i = ty; i < kb; i += 8) x[i][tx] = ok ? X[(size_t)(k0 + i) * ldx + c] : 0.0;
-  __syncthreads();
-  for (int k = kb - 1; k >= 0; k--) {
-    if (ty == (k & 7)) x[k][tx] = x[k][tx] / U[k][k];
-    __syncthreads();
-    const double xk = x[k][tx];
-    for (int i = ty; i < k; i += 8) {
-      if (EXACT)
-        x[i][tx] = __dsub_rn(x[i][tx], __dmul_rn(xk, U[i][k]));
-      else
-        x[i][tx] = fma(-xk, U[i][k], x[i][tx]);
-    }
-    __syncthreads();
-  }
-  if (ok)
-    for (int i = ty; i < kb; i += 8) X[(size_t)(k0 + i) * ldx + c] = x[i][tx];
-}
-
 // ---- after the factorization: permutation vector, sign, zero diagonal ------
 // The swap list (LAPACK ipiv form) is replayed in order on a permutation
 // vector (lu.rs:147-149), the sign flips once per real swap (lu.rs:151), and
 // U's diagonal is scanned for an exact zero (lu.rs:177).
 __global__ void lu_finish_kernel(const int* __restrict__ ipiv, uint64_t* piv, int m, int kmin,
-                                 const double* LU, size_t ld, int* flags) {
+                                 const double* LU, size_t ld, int* flags, int smem_rows) {
+  extern __shared__ int sperm[];  // permutation in shared memory when m fits
   __shared__ int zero;
   if (threadIdx.x == 0) zero = 0;
-  for (int i = threadIdx.x; i < m; i += blockDim.x) piv[i] = (uint64_t)i;
+  const bool in_smem = m <= smem_rows;
+  if (in_smem) {
+    for (int i = threadIdx.x; i < m; i += blockDim.x) sperm[i] = i;
+  } else {
+    for (int i = threadIdx.x; i < m; i += blockDim.x) piv[i] = (uint64_t)i;
+  }
   __syncthreads();
   for (int j = threadIdx.x; j < kmin; j += blockDim.x)
     if (LU[(size_t)j * ld + j] == 0.0) atomicOr(&zero, 1);
@@ -171,15 +109,23 @@ __global__ void lu_finish_kernel(const int* __restrict__ ipiv, uint64_t* piv, in
     for (int j = 0; j < kmin; j++) {
       int p = ipiv[j];
       if (p != j) {
-        uint64_t t = piv[p];
-        piv[p] = piv[j];
-        piv[j] = t;
+        if (in_smem) {
+          int t = sperm[p];
+          sperm[p] = sperm[j];
+          sperm[j] = t;
+        } else {
+          uint64_t t = piv[p];
+          piv[p] = piv[j];
+          piv[j] = t;
+        }
         pos = !pos;
       }
     }
     flags[0] = pos;
   }
   __syncthreads();
+  if (in_smem)
+    for (int i = threadIdx.x; i < m; i += blockDim.x) piv[i] = (uint64_t)sperm[i];
   if (threadIdx.x == 0) flags[1] = zero;
 }
 
@@ -257,14 +203,6 @@ void configure_smem_attrs() {
                        (int)TRSM_SMEM_EXACT);
   cudaFuncSetAttribute(trsm_rowpanel_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)TRSM_SMEM_FAST);
-  cudaFuncSetAttribute(solve_diag_fwd_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)SOLVE_SMEM);
-  cudaFuncSetAttribute(solve_diag_fwd_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)SOLVE_SMEM);
-  cudaFuncSetAttribute(solve_diag_bwd_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)SOLVE_SMEM);
-  cudaFuncSetAttribute(solve_diag_bwd_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)SOLVE_SMEM);
   done = true;
 }
 
@@ -304,38 +242,19 @@ la_status launch_trsm_rowpanel(la_ctx ctx, bool exact, double* A, double* S, siz
   return la_check_launch(ctx, "trsm_rowpanel_kernel");
 }
 
-la_status launch_solve_diag_fwd(la_ctx ctx, bool exact, const double* LU, size_t ld, int k0,
-                                int kb, double* X, size_t ldx, int nrhs) {
-  dim3 grid((nrhs + TR_COLS - 1) / TR_COLS);
-  configure_smem_attrs();
-  if (exact)
-    solve_diag_fwd_kernel<true><<<grid, 256, SOLVE_SMEM, ctx->stream>>>(LU, ld, k0, kb, X, ldx,
-                                                                          nrhs);
-  else
-    solve_diag_fwd_kernel<false><<<grid, 256, SOLVE_SMEM, ctx->stream>>>(LU, ld, k0, kb, X,
-                                                                           ldx, nrhs);
-  ctx->launches++;
-  return la_check_launch(ctx, "solve_diag_fwd_kernel");
-}
-
-la_status launch_solve_diag_bwd(la_ctx ctx, bool exact, const double* LU, size_t ld, int k0,
-                                int kb, double* X, size_t ldx, int nrhs) {
-  dim3 grid((nrhs + TR_COLS - 1) / TR_COLS);
-  configure_smem_attrs();
-  if (exact)
-    solve_diag_bwd_kernel<true><<<grid, 256, SOLVE_SMEM, ctx->stream>>>(LU, ld, k0, kb, X, ldx,
-                                                                          nrhs);
-  else
-    solve_diag_bwd_kernel<false><<<grid, 256, SOLVE_SMEM, ctx->stream>>>(LU, ld, k0, kb, X,
-                                                                           ldx, nrhs);
-  ctx->launches++;
-  return la_check_launch(ctx, "solve_diag_bwd_kernel");
-}
-
 la_status launch_lu_finish(la_ctx ctx, la_lu h) {
   const int kmin = (int)std::min(h->m, h->n);
-  lu_finish_kernel<<<1, 1024, 0, ctx->stream>>>(h->d_ipiv, h->d_piv, (int)h->m, kmin, h->d_lu,
-                                                h->ld, reinterpret_cast<int*>(ctx->d_small));
+  const int smem_rows = 50000;  // 200 KB of int32 (opt-in); larger m replays in global memory
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(lu_finish_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         smem_rows * (int)sizeof(int));
+    configured = true;
+  }
+  const size_t smem = (size_t)std::min((int)h->m, smem_rows) * sizeof(int);
+  lu_finish_kernel<<<1, 1024, smem, ctx->stream>>>(h->d_ipiv, h->d_piv, (int)h->m, kmin, h->d_lu,
+                                                   h->ld, reinterpret_cast<int*>(ctx->d_small),
+                                                   smem_rows);
   ctx->launches++;
   return la_check_launch(ctx, "lu_finish_kernel");
 }

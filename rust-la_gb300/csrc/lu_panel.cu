@@ -48,26 +48,31 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
   return t;
 }
 
-// Grid barrier on a monotonically increasing counter. Returns false when the
-// wait gave up (this CTA timed out or another CTA reported an error).
+// Grid barrier on a monotonically increasing counter (the pattern of a
+// cooperative-groups grid sync: CTA barrier, one thread fences, arrives with a
+// release add and polls with acquire loads). Returns false when the wait gave up
+// (this CTA timed out or another CTA reported an error).
 __device__ bool grid_barrier(unsigned* counter, unsigned target, int* err) {
   __shared__ int ok;
-  __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
-    atomicAdd(counter, 1u);
+    __threadfence();
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(counter), "r"(1u) : "memory");
     int good = 1;
-    unsigned long long t0 = globaltimer_ns();
+    unsigned long long t0 = 0;
     unsigned spins = 0;
     while (ld_acquire_u32(counter) < target) {
-      if (ld_volatile_i32(err) != 0) { good = 0; break; }
-      if ((++spins & 63u) == 0 && globaltimer_ns() - t0 > WAIT_LIMIT_NS) {
-        atomicCAS(err, 0, (int)DERR_PANEL_TIMEOUT);
-        good = 0;
-        break;
+      if ((++spins & 63u) == 0) {
+        if (ld_volatile_i32(err) != 0) { good = 0; break; }
+        unsigned long long now = globaltimer_ns();
+        if (t0 == 0) t0 = now;
+        else if (now - t0 > WAIT_LIMIT_NS) {
+          atomicCAS(err, 0, (int)DERR_PANEL_TIMEOUT);
+          good = 0;
+          break;
+        }
       }
     }
-    __threadfence();
     ok = good;
   }
   __syncthreads();
@@ -110,22 +115,25 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
   extern __shared__ __align__(16) double sm[];
   constexpr int W = MAX_PANEL_W;
   const int rpc = p.rpc;
-  double* va = sm;                              // [rpc][W]  value (FAST) / a (EXACT)
-  double* vs = EXACT ? sm + rpc * W : nullptr;  // [rpc][W]  running sum s (EXACT)
+  double* va = sm;                                // [rpc][W]  value (FAST) / a (EXACT)
+  double* vs = EXACT ? sm + rpc * W : nullptr;    // [rpc][W]  running sum s (EXACT)
   double* urow = sm + (EXACT ? 2 : 1) * rpc * W;  // [W] pivot row
-  double* lrow = urow + W;                        // [rpc] multipliers of this step
+  double* drow_a = urow + W;                      // [W] row j as published (raw)
+  double* drow_s = drow_a + W;                    // [W] its running sums (EXACT)
+  double* lrow = drow_s + W;                      // [rpc] multipliers of this step
   __shared__ double red_k[PT / 32];
   __shared__ int red_p[PT / 32];
   __shared__ int s_win_pos;
+  __shared__ double s_scale;
   __shared__ int s_pivs[W];
 
   const int g = blockIdx.x;
   const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
   const int jb = p.jb;
   const int row0 = p.j0 + g * rpc;                  // position of local row 0
   const int nrows = max(0, min(rpc, p.m - row0));   // rows owned by this CTA
 
-  // Load the owned rows of the panel.
   for (int idx = tid; idx < rpc * W; idx += PT) {
     int r = idx / W, c = idx % W;
     double a = 0.0, s = 0.0;
@@ -145,9 +153,8 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
     // 1. local candidate over owned rows at positions >= j.
     double bk = 0.0;
     int bp = -1;
-    for (int r = tid; r < nrows; r += PT) {
-      int pos = row0 + r;
-      if (pos < j) continue;
+    for (int r = max(0, j - row0) + tid; r < nrows; r += PT) {
+      const int pos = row0 + r;
       double v = EXACT ? __dsub_rn(va[r * W + c], vs[r * W + c]) : va[r * W + c];
       double k = pivot_key(v, pos, j);
       if (better(k, pos, bk, bp)) { bk = k; bp = pos; }
@@ -158,40 +165,54 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
       int op = __shfl_down_sync(0xffffffffu, bp, off);
       if (better(ok, op, bk, bp)) { bk = ok; bp = op; }
     }
-    if ((tid & 31) == 0) { red_k[tid >> 5] = bk; red_p[tid >> 5] = bp; }
+    if (lane == 0) { red_k[warp] = bk; red_p[warp] = bp; }
     __syncthreads();
-    if (tid == 0) {
-      for (int w = 1; w < PT / 32; w++)
-        if (better(red_k[w], red_p[w], bk, bp)) { bk = red_k[w]; bp = red_p[w]; }
-      p.cand_abs[par * MAX_PANEL_CTAS + g] = bk;
-      p.cand_pos[par * MAX_PANEL_CTAS + g] = bp;
-      red_p[0] = bp;
+    if (warp == 0) {
+      bk = lane < PT / 32 ? red_k[lane] : 0.0;
+      bp = lane < PT / 32 ? red_p[lane] : -1;
+#pragma unroll
+      for (int off = 4; off > 0; off >>= 1) {
+        double ok = __shfl_down_sync(0xffffffffu, bk, off);
+        int op = __shfl_down_sync(0xffffffffu, bp, off);
+        if (better(ok, op, bk, bp)) { bk = ok; bp = op; }
+      }
+      if (lane == 0) {
+        p.cand_abs[par * MAX_PANEL_CTAS + g] = bk;
+        p.cand_pos[par * MAX_PANEL_CTAS + g] = bp;
+        s_win_pos = bp;
+      }
     }
     __syncthreads();
     // 2. publish the candidate row (finished values) and, if owned, row j.
     {
-      const int cp = red_p[0];
+      const int cp = s_win_pos;
       if (cp >= 0 && tid < W) {
         int r = cp - row0;
         double v = EXACT ? __dsub_rn(va[r * W + tid], vs[r * W + tid]) : va[r * W + tid];
         p.cand_row[((size_t)par * MAX_PANEL_CTAS + g) * W + tid] = v;
       }
-      if (j >= row0 && j < row0 + nrows && tid < W) {
-        int r = j - row0;
-        p.diag_a[par * W + tid] = va[r * W + tid];
-        if (EXACT) p.diag_s[par * W + tid] = vs[r * W + tid];
+      if (j >= row0 && j < row0 + nrows && tid >= PT - W) {
+        const int t = tid - (PT - W);
+        const int r = j - row0;
+        p.diag_a[par * W + t] = va[r * W + t];
+        if (EXACT) p.diag_s[par * W + t] = vs[r * W + t];
       }
     }
     if (!grid_barrier(p.bar, p.bar_base + (unsigned)(p.G * (c + 1)), p.err)) return;
 
-    // 3. global winner (identical in every CTA).
-    if (tid < 32) {
+    // 3. global winner (identical in every CTA): one candidate per thread; the
+    //    last W threads fetch row j at the same time (needed if it moves here).
+    {
       double k = 0.0;
       int ps = -1;
-      for (int q = tid; q < p.G; q += 32) {
-        double qk = __ldcg(p.cand_abs + par * MAX_PANEL_CTAS + q);
-        int qp = __ldcg(p.cand_pos + par * MAX_PANEL_CTAS + q);
-        if (better(qk, qp, k, ps)) { k = qk; ps = qp; }
+      if (tid < p.G) {
+        k = __ldcg(p.cand_abs + par * MAX_PANEL_CTAS + tid);
+        ps = __ldcg(p.cand_pos + par * MAX_PANEL_CTAS + tid);
+      }
+      if (tid >= PT - W) {
+        const int t = tid - (PT - W);
+        drow_a[t] = __ldcg(p.diag_a + par * W + t);
+        if (EXACT) drow_s[t] = __ldcg(p.diag_s + par * W + t);
       }
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) {
@@ -199,63 +220,82 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
         int op = __shfl_down_sync(0xffffffffu, ps, off);
         if (better(ok, op, k, ps)) { k = ok; ps = op; }
       }
-      if (tid == 0) {
-        // Find which CTA published the winner (owner of that position).
-        s_win_pos = ps;
-        s_pivs[c] = ps;
-        if (g == 0) p.ipiv[j] = ps;
+      if (lane == 0) { red_k[warp] = k; red_p[warp] = ps; }
+      __syncthreads();
+      if (warp == 0) {
+        k = lane < PT / 32 ? red_k[lane] : 0.0;
+        ps = lane < PT / 32 ? red_p[lane] : -1;
+#pragma unroll
+        for (int off = 4; off > 0; off >>= 1) {
+          double ok = __shfl_down_sync(0xffffffffu, k, off);
+          int op = __shfl_down_sync(0xffffffffu, ps, off);
+          if (better(ok, op, k, ps)) { k = ok; ps = op; }
+        }
+        if (lane == 0) {
+          s_win_pos = ps;
+          s_pivs[c] = ps;
+          if (g == 0) p.ipiv[j] = ps;
+        }
       }
+      __syncthreads();
     }
-    __syncthreads();
     const int piv = s_win_pos;
     const int wg = (piv - p.j0) / rpc;  // CTA that owns the winning row
     if (tid < W) urow[tid] = __ldcg(p.cand_row + ((size_t)par * MAX_PANEL_CTAS + wg) * W + tid);
     __syncthreads();
+    if (tid == 0) {
+      const double d = urow[c];
+      // FAST scales by the reciprocal (as LAPACK's getf2 does); EXACT divides.
+      s_scale = (d != 0.0) ? 1.0 / d : 1.0;
+    }
     // Swap: row j <- pivot row (finished), row piv <- old row j (raw storage).
     if (tid < W) {
       if (piv != j && piv >= row0 && piv < row0 + nrows) {
-        int r = piv - row0;
-        va[r * W + tid] = __ldcg(p.diag_a + par * W + tid);
-        if (EXACT) vs[r * W + tid] = __ldcg(p.diag_s + par * W + tid);
+        const int r = piv - row0;
+        va[r * W + tid] = drow_a[tid];
+        if (EXACT) vs[r * W + tid] = drow_s[tid];
       }
       if (j >= row0 && j < row0 + nrows) {
-        int r = j - row0;
+        const int r = j - row0;
         va[r * W + tid] = urow[tid];
         if (EXACT) vs[r * W + tid] = 0.0;
       }
     }
     __syncthreads();
-    // 4a. multipliers l_i = v_i / u_jj for owned rows below j.
-    const double d = urow[c];
-    for (int r = tid; r < nrows; r += PT) {
-      int pos = row0 + r;
-      if (pos <= j) continue;
-      double v = EXACT ? __dsub_rn(va[r * W + c], vs[r * W + c]) : va[r * W + c];
-      double l = (d != 0.0) ? v / d : v;
-      va[r * W + c] = l;
-      if (EXACT) vs[r * W + c] = 0.0;
-      lrow[r] = l;
+    // 4a. multipliers l_i = v_i / u_jj for owned rows below j; rows are spread
+    //     over all warps (row = lane * 8 + warp) so every SM sub-partition works.
+    const int first = max(0, j + 1 - row0);
+    const int cnt = nrows - first;
+    {
+      const double d = urow[c];
+      const double sc = s_scale;
+      for (int q = lane * (PT / 32) + warp; q < cnt; q += PT) {
+        const int r = first + q;
+        double v = EXACT ? __dsub_rn(va[r * W + c], vs[r * W + c]) : va[r * W + c];
+        double l = (d != 0.0) ? (EXACT ? v / d : v * sc) : v;
+        va[r * W + c] = l;
+        if (EXACT) vs[r * W + c] = 0.0;
+        lrow[r] = l;
+      }
     }
     __syncthreads();
-    // 4b. rank-1 update of the remaining panel columns.
-    const int ncols = jb - c - 1;
-    if (ncols > 0) {
-      const int first = max(0, j + 1 - row0);
-      const int cnt = nrows - first;
-      for (int idx = tid; idx < cnt * ncols; idx += PT) {
-        int r = first + idx / ncols;
-        int cc = c + 1 + idx % ncols;
-        double l = lrow[r];
+    // 4b. rank-1 update of the remaining panel columns: thread = (column lane,
+    //     row group of 4).
+    const int cc = c + 1 + (tid & (W - 1));
+    if (cc < jb) {
+      const double u = urow[cc];
+      for (int q = tid / W; q < cnt; q += PT / W) {
+        const int r = first + q;
+        const double l = lrow[r];
         if (EXACT)
-          vs[r * W + cc] = __dadd_rn(vs[r * W + cc], __dmul_rn(l, urow[cc]));
+          vs[r * W + cc] = __dadd_rn(vs[r * W + cc], __dmul_rn(l, u));
         else
-          va[r * W + cc] = fma(-l, urow[cc], va[r * W + cc]);
+          va[r * W + cc] = fma(-l, u, va[r * W + cc]);
       }
     }
     __syncthreads();
   }
 
-  // Write the finished panel back.
   for (int idx = tid; idx < nrows * W; idx += PT) {
     int r = idx / W, c = idx % W;
     if (c < jb) {
@@ -283,7 +323,6 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
       src[a] = src[b];
       src[b] = t;
     }
-    // Keep only real moves.
     int k = 0;
     for (int q = 0; q < cnt; q++)
       if (src[q] != dst[q]) { dst[k] = dst[q]; src[k] = src[q]; k++; }
@@ -293,18 +332,18 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
 
 }  // namespace
 
-la_status launch_panel(la_ctx ctx, bool exact, double* A, double* S, size_t ld, int m, int j0,
-                       int jb, int* d_ipiv, unsigned* bar_base) {
+la_status launch_panel(la_ctx ctx, cudaStream_t stream, bool exact, double* A, double* S,
+                       size_t ld, int m, int j0, int jb, int* d_ipiv, unsigned* bar_base) {
   const int R = m - j0;
   if (R <= 0 || jb <= 0) return LA_OK;
   const int W = MAX_PANEL_W;
   int maxG = ctx->panel_ctas > 0 ? std::min(ctx->panel_ctas, ctx->sm_count) : ctx->sm_count;
-  maxG = std::min(maxG, MAX_PANEL_CTAS);
+  maxG = std::min(maxG, PT);  // one candidate per thread when picking the winner
   // At least 32 rows per CTA: fewer CTAs keep the per-column barrier cheap.
   int G = std::max(1, std::min(maxG, (R + 31) / 32));
   int rpc = (R + G - 1) / G;
   const size_t per_row = (size_t)W * sizeof(double) * (exact ? 2 : 1) + sizeof(double);
-  const size_t fixed = (size_t)W * sizeof(double);
+  const size_t fixed = (size_t)3 * W * sizeof(double);
   size_t smem = fixed + per_row * rpc;
   if (smem > ctx->smem_optin) return LA_UNSUPPORTED;
   G = (R + rpc - 1) / rpc;
@@ -337,7 +376,7 @@ la_status launch_panel(la_ctx ctx, bool exact, double* A, double* S, size_t ld, 
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, PT, smem);
   if (e != cudaSuccess) return la_cuda_fail(ctx, e, "occupancy(panel)");
   if (per_sm * ctx->sm_count < G) return LA_UNSUPPORTED;
-  e = cudaLaunchCooperativeKernel(fn, dim3(G), dim3(PT), args, smem, ctx->stream);
+  e = cudaLaunchCooperativeKernel(fn, dim3(G), dim3(PT), args, smem, stream);
   if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaLaunchCooperativeKernel(panel)");
   ctx->launches++;
   *bar_base += (unsigned)(G * jb);

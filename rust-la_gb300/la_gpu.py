@@ -25,7 +25,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "liblagpu.so")
 
 OK, SINGULAR, BADSHAPE, INVALID, NOMEM, CUDA_ERROR, TIMEOUT, NOT_CONVERGED, UNSUPPORTED = range(9)
-OPT_ARITH, OPT_PANEL_WIDTH, OPT_PANEL_CTAS, OPT_PROFILE = 1, 2, 3, 4
+OPT_ARITH, OPT_PANEL_WIDTH, OPT_PANEL_CTAS, OPT_PROFILE, OPT_LOOKAHEAD = 1, 2, 3, 4, 5
 ARITH_FAST, ARITH_EXACT = 0, 1
 
 
@@ -78,6 +78,8 @@ SIGNATURES = {
     "la_matrix_mul": ([_P, _P, _S, _S, _P, _S, _S, _P], _I),
     "la_matrix_mmul": ([_P, _P, _S, _S, _P, _S, _S, _P, _S, _S], _I),
     "la_matrix_mul_device": ([_P, _P, _S, _P, _S, _P, _S, _S, _S, _S], _I),
+    "la_backward_error_device": ([_P, _P, _S, _P, _S, _P, _S, _S, _S, _P], _I),
+    "la_backward_error": ([_P, _P, _P, _P, _S, _S, _P], _I),
 }
 
 
@@ -379,6 +381,25 @@ class LUDecomposition:
         st = lib().la_lu_solve_device(self.h, ctypes.c_void_p(b_ptr), ldb, brows, nrhs,
                                       ctypes.c_void_p(x_ptr), ldx)
         return _check(self.ctx, st, (OK, SINGULAR))
+
+
+def backward_error(ctx, a, x, b):
+    """eta = max_j ||b_j - A x_j||_inf / (||A||_inf ||x_j||_inf + ||b_j||_inf), on the GPU."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    x = np.ascontiguousarray(x, dtype=np.float64).reshape(a.shape[0], -1)
+    b = np.ascontiguousarray(b, dtype=np.float64).reshape(a.shape[0], -1)
+    out = ctypes.c_double()
+    _check(ctx, lib().la_backward_error(ctx.h, _ptr(a), _ptr(x), _ptr(b), a.shape[0], x.shape[1],
+                                        ctypes.byref(out)))
+    return out.value
+
+
+def backward_error_device(ctx, a_ptr, lda, x_ptr, ldx, b_ptr, ldb, n, nrhs):
+    out = ctypes.c_double()
+    _check(ctx, lib().la_backward_error_device(ctx.h, ctypes.c_void_p(a_ptr), lda,
+                                               ctypes.c_void_p(x_ptr), ldx, ctypes.c_void_p(b_ptr),
+                                               ldb, n, nrhs, ctypes.byref(out)))
+    return out.value
 
 
 def matrix_mul_device(ctx, a_ptr, lda, b_ptr, ldb, c_ptr, ldc, m_, k, n):

@@ -350,3 +350,40 @@ def test_n2048_fast_pivots_and_eta(lagpu, ctx_fast):
     assert np.array_equal(lu.get_piv(), ref.piv)
     x = lu.solve(lagpu.Matrix(b, ctx_fast)).data
     assert oracle.backward_error(a, x, b) <= ETA_MAX
+
+
+def test_lookahead_on_off_agree(lagpu, ctx_fast, ctx_exact):
+    rng = np.random.default_rng(91)
+    a = rng.uniform(-1, 1, size=(700, 700))
+    ref = oracle.lu_factor(a, threads=4)
+    for la in (1, 0):
+        ctx_fast.set_option(lagpu.OPT_LOOKAHEAD, la)
+        assert np.array_equal(lagpu.LUDecomposition.new(a, ctx_fast).get_piv(), ref.piv)
+        ctx_exact.set_option(lagpu.OPT_LOOKAHEAD, la)
+        assert np.array_equal(lagpu.LUDecomposition.new(a, ctx_exact).get_packed().data, ref.lu)
+    ctx_fast.set_option(lagpu.OPT_LOOKAHEAD, 1)
+    ctx_exact.set_option(lagpu.OPT_LOOKAHEAD, 1)
+
+
+@pytest.mark.parametrize("nrhs", [1, 2, 31, 33, 100])
+def test_solve_many_rhs(lagpu, ctx_fast, ctx_exact, nrhs):
+    rng = np.random.default_rng(400 + nrhs)
+    n = 150
+    a = rng.uniform(-1, 1, size=(n, n))
+    b = rng.uniform(-1, 1, size=(n, nrhs))
+    ref = oracle.lu_factor(a)
+    xe = lagpu.LUDecomposition.new(a, ctx_exact).solve(lagpu.Matrix(b, ctx_exact)).data
+    assert np.array_equal(xe, oracle.solve(ref, b))
+    xf = lagpu.LUDecomposition.new(a, ctx_fast).solve(lagpu.Matrix(b, ctx_fast)).data
+    assert oracle.backward_error(a, xf, b) <= ETA_MAX
+
+
+def test_device_backward_error_matches_oracle(lagpu, ctx_fast):
+    rng = np.random.default_rng(17)
+    n = 300
+    a = rng.standard_normal((n, n))
+    b = rng.standard_normal((n, 3))
+    x = np.linalg.solve(a, b) + rng.standard_normal((n, 3)) * 1e-9
+    got = lagpu.backward_error(ctx_fast, a, x, b)
+    want = oracle.backward_error(a, x, b)
+    assert abs(got - want) <= 1e-3 * want
