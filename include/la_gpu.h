@@ -149,6 +149,26 @@ la_status la_matrix_mmul(la_ctx ctx, const double* a, size_t m, size_t k, const 
 la_status la_matrix_mul_device(la_ctx ctx, const double* d_a, size_t lda, const double* d_b,
                                size_t ldb, double* d_c, size_t ldc, size_t m, size_t k, size_t n);
 
+/* ---- allocation-free factorization (no reference counterpart) ------------ */
+
+/* LU factorization (FAST arithmetic) for callers that cannot allocate device
+ * memory, e.g. code whose device memory is owned by a pool or framework that
+ * forbids cudaMalloc, or that must keep a fixed footprint. It allocates
+ * nothing and needs no la_ctx: it factors d_a (m x n, row-major, pitch lda,
+ * 16-byte aligned, lda even) in place on `stream` (a cudaStream_t, NULL for
+ * the default stream) and writes the swap list d_ipiv (min(m,n) int32), the
+ * permutation vector d_piv (m uint64, the form of lu.rs piv) and d_flags[0] =
+ * pospivsign, d_flags[1] = 1 if U has an exact zero on its diagonal. Returns
+ * after the stream has finished the factorization.
+ * Limit: m <= 16384 (LA_UNSUPPORTED beyond). Its working memory is one static
+ * device array of about 70 KB per device, kept until the process exits and
+ * shared by every call: calls that overlap on the GPU (other host threads,
+ * other streams) race and must be serialized by the caller. The first call on
+ * a device looks up that array's device address; make it before any stream
+ * capture. */
+la_status la_lu_factor_noalloc(void* stream, double* d_a, size_t lda, size_t m, size_t n,
+                               int* d_ipiv, uint64_t* d_piv, int* d_flags);
+
 /* ---- accuracy check (no reference counterpart) --------------------------- */
 
 /* Normwise backward error of a computed solution X of A X = B (A n x n):

@@ -27,6 +27,9 @@ enum GemmMode : int {
   GM_FMA_SUB_DESC = 6    // C = C - A*B   fused, descending k
 };
 
+constexpr int MAX_PANEL_CTAS = 1024;
+constexpr int MAX_PANEL_W = 64;
+
 // Device-side error codes written to la_context::d_err.
 enum DeviceErr : int {
   DERR_NONE = 0,
@@ -58,6 +61,7 @@ struct la_context {
   int* d_err = nullptr;          // inside d_scratch
   unsigned* d_bar = nullptr;     // barrier counters (one per panel)
   size_t bar_count = 0;
+  int cand_stride = MAX_PANEL_CTAS;  // candidate slots per parity in the buffers below
   double* d_cand_abs = nullptr;  // [2][MAX_PANEL_CTAS]
   int* d_cand_pos = nullptr;     // [2][MAX_PANEL_CTAS]
   double* d_cand_row = nullptr;  // [2][MAX_PANEL_CTAS][64]
@@ -79,8 +83,6 @@ struct la_lu_handle {
   int arith = LA_ARITH_FAST;
 };
 
-constexpr int MAX_PANEL_CTAS = 1024;
-constexpr int MAX_PANEL_W = 64;
 
 // Host helpers (context.cu).
 la_status la_cuda_fail(la_ctx ctx, cudaError_t e, const char* what);
@@ -112,7 +114,10 @@ la_status launch_laswp(la_ctx ctx, bool exact, double* A, double* S, size_t ld, 
                        int jb);
 la_status launch_trsm_rowpanel(la_ctx ctx, bool exact, double* A, double* S, size_t ld, int j0,
                                int jb, int c_begin, int c_end);
-la_status launch_lu_finish(la_ctx ctx, la_lu h);
+la_status launch_lu_finish(la_ctx ctx, la_lu h, int* d_flags);
+// Enqueues the whole factorization of h (no readback, no synchronization);
+// lu_finish writes {pospivsign, zero-on-diagonal} to d_flags.
+la_status lu_factor_enqueue(la_ctx ctx, la_lu h, int* d_flags);
 la_status launch_lu_solve(la_ctx ctx, bool exact, const double* LU, size_t ld, double* X,
                           size_t ldx, int n, int nrhs);
 la_status launch_permute_rows(la_ctx ctx, const uint64_t* d_piv, const double* B, size_t ldb,

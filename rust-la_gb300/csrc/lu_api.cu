@@ -84,7 +84,9 @@ constexpr size_t GEMM_SMEM_WITH_PANEL = 78 * 1024;
 // trailing update runs on the main stream. The two touch disjoint columns:
 // panel p+1 owns columns [j1, j2) of rows >= j1, the rest of the update writes
 // columns >= j2 and reads L21 (columns < j1) and U12 (rows < j1).
-la_status lu_factor(la_ctx ctx, la_lu h) {
+}  // namespace
+
+la_status lu_factor_enqueue(la_ctx ctx, la_lu h, int* d_flags) {
   const bool exact = (h->arith == LA_ARITH_EXACT);
   const int m = (int)h->m, n = (int)h->n;
   const size_t ld = h->ld;
@@ -153,12 +155,26 @@ la_status lu_factor(la_ctx ctx, la_lu h) {
   }
   // m < n: the columns right of the last panel got their triangular update above.
   size_t b = t.begin(ms);
-  LA_TRY(launch_lu_finish(ctx, h));
-  int* flags = static_cast<int*>(ctx->h_pinned);
-  LA_CUDA(ctx, cudaMemcpyAsync(flags, ctx->d_small, 2 * sizeof(int), cudaMemcpyDeviceToHost, ms));
+  LA_TRY(launch_lu_finish(ctx, h, d_flags));
   t.end(ms, b, PH_OTHER);
+  if (t.on) {
+    LA_CUDA(ctx, cudaStreamSynchronize(ms));
+    t.finish();
+  } else {
+    for (int i = 0; i < 5; i++) ctx->phase_ms[i] = 0;
+  }
+  return LA_OK;
+}
+
+namespace {
+
+la_status lu_factor(la_ctx ctx, la_lu h) {
+  int* d_flags = reinterpret_cast<int*>(ctx->d_small);
+  LA_TRY(lu_factor_enqueue(ctx, h, d_flags));
+  int* flags = static_cast<int*>(ctx->h_pinned);
+  LA_CUDA(ctx, cudaMemcpyAsync(flags, d_flags, 2 * sizeof(int), cudaMemcpyDeviceToHost,
+                               ctx->stream));
   LA_TRY(la_sync_and_check(ctx, "lu factorization"));
-  t.finish();
   h->pospivsign = flags[0];
   h->zero_diag = flags[1];
   return LA_OK;

@@ -242,7 +242,7 @@ la_status launch_trsm_rowpanel(la_ctx ctx, bool exact, double* A, double* S, siz
   return la_check_launch(ctx, "trsm_rowpanel_kernel");
 }
 
-la_status launch_lu_finish(la_ctx ctx, la_lu h) {
+la_status launch_lu_finish(la_ctx ctx, la_lu h, int* d_flags) {
   const int kmin = (int)std::min(h->m, h->n);
   const int smem_rows = 50000;  // 200 KB of int32 (opt-in); larger m replays in global memory
   static bool configured = false;
@@ -253,8 +253,7 @@ la_status launch_lu_finish(la_ctx ctx, la_lu h) {
   }
   const size_t smem = (size_t)std::min((int)h->m, smem_rows) * sizeof(int);
   lu_finish_kernel<<<1, 1024, smem, ctx->stream>>>(h->d_ipiv, h->d_piv, (int)h->m, kmin, h->d_lu,
-                                                   h->ld, reinterpret_cast<int*>(ctx->d_small),
-                                                   smem_rows);
+                                                   h->ld, d_flags, smem_rows);
   ctx->launches++;
   return la_check_launch(ctx, "lu_finish_kernel");
 }

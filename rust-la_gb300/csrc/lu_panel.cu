@@ -108,6 +108,7 @@ struct PanelParams {
   double* diag_a;
   double* diag_s;
   int* swaps;  // [0] = count, then (dest, src) pairs of the composed row moves
+  int cstride; // candidate slots per parity (>= G)
 };
 
 template <bool EXACT>
@@ -177,8 +178,8 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
         if (better(ok, op, bk, bp)) { bk = ok; bp = op; }
       }
       if (lane == 0) {
-        p.cand_abs[par * MAX_PANEL_CTAS + g] = bk;
-        p.cand_pos[par * MAX_PANEL_CTAS + g] = bp;
+        p.cand_abs[par * p.cstride + g] = bk;
+        p.cand_pos[par * p.cstride + g] = bp;
         s_win_pos = bp;
       }
     }
@@ -189,7 +190,7 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
       if (cp >= 0 && tid < W) {
         int r = cp - row0;
         double v = EXACT ? __dsub_rn(va[r * W + tid], vs[r * W + tid]) : va[r * W + tid];
-        p.cand_row[((size_t)par * MAX_PANEL_CTAS + g) * W + tid] = v;
+        p.cand_row[((size_t)par * p.cstride + g) * W + tid] = v;
       }
       if (j >= row0 && j < row0 + nrows && tid >= PT - W) {
         const int t = tid - (PT - W);
@@ -206,8 +207,8 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
       double k = 0.0;
       int ps = -1;
       if (tid < p.G) {
-        k = __ldcg(p.cand_abs + par * MAX_PANEL_CTAS + tid);
-        ps = __ldcg(p.cand_pos + par * MAX_PANEL_CTAS + tid);
+        k = __ldcg(p.cand_abs + par * p.cstride + tid);
+        ps = __ldcg(p.cand_pos + par * p.cstride + tid);
       }
       if (tid >= PT - W) {
         const int t = tid - (PT - W);
@@ -241,7 +242,7 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
     }
     const int piv = s_win_pos;
     const int wg = (piv - p.j0) / rpc;  // CTA that owns the winning row
-    if (tid < W) urow[tid] = __ldcg(p.cand_row + ((size_t)par * MAX_PANEL_CTAS + wg) * W + tid);
+    if (tid < W) urow[tid] = __ldcg(p.cand_row + ((size_t)par * p.cstride + wg) * W + tid);
     __syncthreads();
     if (tid == 0) {
       const double d = urow[c];
@@ -339,6 +340,7 @@ la_status launch_panel(la_ctx ctx, cudaStream_t stream, bool exact, double* A, d
   const int W = MAX_PANEL_W;
   int maxG = ctx->panel_ctas > 0 ? std::min(ctx->panel_ctas, ctx->sm_count) : ctx->sm_count;
   maxG = std::min(maxG, PT);  // one candidate per thread when picking the winner
+  maxG = std::min(maxG, ctx->cand_stride);
   // At least 32 rows per CTA: fewer CTAs keep the per-column barrier cheap.
   int G = std::max(1, std::min(maxG, (R + 31) / 32));
   int rpc = (R + G - 1) / G;
@@ -367,6 +369,7 @@ la_status launch_panel(la_ctx ctx, cudaStream_t stream, bool exact, double* A, d
   p.diag_a = ctx->d_diag_a;
   p.diag_s = ctx->d_diag_s;
   p.swaps = ctx->d_swaps;
+  p.cstride = ctx->cand_stride;
 
   void* args[] = {&p};
   const void* fn = exact ? (const void*)panel_kernel<true> : (const void*)panel_kernel<false>;

@@ -80,6 +80,7 @@ SIGNATURES = {
     "la_matrix_mul_device": ([_P, _P, _S, _P, _S, _P, _S, _S, _S, _S], _I),
     "la_backward_error_device": ([_P, _P, _S, _P, _S, _P, _S, _S, _S, _P], _I),
     "la_backward_error": ([_P, _P, _P, _P, _S, _S, _P], _I),
+    "la_lu_factor_noalloc": ([_P, _P, _S, _S, _S, _P, _P, _P], _I),
 }
 
 
