@@ -149,6 +149,39 @@ la_status la_matrix_mmul(la_ctx ctx, const double* a, size_t m, size_t k, const 
 la_status la_matrix_mul_device(la_ctx ctx, const double* d_a, size_t lda, const double* d_b,
                                size_t ldb, double* d_c, size_t ldc, size_t m, size_t k, size_t n);
 
+/* ---- mixed precision + iterative refinement (no reference counterpart) ---- */
+
+/* Precision of the trailing-update products of the mixed LU. */
+#define LA_PREC_BF16 1  /* tcgen05 BF16 x BF16 -> FP32 */
+#define LA_PREC_FP16 2  /* tcgen05 FP16 x FP16 -> FP32, per-panel power-of-two scaling */
+#define LA_PREC_FP32 3  /* FP32 FMA (no tensor cores) */
+
+typedef struct la_refine_stats {
+  int iterations;    /* correction solves applied */
+  int converged;     /* 1 when eta <= tol was reached */
+  double eta;        /* final normwise backward error (FP64 residual) */
+  int fell_back;     /* 1 when the plain FP64 LU produced the answer */
+  int precision;     /* LA_PREC_* actually used for the answer (0: plain FP64) */
+} la_refine_stats;
+
+/* Factors a square FP64 matrix (device, pitch lda) in FP32 with the trailing
+ * updates in `prec`; the handle keeps the FP64 matrix for residuals. Pivoting
+ * is partial pivoting on the FP32 values. */
+la_status la_lu_mixed_new_device(la_ctx ctx, const double* d_a, size_t lda, size_t n, int prec,
+                                 la_lu* out);
+/* Iterative refinement with the mixed factors: x = 0, r = b; d = LU \ r (FP32),
+ * x += d, r = b - A x (FP64) until eta <= tol or max_iters or a stall
+ * (LA_NOT_CONVERGED). nrhs <= 16. */
+la_status la_lu_solve_refined_device(la_lu lu, const double* d_b, size_t ldb, size_t nrhs,
+                                     double* d_x, size_t ldx, int max_iters, double tol,
+                                     la_refine_stats* stats);
+/* Tensor-core building block of the mixed LU, exposed for testing:
+ * C (m x n f32, pitch ldc) -= alpha * A (m x k) * B^T (B: n x k), A and B 16-bit
+ * (fmt 1 = BF16, 2 = FP16) K-major with pitches multiple of 8 elements. */
+la_status la_lowp_update_device(la_ctx ctx, int fmt, size_t m, size_t n, size_t k,
+                                const void* d_a16, size_t lda, const void* d_b16, size_t ldb,
+                                float* d_c, size_t ldc, float alpha);
+
 /* ---- allocation-free factorization (no reference counterpart) ------------ */
 
 /* LU factorization (FAST arithmetic) for callers that cannot allocate device

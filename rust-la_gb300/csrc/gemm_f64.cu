@@ -29,41 +29,42 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
 __device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;\n" ::); }
 
-// Loads one K slab: A rows [m0, m0+64) x k [k0, k0+32) and B k [k0, k0+32) x cols [n0, n0+BN).
-// Out-of-range 16-byte chunks are zero-filled (src size 0 or 8), never read.
-template <int BN>
-__device__ __forceinline__ void load_slab(double* As, double* Bs, const double* A, size_t lda,
-                                          const double* B, size_t ldb, int M, int N, int K,
-                                          int m0, int n0, int k0) {
+// Loads one K slab: A rows [m0, m0+64) x k [k0, k0+32) and B k [k0, k0+32) x cols [n0, n0+BN)
+// in 16-byte chunks (EPC elements). Out-of-range parts of a chunk are
+// zero-filled by cp.async's source size, never read.
+template <typename T, int BN>
+__device__ __forceinline__ void load_slab(T* As, T* Bs, const T* A, size_t lda, const T* B,
+                                          size_t ldb, int M, int N, int K, int m0, int n0,
+                                          int k0) {
+  constexpr int EPC = 16 / sizeof(T);
   const int tid = threadIdx.x;
-  // A: 64 rows x 32 k = 1024 chunks of 2 doubles, 4 per thread.
+  constexpr int ACH = BM * BK / EPC;
 #pragma unroll
-  for (int t = 0; t < (BM * BK / 2) / THREADS; t++) {
+  for (int t = 0; t < ACH / THREADS; t++) {
     int chunk = tid + t * THREADS;
-    int r = chunk / (BK / 2);
-    int kc = (chunk % (BK / 2)) * 2;
+    int r = chunk / (BK / EPC);
+    int kc = (chunk % (BK / EPC)) * EPC;
     int gr = m0 + r, gk = k0 + kc;
     int bytes = 0;
-    const double* src = A;
+    const T* src = A;
     if (gr < M && gk < K) {
-      bytes = (gk + 1 < K) ? 16 : 8;
+      bytes = min(EPC, K - gk) * (int)sizeof(T);
       src = A + (size_t)gr * lda + gk;
     }
     cp_async16(As + r * BK + kc, src, bytes);
   }
-  // B: 32 k x BN cols.
-  constexpr int BCH = BK * BN / 2;
+  constexpr int BCH = BK * BN / EPC;
 #pragma unroll
   for (int t = 0; t < (BCH + THREADS - 1) / THREADS; t++) {
     int chunk = tid + t * THREADS;
     if (chunk < BCH) {
-      int kr = chunk / (BN / 2);
-      int cc = (chunk % (BN / 2)) * 2;
+      int kr = chunk / (BN / EPC);
+      int cc = (chunk % (BN / EPC)) * EPC;
       int gk = k0 + kr, gc = n0 + cc;
       int bytes = 0;
-      const double* src = B;
+      const T* src = B;
       if (gk < K && gc < N) {
-        bytes = (gc + 1 < N) ? 16 : 8;
+        bytes = min(EPC, N - gc) * (int)sizeof(T);
         src = B + (size_t)gk * ldb + gc;
       }
       cp_async16(Bs + kr * BN + cc, src, bytes);
@@ -73,19 +74,20 @@ __device__ __forceinline__ void load_slab(double* As, double* Bs, const double* 
 
 // 256 threads; thread (tx = tid % 16, ty = tid / 16) owns rows ty + 16*i (i < 4)
 // and cols tx + 16*j (j < BN/16) of the 64 x BN output tile.
-template <int MODE, int BN>
+template <typename T, int MODE, int BN>
 __global__ void __launch_bounds__(THREADS)
-gemm_f64_kernel(int M, int N, int K, const double* __restrict__ A, size_t lda,
-                const double* __restrict__ B, size_t ldb, double* __restrict__ C, size_t ldc) {
+gemm_f64_kernel(int M, int N, int K, const T* __restrict__ A, size_t lda,
+                const T* __restrict__ B, size_t ldb, T* __restrict__ C, size_t ldc) {
   constexpr int TN = BN / 16;
-  extern __shared__ __align__(16) double smem[];
-  double* As = smem;                 // [2][BM][BK]
-  double* Bs = smem + 2 * BM * BK;   // [2][BK][BN]
+  extern __shared__ __align__(16) double smem_raw[];
+  T* smem = reinterpret_cast<T*>(smem_raw);
+  T* As = smem;                 // [2][BM][BK]
+  T* Bs = smem + 2 * BM * BK;   // [2][BK][BN]
 
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
 
-  double acc[4][TN];
+  T acc[4][TN];
   constexpr bool ZERO = (MODE == GM_FMA_ZERO || MODE == GM_EXACT_ZERO);
   constexpr bool DESC = (MODE == GM_EXACT_SUB_DESC || MODE == GM_FMA_SUB_DESC);
 #pragma unroll
@@ -93,36 +95,36 @@ gemm_f64_kernel(int M, int N, int K, const double* __restrict__ A, size_t lda,
 #pragma unroll
     for (int j = 0; j < TN; j++) {
       int r = m0 + ty + 16 * i, c = n0 + tx + 16 * j;
-      acc[i][j] = (!ZERO && r < M && c < N) ? C[(size_t)r * ldc + c] : 0.0;
+      acc[i][j] = (!ZERO && r < M && c < N) ? C[(size_t)r * ldc + c] : T(0);
     }
 
   const int nslab = (K + BK - 1) / BK;
   // Slab order: ascending, or descending for back substitution.
   auto slab_k0 = [&](int s) { return DESC ? (nslab - 1 - s) * BK : s * BK; };
 
-  load_slab<BN>(As, Bs, A, lda, B, ldb, M, N, K, m0, n0, slab_k0(0));
+  load_slab<T, BN>(As, Bs, A, lda, B, ldb, M, N, K, m0, n0, slab_k0(0));
   cp_async_commit();
 
   for (int s = 0; s < nslab; s++) {
     const int buf = s & 1;
     if (s + 1 < nslab) {
-      load_slab<BN>(As + (buf ^ 1) * BM * BK, Bs + (buf ^ 1) * BK * BN, A, lda, B, ldb, M, N, K,
-                    m0, n0, slab_k0(s + 1));
+      load_slab<T, BN>(As + (buf ^ 1) * BM * BK, Bs + (buf ^ 1) * BK * BN, A, lda, B, ldb, M, N,
+                       K, m0, n0, slab_k0(s + 1));
       cp_async_commit();
       cp_async_wait_1();
     } else {
       cp_async_wait_all();
     }
     __syncthreads();
-    const double* as = As + buf * BM * BK;
-    const double* bs = Bs + buf * BK * BN;
+    const T* as = As + buf * BM * BK;
+    const T* bs = Bs + buf * BK * BN;
     const int k0 = slab_k0(s);
     const int kn = min(BK, K - k0);
     if (kn == BK) {
 #pragma unroll 8
       for (int kk = 0; kk < BK; kk++) {
         const int k = DESC ? (BK - 1 - kk) : kk;
-        double a[4], b[TN];
+        T a[4], b[TN];
 #pragma unroll
         for (int i = 0; i < 4; i++) a[i] = as[(ty + 16 * i) * BK + k];
 #pragma unroll
@@ -145,7 +147,7 @@ gemm_f64_kernel(int M, int N, int K, const double* __restrict__ A, size_t lda,
       // Ragged last slab: only the kn valid k are applied (no padded terms).
       for (int kk = 0; kk < kn; kk++) {
         const int k = DESC ? (kn - 1 - kk) : kk;
-        double a[4], b[TN];
+        T a[4], b[TN];
 #pragma unroll
         for (int i = 0; i < 4; i++) a[i] = as[(ty + 16 * i) * BK + k];
 #pragma unroll
@@ -179,23 +181,22 @@ gemm_f64_kernel(int M, int N, int K, const double* __restrict__ A, size_t lda,
 
 constexpr size_t GEMM_SMEM_CAP = 96 * 1024;
 
-template <int MODE, int BN>
-la_status launch_mode(la_ctx ctx, int M, int N, int K, const double* A, size_t lda,
-                      const double* B, size_t ldb, double* C, size_t ldc, size_t min_smem) {
+template <int MODE, int BN, typename T = double>
+la_status launch_mode(la_ctx ctx, int M, int N, int K, const T* A, size_t lda, const T* B,
+                      size_t ldb, T* C, size_t ldc, size_t min_smem) {
   const size_t smem =
-      std::min(GEMM_SMEM_CAP,
-               std::max((size_t)2 * (BM * BK + BK * BN) * sizeof(double), min_smem));
+      std::min(GEMM_SMEM_CAP, std::max((size_t)2 * (BM * BK + BK * BN) * sizeof(T), min_smem));
   static bool configured = false;  // one attribute call per instantiation
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(gemm_f64_kernel<MODE, BN>,
+    cudaError_t e = cudaFuncSetAttribute(gemm_f64_kernel<T, MODE, BN>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)GEMM_SMEM_CAP);
     if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaFuncSetAttribute(gemm)");
     configured = true;
   }
   dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
-  gemm_f64_kernel<MODE, BN><<<grid, THREADS, smem, ctx->stream>>>(M, N, K, A, lda, B, ldb, C,
-                                                                  ldc);
+  gemm_f64_kernel<T, MODE, BN><<<grid, THREADS, smem, ctx->stream>>>(M, N, K, A, lda, B, ldb, C,
+                                                                     ldc);
   ctx->launches++;
   return la_check_launch(ctx, "gemm_f64_kernel");
 }
@@ -227,4 +228,14 @@ la_status launch_gemm(la_ctx ctx, int mode, int M, int N, int K, const double* A
   if (K <= 0 && mode != GM_FMA_ZERO && mode != GM_EXACT_ZERO) return LA_OK;
   if (N <= 16) return launch_bn<16>(ctx, mode, M, N, K, A, lda, B, ldb, C, ldc, min_smem);
   return launch_bn<64>(ctx, mode, M, N, K, A, lda, B, ldb, C, ldc, min_smem);
+}
+
+// FP32 form (FAST arithmetic only) for the panels and triangular updates of the
+// mixed-precision LU. Pointers 16-byte aligned, pitches multiples of 4.
+la_status launch_gemm_f32(la_ctx ctx, int mode, int M, int N, int K, const float* A, size_t lda,
+                          const float* B, size_t ldb, float* C, size_t ldc) {
+  if (M <= 0 || N <= 0 || K <= 0) return LA_OK;
+  if (mode != GM_FMA_SUB) return LA_INVALID;
+  if (N <= 16) return launch_mode<GM_FMA_SUB, 16, float>(ctx, M, N, K, A, lda, B, ldb, C, ldc, 0);
+  return launch_mode<GM_FMA_SUB, 64, float>(ctx, M, N, K, A, lda, B, ldb, C, ldc, 0);
 }

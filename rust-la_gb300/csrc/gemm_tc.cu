@@ -1,0 +1,337 @@
+// Tensor-core trailing update of the mixed-precision LU:
+//   C (M x N, f32, row-major) -= alpha * A (M x K, 16-bit) * B^T (B: N x K, 16-bit)
+// with A and B both K-major (K contiguous), in BF16 or FP16, accumulated in
+// FP32 by tcgen05.mma into tensor memory.
+//
+// One CTA per 128 x 128 output tile, 128 threads:
+//   warp 0 lane 0 : TMA producer. 64-deep K chunks of A and B (16 KB each,
+//                   128B swizzle) into a 3-stage ring, one mbarrier per stage
+//   warp 1 lane 0 : MMA issuer. 4 x tcgen05.mma (M=128, N=128, K=16) per chunk;
+//                   tcgen05.commit releases the stage
+//   all 4 warps   : epilogue. tcgen05.ld of the warp's 32 TMEM lanes (rows),
+//                   then C -= alpha * acc
+// Shared memory is 3 x 32 KB per CTA, so two CTAs share an SM and one CTA's
+// epilogue overlaps the other's MMAs. Every mbarrier wait is bounded (2 s by
+// %globaltimer). On timeout the CTA records an error, waits (bounded) for its
+// own copies in flight, frees its tensor memory and returns.
+#include <cuda.h>
+
+#include "la_internal.cuh"
+
+namespace {
+
+constexpr int TM = 128, TN = 128, TK = 64;
+constexpr int STAGES = 3;
+constexpr int TC_THREADS = 128;
+constexpr uint32_t A_BYTES = TM * TK * 2;  // 16 KB
+constexpr uint32_t B_BYTES = TN * TK * 2;  // 16 KB
+constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr size_t TC_SMEM = (size_t)STAGES * STAGE_BYTES + 1024;  // + alignment slack
+constexpr uint32_t TMEM_COLS = 128;
+constexpr unsigned long long TC_WAIT_NS = 2000000000ull;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait on an mbarrier phase. false: gave up (timeout or error word set).
+__device__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err) {
+  unsigned long long t0 = 0;
+  for (unsigned i = 0;; i++) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 255u) == 255u) {
+      if (*reinterpret_cast<volatile int*>(err) != 0) return false;
+      unsigned long long now = gtimer();
+      if (t0 == 0) t0 = now;
+      else if (now - t0 > TC_WAIT_NS) {
+        atomicCAS(err, 0, (int)DERR_TC_TIMEOUT);
+        return false;
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row
+// core-matrix groups 1024 bytes apart (SBO); LBO unused for this layout.
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(1024u >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+// Instruction descriptor of kind::f16: D f32, A/B bf16 (1) or f16 (0), both
+// K-major, N = 128, M = 128.
+__host__ __device__ constexpr uint32_t idesc_f16(uint32_t ab_fmt) {
+  return (1u << 4) | (ab_fmt << 7) | (ab_fmt << 10) | ((uint32_t)(TN >> 3) << 17) |
+         ((uint32_t)(TM >> 4) << 24);
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+tc_update_kernel(const __grid_constant__ CUtensorMap tmap_a,
+                 const __grid_constant__ CUtensorMap tmap_b, float* __restrict__ C, size_t ldc,
+                 int M, int N, int K, const float* __restrict__ alpha_ptr, uint32_t idesc,
+                 int* err) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], done;
+  __shared__ uint32_t tmem_holder;
+  __shared__ int s_fail;
+
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
+  const int nk = (K + TK - 1) / TK;
+
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(&done, 1);
+    s_fail = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_holder)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tmem_holder;
+
+  int issued = 0;  // chunks whose TMA the producer issued
+  if (warp == 0 && lane == 0) {
+    for (int kc = 0; kc < nk; kc++) {
+      const int s = kc % STAGES;
+      if (kc >= STAGES && !mbar_wait(&empty[s], (uint32_t)((kc / STAGES - 1) & 1), err)) {
+        s_fail = 1;
+        break;
+      }
+      unsigned char* sa = smem + s * STAGE_BYTES;
+      unsigned char* sb = sa + A_BYTES;
+      mbar_expect_tx(&full[s], STAGE_BYTES);
+      tma_load_2d(sa, &tmap_a, kc * TK, m0, &full[s]);
+      tma_load_2d(sb, &tmap_b, kc * TK, n0, &full[s]);
+      issued = kc + 1;
+    }
+  } else if (warp == 1 && lane == 0) {
+    bool ok = true;
+    for (int kc = 0; kc < nk; kc++) {
+      const int s = kc % STAGES;
+      if (!mbar_wait(&full[s], (uint32_t)((kc / STAGES) & 1), err)) {
+        s_fail = 1;
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t sa = smem_u32(smem + s * STAGE_BYTES);
+      const uint32_t sb = sa + A_BYTES;
+#pragma unroll
+      for (int k = 0; k < TK / 16; k++) {
+        const uint64_t ad = sdesc(sa + k * 32);
+        const uint64_t bd = sdesc(sb + k * 32);
+        const uint32_t acc = (kc > 0 || k > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              smem_u32(&empty[s]))
+          : "memory");
+    }
+    if (ok)
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              smem_u32(&done))
+          : "memory");
+  }
+  __syncwarp();
+
+  // Epilogue: every thread owns one accumulator row (TMEM lane). The decision
+  // is block-uniform so the warp-collective tcgen05.ld runs on full warps.
+  const bool waited = mbar_wait(&done, 0, err);
+  const bool have = __syncthreads_and(waited ? 1 : 0) && !s_fail;
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if (have) {
+    const float alpha = *alpha_ptr;
+    const int row = m0 + warp * 32 + lane;
+#pragma unroll 1
+    for (int cc = 0; cc < TN / 32; cc++) {
+      uint32_t r[32];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cc * 32);
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+          "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+            "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+            "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+            "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+            "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+            "=r"(r[31])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      const int c0 = n0 + cc * 32;
+      if (row < M) {
+        float* crow = C + (size_t)row * ldc + c0;
+        if (c0 + 32 <= N) {
+#pragma unroll
+          for (int j = 0; j < 32; j += 4) {
+            float4 v = *reinterpret_cast<float4*>(crow + j);
+            v.x -= alpha * __uint_as_float(r[j]);
+            v.y -= alpha * __uint_as_float(r[j + 1]);
+            v.z -= alpha * __uint_as_float(r[j + 2]);
+            v.w -= alpha * __uint_as_float(r[j + 3]);
+            *reinterpret_cast<float4*>(crow + j) = v;
+          }
+        } else {
+          for (int j = 0; j < 32; j++)
+            if (c0 + j < N) crow[j] -= alpha * __uint_as_float(r[j]);
+        }
+      }
+    }
+  }
+  // On failure: wait (bounded) for this CTA's copies still in flight.
+  if (!have && warp == 0 && lane == 0) {
+    for (int kc = 0; kc < issued; kc++) {
+      const int s = kc % STAGES;
+      unsigned long long t0 = gtimer();
+      while (!mbar_try_wait(&full[s], (uint32_t)((kc / STAGES) & 1)))
+        if (gtimer() - t0 > TC_WAIT_NS) break;
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TMEM_COLS));
+}
+
+// Driver entry point for tensor-map encoding, fetched once through the runtime
+// (no link-time dependency on libcuda).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn get_encoder(la_ctx ctx) {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e =
+        cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p) {
+      if (ctx) ctx->last_error = "cuTensorMapEncodeTiled unavailable";
+      return nullptr;
+    }
+    fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+// 2-D K-major operand map: `rows` rows of `k` 16-bit elements, pitch `ld`
+// elements (ld * 2 bytes must be a multiple of 16), box 64 (K) x 128 (rows).
+bool encode_operand(la_ctx ctx, CUtensorMap* map, const void* base, int fmt, size_t rows,
+                    size_t k, size_t ld) {
+  EncodeTiledFn enc = get_encoder(ctx);
+  if (!enc) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)k, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+  cuuint32_t box[2] = {(cuuint32_t)TK, (cuuint32_t)TM};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(map, fmt == LA_LOWP_BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
+                                            : CU_TENSOR_MAP_DATA_TYPE_FLOAT16,
+                   2, const_cast<void*>(base), dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    if (ctx) ctx->last_error = "cuTensorMapEncodeTiled failed";
+    return false;
+  }
+  return true;
+}
+
+}  // namespace
+
+// C (M x N f32, pitch ldc, 16-byte aligned rows) -= alpha * A * B^T where A is
+// M x K and B is N x K, both 16-bit K-major with pitches lda, ldb (multiples of
+// 8 elements, 16-byte aligned bases). alpha is read on the device.
+la_status launch_tc_update(la_ctx ctx, cudaStream_t stream, int fmt, int M, int N, int K,
+                           const void* A, size_t lda, const void* B, size_t ldb, float* C,
+                           size_t ldc, const float* d_alpha) {
+  if (M <= 0 || N <= 0 || K <= 0) return LA_OK;
+  if ((lda % 8) || (ldb % 8) || (ldc % 4) || (reinterpret_cast<uintptr_t>(A) % 16) ||
+      (reinterpret_cast<uintptr_t>(B) % 16) || (reinterpret_cast<uintptr_t>(C) % 16))
+    return LA_INVALID;
+  CUtensorMap ta, tb;
+  if (!encode_operand(ctx, &ta, A, fmt, (size_t)M, (size_t)K, lda)) return LA_CUDA_ERROR;
+  if (!encode_operand(ctx, &tb, B, fmt, (size_t)N, (size_t)K, ldb)) return LA_CUDA_ERROR;
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(tc_update_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
+    if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaFuncSetAttribute(tc_update)");
+    configured = true;
+  }
+  dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM);
+  const uint32_t idesc = idesc_f16(fmt == LA_LOWP_BF16 ? 1u : 0u);
+  tc_update_kernel<<<grid, TC_THREADS, TC_SMEM, stream>>>(ta, tb, C, ldc, M, N, K, d_alpha, idesc,
+                                                           ctx->d_err);
+  ctx->launches++;
+  return la_check_launch(ctx, "tc_update_kernel");
+}
+
+extern "C" la_status la_lowp_update_device(la_ctx ctx, int fmt, size_t m, size_t n, size_t k,
+                                           const void* d_a16, size_t lda, const void* d_b16,
+                                           size_t ldb, float* d_c, size_t ldc, float alpha) {
+  if (!ctx || !d_a16 || !d_b16 || !d_c) return LA_INVALID;
+  if (fmt != LA_LOWP_BF16 && fmt != LA_LOWP_FP16) return LA_INVALID;
+  if (m > INT32_MAX || n > INT32_MAX || k > INT32_MAX) return LA_UNSUPPORTED;
+  LA_CUDA(ctx, cudaSetDevice(ctx->device));
+  float* d_alpha = reinterpret_cast<float*>(ctx->d_small + 4);
+  LA_CUDA(ctx, cudaMemcpyAsync(d_alpha, &alpha, sizeof(float), cudaMemcpyHostToDevice,
+                               ctx->stream));
+  LA_TRY(launch_tc_update(ctx, ctx->stream, fmt, (int)m, (int)n, (int)k, d_a16, lda, d_b16, ldb,
+                          d_c, ldc, d_alpha));
+  return la_sync_and_check(ctx, "lowp update");
+}

@@ -1,6 +1,8 @@
 // Internal declarations shared by the liblagpu translation units.
 #pragma once
 
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -34,8 +36,12 @@ constexpr int MAX_PANEL_W = 64;
 enum DeviceErr : int {
   DERR_NONE = 0,
   DERR_PANEL_TIMEOUT = 1,
-  DERR_PANEL_CAPACITY = 2
+  DERR_PANEL_CAPACITY = 2,
+  DERR_TC_TIMEOUT = 3
 };
+
+// 16-bit operand formats of the tensor-core update.
+enum LowpFormat : int { LA_LOWP_BF16 = 1, LA_LOWP_FP16 = 2 };
 
 struct la_context {
   int device = 0;
@@ -81,6 +87,11 @@ struct la_lu_handle {
   int pospivsign = 1;
   int zero_diag = 0;             // an exact 0 on U's diagonal (j < min(m,n))
   int arith = LA_ARITH_FAST;
+  // Mixed-precision factorization: FP32 factors (d_lu32, pitch ld32) of the
+  // FP64 matrix kept in d_lu (used for residuals); null for plain FP64.
+  float* d_lu32 = nullptr;
+  size_t ld32 = 0;
+  int lowp = 0;                  // LA_PREC_* of the trailing update
 };
 
 
@@ -104,6 +115,9 @@ la_status la_sync_and_check(la_ctx ctx, const char* what);
   } while (0)
 
 // Kernel launchers (one per translation unit of kernels).
+la_status launch_tc_update(la_ctx ctx, cudaStream_t stream, int fmt, int M, int N, int K,
+                           const void* A, size_t lda, const void* B, size_t ldb, float* C,
+                           size_t ldc, const float* d_alpha);
 // min_smem > 0 raises the GEMM's dynamic shared memory so fewer CTAs share an
 // SM (room for a concurrent panel CTA).
 la_status launch_gemm(la_ctx ctx, int mode, int M, int N, int K, const double* A, size_t lda,
@@ -114,6 +128,15 @@ la_status launch_laswp(la_ctx ctx, bool exact, double* A, double* S, size_t ld, 
                        int jb);
 la_status launch_trsm_rowpanel(la_ctx ctx, bool exact, double* A, double* S, size_t ld, int j0,
                                int jb, int c_begin, int c_end);
+la_status launch_panel_f32(la_ctx ctx, cudaStream_t stream, float* A, size_t ld, int m, int j0,
+                           int jb, int* d_ipiv, unsigned* bar_base);
+la_status launch_laswp_f32(la_ctx ctx, float* A, size_t ld, int n, int j0, int jb);
+la_status launch_trsm_rowpanel_f32(la_ctx ctx, float* A, size_t ld, int j0, int jb, int c_begin,
+                                   int c_end);
+la_status launch_gemm_f32(la_ctx ctx, int mode, int M, int N, int K, const float* A, size_t lda,
+                          const float* B, size_t ldb, float* C, size_t ldc);
+la_status launch_lu_solve_f32(la_ctx ctx, const float* LU, size_t ld, float* X, size_t ldx, int n,
+                              int nrhs);
 la_status launch_lu_finish(la_ctx ctx, la_lu h, int* d_flags);
 // Enqueues the whole factorization of h (no readback, no synchronization);
 // lu_finish writes {pospivsign, zero-on-diagonal} to d_flags.

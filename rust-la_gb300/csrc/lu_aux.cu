@@ -8,16 +8,17 @@ namespace {
 // [c_begin, c_end) of one matrix. All sources are read into shared memory
 // before any destination is written, so the moves act as one permutation.
 constexpr int SW_COLS = 32;
+template <typename T>
 __global__ void __launch_bounds__(256)
-laswp_kernel(double* M0, double* M1, double* M2, size_t ld, int b0, int e0, int b1, int e1,
+laswp_kernel(T* M0, T* M1, T* M2, size_t ld, int b0, int e0, int b1, int e1,
              int b2, int e2, const int* __restrict__ swaps) {
-  __shared__ double tmp[2 * MAX_PANEL_W][SW_COLS];
+  __shared__ T tmp[2 * MAX_PANEL_W][SW_COLS];
   const int cnt = swaps[0];
   if (cnt == 0) return;
   const int* dst = swaps + 1;
   const int* src = swaps + 1 + 2 * MAX_PANEL_W;
   // blockIdx.y selects the segment.
-  double* M;
+  T* M;
   int cb, ce;
   if (blockIdx.y == 0) { M = M0; cb = b0; ce = e0; }
   else if (blockIdx.y == 1) { M = M1; cb = b1; ce = e1; }
@@ -41,18 +42,20 @@ laswp_kernel(double* M0, double* M1, double* M2, size_t ld, int b0, int e0, int 
 // in ascending k, like lu.rs:124-128 (EXACT: s += l*u, u = a - s) or with FMA.
 constexpr int TR_COLS = 32;
 constexpr int LP = MAX_PANEL_W + 1;  // padded row of the triangular block in shared memory
-constexpr size_t TRSM_SMEM_FAST = (size_t)(MAX_PANEL_W * LP + MAX_PANEL_W * TR_COLS) * 8;
-constexpr size_t TRSM_SMEM_EXACT = TRSM_SMEM_FAST + (size_t)MAX_PANEL_W * TR_COLS * 8;
+template <typename T>
+constexpr size_t trsm_smem(bool exact) {
+  return (size_t)(MAX_PANEL_W * LP + MAX_PANEL_W * TR_COLS * (exact ? 2 : 1)) * sizeof(T);
+}
 
-template <bool EXACT>
+template <typename T, bool EXACT>
 __global__ void __launch_bounds__(256)
-trsm_rowpanel_kernel(double* A, const double* S, size_t ld, int j0, int jb, int c_begin,
-                     int c_end) {
-  extern __shared__ __align__(16) double dsm[];
-  double(*L)[LP] = reinterpret_cast<double(*)[LP]>(dsm);
-  double(*xa)[TR_COLS] = reinterpret_cast<double(*)[TR_COLS]>(dsm + MAX_PANEL_W * LP);
-  double(*xs)[TR_COLS] =
-      reinterpret_cast<double(*)[TR_COLS]>(dsm + MAX_PANEL_W * LP + MAX_PANEL_W * TR_COLS);
+trsm_rowpanel_kernel(T* A, const T* S, size_t ld, int j0, int jb, int c_begin, int c_end) {
+  extern __shared__ __align__(16) double dsm_raw[];
+  T* dsm = reinterpret_cast<T*>(dsm_raw);
+  T(*L)[LP] = reinterpret_cast<T(*)[LP]>(dsm);
+  T(*xa)[TR_COLS] = reinterpret_cast<T(*)[TR_COLS]>(dsm + MAX_PANEL_W * LP);
+  T(*xs)[TR_COLS] =
+      reinterpret_cast<T(*)[TR_COLS]>(dsm + MAX_PANEL_W * LP + MAX_PANEL_W * TR_COLS);
   const int tx = threadIdx.x % TR_COLS, ty = threadIdx.x / TR_COLS;  // ty 0..7
   const int c = c_begin + blockIdx.x * TR_COLS + tx;
   const bool ok = c < c_end;
@@ -62,8 +65,8 @@ trsm_rowpanel_kernel(double* A, const double* S, size_t ld, int j0, int jb, int 
   }
   for (int i = ty; i < jb; i += 8) {
     size_t off = (size_t)(j0 + i) * ld + c;
-    xa[i][tx] = ok ? A[off] : 0.0;
-    if (EXACT) xs[i][tx] = ok ? S[off] : 0.0;
+    xa[i][tx] = ok ? A[off] : T(0);
+    if (EXACT) xs[i][tx] = ok ? S[off] : T(0);
   }
   __syncthreads();
   for (int k = 0; k < jb; k++) {
@@ -72,7 +75,7 @@ trsm_rowpanel_kernel(double* A, const double* S, size_t ld, int j0, int jb, int 
       xa[k][tx] = __dsub_rn(xa[k][tx], xs[k][tx]);
     }
     __syncthreads();
-    const double uk = xa[k][tx];
+    const T uk = xa[k][tx];
     for (int i = ty; i < jb; i += 8) {
       if (i <= k) continue;
       if (EXACT)
@@ -90,8 +93,9 @@ trsm_rowpanel_kernel(double* A, const double* S, size_t ld, int j0, int jb, int 
 // The swap list (LAPACK ipiv form) is replayed in order on a permutation
 // vector (lu.rs:147-149), the sign flips once per real swap (lu.rs:151), and
 // U's diagonal is scanned for an exact zero (lu.rs:177).
+template <typename T>
 __global__ void lu_finish_kernel(const int* __restrict__ ipiv, uint64_t* piv, int m, int kmin,
-                                 const double* LU, size_t ld, int* flags, int smem_rows) {
+                                 const T* LU, size_t ld, int* flags, int smem_rows) {
   extern __shared__ int sperm[];  // permutation in shared memory when m fits
   __shared__ int zero;
   if (threadIdx.x == 0) zero = 0;
@@ -103,7 +107,7 @@ __global__ void lu_finish_kernel(const int* __restrict__ ipiv, uint64_t* piv, in
   }
   __syncthreads();
   for (int j = threadIdx.x; j < kmin; j += blockDim.x)
-    if (LU[(size_t)j * ld + j] == 0.0) atomicOr(&zero, 1);
+    if (LU[(size_t)j * ld + j] == T(0)) atomicOr(&zero, 1);
   if (threadIdx.x == 0) {
     int pos = 1;
     for (int j = 0; j < kmin; j++) {
@@ -199,10 +203,12 @@ __global__ void copy2d_kernel(const double* __restrict__ src, size_t lds, double
 void configure_smem_attrs() {
   static bool done = false;
   if (done) return;
-  cudaFuncSetAttribute(trsm_rowpanel_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)TRSM_SMEM_EXACT);
-  cudaFuncSetAttribute(trsm_rowpanel_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)TRSM_SMEM_FAST);
+  cudaFuncSetAttribute(trsm_rowpanel_kernel<double, true>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)trsm_smem<double>(true));
+  cudaFuncSetAttribute(trsm_rowpanel_kernel<double, false>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)trsm_smem<double>(false));
+  cudaFuncSetAttribute(trsm_rowpanel_kernel<float, false>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)trsm_smem<float>(false));
   done = true;
 }
 
@@ -214,32 +220,51 @@ int grid_for(la_ctx ctx, size_t total) {
 
 }  // namespace
 
-la_status launch_laswp(la_ctx ctx, bool exact, double* A, double* S, size_t ld, int n, int j0,
-                       int jb) {
+template <typename T>
+la_status launch_laswp_t(la_ctx ctx, cudaStream_t stream, bool exact, T* A, T* S, size_t ld,
+                         int n, int j0, int jb) {
   const int j1 = j0 + jb;
   const int left = j0, right = n - j1;
   const int gx = std::max((left + SW_COLS - 1) / SW_COLS, (right + SW_COLS - 1) / SW_COLS);
   if (gx == 0) return LA_OK;
   dim3 grid(gx, exact ? 3 : 2);
-  laswp_kernel<<<grid, 256, 0, ctx->stream>>>(A, A, exact ? S : nullptr, ld, 0, j0, j1, n, j1, n,
-                                              ctx->d_swaps);
+  laswp_kernel<T><<<grid, 256, 0, stream>>>(A, A, exact ? S : nullptr, ld, 0, j0, j1, n, j1, n,
+                                            ctx->d_swaps);
   ctx->launches++;
   return la_check_launch(ctx, "laswp_kernel");
 }
 
-la_status launch_trsm_rowpanel(la_ctx ctx, bool exact, double* A, double* S, size_t ld, int j0,
-                               int jb, int c_begin, int c_end) {
+la_status launch_laswp(la_ctx ctx, bool exact, double* A, double* S, size_t ld, int n, int j0,
+                       int jb) {
+  return launch_laswp_t<double>(ctx, ctx->stream, exact, A, S, ld, n, j0, jb);
+}
+la_status launch_laswp_f32(la_ctx ctx, float* A, size_t ld, int n, int j0, int jb) {
+  return launch_laswp_t<float>(ctx, ctx->stream, false, A, nullptr, ld, n, j0, jb);
+}
+
+template <typename T>
+la_status launch_trsm_t(la_ctx ctx, bool exact, T* A, T* S, size_t ld, int j0, int jb,
+                        int c_begin, int c_end) {
   if (c_end <= c_begin) return LA_OK;
-  dim3 grid((c_end - c_begin + TR_COLS - 1) / TR_COLS);
   configure_smem_attrs();
+  dim3 grid((c_end - c_begin + TR_COLS - 1) / TR_COLS);
   if (exact)
-    trsm_rowpanel_kernel<true><<<grid, 256, TRSM_SMEM_EXACT, ctx->stream>>>(A, S, ld, j0, jb,
-                                                                            c_begin, c_end);
+    trsm_rowpanel_kernel<T, true><<<grid, 256, trsm_smem<T>(true), ctx->stream>>>(A, S, ld, j0, jb,
+                                                                               c_begin, c_end);
   else
-    trsm_rowpanel_kernel<false><<<grid, 256, TRSM_SMEM_FAST, ctx->stream>>>(A, S, ld, j0, jb,
-                                                                            c_begin, c_end);
+    trsm_rowpanel_kernel<T, false><<<grid, 256, trsm_smem<T>(false), ctx->stream>>>(
+        A, S, ld, j0, jb, c_begin, c_end);
   ctx->launches++;
   return la_check_launch(ctx, "trsm_rowpanel_kernel");
+}
+
+la_status launch_trsm_rowpanel(la_ctx ctx, bool exact, double* A, double* S, size_t ld, int j0,
+                               int jb, int c_begin, int c_end) {
+  return launch_trsm_t<double>(ctx, exact, A, S, ld, j0, jb, c_begin, c_end);
+}
+la_status launch_trsm_rowpanel_f32(la_ctx ctx, float* A, size_t ld, int j0, int jb, int c_begin,
+                                   int c_end) {
+  return launch_trsm_t<float>(ctx, false, A, nullptr, ld, j0, jb, c_begin, c_end);
 }
 
 la_status launch_lu_finish(la_ctx ctx, la_lu h, int* d_flags) {
@@ -247,13 +272,19 @@ la_status launch_lu_finish(la_ctx ctx, la_lu h, int* d_flags) {
   const int smem_rows = 50000;  // 200 KB of int32 (opt-in); larger m replays in global memory
   static bool configured = false;
   if (!configured) {
-    cudaFuncSetAttribute(lu_finish_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(lu_finish_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         smem_rows * (int)sizeof(int));
+    cudaFuncSetAttribute(lu_finish_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          smem_rows * (int)sizeof(int));
     configured = true;
   }
   const size_t smem = (size_t)std::min((int)h->m, smem_rows) * sizeof(int);
-  lu_finish_kernel<<<1, 1024, smem, ctx->stream>>>(h->d_ipiv, h->d_piv, (int)h->m, kmin, h->d_lu,
-                                                   h->ld, d_flags, smem_rows);
+  if (h->d_lu32)
+    lu_finish_kernel<float><<<1, 1024, smem, ctx->stream>>>(h->d_ipiv, h->d_piv, (int)h->m, kmin,
+                                                            h->d_lu32, h->ld32, d_flags, smem_rows);
+  else
+    lu_finish_kernel<double><<<1, 1024, smem, ctx->stream>>>(h->d_ipiv, h->d_piv, (int)h->m, kmin,
+                                                             h->d_lu, h->ld, d_flags, smem_rows);
   ctx->launches++;
   return la_check_launch(ctx, "lu_finish_kernel");
 }

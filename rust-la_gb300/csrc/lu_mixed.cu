@@ -1,0 +1,429 @@
+// Mixed-precision LU with FP64 iterative refinement (not in the reference; it
+// replaces LUDecomposition::new + solve, lu.rs:104-278, for well- to
+// ill-conditioned systems at a fraction of the FP64 cost).
+//
+// Factorization of an FP32 copy of A, two-level blocked right-looking:
+//   outer panels of width WO = 256, each factored by the FP32 form of the
+//   plain path (cooperative panel kernel, row swaps, row-panel triangular update
+//   and FP32 SIMT updates, inner width 64);
+//   outer row-panel triangular update U12 = L11^-1 A12 in FP32;
+//   trailing update A22 -= L21 * U12 on the tensor cores (gemm_tc.cu) with
+//   BF16 or FP16 operands and FP32 accumulation, or in FP32 SIMT (LA_PREC_FP32).
+//   FP16 operands use a per-panel power-of-two scale of U12 (L's entries are
+//   bounded by 1 under partial pivoting); the scale is undone in the epilogue.
+// Solve: x0 = 0, r = b; repeat d = LU32 \ (r scaled to unit max per column),
+// x += d (FP64), r = b - A x in FP64 (A kept in FP64), until the normwise
+// backward error max_j ||r_j|| / (||A|| ||x_j|| + ||b_j||) <= tol or the
+// refinement stalls.
+#include "la_internal.cuh"
+
+namespace {
+
+constexpr int WO = 256;  // outer panel width (K of the tensor-core update)
+constexpr int WI = 64;   // inner panel width
+
+size_t pad8(size_t x) { return (x + 7) & ~size_t(7); }
+
+__global__ void f64_to_f32_kernel(const double* __restrict__ src, size_t lds, float* __restrict__ dst,
+                                  size_t ldd, int rows, int cols) {
+  size_t total = (size_t)rows * cols;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    int r = (int)(i / cols), c = (int)(i % cols);
+    dst[(size_t)r * ldd + c] = (float)src[(size_t)r * lds + c];
+  }
+}
+
+template <int FMT>
+__device__ __forceinline__ uint16_t to16(float v) {
+  if (FMT == LA_LOWP_BF16) {
+    __nv_bfloat16 h = __float2bfloat16_rn(v);
+    return *reinterpret_cast<uint16_t*>(&h);
+  } else {
+    __half h = __float2half_rn(v);
+    return *reinterpret_cast<uint16_t*>(&h);
+  }
+}
+
+// L21 (rows x k, pitch lds) -> 16-bit K-major (pitch ldd).
+template <int FMT>
+__global__ void pack_l_kernel(const float* __restrict__ src, size_t lds, uint16_t* __restrict__ dst,
+                              size_t ldd, int rows, int k) {
+  size_t total = (size_t)rows * ldd;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    int r = (int)(i / ldd), c = (int)(i % ldd);
+    dst[i] = c < k ? to16<FMT>(src[(size_t)r * lds + c]) : (uint16_t)0;
+  }
+}
+
+__device__ __forceinline__ void atomic_max_nonneg_f(float* a, float v) {
+  atomicMax(reinterpret_cast<unsigned*>(a), __float_as_uint(v));
+}
+
+// max |U12| for the FP16 scale (stat[0] must start at 0).
+__global__ void absmax_kernel(const float* __restrict__ src, size_t lds, int rows, int cols,
+                              float* stat) {
+  float m = 0.f;
+  size_t total = (size_t)rows * cols;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    int r = (int)(i / cols), c = (int)(i % cols);
+    float v = fabsf(src[(size_t)r * lds + c]);
+    if (v > m) m = v;  // NaN never raises the max
+  }
+  for (int off = 16; off > 0; off >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, off));
+  if ((threadIdx.x & 31) == 0) atomic_max_nonneg_f(stat, m);
+}
+
+// U12 (k x cols, pitch lds) -> U^T 16-bit K-major (cols x ldd), times scale;
+// stat[1] receives alpha = 1/scale. 32x32 tiles through shared memory.
+template <int FMT>
+__global__ void pack_ut_kernel(const float* __restrict__ src, size_t lds, uint16_t* __restrict__ dst,
+                               size_t ldd, int k, int cols, float* stat) {
+  __shared__ float t[32][33];
+  float scale = 1.f;
+  if (FMT == LA_LOWP_FP16) {
+    // Largest magnitude to about 2^14: far from FP16 overflow, and products
+    // accumulate in FP32.
+    float mx = stat[0];
+    int e = 0;
+    if (mx > 0.f && mx < INFINITY) {
+      frexpf(mx, &e);
+      scale = ldexpf(1.f, 14 - e);
+    }
+  }
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0)
+    stat[1] = 1.f / scale;
+  const int c0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    int kk = k0 + i, cc = c0 + threadIdx.x;
+    t[i][threadIdx.x] = (kk < k && cc < cols) ? src[(size_t)kk * lds + cc] * scale : 0.f;
+  }
+  __syncthreads();
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    int cc = c0 + i, kk = k0 + threadIdx.x;
+    if (cc < cols && kk < (int)ldd) dst[(size_t)cc * ldd + kk] = to16<FMT>(t[threadIdx.x][i]);
+  }
+}
+
+__global__ void set_alpha_one(float* stat) { stat[0] = 0.f; stat[1] = 1.f; }
+
+// r = b - A x in FP64 for nrhs <= 16: one warp per row, each lane sums its
+// strided terms with FMA, the warp adds the lane sums in a tree. Also the
+// per-column maxima of |r| (into colmax[0..nrhs)).
+template <int R>
+__global__ void __launch_bounds__(256)
+residual_f64_kernel(const double* __restrict__ A, size_t lda, const double* __restrict__ X,
+                    size_t ldx, const double* __restrict__ B, size_t ldb, double* __restrict__ Rout,
+                    size_t ldr, int n, int nrhs, double* colmax) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int i = warp; i < n; i += nwarps) {
+    double s[R];
+#pragma unroll
+    for (int j = 0; j < R; j++) s[j] = 0.0;
+    const double* arow = A + (size_t)i * lda;
+    for (int k = lane; k < n; k += 32) {
+      const double a = arow[k];
+      const double* xr = X + (size_t)k * ldx;
+#pragma unroll
+      for (int j = 0; j < R; j++)
+        if (j < nrhs) s[j] = fma(a, xr[j], s[j]);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+      for (int j = 0; j < R; j++) s[j] += __shfl_down_sync(0xffffffffu, s[j], off);
+    if (lane == 0) {
+#pragma unroll
+      for (int j = 0; j < R; j++) {
+        if (j < nrhs) {
+          const double r = B[(size_t)i * ldb + j] - s[j];
+          Rout[(size_t)i * ldr + j] = r;
+          atomicMax(reinterpret_cast<unsigned long long*>(colmax + j),
+                    (unsigned long long)__double_as_longlong(fabs(r)));
+        }
+      }
+    }
+  }
+}
+
+// Column maxima of |M| (rows x cols) into out[0..cols) (non-negative IEEE bits).
+__global__ void colmax_kernel(const double* __restrict__ M, size_t ld, int rows, int cols,
+                              double* out) {
+  size_t total = (size_t)rows * cols;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    int r = (int)(i / cols), c = (int)(i % cols);
+    double v = fabs(M[(size_t)r * ld + c]);
+    atomicMax(reinterpret_cast<unsigned long long*>(out + c),
+              (unsigned long long)__double_as_longlong(v));
+  }
+}
+
+// ||A||_inf: max row sum of |a_ij|.
+__global__ void rownorm_kernel(const double* __restrict__ A, size_t lda, int n, double* out) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int i = warp; i < n; i += nwarps) {
+    double s = 0.0;
+    for (int k = lane; k < n; k += 32) s += fabs(A[(size_t)i * lda + k]);
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    if (lane == 0)
+      atomicMax(reinterpret_cast<unsigned long long*>(out),
+                (unsigned long long)__double_as_longlong(s));
+  }
+}
+
+// w32 = (r(piv,:) / rscale_j) in FP32, the right-hand side of a correction solve.
+__global__ void scale_permute_kernel(const uint64_t* __restrict__ piv, const double* __restrict__ R,
+                                     size_t ldr, const double* __restrict__ rscale,
+                                     float* __restrict__ W, size_t ldw, int n, int nrhs) {
+  size_t total = (size_t)n * nrhs;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    int r = (int)(i / nrhs), c = (int)(i % nrhs);
+    const double s = rscale[c];
+    const double v = R[(size_t)piv[r] * ldr + c];
+    W[(size_t)r * ldw + c] = s > 0 ? (float)(v / s) : 0.f;
+  }
+}
+
+// x += d * rscale_j (FP64 update of the solution).
+__global__ void update_x_kernel(double* __restrict__ X, size_t ldx, const float* __restrict__ D,
+                                size_t ldd, const double* __restrict__ rscale, int n, int nrhs) {
+  size_t total = (size_t)n * nrhs;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    int r = (int)(i / nrhs), c = (int)(i % nrhs);
+    X[(size_t)r * ldx + c] += (double)D[(size_t)r * ldd + c] * rscale[c];
+  }
+}
+
+int grid_for(la_ctx ctx, size_t total) {
+  size_t g = (total + 255) / 256;
+  return (int)std::max<size_t>(1, std::min(g, (size_t)ctx->sm_count * 8));
+}
+
+struct Buf {
+  la_ctx ctx;
+  void* p = nullptr;
+  explicit Buf(la_ctx c) : ctx(c) {}
+  ~Buf() { la_device_free(ctx, p); }
+  la_status alloc(size_t bytes) { return la_device_alloc(ctx, &p, bytes); }
+  template <typename T> T* as() { return static_cast<T*>(p); }
+};
+
+// Factors h->d_lu32 (m x n, pitch ld32) in place; pivots into h->d_ipiv.
+la_status mixed_factor(la_ctx ctx, la_lu h, int prec) {
+  const int m = (int)h->m, n = (int)h->n;
+  const int kmin = std::min(m, n);
+  float* A = h->d_lu32;
+  const size_t ld = h->ld32;
+  cudaStream_t st = ctx->stream;
+  LA_CUDA(ctx, cudaMemsetAsync(ctx->d_bar, 0, sizeof(unsigned), st));
+  unsigned bar_base = 0;
+  Buf lh(ctx), uh(ctx), stat(ctx);
+  const size_t ldk = pad8(WO);
+  if (prec != LA_PREC_FP32) {
+    LA_TRY(lh.alloc((size_t)m * ldk * 2 + 256));
+    LA_TRY(uh.alloc((size_t)n * ldk * 2 + 256));
+  }
+  LA_TRY(stat.alloc(256));
+  float* d_stat = stat.as<float>();
+
+  for (int j0 = 0; j0 < kmin; j0 += WO) {
+    const int jbo = std::min(WO, kmin - j0);
+    const int j1o = j0 + jbo;
+    // Inner blocked LU of the outer panel's columns.
+    for (int i0 = j0; i0 < j1o; i0 += WI) {
+      const int ib = std::min(WI, j1o - i0);
+      const int i1 = i0 + ib;
+      LA_TRY(launch_panel_f32(ctx, st, A, ld, m, i0, ib, h->d_ipiv, &bar_base));
+      LA_TRY(launch_laswp_f32(ctx, A, ld, n, i0, ib));
+      if (i1 < j1o) {
+        LA_TRY(launch_trsm_rowpanel_f32(ctx, A, ld, i0, ib, i1, j1o));
+        if (i1 < m)
+          LA_TRY(launch_gemm_f32(ctx, GM_FMA_SUB, m - i1, j1o - i1, ib, A + (size_t)i1 * ld + i0,
+                                 ld, A + (size_t)i0 * ld + i1, ld, A + (size_t)i1 * ld + i1, ld));
+      }
+    }
+    if (j1o >= n) continue;
+    // Outer row-panel triangular update U12 = L11^-1 A12, blocked by WI.
+    for (int i0 = j0; i0 < j1o; i0 += WI) {
+      const int ib = std::min(WI, j1o - i0);
+      const int i1 = i0 + ib;
+      LA_TRY(launch_trsm_rowpanel_f32(ctx, A, ld, i0, ib, j1o, n));
+      if (i1 < j1o)
+        LA_TRY(launch_gemm_f32(ctx, GM_FMA_SUB, j1o - i1, n - j1o, ib, A + (size_t)i1 * ld + i0, ld,
+                               A + (size_t)i0 * ld + j1o, ld, A + (size_t)i1 * ld + j1o, ld));
+    }
+    if (j1o >= m) continue;
+    // Trailing update A22 -= L21 * U12.
+    const int M = m - j1o, N = n - j1o;
+    float* C = A + (size_t)j1o * ld + j1o;
+    if (prec == LA_PREC_FP32) {
+      LA_TRY(launch_gemm_f32(ctx, GM_FMA_SUB, M, N, jbo, A + (size_t)j1o * ld + j0, ld,
+                             A + (size_t)j0 * ld + j1o, ld, C, ld));
+      continue;
+    }
+    const int fmt = prec == LA_PREC_BF16 ? LA_LOWP_BF16 : LA_LOWP_FP16;
+    const float* L21 = A + (size_t)j1o * ld + j0;
+    const float* U12 = A + (size_t)j0 * ld + j1o;
+    if (fmt == LA_LOWP_FP16) {
+      LA_CUDA(ctx, cudaMemsetAsync(d_stat, 0, 2 * sizeof(float), st));
+      absmax_kernel<<<grid_for(ctx, (size_t)jbo * N), 256, 0, st>>>(U12, ld, jbo, N, d_stat);
+      ctx->launches++;
+      LA_TRY(la_check_launch(ctx, "absmax_kernel"));
+    } else {
+      set_alpha_one<<<1, 1, 0, st>>>(d_stat);
+      ctx->launches++;
+      LA_TRY(la_check_launch(ctx, "set_alpha_one"));
+    }
+    if (fmt == LA_LOWP_BF16)
+      pack_l_kernel<LA_LOWP_BF16><<<grid_for(ctx, (size_t)M * ldk), 256, 0, st>>>(
+          L21, ld, lh.as<uint16_t>(), ldk, M, jbo);
+    else
+      pack_l_kernel<LA_LOWP_FP16><<<grid_for(ctx, (size_t)M * ldk), 256, 0, st>>>(
+          L21, ld, lh.as<uint16_t>(), ldk, M, jbo);
+    ctx->launches++;
+    LA_TRY(la_check_launch(ctx, "pack_l_kernel"));
+    dim3 pg((N + 31) / 32, ((int)ldk + 31) / 32);
+    if (fmt == LA_LOWP_BF16)
+      pack_ut_kernel<LA_LOWP_BF16><<<pg, dim3(32, 8), 0, st>>>(U12, ld, uh.as<uint16_t>(), ldk,
+                                                               jbo, N, d_stat);
+    else
+      pack_ut_kernel<LA_LOWP_FP16><<<pg, dim3(32, 8), 0, st>>>(U12, ld, uh.as<uint16_t>(), ldk,
+                                                               jbo, N, d_stat);
+    ctx->launches++;
+    LA_TRY(la_check_launch(ctx, "pack_ut_kernel"));
+    LA_TRY(launch_tc_update(ctx, st, fmt, M, N, jbo, lh.p, ldk, uh.p, ldk, C, ld, d_stat + 1));
+  }
+  return LA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+la_status la_lu_mixed_new_device(la_ctx ctx, const double* d_a, size_t lda, size_t n, int prec,
+                                 la_lu* out) {
+  if (!ctx || !d_a || !out || lda < n) return LA_INVALID;
+  if (n == 0) return LA_BADSHAPE;
+  if (n > (size_t)INT32_MAX / 4) return LA_UNSUPPORTED;
+  if (prec != LA_PREC_BF16 && prec != LA_PREC_FP16 && prec != LA_PREC_FP32) return LA_INVALID;
+  LA_CUDA(ctx, cudaSetDevice(ctx->device));
+  *out = nullptr;
+  la_lu h = new (std::nothrow) la_lu_handle();
+  if (!h) return LA_NOMEM;
+  h->ctx = ctx;
+  h->m = h->n = n;
+  h->ld = (n + 3) & ~size_t(3);
+  h->ld32 = pad8(n);
+  h->lowp = prec;
+  h->arith = LA_ARITH_FAST;
+  void* p = nullptr;
+  la_status s = la_device_alloc(ctx, &p, n * h->ld * sizeof(double));
+  if (s == LA_OK) { h->d_lu = static_cast<double*>(p); s = la_device_alloc(ctx, &p, n * h->ld32 * 4); }
+  if (s == LA_OK) { h->d_lu32 = static_cast<float*>(p); s = la_device_alloc(ctx, &p, n * sizeof(int)); }
+  if (s == LA_OK) { h->d_ipiv = static_cast<int*>(p); s = la_device_alloc(ctx, &p, n * 8); }
+  if (s == LA_OK) h->d_piv = static_cast<uint64_t*>(p);
+  if (s != LA_OK) { la_lu_free(h); return s; }
+  cudaError_t e = cudaMemcpy2DAsync(h->d_lu, h->ld * 8, d_a, lda * 8, n * 8, n,
+                                    cudaMemcpyDeviceToDevice, ctx->stream);
+  if (e != cudaSuccess) { s = la_cuda_fail(ctx, e, "copy A"); la_lu_free(h); return s; }
+  f64_to_f32_kernel<<<grid_for(ctx, n * n), 256, 0, ctx->stream>>>(h->d_lu, h->ld, h->d_lu32,
+                                                                    h->ld32, (int)n, (int)n);
+  ctx->launches++;
+  s = la_check_launch(ctx, "f64_to_f32_kernel");
+  if (s == LA_OK) s = mixed_factor(ctx, h, prec);
+  if (s == LA_OK) s = launch_lu_finish(ctx, h, reinterpret_cast<int*>(ctx->d_small));
+  int* flags = static_cast<int*>(ctx->h_pinned);
+  if (s == LA_OK) {
+    e = cudaMemcpyAsync(flags, ctx->d_small, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e != cudaSuccess) s = la_cuda_fail(ctx, e, "flags");
+  }
+  if (s == LA_OK) s = la_sync_and_check(ctx, "mixed factorization");
+  if (s != LA_OK) { la_lu_free(h); return s; }
+  h->pospivsign = flags[0];
+  h->zero_diag = flags[1];
+  *out = h;
+  return LA_OK;
+}
+
+la_status la_lu_solve_refined_device(la_lu h, const double* d_b, size_t ldb, size_t nrhs,
+                                     double* d_x, size_t ldx, int max_iters, double tol,
+                                     la_refine_stats* stats) {
+  if (!h || !d_b || !d_x || ldb < nrhs || ldx < nrhs || !h->d_lu32) return LA_INVALID;
+  if (nrhs == 0 || nrhs > 16) return LA_UNSUPPORTED;
+  la_ctx ctx = h->ctx;
+  LA_CUDA(ctx, cudaSetDevice(ctx->device));
+  if (h->zero_diag) return LA_SINGULAR;
+  const int n = (int)h->n, R = (int)nrhs;
+  cudaStream_t st = ctx->stream;
+  const size_t ldw = 4 * ((nrhs + 3) / 4);
+  Buf rbuf(ctx), wbuf(ctx), norms(ctx);
+  LA_TRY(rbuf.alloc((size_t)n * nrhs * 8));
+  LA_TRY(wbuf.alloc((size_t)n * ldw * 4));
+  // norms: [0] ||A||, [8..8+R) rmax, [32..32+R) xmax, [56..56+R) bmax
+  LA_TRY(norms.alloc(128 * 8));
+  double* d_norm = norms.as<double>();
+  double* d_r = rbuf.as<double>();
+  float* d_w = wbuf.as<float>();
+  LA_CUDA(ctx, cudaMemsetAsync(d_norm, 0, 128 * 8, st));
+  rownorm_kernel<<<grid_for(ctx, (size_t)n * 32), 256, 0, st>>>(h->d_lu, h->ld, n, d_norm);
+  colmax_kernel<<<grid_for(ctx, (size_t)n * nrhs), 256, 0, st>>>(d_b, ldb, n, R, d_norm + 56);
+  ctx->launches += 2;
+  // x = 0, r = b
+  LA_CUDA(ctx, cudaMemset2DAsync(d_x, ldx * 8, 0, nrhs * 8, n, st));
+  LA_CUDA(ctx, cudaMemcpy2DAsync(d_r, nrhs * 8, d_b, ldb * 8, nrhs * 8, n,
+                                 cudaMemcpyDeviceToDevice, st));
+  LA_CUDA(ctx, cudaMemcpyAsync(d_norm + 8, d_norm + 56, R * 8, cudaMemcpyDeviceToDevice, st));
+  double* host = static_cast<double*>(ctx->h_pinned);
+  double prev = INFINITY, eta = INFINITY;
+  int it = 0;
+  bool converged = false;
+  for (;;) {
+    // eta from the current residual norms
+    LA_CUDA(ctx, cudaMemsetAsync(d_norm + 32, 0, 16 * 8, st));
+    colmax_kernel<<<grid_for(ctx, (size_t)n * nrhs), 256, 0, st>>>(d_x, ldx, n, R, d_norm + 32);
+    ctx->launches++;
+    LA_CUDA(ctx, cudaMemcpyAsync(host, d_norm, 72 * 8, cudaMemcpyDeviceToHost, st));
+    LA_TRY(la_sync_and_check(ctx, "refinement norms"));
+    eta = 0.0;
+    for (int j = 0; j < R; j++) {
+      const double den = host[0] * host[32 + j] + host[56 + j];
+      const double v = den > 0 ? host[8 + j] / den : (host[8 + j] > 0 ? INFINITY : 0.0);
+      if (!(v <= eta)) eta = v;
+    }
+    if (eta <= tol) { converged = true; break; }
+    if (it >= max_iters || !(eta < 0.9 * prev)) break;  // cap reached, or stalled
+    prev = eta;
+    it++;
+    // d = LU32 \ (r(piv) / rmax), x += d * rmax
+    scale_permute_kernel<<<grid_for(ctx, (size_t)n * nrhs), 256, 0, st>>>(
+        h->d_piv, d_r, nrhs, d_norm + 8, d_w, ldw, n, R);
+    ctx->launches++;
+    LA_TRY(launch_lu_solve_f32(ctx, h->d_lu32, h->ld32, d_w, ldw, n, R));
+    update_x_kernel<<<grid_for(ctx, (size_t)n * nrhs), 256, 0, st>>>(d_x, ldx, d_w, ldw,
+                                                                      d_norm + 8, n, R);
+    ctx->launches++;
+    // r = b - A x
+    LA_CUDA(ctx, cudaMemsetAsync(d_norm + 8, 0, 16 * 8, st));
+    residual_f64_kernel<16><<<std::min((n + 7) / 8, ctx->sm_count * 8), 256, 0, st>>>(
+        h->d_lu, h->ld, d_x, ldx, d_b, ldb, d_r, nrhs, n, R, d_norm + 8);
+    ctx->launches++;
+    LA_TRY(la_check_launch(ctx, "refinement"));
+  }
+  if (stats) {
+    stats->iterations = it;
+    stats->eta = eta;
+    stats->converged = converged ? 1 : 0;
+  }
+  return converged ? LA_OK : LA_NOT_CONVERGED;
+}
+
+}  // extern "C"

@@ -94,8 +94,8 @@ __device__ __forceinline__ bool better(double ka, int pa, double kb, int pb) {
 }
 
 struct PanelParams {
-  double* A;
-  double* S;
+  void* A;        // element type of the kernel instantiation
+  void* S;
   size_t ld;
   int m, j0, jb, rpc, G;
   int* ipiv;
@@ -111,21 +111,25 @@ struct PanelParams {
   int cstride; // candidate slots per parity (>= G)
 };
 
-template <bool EXACT>
+// T is the element type of the panel (double, or float for the mixed-precision
+// LU); the exchange buffers in global memory always hold doubles (exact for
+// both). EXACT exists for double only.
+template <typename T, bool EXACT>
 __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
-  extern __shared__ __align__(16) double sm[];
+  extern __shared__ __align__(16) double sm_raw[];
+  T* sm = reinterpret_cast<T*>(sm_raw);
   constexpr int W = MAX_PANEL_W;
   const int rpc = p.rpc;
-  double* va = sm;                                // [rpc][W]  value (FAST) / a (EXACT)
-  double* vs = EXACT ? sm + rpc * W : nullptr;    // [rpc][W]  running sum s (EXACT)
-  double* urow = sm + (EXACT ? 2 : 1) * rpc * W;  // [W] pivot row
-  double* drow_a = urow + W;                      // [W] row j as published (raw)
-  double* drow_s = drow_a + W;                    // [W] its running sums (EXACT)
-  double* lrow = drow_s + W;                      // [rpc] multipliers of this step
+  T* va = sm;                                // [rpc][W]  value (FAST) / a (EXACT)
+  T* vs = EXACT ? sm + rpc * W : nullptr;    // [rpc][W]  running sum s (EXACT)
+  T* urow = sm + (EXACT ? 2 : 1) * rpc * W;  // [W] pivot row
+  T* drow_a = urow + W;                      // [W] row j as published (raw)
+  T* drow_s = drow_a + W;                    // [W] its running sums (EXACT)
+  T* lrow = drow_s + W;                      // [rpc] multipliers of this step
   __shared__ double red_k[PT / 32];
   __shared__ int red_p[PT / 32];
   __shared__ int s_win_pos;
-  __shared__ double s_scale;
+  __shared__ T s_scale;
   __shared__ int s_pivs[W];
 
   const int g = blockIdx.x;
@@ -137,11 +141,11 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
 
   for (int idx = tid; idx < rpc * W; idx += PT) {
     int r = idx / W, c = idx % W;
-    double a = 0.0, s = 0.0;
+    T a = T(0), s = T(0);
     if (r < nrows && c < jb) {
       size_t off = (size_t)(row0 + r) * p.ld + p.j0 + c;
-      a = p.A[off];
-      if (EXACT) s = p.S[off];
+      a = static_cast<const T*>(p.A)[off];
+      if (EXACT) s = static_cast<const T*>(p.S)[off];
     }
     va[idx] = a;
     if (EXACT) vs[idx] = s;
@@ -156,7 +160,7 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
     int bp = -1;
     for (int r = max(0, j - row0) + tid; r < nrows; r += PT) {
       const int pos = row0 + r;
-      double v = EXACT ? __dsub_rn(va[r * W + c], vs[r * W + c]) : va[r * W + c];
+      double v = EXACT ? __dsub_rn(va[r * W + c], vs[r * W + c]) : (double)va[r * W + c];
       double k = pivot_key(v, pos, j);
       if (better(k, pos, bk, bp)) { bk = k; bp = pos; }
     }
@@ -189,14 +193,14 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
       const int cp = s_win_pos;
       if (cp >= 0 && tid < W) {
         int r = cp - row0;
-        double v = EXACT ? __dsub_rn(va[r * W + tid], vs[r * W + tid]) : va[r * W + tid];
+        double v = EXACT ? __dsub_rn(va[r * W + tid], vs[r * W + tid]) : (double)va[r * W + tid];
         p.cand_row[((size_t)par * p.cstride + g) * W + tid] = v;
       }
       if (j >= row0 && j < row0 + nrows && tid >= PT - W) {
         const int t = tid - (PT - W);
         const int r = j - row0;
-        p.diag_a[par * W + t] = va[r * W + t];
-        if (EXACT) p.diag_s[par * W + t] = vs[r * W + t];
+        p.diag_a[par * W + t] = (double)va[r * W + t];
+        if (EXACT) p.diag_s[par * W + t] = (double)vs[r * W + t];
       }
     }
     if (!grid_barrier(p.bar, p.bar_base + (unsigned)(p.G * (c + 1)), p.err)) return;
@@ -212,8 +216,8 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
       }
       if (tid >= PT - W) {
         const int t = tid - (PT - W);
-        drow_a[t] = __ldcg(p.diag_a + par * W + t);
-        if (EXACT) drow_s[t] = __ldcg(p.diag_s + par * W + t);
+        drow_a[t] = (T)__ldcg(p.diag_a + par * W + t);
+        if (EXACT) drow_s[t] = (T)__ldcg(p.diag_s + par * W + t);
       }
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) {
@@ -242,12 +246,12 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
     }
     const int piv = s_win_pos;
     const int wg = (piv - p.j0) / rpc;  // CTA that owns the winning row
-    if (tid < W) urow[tid] = __ldcg(p.cand_row + ((size_t)par * p.cstride + wg) * W + tid);
+    if (tid < W) urow[tid] = (T)__ldcg(p.cand_row + ((size_t)par * p.cstride + wg) * W + tid);
     __syncthreads();
     if (tid == 0) {
-      const double d = urow[c];
+      const T d = urow[c];
       // FAST scales by the reciprocal (as LAPACK's getf2 does); EXACT divides.
-      s_scale = (d != 0.0) ? 1.0 / d : 1.0;
+      s_scale = (d != T(0)) ? T(1) / d : T(1);
     }
     // Swap: row j <- pivot row (finished), row piv <- old row j (raw storage).
     if (tid < W) {
@@ -259,7 +263,7 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
       if (j >= row0 && j < row0 + nrows) {
         const int r = j - row0;
         va[r * W + tid] = urow[tid];
-        if (EXACT) vs[r * W + tid] = 0.0;
+        if (EXACT) vs[r * W + tid] = T(0);
       }
     }
     __syncthreads();
@@ -268,14 +272,14 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
     const int first = max(0, j + 1 - row0);
     const int cnt = nrows - first;
     {
-      const double d = urow[c];
-      const double sc = s_scale;
+      const T d = urow[c];
+      const T sc = s_scale;
       for (int q = lane * (PT / 32) + warp; q < cnt; q += PT) {
         const int r = first + q;
-        double v = EXACT ? __dsub_rn(va[r * W + c], vs[r * W + c]) : va[r * W + c];
-        double l = (d != 0.0) ? (EXACT ? v / d : v * sc) : v;
+        T v = EXACT ? (T)__dsub_rn(va[r * W + c], vs[r * W + c]) : va[r * W + c];
+        T l = (d != T(0)) ? (EXACT ? v / d : v * sc) : v;
         va[r * W + c] = l;
-        if (EXACT) vs[r * W + c] = 0.0;
+        if (EXACT) vs[r * W + c] = T(0);
         lrow[r] = l;
       }
     }
@@ -284,10 +288,10 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
     //     row group of 4).
     const int cc = c + 1 + (tid & (W - 1));
     if (cc < jb) {
-      const double u = urow[cc];
+      const T u = urow[cc];
       for (int q = tid / W; q < cnt; q += PT / W) {
         const int r = first + q;
-        const double l = lrow[r];
+        const T l = lrow[r];
         if (EXACT)
           vs[r * W + cc] = __dadd_rn(vs[r * W + cc], __dmul_rn(l, u));
         else
@@ -300,8 +304,8 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
   for (int idx = tid; idx < nrows * W; idx += PT) {
     int r = idx / W, c = idx % W;
     if (c < jb) {
-      double v = EXACT ? __dsub_rn(va[idx], vs[idx]) : va[idx];
-      p.A[(size_t)(row0 + r) * p.ld + p.j0 + c] = v;
+      T v = EXACT ? (T)__dsub_rn(va[idx], vs[idx]) : va[idx];
+      static_cast<T*>(p.A)[(size_t)(row0 + r) * p.ld + p.j0 + c] = v;
     }
   }
   // Compose this panel's swaps into a list of row moves (dest <- src) for the
@@ -333,10 +337,12 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
 
 }  // namespace
 
-la_status launch_panel(la_ctx ctx, cudaStream_t stream, bool exact, double* A, double* S,
-                       size_t ld, int m, int j0, int jb, int* d_ipiv, unsigned* bar_base) {
+template <typename T>
+la_status launch_panel_t(la_ctx ctx, cudaStream_t stream, bool exact, T* A, T* S, size_t ld,
+                         int m, int j0, int jb, int* d_ipiv, unsigned* bar_base) {
   const int R = m - j0;
   if (R <= 0 || jb <= 0) return LA_OK;
+  if (exact && sizeof(T) != sizeof(double)) return LA_INVALID;
   const int W = MAX_PANEL_W;
   int maxG = ctx->panel_ctas > 0 ? std::min(ctx->panel_ctas, ctx->sm_count) : ctx->sm_count;
   maxG = std::min(maxG, PT);  // one candidate per thread when picking the winner
@@ -344,8 +350,8 @@ la_status launch_panel(la_ctx ctx, cudaStream_t stream, bool exact, double* A, d
   // At least 32 rows per CTA: fewer CTAs keep the per-column barrier cheap.
   int G = std::max(1, std::min(maxG, (R + 31) / 32));
   int rpc = (R + G - 1) / G;
-  const size_t per_row = (size_t)W * sizeof(double) * (exact ? 2 : 1) + sizeof(double);
-  const size_t fixed = (size_t)3 * W * sizeof(double);
+  const size_t per_row = (size_t)W * sizeof(T) * (exact ? 2 : 1) + sizeof(T);
+  const size_t fixed = (size_t)3 * W * sizeof(T) + 16;
   size_t smem = fixed + per_row * rpc;
   if (smem > ctx->smem_optin) return LA_UNSUPPORTED;
   G = (R + rpc - 1) / rpc;
@@ -372,7 +378,11 @@ la_status launch_panel(la_ctx ctx, cudaStream_t stream, bool exact, double* A, d
   p.cstride = ctx->cand_stride;
 
   void* args[] = {&p};
-  const void* fn = exact ? (const void*)panel_kernel<true> : (const void*)panel_kernel<false>;
+  const void* fn;
+  if (sizeof(T) == sizeof(double))
+    fn = exact ? (const void*)panel_kernel<double, true> : (const void*)panel_kernel<double, false>;
+  else
+    fn = (const void*)panel_kernel<float, false>;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaFuncSetAttribute(panel)");
   int per_sm = 0;
@@ -384,4 +394,14 @@ la_status launch_panel(la_ctx ctx, cudaStream_t stream, bool exact, double* A, d
   ctx->launches++;
   *bar_base += (unsigned)(G * jb);
   return la_check_launch(ctx, "panel_kernel");
+}
+
+la_status launch_panel(la_ctx ctx, cudaStream_t stream, bool exact, double* A, double* S,
+                       size_t ld, int m, int j0, int jb, int* d_ipiv, unsigned* bar_base) {
+  return launch_panel_t<double>(ctx, stream, exact, A, S, ld, m, j0, jb, d_ipiv, bar_base);
+}
+
+la_status launch_panel_f32(la_ctx ctx, cudaStream_t stream, float* A, size_t ld, int m, int j0,
+                           int jb, int* d_ipiv, unsigned* bar_base) {
+  return launch_panel_t<float>(ctx, stream, false, A, nullptr, ld, m, j0, jb, d_ipiv, bar_base);
 }

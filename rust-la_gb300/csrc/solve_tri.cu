@@ -22,22 +22,23 @@ constexpr int RT = 32;    // rows per update tile
 constexpr int CT = 32;    // right-hand-side columns per CTA
 constexpr int ST = 256;   // threads
 
-template <bool EXACT>
-__device__ __forceinline__ double apply(double x, double xk, double l) {
-  return EXACT ? __dsub_rn(x, __dmul_rn(xk, l)) : fma(-xk, l, x);
+template <bool EXACT, typename T>
+__device__ __forceinline__ T apply(T x, T xk, T l) {
+  if constexpr (EXACT) return __dsub_rn(x, __dmul_rn(xk, l));
+  else return fma(-xk, l, x);
 }
 
 // UPPER = false: forward with unit L; UPPER = true: backward with U.
 // kb_prev = size of the finished block at [k0, k0 + kb_prev) (0: no finished
 // block, only solve the block that starts at `next0`).
-template <bool EXACT, bool UPPER>
+template <typename T, bool EXACT, bool UPPER>
 __global__ void __launch_bounds__(ST)
-solve_step_kernel(const double* __restrict__ LU, size_t ld, double* __restrict__ X, size_t ldx,
+solve_step_kernel(const T* __restrict__ LU, size_t ld, T* __restrict__ X, size_t ldx,
                   int n, int nrhs, int k0, int kb_prev, int next0, int nextb) {
-  __shared__ double xk[SB][CT];        // finished block's solution rows
-  __shared__ double lt[RT][SB + 1];    // L/U entries of this tile against the finished block
-  __shared__ double dg[SB][SB + 1];    // diagonal block (tile 0)
-  __shared__ double xt[RT][CT];        // this tile's rows of X
+  __shared__ T xk[SB][CT];        // finished block's solution rows
+  __shared__ T lt[RT][SB + 1];    // L/U entries of this tile against the finished block
+  __shared__ T dg[SB][SB + 1];    // diagonal block (tile 0)
+  __shared__ T xt[RT][CT];        // this tile's rows of X
   const int c0 = blockIdx.y * CT;
   const int tx = threadIdx.x % CT, ty = threadIdx.x / CT;  // ty 0..7
   const int col = c0 + tx;
@@ -62,13 +63,13 @@ solve_step_kernel(const double* __restrict__ LU, size_t ld, double* __restrict__
 
   if (kb_prev > 0) {
     for (int i = ty; i < kb_prev; i += ST / CT)
-      xk[i][tx] = colok ? X[(size_t)(k0 + i) * ldx + col] : 0.0;
+      xk[i][tx] = colok ? X[(size_t)(k0 + i) * ldx + col] : T(0);
     for (int idx = threadIdx.x; idx < rn * kb_prev; idx += ST) {
       const int i = idx / kb_prev, k = idx % kb_prev;
       lt[i][k] = LU[(size_t)(r0 + i) * ld + k0 + k];
     }
   }
-  for (int i = ty; i < rn; i += ST / CT) xt[i][tx] = colok ? X[(size_t)(r0 + i) * ldx + col] : 0.0;
+  for (int i = ty; i < rn; i += ST / CT) xt[i][tx] = colok ? X[(size_t)(r0 + i) * ldx + col] : T(0);
   if (tile == 0) {
     for (int idx = threadIdx.x; idx < rn * rn; idx += ST) {
       const int i = idx / rn, k = idx % rn;
@@ -80,11 +81,11 @@ solve_step_kernel(const double* __restrict__ LU, size_t ld, double* __restrict__
   // Terms of the finished block.
   if (kb_prev > 0) {
     for (int i = ty; i < rn; i += ST / CT) {
-      double x = xt[i][tx];
+      T x = xt[i][tx];
       if (!UPPER) {
-        for (int k = 0; k < kb_prev; k++) x = apply<EXACT>(x, xk[k][tx], lt[i][k]);
+        for (int k = 0; k < kb_prev; k++) x = apply<EXACT, T>(x, xk[k][tx], lt[i][k]);
       } else {
-        for (int k = kb_prev - 1; k >= 0; k--) x = apply<EXACT>(x, xk[k][tx], lt[i][k]);
+        for (int k = kb_prev - 1; k >= 0; k--) x = apply<EXACT, T>(x, xk[k][tx], lt[i][k]);
       }
       xt[i][tx] = x;
     }
@@ -94,17 +95,17 @@ solve_step_kernel(const double* __restrict__ LU, size_t ld, double* __restrict__
     __syncthreads();
     if (!UPPER) {
       for (int k = 0; k < rn; k++) {
-        const double v = xt[k][tx];
+        const T v = xt[k][tx];
         for (int i = ty; i < rn; i += ST / CT)
-          if (i > k) xt[i][tx] = apply<EXACT>(xt[i][tx], v, dg[i][k]);
+          if (i > k) xt[i][tx] = apply<EXACT, T>(xt[i][tx], v, dg[i][k]);
         __syncthreads();
       }
     } else {
       for (int k = rn - 1; k >= 0; k--) {
         if (ty == (k % (ST / CT))) xt[k][tx] = xt[k][tx] / dg[k][k];
         __syncthreads();
-        const double v = xt[k][tx];
-        for (int i = ty; i < k; i += ST / CT) xt[i][tx] = apply<EXACT>(xt[i][tx], v, dg[i][k]);
+        const T v = xt[k][tx];
+        for (int i = ty; i < k; i += ST / CT) xt[i][tx] = apply<EXACT, T>(xt[i][tx], v, dg[i][k]);
         __syncthreads();
       }
     }
@@ -114,38 +115,37 @@ solve_step_kernel(const double* __restrict__ LU, size_t ld, double* __restrict__
     for (int i = ty; i < rn; i += ST / CT) X[(size_t)(r0 + i) * ldx + col] = xt[i][tx];
 }
 
-template <bool EXACT, bool UPPER>
-la_status launch_step(la_ctx ctx, const double* LU, size_t ld, double* X, size_t ldx, int n,
+template <typename T, bool EXACT, bool UPPER>
+la_status launch_step(la_ctx ctx, const T* LU, size_t ld, T* X, size_t ldx, int n,
                       int nrhs, int k0, int kb_prev, int next0, int nextb) {
   int rest;
   if (!UPPER) rest = n - (next0 + nextb);
   else rest = next0;
   if (kb_prev == 0) rest = 0;
   dim3 grid(1 + (rest + RT - 1) / RT, (nrhs + CT - 1) / CT);
-  solve_step_kernel<EXACT, UPPER><<<grid, ST, 0, ctx->stream>>>(LU, ld, X, ldx, n, nrhs, k0,
-                                                                kb_prev, next0, nextb);
+  solve_step_kernel<T, EXACT, UPPER><<<grid, ST, 0, ctx->stream>>>(LU, ld, X, ldx, n, nrhs, k0,
+                                                                   kb_prev, next0, nextb);
   ctx->launches++;
   return la_check_launch(ctx, "solve_step_kernel");
 }
 
-template <bool EXACT>
-la_status solve_all(la_ctx ctx, const double* LU, size_t ld, double* X, size_t ldx, int n,
-                     int nrhs) {
+template <typename T, bool EXACT>
+la_status solve_all(la_ctx ctx, const T* LU, size_t ld, T* X, size_t ldx, int n, int nrhs) {
   // Forward: block 0 alone, then one step per finished block.
   const int nb = (n + SB - 1) / SB;
-  LA_TRY((launch_step<EXACT, false>(ctx, LU, ld, X, ldx, n, nrhs, 0, 0, 0, std::min(SB, n))));
+  LA_TRY((launch_step<T, EXACT, false>(ctx, LU, ld, X, ldx, n, nrhs, 0, 0, 0, std::min(SB, n))));
   for (int b = 0; b + 1 < nb; b++) {
     const int k0 = b * SB, kb = std::min(SB, n - k0);
     const int nx0 = k0 + kb, nxb = std::min(SB, n - nx0);
-    LA_TRY((launch_step<EXACT, false>(ctx, LU, ld, X, ldx, n, nrhs, k0, kb, nx0, nxb)));
+    LA_TRY((launch_step<T, EXACT, false>(ctx, LU, ld, X, ldx, n, nrhs, k0, kb, nx0, nxb)));
   }
   // Backward: last block alone, then upward.
   const int last0 = (nb - 1) * SB;
-  LA_TRY((launch_step<EXACT, true>(ctx, LU, ld, X, ldx, n, nrhs, 0, 0, last0, n - last0)));
+  LA_TRY((launch_step<T, EXACT, true>(ctx, LU, ld, X, ldx, n, nrhs, 0, 0, last0, n - last0)));
   for (int b = nb - 1; b > 0; b--) {
     const int k0 = b * SB, kb = std::min(SB, n - k0);
     const int nx0 = (b - 1) * SB;
-    LA_TRY((launch_step<EXACT, true>(ctx, LU, ld, X, ldx, n, nrhs, k0, kb, nx0, SB)));
+    LA_TRY((launch_step<T, EXACT, true>(ctx, LU, ld, X, ldx, n, nrhs, k0, kb, nx0, SB)));
   }
   return LA_OK;
 }
@@ -157,6 +157,13 @@ la_status solve_all(la_ctx ctx, const double* LU, size_t ld, double* X, size_t l
 la_status launch_lu_solve(la_ctx ctx, bool exact, const double* LU, size_t ld, double* X,
                           size_t ldx, int n, int nrhs) {
   if (n <= 0 || nrhs <= 0) return LA_OK;
-  return exact ? solve_all<true>(ctx, LU, ld, X, ldx, n, nrhs)
-               : solve_all<false>(ctx, LU, ld, X, ldx, n, nrhs);
+  return exact ? solve_all<double, true>(ctx, LU, ld, X, ldx, n, nrhs)
+               : solve_all<double, false>(ctx, LU, ld, X, ldx, n, nrhs);
+}
+
+// FP32 factors and right-hand sides (the correction solves of iterative refinement).
+la_status launch_lu_solve_f32(la_ctx ctx, const float* LU, size_t ld, float* X, size_t ldx, int n,
+                              int nrhs) {
+  if (n <= 0 || nrhs <= 0) return LA_OK;
+  return solve_all<float, false>(ctx, LU, ld, X, ldx, n, nrhs);
 }

@@ -81,7 +81,18 @@ SIGNATURES = {
     "la_backward_error_device": ([_P, _P, _S, _P, _S, _P, _S, _S, _S, _P], _I),
     "la_backward_error": ([_P, _P, _P, _P, _S, _S, _P], _I),
     "la_lu_factor_noalloc": ([_P, _P, _S, _S, _S, _P, _P, _P], _I),
+    "la_lu_mixed_new_device": ([_P, _P, _S, _S, _I, _P], _I),
+    "la_lu_solve_refined_device": ([_P, _P, _S, _S, _P, _S, _I, _D, _P], _I),
+    "la_lowp_update_device": ([_P, _I, _S, _S, _S, _P, _S, _P, _S, _P, _S, ctypes.c_float], _I),
 }
+
+PREC_BF16, PREC_FP16, PREC_FP32 = 1, 2, 3
+
+
+class RefineStats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("converged", ctypes.c_int),
+                ("eta", ctypes.c_double), ("fell_back", ctypes.c_int),
+                ("precision", ctypes.c_int)]
 
 
 def lib():
@@ -401,6 +412,29 @@ def backward_error_device(ctx, a_ptr, lda, x_ptr, ldx, b_ptr, ldb, n, nrhs):
                                                ctypes.c_void_p(x_ptr), ldx, ctypes.c_void_p(b_ptr),
                                                ldb, n, nrhs, ctypes.byref(out)))
     return out.value
+
+
+def lu_mixed_new_device(ctx, a_ptr, lda, n, prec):
+    h = ctypes.c_void_p()
+    _check(ctx, lib().la_lu_mixed_new_device(ctx.h, ctypes.c_void_p(a_ptr), lda, n, prec,
+                                             ctypes.byref(h)))
+    return LUDecomposition(h, ctx, n, n)
+
+
+def lu_solve_refined_device(lu, b_ptr, ldb, nrhs, x_ptr, ldx, max_iters=50, tol=1e-14):
+    stats = RefineStats()
+    st = lib().la_lu_solve_refined_device(lu.h, ctypes.c_void_p(b_ptr), ldb, nrhs,
+                                          ctypes.c_void_p(x_ptr), ldx, max_iters, tol,
+                                          ctypes.byref(stats))
+    _check(lu.ctx, st, (OK, NOT_CONVERGED, SINGULAR))
+    return st, stats
+
+
+def lowp_update_device(ctx, fmt, m_, n, k, a_ptr, lda, b_ptr, ldb, c_ptr, ldc, alpha):
+    st = lib().la_lowp_update_device(ctx.h, fmt, m_, n, k, ctypes.c_void_p(a_ptr), lda,
+                                     ctypes.c_void_p(b_ptr), ldb, ctypes.c_void_p(c_ptr), ldc,
+                                     ctypes.c_float(alpha))
+    return _check(ctx, st)
 
 
 def matrix_mul_device(ctx, a_ptr, lda, b_ptr, ldb, c_ptr, ldc, m_, k, n):

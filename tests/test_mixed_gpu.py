@@ -1,0 +1,80 @@
+"""Mixed-precision path: the tcgen05 trailing-update kernel against an FP64
+reference of the same op, and the FP32-factor LU with FP64 iterative refinement
+reaching a normwise backward error <= 1e-14 (checked with the oracle's
+compensated residual)."""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+ETA_MAX = 1e-14
+
+
+@pytest.fixture(scope="module")
+def torch():
+    return pytest.importorskip("torch")
+
+
+@pytest.mark.parametrize("fmt", [1, 2], ids=["bf16", "fp16"])
+@pytest.mark.parametrize("mnk", [(128, 128, 64), (1, 1, 16), (200, 300, 100), (256, 384, 256),
+                                 (1000, 130, 512), (129, 257, 8)])
+def test_tc_update_matches_fp64_reference(lagpu, ctx_fast, torch, fmt, mnk):
+    m, n, k = mnk
+    dt = torch.bfloat16 if fmt == 1 else torch.float16
+    g = torch.Generator(device="cuda").manual_seed(m * 7 + n * 3 + k)
+    ldk = (k + 7) // 8 * 8
+    ldc = (n + 3) // 4 * 4
+    a = torch.zeros((m, ldk), dtype=dt, device="cuda")
+    b = torch.zeros((n, ldk), dtype=dt, device="cuda")
+    a[:, :k] = torch.randn((m, k), generator=g, device="cuda").to(dt)
+    b[:, :k] = torch.randn((n, k), generator=g, device="cuda").to(dt)
+    c = torch.randn((m, ldc), generator=g, device="cuda", dtype=torch.float32)
+    alpha = 0.75
+    ref = c[:, :n].double() - alpha * (a[:, :k].double() @ b[:, :k].double().T)
+    torch.cuda.synchronize()
+    lagpu.lowp_update_device(ctx_fast, fmt, m, n, k, a.data_ptr(), ldk, b.data_ptr(), ldk,
+                             c.data_ptr(), ldc, alpha)
+    got = c[:, :n].double()
+    scale = 1.0 + alpha * (a[:, :k].double().abs() @ b[:, :k].double().abs().T)
+    err = ((got - ref).abs() / scale).max().item()
+    assert err < 4 * k * 2.0 ** -24 + 1e-6, err
+    # columns beyond n in the padded pitch are untouched
+    if ldc > n:
+        assert torch.isfinite(c[:, n:]).all()
+
+
+def _problem(n, nrhs, seed, shift=0.0):
+    rng = np.random.default_rng(seed)
+    a = rng.standard_normal((n, n)) + shift * np.eye(n)
+    b = rng.standard_normal((n, nrhs))
+    return a, b
+
+
+@pytest.mark.parametrize("prec", [1, 2, 3], ids=["bf16", "fp16", "fp32"])
+@pytest.mark.parametrize("n", [64, 300, 1000, 1536])
+def test_mixed_lu_ir_reaches_fp64_backward_error(lagpu, ctx_fast, torch, prec, n):
+    a, b = _problem(n, 4, 100 + n, shift=0.0 if prec == 3 else 2.0 * np.sqrt(n))
+    ta = torch.from_numpy(a).cuda()
+    tb = torch.from_numpy(b).cuda()
+    tx = torch.zeros((n, 4), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    lu = lagpu.lu_mixed_new_device(ctx_fast, ta.data_ptr(), n, n, prec)
+    st, stats = lagpu.lu_solve_refined_device(lu, tb.data_ptr(), 4, 4, tx.data_ptr(), 4,
+                                              max_iters=60, tol=5e-15)
+    lu.free()
+    x = tx.cpu().numpy()
+    assert st == lagpu.OK, (stats.iterations, stats.eta)
+    assert oracle.backward_error(a, x, b) <= ETA_MAX
+    assert stats.iterations >= 1
+
+
+def test_mixed_fp32_factor_pivots_match_fp32_partial_pivoting(lagpu, ctx_fast, torch):
+    # The FP32 factorization follows partial pivoting on its own FP32 values;
+    # on a diagonally dominant matrix no row is swapped at all.
+    n = 700
+    a, _ = _problem(n, 1, 5, shift=4.0 * n)
+    ta = torch.from_numpy(a).cuda()
+    lu = lagpu.lu_mixed_new_device(ctx_fast, ta.data_ptr(), n, n, 1)
+    assert np.array_equal(lu.get_piv(), np.arange(n, dtype=np.uint64))
+    lu.free()
