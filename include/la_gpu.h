@@ -157,11 +157,12 @@ la_status la_matrix_mul_device(la_ctx ctx, const double* d_a, size_t lda, const 
 #define LA_PREC_FP32 3  /* FP32 FMA (no tensor cores) */
 
 typedef struct la_refine_stats {
-  int iterations;    /* correction solves applied */
+  int iterations;    /* refinement steps (plain and GMRES) */
   int converged;     /* 1 when eta <= tol was reached */
   double eta;        /* final normwise backward error (FP64 residual) */
   int fell_back;     /* 1 when the plain FP64 LU produced the answer */
   int precision;     /* LA_PREC_* actually used for the answer (0: plain FP64) */
+  int gmres_steps;   /* Arnoldi steps of GMRES-IR (0: plain refinement sufficed) */
 } la_refine_stats;
 
 /* Factors a square FP64 matrix (device, pitch lda) in FP32 with the trailing
@@ -170,8 +171,10 @@ typedef struct la_refine_stats {
 la_status la_lu_mixed_new_device(la_ctx ctx, const double* d_a, size_t lda, size_t n, int prec,
                                  la_lu* out);
 /* Iterative refinement with the mixed factors: x = 0, r = b; d = LU \ r (FP32),
- * x += d, r = b - A x (FP64) until eta <= tol or max_iters or a stall
- * (LA_NOT_CONVERGED). nrhs <= 16. */
+ * x += d, r = b - A x (FP64) until eta <= tol. When that stalls it continues
+ * with GMRES-IR (GMRES on M^-1 A d = M^-1 r, M the low-precision LU) until
+ * eta <= tol, max_iters steps in all, or a stall (LA_NOT_CONVERGED).
+ * nrhs <= 16. */
 la_status la_lu_solve_refined_device(la_lu lu, const double* d_b, size_t ldb, size_t nrhs,
                                      double* d_x, size_t ldx, int max_iters, double tol,
                                      la_refine_stats* stats);

@@ -37,7 +37,8 @@ enum DeviceErr : int {
   DERR_NONE = 0,
   DERR_PANEL_TIMEOUT = 1,
   DERR_PANEL_CAPACITY = 2,
-  DERR_TC_TIMEOUT = 3
+  DERR_TC_TIMEOUT = 3,
+  DERR_TRSV_TIMEOUT = 4
 };
 
 // 16-bit operand formats of the tensor-core update.
@@ -91,6 +92,7 @@ struct la_lu_handle {
   // FP64 matrix kept in d_lu (used for residuals); null for plain FP64.
   float* d_lu32 = nullptr;
   size_t ld32 = 0;
+  double* d_dinv = nullptr;      // inverted 64x64 diagonal blocks of L and U (lazy, FP64)
   int lowp = 0;                  // LA_PREC_* of the trailing update
 };
 
@@ -137,6 +139,9 @@ la_status launch_gemm_f32(la_ctx ctx, int mode, int M, int N, int K, const float
                           const float* B, size_t ldb, float* C, size_t ldc);
 la_status launch_lu_solve_f32(la_ctx ctx, const float* LU, size_t ld, float* X, size_t ldx, int n,
                               int nrhs);
+la_status launch_invert_diag_f32(la_ctx ctx, const float* LU, size_t ld, int n, double* dinv);
+la_status launch_trsv_wave_f32(la_ctx ctx, const float* LU, size_t ld, const double* dinv,
+                               double* X, size_t ldx, int n, int nrhs, int* sync);
 la_status launch_lu_finish(la_ctx ctx, la_lu h, int* d_flags);
 // Enqueues the whole factorization of h (no readback, no synchronization);
 // lu_finish writes {pospivsign, zero-on-diagonal} to d_flags.

@@ -331,6 +331,7 @@ void la_lu_free(la_lu h) {
   cudaSetDevice(ctx->device);
   la_device_free(ctx, h->d_lu);
   la_device_free(ctx, h->d_lu32);
+  la_device_free(ctx, h->d_dinv);
   la_device_free(ctx, h->d_ipiv);
   la_device_free(ctx, h->d_piv);
   delete h;

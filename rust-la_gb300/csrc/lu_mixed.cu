@@ -178,28 +178,28 @@ __global__ void rownorm_kernel(const double* __restrict__ A, size_t lda, int n, 
   }
 }
 
-// w32 = (r(piv,:) / rscale_j) in FP32, the right-hand side of a correction solve.
+// w = r(piv,:) / rscale_j, the right-hand side of a correction solve.
 __global__ void scale_permute_kernel(const uint64_t* __restrict__ piv, const double* __restrict__ R,
                                      size_t ldr, const double* __restrict__ rscale,
-                                     float* __restrict__ W, size_t ldw, int n, int nrhs) {
+                                     double* __restrict__ W, size_t ldw, int n, int nrhs) {
   size_t total = (size_t)n * nrhs;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
        i += (size_t)gridDim.x * blockDim.x) {
     int r = (int)(i / nrhs), c = (int)(i % nrhs);
     const double s = rscale[c];
     const double v = R[(size_t)piv[r] * ldr + c];
-    W[(size_t)r * ldw + c] = s > 0 ? (float)(v / s) : 0.f;
+    W[(size_t)r * ldw + c] = s > 0 ? v / s : 0.0;
   }
 }
 
 // x += d * rscale_j (FP64 update of the solution).
-__global__ void update_x_kernel(double* __restrict__ X, size_t ldx, const float* __restrict__ D,
+__global__ void update_x_kernel(double* __restrict__ X, size_t ldx, const double* __restrict__ D,
                                 size_t ldd, const double* __restrict__ rscale, int n, int nrhs) {
   size_t total = (size_t)n * nrhs;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
        i += (size_t)gridDim.x * blockDim.x) {
     int r = (int)(i / nrhs), c = (int)(i % nrhs);
-    X[(size_t)r * ldx + c] += (double)D[(size_t)r * ldd + c] * rscale[c];
+    X[(size_t)r * ldx + c] += D[(size_t)r * ldd + c] * rscale[c];
   }
 }
 
@@ -216,6 +216,23 @@ struct Buf {
   la_status alloc(size_t bytes) { return la_device_alloc(ctx, &p, bytes); }
   template <typename T> T* as() { return static_cast<T*>(p); }
 };
+
+}  // namespace
+
+la_status gmres_correction(la_ctx ctx, la_lu h, const double* R, size_t ldr, int col, double* X,
+                           size_t ldx, int m, double tau, int* steps);
+
+namespace {
+
+// Inverted diagonal blocks for the wavefront triangular solves (once per handle).
+la_status ensure_dinv(la_ctx ctx, la_lu h) {
+  if (h->d_dinv) return LA_OK;
+  const size_t nb = (h->n + 63) / 64;
+  void* p = nullptr;
+  LA_TRY(la_device_alloc(ctx, &p, nb * 2 * 64 * 64 * sizeof(double)));
+  h->d_dinv = static_cast<double*>(p);
+  return launch_invert_diag_f32(ctx, h->d_lu32, h->ld32, (int)h->n, h->d_dinv);
+}
 
 // Factors h->d_lu32 (m x n, pitch ld32) in place; pivots into h->d_ipiv.
 la_status mixed_factor(la_ctx ctx, la_lu h, int prec) {
@@ -365,14 +382,17 @@ la_status la_lu_solve_refined_device(la_lu h, const double* d_b, size_t ldb, siz
   const int n = (int)h->n, R = (int)nrhs;
   cudaStream_t st = ctx->stream;
   const size_t ldw = 4 * ((nrhs + 3) / 4);
-  Buf rbuf(ctx), wbuf(ctx), norms(ctx);
+  Buf rbuf(ctx), wbuf(ctx), norms(ctx), sync(ctx);
   LA_TRY(rbuf.alloc((size_t)n * nrhs * 8));
-  LA_TRY(wbuf.alloc((size_t)n * ldw * 4));
+  LA_TRY(wbuf.alloc((size_t)n * ldw * 8));
+  const int nb64 = (n + 63) / 64;
+  LA_TRY(sync.alloc((size_t)(2 * nb64 + 2) * sizeof(int)));
+  LA_TRY(ensure_dinv(ctx, h));
   // norms: [0] ||A||, [8..8+R) rmax, [32..32+R) xmax, [56..56+R) bmax
   LA_TRY(norms.alloc(128 * 8));
   double* d_norm = norms.as<double>();
   double* d_r = rbuf.as<double>();
-  float* d_w = wbuf.as<float>();
+  double* d_w = wbuf.as<double>();
   LA_CUDA(ctx, cudaMemsetAsync(d_norm, 0, 128 * 8, st));
   rownorm_kernel<<<grid_for(ctx, (size_t)n * 32), 256, 0, st>>>(h->d_lu, h->ld, n, d_norm);
   colmax_kernel<<<grid_for(ctx, (size_t)n * nrhs), 256, 0, st>>>(d_b, ldb, n, R, d_norm + 56);
@@ -383,11 +403,10 @@ la_status la_lu_solve_refined_device(la_lu h, const double* d_b, size_t ldb, siz
                                  cudaMemcpyDeviceToDevice, st));
   LA_CUDA(ctx, cudaMemcpyAsync(d_norm + 8, d_norm + 56, R * 8, cudaMemcpyDeviceToDevice, st));
   double* host = static_cast<double*>(ctx->h_pinned);
-  double prev = INFINITY, eta = INFINITY;
-  int it = 0;
-  bool converged = false;
-  for (;;) {
-    // eta from the current residual norms
+  double eta_col[16];
+  double eta = INFINITY;
+  // eta from the current r (norms in d_norm) and x.
+  auto measure = [&]() -> la_status {
     LA_CUDA(ctx, cudaMemsetAsync(d_norm + 32, 0, 16 * 8, st));
     colmax_kernel<<<grid_for(ctx, (size_t)n * nrhs), 256, 0, st>>>(d_x, ldx, n, R, d_norm + 32);
     ctx->launches++;
@@ -397,31 +416,62 @@ la_status la_lu_solve_refined_device(la_lu h, const double* d_b, size_t ldb, siz
     for (int j = 0; j < R; j++) {
       const double den = host[0] * host[32 + j] + host[56 + j];
       const double v = den > 0 ? host[8 + j] / den : (host[8 + j] > 0 ? INFINITY : 0.0);
+      eta_col[j] = v;
       if (!(v <= eta)) eta = v;
     }
-    if (eta <= tol) { converged = true; break; }
-    if (it >= max_iters || !(eta < 0.9 * prev)) break;  // cap reached, or stalled
-    prev = eta;
-    it++;
-    // d = LU32 \ (r(piv) / rmax), x += d * rmax
-    scale_permute_kernel<<<grid_for(ctx, (size_t)n * nrhs), 256, 0, st>>>(
-        h->d_piv, d_r, nrhs, d_norm + 8, d_w, ldw, n, R);
-    ctx->launches++;
-    LA_TRY(launch_lu_solve_f32(ctx, h->d_lu32, h->ld32, d_w, ldw, n, R));
-    update_x_kernel<<<grid_for(ctx, (size_t)n * nrhs), 256, 0, st>>>(d_x, ldx, d_w, ldw,
-                                                                      d_norm + 8, n, R);
-    ctx->launches++;
-    // r = b - A x
+    return LA_OK;
+  };
+  // r = b - A x and its column maxima.
+  auto residual = [&]() -> la_status {
     LA_CUDA(ctx, cudaMemsetAsync(d_norm + 8, 0, 16 * 8, st));
     residual_f64_kernel<16><<<std::min((n + 7) / 8, ctx->sm_count * 8), 256, 0, st>>>(
         h->d_lu, h->ld, d_x, ldx, d_b, ldb, d_r, nrhs, n, R, d_norm + 8);
     ctx->launches++;
-    LA_TRY(la_check_launch(ctx, "refinement"));
+    return la_check_launch(ctx, "residual");
+  };
+  LA_TRY(measure());
+  double prev = INFINITY;
+  int it = 0, gsteps = 0;
+  bool converged = eta <= tol;
+  // Plain refinement: d = LU32 \ (r(piv) / rmax), x += d * rmax.
+  while (!converged && it < max_iters && eta < 0.9 * prev) {
+    prev = eta;
+    it++;
+    scale_permute_kernel<<<grid_for(ctx, (size_t)n * nrhs), 256, 0, st>>>(
+        h->d_piv, d_r, nrhs, d_norm + 8, d_w, ldw, n, R);
+    ctx->launches++;
+    LA_TRY(launch_trsv_wave_f32(ctx, h->d_lu32, h->ld32, h->d_dinv, d_w, ldw, n, R,
+                                sync.as<int>()));
+    update_x_kernel<<<grid_for(ctx, (size_t)n * nrhs), 256, 0, st>>>(d_x, ldx, d_w, ldw,
+                                                                      d_norm + 8, n, R);
+    ctx->launches++;
+    LA_TRY(residual());
+    LA_TRY(measure());
+    converged = eta <= tol;
+  }
+  // GMRES-IR once plain refinement stalls.
+  int outer = 0;
+  prev = INFINITY;
+  while (!converged && it + outer < max_iters && eta < 0.5 * prev) {
+    prev = eta;
+    outer++;
+    for (int j = 0; j < R; j++) {
+      if (eta_col[j] <= tol) continue;
+      int steps = 0;
+      LA_TRY(gmres_correction(ctx, h, d_r, nrhs, j, d_x, ldx, 60, 1e-10, &steps));
+      gsteps += steps;
+    }
+    LA_TRY(residual());
+    LA_TRY(measure());
+    converged = eta <= tol;
   }
   if (stats) {
-    stats->iterations = it;
+    stats->iterations = it + outer;
     stats->eta = eta;
     stats->converged = converged ? 1 : 0;
+    stats->gmres_steps = gsteps;
+    stats->precision = h->lowp;
+    stats->fell_back = 0;
   }
   return converged ? LA_OK : LA_NOT_CONVERGED;
 }

@@ -92,7 +92,7 @@ PREC_BF16, PREC_FP16, PREC_FP32 = 1, 2, 3
 class RefineStats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("converged", ctypes.c_int),
                 ("eta", ctypes.c_double), ("fell_back", ctypes.c_int),
-                ("precision", ctypes.c_int)]
+                ("precision", ctypes.c_int), ("gmres_steps", ctypes.c_int)]
 
 
 def lib():

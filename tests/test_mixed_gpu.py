@@ -78,3 +78,36 @@ def test_mixed_fp32_factor_pivots_match_fp32_partial_pivoting(lagpu, ctx_fast, t
     lu = lagpu.lu_mixed_new_device(ctx_fast, ta.data_ptr(), n, n, 1)
     assert np.array_equal(lu.get_piv(), np.arange(n, dtype=np.uint64))
     lu.free()
+
+
+def _hh(torch, n, kappa, seed):
+    rng = np.random.default_rng(seed)
+    s = torch.from_numpy(kappa ** (-np.arange(n) / (n - 1))).cuda()
+    a = torch.diag(s)
+    for side in ("right", "left"):
+        for _ in range(4):
+            v = torch.from_numpy(rng.standard_normal(n)).cuda()
+            vv = float(v @ v)
+            if side == "right":
+                a -= (2.0 / vv) * torch.outer(a @ v, v)
+            else:
+                a -= (2.0 / vv) * torch.outer(v, v @ a)
+    return a.contiguous()
+
+
+@pytest.mark.parametrize("prec,kappa", [(1, 1e6), (2, 1e8), (3, 1e10)],
+                         ids=["bf16-1e6", "fp16-1e8", "fp32-1e10"])
+def test_ill_conditioned_refinement_converges(lagpu, ctx_fast, torch, prec, kappa):
+    n = 1024
+    a = _hh(torch, n, kappa, 7)
+    rng = np.random.default_rng(8)
+    b = torch.from_numpy(rng.standard_normal((n, 2))).cuda()
+    x = torch.zeros((n, 2), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    lu = lagpu.lu_mixed_new_device(ctx_fast, a.data_ptr(), n, n, prec)
+    st, stats = lagpu.lu_solve_refined_device(lu, b.data_ptr(), 2, 2, x.data_ptr(), 2,
+                                              max_iters=40, tol=5e-15)
+    lu.free()
+    assert st == lagpu.OK, (stats.iterations, stats.gmres_steps, stats.eta)
+    eta = oracle.backward_error(a.cpu().numpy(), x.cpu().numpy(), b.cpu().numpy())
+    assert eta <= ETA_MAX
