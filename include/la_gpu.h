@@ -76,7 +76,10 @@ typedef enum la_option {
   LA_OPT_PROFILE = 4,
   /* 1 (default): factor the next panel on a second stream while the rest of
    * the trailing update runs; 0: strictly one phase after the other. */
-  LA_OPT_LOOKAHEAD = 5
+  LA_OPT_LOOKAHEAD = 5,
+  /* 1 (default): the FP32 panels of the mixed LU run on one thread-block
+   * cluster (distributed shared memory); 0: the cooperative multi-CTA kernel. */
+  LA_OPT_CLUSTER_PANEL = 6
 } la_option;
 
 #define LA_ARITH_FAST 0

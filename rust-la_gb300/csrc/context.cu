@@ -228,6 +228,9 @@ la_status la_ctx_set_option(la_ctx ctx, int option, int64_t value) {
     case LA_OPT_LOOKAHEAD:
       ctx->lookahead = value ? 1 : 0;
       return LA_OK;
+    case LA_OPT_CLUSTER_PANEL:
+      ctx->cluster_panels = value ? 1 : 0;
+      return LA_OK;
   }
   return LA_INVALID;
 }
@@ -240,6 +243,7 @@ la_status la_ctx_get_option(la_ctx ctx, int option, int64_t* value) {
     case LA_OPT_PANEL_CTAS: *value = ctx->panel_ctas; return LA_OK;
     case LA_OPT_PROFILE: *value = ctx->profile; return LA_OK;
     case LA_OPT_LOOKAHEAD: *value = ctx->lookahead; return LA_OK;
+    case LA_OPT_CLUSTER_PANEL: *value = ctx->cluster_panels; return LA_OK;
   }
   return LA_INVALID;
 }

@@ -51,6 +51,7 @@ struct la_context {
   cudaStream_t side_stream = nullptr;    // high priority: lookahead panels
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int lookahead = 1;
+  int cluster_panels = 1;                // FP32 panels on one thread-block cluster
   int sm_count = 0;
   size_t smem_optin = 0;
   int arith = LA_ARITH_FAST;
@@ -93,6 +94,7 @@ struct la_lu_handle {
   float* d_lu32 = nullptr;
   size_t ld32 = 0;
   double* d_dinv = nullptr;      // inverted 64x64 diagonal blocks of L and U (lazy, FP64)
+  float* d_dinvf = nullptr;      // the same in FP32 (plain refinement)
   int lowp = 0;                  // LA_PREC_* of the trailing update
 };
 
@@ -133,6 +135,8 @@ la_status launch_trsm_rowpanel(la_ctx ctx, bool exact, double* A, double* S, siz
 la_status launch_panel_f32(la_ctx ctx, cudaStream_t stream, float* A, size_t ld, int m, int j0,
                            int jb, int* d_ipiv, unsigned* bar_base);
 la_status launch_laswp_f32(la_ctx ctx, float* A, size_t ld, int n, int j0, int jb);
+la_status launch_panel_cluster_f32(la_ctx ctx, float* A, size_t ld, int m, int j0, int jb,
+                                   int* d_ipiv);
 la_status launch_trsm_rowpanel_f32(la_ctx ctx, float* A, size_t ld, int j0, int jb, int c_begin,
                                    int c_end);
 la_status launch_gemm_f32(la_ctx ctx, int mode, int M, int N, int K, const float* A, size_t lda,
@@ -142,6 +146,9 @@ la_status launch_lu_solve_f32(la_ctx ctx, const float* LU, size_t ld, float* X, 
 la_status launch_invert_diag_f32(la_ctx ctx, const float* LU, size_t ld, int n, double* dinv);
 la_status launch_trsv_wave_f32(la_ctx ctx, const float* LU, size_t ld, const double* dinv,
                                double* X, size_t ldx, int n, int nrhs, int* sync);
+la_status launch_invert_diag_f32f(la_ctx ctx, const float* LU, size_t ld, int n, float* dinv);
+la_status launch_trsv_wave_f32f(la_ctx ctx, const float* LU, size_t ld, const float* dinv,
+                                float* X, size_t ldx, int n, int nrhs, int* sync);
 la_status launch_lu_finish(la_ctx ctx, la_lu h, int* d_flags);
 // Enqueues the whole factorization of h (no readback, no synchronization);
 // lu_finish writes {pospivsign, zero-on-diagonal} to d_flags.

@@ -332,6 +332,7 @@ void la_lu_free(la_lu h) {
   la_device_free(ctx, h->d_lu);
   la_device_free(ctx, h->d_lu32);
   la_device_free(ctx, h->d_dinv);
+  la_device_free(ctx, h->d_dinvf);
   la_device_free(ctx, h->d_ipiv);
   la_device_free(ctx, h->d_piv);
   delete h;

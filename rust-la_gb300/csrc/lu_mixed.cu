@@ -4,8 +4,9 @@
 //
 // Factorization of an FP32 copy of A, two-level blocked right-looking:
 //   outer panels of width WO = 256, each factored by the FP32 form of the
-//   plain path (cooperative panel kernel, row swaps, row-panel triangular update
-//   and FP32 SIMT updates, inner width 64);
+//   plain path with inner width 32 (panel on one thread-block cluster,
+//   panel_cluster.cu, or the cooperative kernel; row swaps, row-panel
+//   triangular update, FP32 SIMT updates);
 //   outer row-panel triangular update U12 = L11^-1 A12 in FP32;
 //   trailing update A22 -= L21 * U12 on the tensor cores (gemm_tc.cu) with
 //   BF16 or FP16 operands and FP32 accumulation, or in FP32 SIMT (LA_PREC_FP32).
@@ -20,7 +21,7 @@
 namespace {
 
 constexpr int WO = 256;  // outer panel width (K of the tensor-core update)
-constexpr int WI = 64;   // inner panel width
+constexpr int WI = 32;   // inner panel width (the cluster panel kernel's width)
 
 size_t pad8(size_t x) { return (x + 7) & ~size_t(7); }
 
@@ -109,45 +110,84 @@ __global__ void pack_ut_kernel(const float* __restrict__ src, size_t lds, uint16
 
 __global__ void set_alpha_one(float* stat) { stat[0] = 0.f; stat[1] = 1.f; }
 
-// r = b - A x in FP64 for nrhs <= 16: one warp per row, each lane sums its
-// strided terms with FMA, the warp adds the lane sums in a tree. Also the
-// per-column maxima of |r| (into colmax[0..nrhs)).
+// r = b - A x in FP64 for nrhs <= R: the CTA stages 256-row chunks of X in
+// shared memory and each of its 8 warps handles RPW rows (lanes stride along
+// the row with FMA, then a warp tree); also the per-column maxima of |r|.
 template <int R>
 __global__ void __launch_bounds__(256)
 residual_f64_kernel(const double* __restrict__ A, size_t lda, const double* __restrict__ X,
                     size_t ldx, const double* __restrict__ B, size_t ldb, double* __restrict__ Rout,
                     size_t ldr, int n, int nrhs, double* colmax) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (int i = warp; i < n; i += nwarps) {
-    double s[R];
+  constexpr int RPW = R >= 16 ? 1 : 16 / R;
+  constexpr int KC = 256;
+  __shared__ double xs[KC][R];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int row0 = (blockIdx.x * 8 + warp) * RPW;
+  double s[RPW][R];
 #pragma unroll
-    for (int j = 0; j < R; j++) s[j] = 0.0;
-    const double* arow = A + (size_t)i * lda;
-    for (int k = lane; k < n; k += 32) {
-      const double a = arow[k];
-      const double* xr = X + (size_t)k * ldx;
+  for (int q = 0; q < RPW; q++)
 #pragma unroll
-      for (int j = 0; j < R; j++)
-        if (j < nrhs) s[j] = fma(a, xr[j], s[j]);
+    for (int j = 0; j < R; j++) s[q][j] = 0.0;
+  for (int k0 = 0; k0 < n; k0 += KC) {
+    for (int idx = threadIdx.x; idx < KC * R; idx += 256) {
+      const int k = idx / R, j = idx % R;
+      xs[k][j] = (k0 + k < n && j < nrhs) ? X[(size_t)(k0 + k) * ldx + j] : 0.0;
     }
+    __syncthreads();
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1)
+    for (int q = 0; q < RPW; q++) {
+      const int row = row0 + q;
+      if (row < n) {
+        const double* arow = A + (size_t)row * lda + k0;
+        for (int t = lane; t < KC && k0 + t < n; t += 32) {
+          const double a = arow[t];
 #pragma unroll
-      for (int j = 0; j < R; j++) s[j] += __shfl_down_sync(0xffffffffu, s[j], off);
-    if (lane == 0) {
+          for (int j = 0; j < R; j++) s[q][j] = fma(a, xs[t][j], s[q][j]);
+        }
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int q = 0; q < RPW; q++)
+#pragma unroll
+    for (int j = 0; j < R; j++)
+      for (int off = 16; off > 0; off >>= 1) s[q][j] += __shfl_down_sync(0xffffffffu, s[q][j], off);
+  if (lane == 0) {
+#pragma unroll
+    for (int q = 0; q < RPW; q++) {
+      const int row = row0 + q;
+      if (row >= n) continue;
 #pragma unroll
       for (int j = 0; j < R; j++) {
         if (j < nrhs) {
-          const double r = B[(size_t)i * ldb + j] - s[j];
-          Rout[(size_t)i * ldr + j] = r;
+          const double r = B[(size_t)row * ldb + j] - s[q][j];
+          Rout[(size_t)row * ldr + j] = r;
           atomicMax(reinterpret_cast<unsigned long long*>(colmax + j),
                     (unsigned long long)__double_as_longlong(fabs(r)));
         }
       }
     }
   }
+}
+
+template <int R>
+void launch_residual_r(int n, cudaStream_t st, const double* A, size_t lda, const double* X,
+                       size_t ldx, const double* B, size_t ldb, double* Rout, size_t ldr, int nrhs,
+                       double* colmax) {
+  constexpr int ROWS = 8 * (R >= 16 ? 1 : 16 / R);
+  residual_f64_kernel<R><<<(n + ROWS - 1) / ROWS, 256, 0, st>>>(A, lda, X, ldx, B, ldb, Rout, ldr,
+                                                                n, nrhs, colmax);
+}
+
+void launch_residual(int n, int nrhs, cudaStream_t st, const double* A, size_t lda, const double* X,
+                     size_t ldx, const double* B, size_t ldb, double* Rout, size_t ldr,
+                     double* colmax) {
+  if (nrhs <= 1) launch_residual_r<1>(n, st, A, lda, X, ldx, B, ldb, Rout, ldr, nrhs, colmax);
+  else if (nrhs <= 2) launch_residual_r<2>(n, st, A, lda, X, ldx, B, ldb, Rout, ldr, nrhs, colmax);
+  else if (nrhs <= 4) launch_residual_r<4>(n, st, A, lda, X, ldx, B, ldb, Rout, ldr, nrhs, colmax);
+  else if (nrhs <= 8) launch_residual_r<8>(n, st, A, lda, X, ldx, B, ldb, Rout, ldr, nrhs, colmax);
+  else launch_residual_r<16>(n, st, A, lda, X, ldx, B, ldb, Rout, ldr, nrhs, colmax);
 }
 
 // Column maxima of |M| (rows x cols) into out[0..cols) (non-negative IEEE bits).
@@ -178,28 +218,28 @@ __global__ void rownorm_kernel(const double* __restrict__ A, size_t lda, int n, 
   }
 }
 
-// w = r(piv,:) / rscale_j, the right-hand side of a correction solve.
+// w = r(piv,:) / rscale_j in FP32, the right-hand side of a correction solve.
 __global__ void scale_permute_kernel(const uint64_t* __restrict__ piv, const double* __restrict__ R,
                                      size_t ldr, const double* __restrict__ rscale,
-                                     double* __restrict__ W, size_t ldw, int n, int nrhs) {
+                                     float* __restrict__ W, size_t ldw, int n, int nrhs) {
   size_t total = (size_t)n * nrhs;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
        i += (size_t)gridDim.x * blockDim.x) {
     int r = (int)(i / nrhs), c = (int)(i % nrhs);
     const double s = rscale[c];
     const double v = R[(size_t)piv[r] * ldr + c];
-    W[(size_t)r * ldw + c] = s > 0 ? v / s : 0.0;
+    W[(size_t)r * ldw + c] = s > 0 ? (float)(v / s) : 0.f;
   }
 }
 
 // x += d * rscale_j (FP64 update of the solution).
-__global__ void update_x_kernel(double* __restrict__ X, size_t ldx, const double* __restrict__ D,
+__global__ void update_x_kernel(double* __restrict__ X, size_t ldx, const float* __restrict__ D,
                                 size_t ldd, const double* __restrict__ rscale, int n, int nrhs) {
   size_t total = (size_t)n * nrhs;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
        i += (size_t)gridDim.x * blockDim.x) {
     int r = (int)(i / nrhs), c = (int)(i % nrhs);
-    X[(size_t)r * ldx + c] += D[(size_t)r * ldd + c] * rscale[c];
+    X[(size_t)r * ldx + c] += (double)D[(size_t)r * ldd + c] * rscale[c];
   }
 }
 
@@ -226,12 +266,19 @@ namespace {
 
 // Inverted diagonal blocks for the wavefront triangular solves (once per handle).
 la_status ensure_dinv(la_ctx ctx, la_lu h) {
-  if (h->d_dinv) return LA_OK;
   const size_t nb = (h->n + 63) / 64;
   void* p = nullptr;
-  LA_TRY(la_device_alloc(ctx, &p, nb * 2 * 64 * 64 * sizeof(double)));
-  h->d_dinv = static_cast<double*>(p);
-  return launch_invert_diag_f32(ctx, h->d_lu32, h->ld32, (int)h->n, h->d_dinv);
+  if (!h->d_dinvf) {
+    LA_TRY(la_device_alloc(ctx, &p, nb * 2 * 64 * 64 * sizeof(float)));
+    h->d_dinvf = static_cast<float*>(p);
+    LA_TRY(launch_invert_diag_f32f(ctx, h->d_lu32, h->ld32, (int)h->n, h->d_dinvf));
+  }
+  if (!h->d_dinv) {
+    LA_TRY(la_device_alloc(ctx, &p, nb * 2 * 64 * 64 * sizeof(double)));
+    h->d_dinv = static_cast<double*>(p);
+    LA_TRY(launch_invert_diag_f32(ctx, h->d_lu32, h->ld32, (int)h->n, h->d_dinv));
+  }
+  return LA_OK;
 }
 
 // Factors h->d_lu32 (m x n, pitch ld32) in place; pivots into h->d_ipiv.
@@ -259,7 +306,13 @@ la_status mixed_factor(la_ctx ctx, la_lu h, int prec) {
     for (int i0 = j0; i0 < j1o; i0 += WI) {
       const int ib = std::min(WI, j1o - i0);
       const int i1 = i0 + ib;
-      LA_TRY(launch_panel_f32(ctx, st, A, ld, m, i0, ib, h->d_ipiv, &bar_base));
+      // One thread-block cluster holds the panel when it fits; else the
+      // cooperative multi-CTA kernel.
+      la_status ps = ctx->cluster_panels ? launch_panel_cluster_f32(ctx, A, ld, m, i0, ib, h->d_ipiv)
+                                         : LA_UNSUPPORTED;
+      if (ps == LA_UNSUPPORTED)
+        ps = launch_panel_f32(ctx, st, A, ld, m, i0, ib, h->d_ipiv, &bar_base);
+      LA_TRY(ps);
       LA_TRY(launch_laswp_f32(ctx, A, ld, n, i0, ib));
       if (i1 < j1o) {
         LA_TRY(launch_trsm_rowpanel_f32(ctx, A, ld, i0, ib, i1, j1o));
@@ -384,7 +437,7 @@ la_status la_lu_solve_refined_device(la_lu h, const double* d_b, size_t ldb, siz
   const size_t ldw = 4 * ((nrhs + 3) / 4);
   Buf rbuf(ctx), wbuf(ctx), norms(ctx), sync(ctx);
   LA_TRY(rbuf.alloc((size_t)n * nrhs * 8));
-  LA_TRY(wbuf.alloc((size_t)n * ldw * 8));
+  LA_TRY(wbuf.alloc((size_t)n * ldw * 4));
   const int nb64 = (n + 63) / 64;
   LA_TRY(sync.alloc((size_t)(2 * nb64 + 2) * sizeof(int)));
   LA_TRY(ensure_dinv(ctx, h));
@@ -392,7 +445,7 @@ la_status la_lu_solve_refined_device(la_lu h, const double* d_b, size_t ldb, siz
   LA_TRY(norms.alloc(128 * 8));
   double* d_norm = norms.as<double>();
   double* d_r = rbuf.as<double>();
-  double* d_w = wbuf.as<double>();
+  float* d_w = wbuf.as<float>();
   LA_CUDA(ctx, cudaMemsetAsync(d_norm, 0, 128 * 8, st));
   rownorm_kernel<<<grid_for(ctx, (size_t)n * 32), 256, 0, st>>>(h->d_lu, h->ld, n, d_norm);
   colmax_kernel<<<grid_for(ctx, (size_t)n * nrhs), 256, 0, st>>>(d_b, ldb, n, R, d_norm + 56);
@@ -424,8 +477,7 @@ la_status la_lu_solve_refined_device(la_lu h, const double* d_b, size_t ldb, siz
   // r = b - A x and its column maxima.
   auto residual = [&]() -> la_status {
     LA_CUDA(ctx, cudaMemsetAsync(d_norm + 8, 0, 16 * 8, st));
-    residual_f64_kernel<16><<<std::min((n + 7) / 8, ctx->sm_count * 8), 256, 0, st>>>(
-        h->d_lu, h->ld, d_x, ldx, d_b, ldb, d_r, nrhs, n, R, d_norm + 8);
+    launch_residual(n, R, st, h->d_lu, h->ld, d_x, ldx, d_b, ldb, d_r, nrhs, d_norm + 8);
     ctx->launches++;
     return la_check_launch(ctx, "residual");
   };
@@ -440,8 +492,8 @@ la_status la_lu_solve_refined_device(la_lu h, const double* d_b, size_t ldb, siz
     scale_permute_kernel<<<grid_for(ctx, (size_t)n * nrhs), 256, 0, st>>>(
         h->d_piv, d_r, nrhs, d_norm + 8, d_w, ldw, n, R);
     ctx->launches++;
-    LA_TRY(launch_trsv_wave_f32(ctx, h->d_lu32, h->ld32, h->d_dinv, d_w, ldw, n, R,
-                                sync.as<int>()));
+    LA_TRY(launch_trsv_wave_f32f(ctx, h->d_lu32, h->ld32, h->d_dinvf, d_w, ldw, n, R,
+                                 sync.as<int>()));
     update_x_kernel<<<grid_for(ctx, (size_t)n * nrhs), 256, 0, st>>>(d_x, ldx, d_w, ldw,
                                                                       d_norm + 8, n, R);
     ctx->launches++;

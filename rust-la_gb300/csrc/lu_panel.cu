@@ -79,14 +79,23 @@ __device__ bool grid_barrier(unsigned* counter, unsigned target, int* err) {
   return ok != 0;
 }
 
-// Ordering key of a pivot candidate. NaN never wins a strict '>' test, so a
-// NaN below the diagonal ranks lowest; a NaN on the diagonal row j is never
-// displaced, so it ranks highest (ties go to the lowest position, which is j).
-__device__ __forceinline__ double pivot_key(double v, int pos, int j) {
-  if (v != v) return pos == j ? __longlong_as_double(0x7ff0000000000000ll) : -1.0;
-  return fabs(v);
+// Ordering key of a pivot candidate, as an integer so that no FP64
+// instruction is spent on comparisons (the FP64 pipe is slow on this GPU):
+// bits(|v|) + 1 orders like |v| for every non-NaN value. NaN never wins a strict
+// '>' test, so a NaN below the diagonal gets 0 (below everything); a NaN on the
+// diagonal row j is never displaced, so it gets the maximum (ties go to the
+// lowest position, which is j).
+__device__ __forceinline__ unsigned long long pivot_key(double v, int pos, int j) {
+  const unsigned long long a = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+  if (a > 0x7ff0000000000000ull) return pos == j ? ~0ull : 0ull;
+  return a + 1ull;
 }
-__device__ __forceinline__ bool better(double ka, int pa, double kb, int pb) {
+__device__ __forceinline__ unsigned long long pivot_key(float v, int pos, int j) {
+  const unsigned a = __float_as_uint(v) & 0x7fffffffu;
+  if (a > 0x7f800000u) return pos == j ? ~0ull : 0ull;
+  return (unsigned long long)a + 1ull;
+}
+__device__ __forceinline__ bool better(unsigned long long ka, int pa, unsigned long long kb, int pb) {
   // a beats b: larger key, or equal key and lower position; pb < 0 means empty.
   if (pb < 0) return pa >= 0;
   if (pa < 0) return false;
@@ -102,7 +111,7 @@ struct PanelParams {
   unsigned* bar;
   unsigned bar_base;  // counter value at kernel start (the counter only grows)
   int* err;
-  double* cand_abs;
+  unsigned long long* cand_key;
   int* cand_pos;
   double* cand_row;
   double* diag_a;
@@ -126,7 +135,7 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
   T* drow_a = urow + W;                      // [W] row j as published (raw)
   T* drow_s = drow_a + W;                    // [W] its running sums (EXACT)
   T* lrow = drow_s + W;                      // [rpc] multipliers of this step
-  __shared__ double red_k[PT / 32];
+  __shared__ unsigned long long red_k[PT / 32];
   __shared__ int red_p[PT / 32];
   __shared__ int s_win_pos;
   __shared__ T s_scale;
@@ -156,33 +165,34 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
     const int j = p.j0 + c;
     const int par = c & 1;
     // 1. local candidate over owned rows at positions >= j.
-    double bk = 0.0;
+    unsigned long long bk = 0ull;
     int bp = -1;
     for (int r = max(0, j - row0) + tid; r < nrows; r += PT) {
       const int pos = row0 + r;
-      double v = EXACT ? __dsub_rn(va[r * W + c], vs[r * W + c]) : (double)va[r * W + c];
-      double k = pivot_key(v, pos, j);
+      const unsigned long long k =
+          EXACT ? pivot_key((double)__dsub_rn(va[r * W + c], vs[r * W + c]), pos, j)
+                : pivot_key(va[r * W + c], pos, j);
       if (better(k, pos, bk, bp)) { bk = k; bp = pos; }
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
-      double ok = __shfl_down_sync(0xffffffffu, bk, off);
+      unsigned long long ok = __shfl_down_sync(0xffffffffu, bk, off);
       int op = __shfl_down_sync(0xffffffffu, bp, off);
       if (better(ok, op, bk, bp)) { bk = ok; bp = op; }
     }
     if (lane == 0) { red_k[warp] = bk; red_p[warp] = bp; }
     __syncthreads();
     if (warp == 0) {
-      bk = lane < PT / 32 ? red_k[lane] : 0.0;
+      bk = lane < PT / 32 ? red_k[lane] : 0ull;
       bp = lane < PT / 32 ? red_p[lane] : -1;
 #pragma unroll
       for (int off = 4; off > 0; off >>= 1) {
-        double ok = __shfl_down_sync(0xffffffffu, bk, off);
+        unsigned long long ok = __shfl_down_sync(0xffffffffu, bk, off);
         int op = __shfl_down_sync(0xffffffffu, bp, off);
         if (better(ok, op, bk, bp)) { bk = ok; bp = op; }
       }
       if (lane == 0) {
-        p.cand_abs[par * p.cstride + g] = bk;
+        p.cand_key[par * p.cstride + g] = bk;
         p.cand_pos[par * p.cstride + g] = bp;
         s_win_pos = bp;
       }
@@ -208,10 +218,10 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
     // 3. global winner (identical in every CTA): one candidate per thread; the
     //    last W threads fetch row j at the same time (needed if it moves here).
     {
-      double k = 0.0;
+      unsigned long long k = 0ull;
       int ps = -1;
       if (tid < p.G) {
-        k = __ldcg(p.cand_abs + par * p.cstride + tid);
+        k = __ldcg(p.cand_key + par * p.cstride + tid);
         ps = __ldcg(p.cand_pos + par * p.cstride + tid);
       }
       if (tid >= PT - W) {
@@ -221,18 +231,18 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
       }
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) {
-        double ok = __shfl_down_sync(0xffffffffu, k, off);
+        unsigned long long ok = __shfl_down_sync(0xffffffffu, k, off);
         int op = __shfl_down_sync(0xffffffffu, ps, off);
         if (better(ok, op, k, ps)) { k = ok; ps = op; }
       }
       if (lane == 0) { red_k[warp] = k; red_p[warp] = ps; }
       __syncthreads();
       if (warp == 0) {
-        k = lane < PT / 32 ? red_k[lane] : 0.0;
+        k = lane < PT / 32 ? red_k[lane] : 0ull;
         ps = lane < PT / 32 ? red_p[lane] : -1;
 #pragma unroll
         for (int off = 4; off > 0; off >>= 1) {
-          double ok = __shfl_down_sync(0xffffffffu, k, off);
+          unsigned long long ok = __shfl_down_sync(0xffffffffu, k, off);
           int op = __shfl_down_sync(0xffffffffu, ps, off);
           if (better(ok, op, k, ps)) { k = ok; ps = op; }
         }
@@ -369,7 +379,7 @@ la_status launch_panel_t(la_ctx ctx, cudaStream_t stream, bool exact, T* A, T* S
   p.bar = ctx->d_bar;
   p.bar_base = *bar_base;
   p.err = ctx->d_err;
-  p.cand_abs = ctx->d_cand_abs;
+  p.cand_key = reinterpret_cast<unsigned long long*>(ctx->d_cand_abs);
   p.cand_pos = ctx->d_cand_pos;
   p.cand_row = ctx->d_cand_row;
   p.diag_a = ctx->d_diag_a;

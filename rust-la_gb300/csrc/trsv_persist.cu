@@ -171,10 +171,17 @@ void configure_wave() {
   cudaFuncSetAttribute(invert_diag_kernel<float, double>,
                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)(2 * BS * (BS + 1) * sizeof(double)));
+  cudaFuncSetAttribute(invert_diag_kernel<float, float>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)(2 * BS * (BS + 1) * sizeof(float)));
   cudaFuncSetAttribute(trsv_wave_kernel<float, double, false>,
                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wave_smem<float, double>());
   cudaFuncSetAttribute(trsv_wave_kernel<float, double, true>,
                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wave_smem<float, double>());
+  cudaFuncSetAttribute(trsv_wave_kernel<float, float, false>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wave_smem<float, float>());
+  cudaFuncSetAttribute(trsv_wave_kernel<float, float, true>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wave_smem<float, float>());
   done = true;
 }
 
@@ -206,6 +213,37 @@ la_status launch_trsv_wave_f32(la_ctx ctx, const float* LU, size_t ld, const dou
   LA_TRY(la_check_launch(ctx, "trsv_wave_kernel"));
   trsv_wave_kernel<float, double, true><<<nb, TT, sm, ctx->stream>>>(LU, ld, dinv, X, ldx, n, nrhs,
                                                                     nb, fu, tickets + 1, ctx->d_err);
+  ctx->launches++;
+  return la_check_launch(ctx, "trsv_wave_kernel");
+}
+
+// FP32 vectors (the correction solves of plain refinement, which only need
+// the factorization's own accuracy): inverted blocks in FP32 too.
+la_status launch_invert_diag_f32f(la_ctx ctx, const float* LU, size_t ld, int n, float* dinv) {
+  const int nb = (n + BS - 1) / BS;
+  configure_wave();
+  invert_diag_kernel<float, float><<<dim3(nb, 2), BS, 2 * BS * (BS + 1) * sizeof(float),
+                                     ctx->stream>>>(LU, ld, n, dinv);
+  ctx->launches++;
+  return la_check_launch(ctx, "invert_diag_kernel");
+}
+
+la_status launch_trsv_wave_f32f(la_ctx ctx, const float* LU, size_t ld, const float* dinv,
+                                float* X, size_t ldx, int n, int nrhs, int* sync) {
+  if (nrhs > MAXR) return LA_UNSUPPORTED;
+  const int nb = (n + BS - 1) / BS;
+  int* fl = sync;
+  int* fu = sync + nb;
+  int* tickets = sync + 2 * nb;
+  LA_CUDA(ctx, cudaMemsetAsync(sync, 0, (2 * nb + 2) * sizeof(int), ctx->stream));
+  configure_wave();
+  const size_t sm = wave_smem<float, float>();
+  trsv_wave_kernel<float, float, false><<<nb, TT, sm, ctx->stream>>>(LU, ld, dinv, X, ldx, n, nrhs,
+                                                                    nb, fl, tickets, ctx->d_err);
+  ctx->launches++;
+  LA_TRY(la_check_launch(ctx, "trsv_wave_kernel"));
+  trsv_wave_kernel<float, float, true><<<nb, TT, sm, ctx->stream>>>(LU, ld, dinv, X, ldx, n, nrhs,
+                                                                   nb, fu, tickets + 1, ctx->d_err);
   ctx->launches++;
   return la_check_launch(ctx, "trsv_wave_kernel");
 }

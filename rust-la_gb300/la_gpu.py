@@ -25,7 +25,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "liblagpu.so")
 
 OK, SINGULAR, BADSHAPE, INVALID, NOMEM, CUDA_ERROR, TIMEOUT, NOT_CONVERGED, UNSUPPORTED = range(9)
-OPT_ARITH, OPT_PANEL_WIDTH, OPT_PANEL_CTAS, OPT_PROFILE, OPT_LOOKAHEAD = 1, 2, 3, 4, 5
+OPT_ARITH, OPT_PANEL_WIDTH, OPT_PANEL_CTAS, OPT_PROFILE, OPT_LOOKAHEAD, OPT_CLUSTER_PANEL = 1, 2, 3, 4, 5, 6
 ARITH_FAST, ARITH_EXACT = 0, 1
 
 

@@ -111,3 +111,19 @@ def test_ill_conditioned_refinement_converges(lagpu, ctx_fast, torch, prec, kapp
     assert st == lagpu.OK, (stats.iterations, stats.gmres_steps, stats.eta)
     eta = oracle.backward_error(a.cpu().numpy(), x.cpu().numpy(), b.cpu().numpy())
     assert eta <= ETA_MAX
+
+
+def test_cluster_and_cooperative_fp32_panels_agree(lagpu, torch):
+    # The two FP32 panel kernels implement the same pivoting: identical factors.
+    n = 1500
+    rng = np.random.default_rng(44)
+    a = torch.from_numpy(rng.standard_normal((n, n))).cuda()
+    outs = []
+    for cl in (1, 0):
+        ctx = lagpu.Context(0)
+        ctx.set_option(lagpu.OPT_CLUSTER_PANEL, cl)
+        lu = lagpu.lu_mixed_new_device(ctx, a.data_ptr(), n, n, 3)
+        outs.append(lu.get_piv())
+        lu.free()
+        ctx.close()
+    assert np.array_equal(outs[0], outs[1])
