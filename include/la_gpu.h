@@ -188,6 +188,47 @@ la_status la_lowp_update_device(la_ctx ctx, int fmt, size_t m, size_t n, size_t 
                                 const void* d_a16, size_t lda, const void* d_b16, size_t ldb,
                                 float* d_c, size_t ldc, float alpha);
 
+/* ---- batched solves of many small systems (no reference counterpart) ----- */
+
+/* One system of a batch: A at d_a + a_offset (n x n, row-major FP64), B and X
+ * at d_b / d_x + b_offset (n x nrhs, row-major FP64); 1 <= n <= 256,
+ * 1 <= nrhs <= 4. */
+typedef struct la_batch_system {
+  size_t a_offset;
+  size_t b_offset;
+  int n;
+  int nrhs;
+} la_batch_system;
+
+#define LA_BATCH_FP64 0   /* plain FP64 LU + solve per system */
+#define LA_BATCH_MIXED 1  /* FP32 LU + FP64 refinement, FP64 redo where it stalls */
+
+typedef struct la_batch_plan_s* la_batch_plan;
+
+/* Builds the work queue (systems sorted by decreasing n), the scratch, and a
+ * CUDA graph holding the whole batch: one persistent fused factor + solve
+ * launch (plus, for LA_BATCH_MIXED, the FP64 pass over systems whose
+ * refinement did not reach `tol` within `max_iters`). ctas_per_sm (1-4) sets
+ * how many CTAs share an SM and hence each CTA's shared memory; systems that
+ * do not fit work in global scratch. The plan runs once while it is built. */
+la_status la_batch_plan_create(la_ctx ctx, const double* d_a, const double* d_b, double* d_x,
+                               const la_batch_system* systems, int count, int mode,
+                               int ctas_per_sm, double tol, int max_iters, la_batch_plan* out);
+/* Launches the plan's graph on the context's stream (asynchronous). */
+la_status la_batch_plan_run(la_batch_plan plan);
+/* Per system (caller's order): refinement steps, final backward error (-1 when
+ * the FP64 kernel produced the answer), and 1 when the FP64 pass redid it.
+ * Any pointer may be NULL. Synchronizes. */
+la_status la_batch_plan_stats(la_batch_plan plan, int* iterations, double* eta, int* fell_back);
+void la_batch_plan_destroy(la_batch_plan plan);
+/* Autotuner: times every ctas_per_sm in 1..4 on this batch and returns the
+ * fastest; appends "mode count mean_n ctas_per_sm ms" lines for all candidates
+ * to table_path when it is not NULL. */
+la_status la_batch_autotune(la_ctx ctx, const double* d_a, const double* d_b, double* d_x,
+                            const la_batch_system* systems, int count, int mode, double tol,
+                            int max_iters, const char* table_path, int* best_ctas_per_sm,
+                            double* best_ms);
+
 /* ---- allocation-free factorization (no reference counterpart) ------------ */
 
 /* LU factorization (FAST arithmetic) for callers that cannot allocate device

@@ -84,7 +84,19 @@ SIGNATURES = {
     "la_lu_mixed_new_device": ([_P, _P, _S, _S, _I, _P], _I),
     "la_lu_solve_refined_device": ([_P, _P, _S, _S, _P, _S, _I, _D, _P], _I),
     "la_lowp_update_device": ([_P, _I, _S, _S, _S, _P, _S, _P, _S, _P, _S, ctypes.c_float], _I),
+    "la_batch_plan_create": ([_P, _P, _P, _P, _P, _I, _I, _I, _D, _I, _P], _I),
+    "la_batch_plan_run": ([_P], _I),
+    "la_batch_plan_stats": ([_P, _P, _P, _P], _I),
+    "la_batch_plan_destroy": ([_P], None),
+    "la_batch_autotune": ([_P, _P, _P, _P, _P, _I, _I, _D, _I, ctypes.c_char_p, _P, _P], _I),
 }
+
+BATCH_FP64, BATCH_MIXED = 0, 1
+
+
+class BatchSystem(ctypes.Structure):
+    _fields_ = [("a_offset", ctypes.c_size_t), ("b_offset", ctypes.c_size_t),
+                ("n", ctypes.c_int), ("nrhs", ctypes.c_int)]
 
 PREC_BF16, PREC_FP16, PREC_FP32 = 1, 2, 3
 
@@ -435,6 +447,62 @@ def lowp_update_device(ctx, fmt, m_, n, k, a_ptr, lda, b_ptr, ldb, c_ptr, ldc, a
                                      ctypes.c_void_p(b_ptr), ldb, ctypes.c_void_p(c_ptr), ldc,
                                      ctypes.c_float(alpha))
     return _check(ctx, st)
+
+
+def batch_systems(ns, nrhss):
+    """Packs per-system sizes into la_batch_system records with dense offsets."""
+    arr = (BatchSystem * len(ns))()
+    ao = bo = 0
+    for i, (n, r) in enumerate(zip(ns, nrhss)):
+        arr[i].a_offset, arr[i].b_offset, arr[i].n, arr[i].nrhs = ao, bo, int(n), int(r)
+        ao += int(n) * int(n)
+        bo += int(n) * int(r)
+    return arr, ao, bo
+
+
+class BatchPlan:
+    """A captured batched factor + solve (la_batch_plan)."""
+
+    def __init__(self, ctx, a_ptr, b_ptr, x_ptr, systems, mode, ctas_per_sm=1, tol=1e-14,
+                 max_iters=10):
+        self.ctx = ctx
+        self.count = len(systems)
+        self.h = ctypes.c_void_p()
+        _check(ctx, lib().la_batch_plan_create(ctx.h, ctypes.c_void_p(a_ptr), ctypes.c_void_p(b_ptr),
+                                               ctypes.c_void_p(x_ptr), systems, self.count, mode,
+                                               ctas_per_sm, tol, max_iters, ctypes.byref(self.h)))
+
+    def run(self):
+        _check(self.ctx, lib().la_batch_plan_run(self.h))
+
+    def stats(self):
+        its = np.empty(self.count, dtype=np.int32)
+        eta = np.empty(self.count, dtype=np.float64)
+        fb = np.empty(self.count, dtype=np.int32)
+        _check(self.ctx, lib().la_batch_plan_stats(self.h, _ptr(its), _ptr(eta), _ptr(fb)))
+        return its, eta, fb
+
+    def free(self):
+        if self.h:
+            lib().la_batch_plan_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def batch_autotune(ctx, a_ptr, b_ptr, x_ptr, systems, mode, tol=1e-14, max_iters=10,
+                   table_path=None):
+    best = ctypes.c_int()
+    ms = ctypes.c_double()
+    _check(ctx, lib().la_batch_autotune(ctx.h, ctypes.c_void_p(a_ptr), ctypes.c_void_p(b_ptr),
+                                        ctypes.c_void_p(x_ptr), systems, len(systems), mode, tol,
+                                        max_iters, table_path.encode() if table_path else None,
+                                        ctypes.byref(best), ctypes.byref(ms)))
+    return best.value, ms.value
 
 
 def matrix_mul_device(ctx, a_ptr, lda, b_ptr, ldb, c_ptr, ldc, m_, k, n):
