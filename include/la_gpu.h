@@ -158,6 +158,7 @@ la_status la_matrix_mul_device(la_ctx ctx, const double* d_a, size_t lda, const 
 #define LA_PREC_BF16 1  /* tcgen05 BF16 x BF16 -> FP32 */
 #define LA_PREC_FP16 2  /* tcgen05 FP16 x FP16 -> FP32, per-panel power-of-two scaling */
 #define LA_PREC_FP32 3  /* FP32 FMA (no tensor cores) */
+#define LA_PREC_FP8 4   /* batched solves: factors stored as FP8 e4m3 (power-of-two scaled) */
 
 typedef struct la_refine_stats {
   int iterations;    /* refinement steps (plain and GMRES) */
@@ -191,29 +192,39 @@ la_status la_lowp_update_device(la_ctx ctx, int fmt, size_t m, size_t n, size_t 
 /* ---- batched solves of many small systems (no reference counterpart) ----- */
 
 /* One system of a batch: A at d_a + a_offset (n x n, row-major FP64), B and X
- * at d_b / d_x + b_offset (n x nrhs, row-major FP64); 1 <= n <= 256,
- * 1 <= nrhs <= 4. */
+ * at d_b / d_x + b_offset (n x nrhs, row-major FP64); 1 <= n <= 512,
+ * 1 <= nrhs <= 4. `precision` (mixed batches) is the storage of its LU
+ * factors: LA_PREC_FP8, LA_PREC_BF16 or LA_PREC_FP32 (0 = FP32); arithmetic is
+ * FP32 either way, and narrower storage lets larger systems stay in shared
+ * memory at the cost of less accurate factors. */
 typedef struct la_batch_system {
   size_t a_offset;
   size_t b_offset;
   int n;
   int nrhs;
+  int precision;
+  int reserved;
 } la_batch_system;
 
 #define LA_BATCH_FP64 0   /* plain FP64 LU + solve per system */
-#define LA_BATCH_MIXED 1  /* FP32 LU + FP64 refinement, FP64 redo where it stalls */
+#define LA_BATCH_MIXED 1  /* low-precision LU + FP64 refinement, FP64 redo where it stalls */
 
 typedef struct la_batch_plan_s* la_batch_plan;
 
 /* Builds the work queue (systems sorted by decreasing n), the scratch, and a
  * CUDA graph holding the whole batch: one persistent fused factor + solve
  * launch (plus, for LA_BATCH_MIXED, the FP64 pass over systems whose
- * refinement did not reach `tol` within `max_iters`). ctas_per_sm (1-4) sets
- * how many CTAs share an SM and hence each CTA's shared memory; systems that
- * do not fit work in global scratch. The plan runs once while it is built. */
+ * refinement did not reach `tol` within `max_iters`). Each system is worked by
+ * one CTA of 32 * warps_per_system threads (2, 4 or 8; 0 = 8); ctas_per_sm
+ * (1-8) such CTAs share an SM and its shared memory, and a system whose
+ * layout does not fit its CTA's share works with its matrix in global
+ * scratch. LA_UNSUPPORTED when the largest system cannot fit even so, or when
+ * ctas_per_sm CTAs of that size cannot be resident on one SM. The plan runs
+ * once while it is built. */
 la_status la_batch_plan_create(la_ctx ctx, const double* d_a, const double* d_b, double* d_x,
                                const la_batch_system* systems, int count, int mode,
-                               int ctas_per_sm, double tol, int max_iters, la_batch_plan* out);
+                               int ctas_per_sm, int warps_per_system, double tol, int max_iters,
+                               la_batch_plan* out);
 /* Launches the plan's graph on the context's stream (asynchronous). */
 la_status la_batch_plan_run(la_batch_plan plan);
 /* Per system (caller's order): refinement steps, final backward error (-1 when
@@ -221,13 +232,77 @@ la_status la_batch_plan_run(la_batch_plan plan);
  * Any pointer may be NULL. Synchronizes. */
 la_status la_batch_plan_stats(la_batch_plan plan, int* iterations, double* eta, int* fell_back);
 void la_batch_plan_destroy(la_batch_plan plan);
-/* Autotuner: times every ctas_per_sm in 1..4 on this batch and returns the
- * fastest; appends "mode count mean_n ctas_per_sm ms" lines for all candidates
- * to table_path when it is not NULL. */
+/* Autotuner: times every supported (ctas_per_sm, warps_per_system) pair in
+ * {1, 2, 4, 8} x {8, 4, 2} on this batch and returns the fastest; appends
+ * "mode count mean_n ctas_per_sm warps_per_system ms" lines for all candidates
+ * to table_path when it is not NULL. best_warps_per_system may be NULL. */
 la_status la_batch_autotune(la_ctx ctx, const double* d_a, const double* d_b, double* d_x,
                             const la_batch_system* systems, int count, int mode, double tol,
                             int max_iters, const char* table_path, int* best_ctas_per_sm,
-                            double* best_ms);
+                            int* best_warps_per_system, double* best_ms);
+
+/* Sets each system's factor storage from d_class (device, caller's order, one
+ * int per system: 0 = FP8, 1 = BF16, 2 = FP32, the classes of the precision
+ * selector) for the following runs of a LA_BATCH_MIXED plan, without
+ * rebuilding it; asynchronous on the context's stream. */
+la_status la_batch_plan_select_device(la_batch_plan plan, const int* d_class);
+/* Phase profile of the last run: SM cycles summed over all CTAs, phase[0..3]
+ * = load (and FP8 scaling), factorization, triangular solves, residuals and
+ * convergence tests of the first pass; phase[4..7] the same for the FP64 redo
+ * pass of a LA_BATCH_MIXED plan. Synchronizes. */
+la_status la_batch_plan_phase_cycles(la_batch_plan plan, long long* phase);
+/* Per system (caller's order): SM clock cycles its CTA spent on it in the last
+ * run, summed over the mixed and the FP64 pass. Synchronizes. */
+la_status la_batch_plan_cycles(la_batch_plan plan, long long* cycles);
+
+/* ---- learned precision selector (no reference counterpart) --------------- */
+
+/* 16 features per system (row-major FP32 [count][16]) for the precision
+ * selector: log2 n / 9, nrhs / 4, log10 of the max row and column sums, of the
+ * Frobenius norm, of max |a_ij|, of the 8-step Lanczos estimate of sigma_max,
+ * of ||A||_F / sigma_max, of the smallest diagonal-dominance ratio, the mean
+ * log10 dominance ratio, the fraction of dominant rows, log10 of the row-sum
+ * and column-sum spreads, the relative asymmetry ||A - A^T||_F / ||A||_F,
+ * log10 min|a_ii| / max|a_ij|, and log10 of the Lanczos estimate of
+ * sigma_max / sigma_min (a lower bound on kappa_2). Systems as in a batch
+ * plan (1 <= n <= 512); synchronizes. */
+la_status la_batch_features_device(la_ctx ctx, const double* d_a, const la_batch_system* systems,
+                                   int count, float* d_features);
+
+/* Householder-conditioned test systems: A_i = H1 diag(s) H2 with
+ * s_k = kappa_i^(-k/(n-1)), log10 kappa_i uniform in [log10_kappa_min,
+ * log10_kappa_max], H1 and H2 products of four random reflectors, B_i iid
+ * N(0,1); all seeded (counter-based, reproducible). d_kappa (count doubles)
+ * may be NULL. Synchronizes. */
+la_status la_generate_conditioned_batch(la_ctx ctx, const la_batch_system* systems, int count,
+                                        double log10_kappa_min, double log10_kappa_max,
+                                        unsigned long long seed, double* d_a, double* d_b,
+                                        double* d_kappa);
+
+/* MLP 16 -> 64 -> 64 -> 3 (ReLU, softmax; FP32) over the classes
+ * 0 = LA_PREC_FP8, 1 = LA_PREC_BF16, 2 = LA_PREC_FP32. Parameters, in order:
+ * W1[64][16], b1[64], W2[64][64], b2[64], W3[3][64], b3[3]
+ * (la_mlp_param_count() floats), then the feature means[16] and standard
+ * deviations[16] the inputs are normalised with. */
+typedef struct la_mlp_s* la_mlp;
+int la_mlp_param_count(void);
+la_status la_mlp_create(la_ctx ctx, unsigned long long seed, la_mlp* out);
+void la_mlp_destroy(la_mlp mlp);
+/* params: la_mlp_param_count() + 32 floats (host). Setting resets Adam. */
+la_status la_mlp_get_params(la_mlp mlp, float* params);
+la_status la_mlp_set_params(la_mlp mlp, const float* params);
+/* Mean softmax cross-entropy over count samples (d_x [count][16], d_y labels
+ * 0..2, device) and its gradient (host, la_mlp_param_count() floats; NULL to
+ * skip); no update. Synchronizes. */
+la_status la_mlp_gradients(la_mlp mlp, const float* d_x, const int* d_y, int count, float* grad,
+                           float* loss);
+/* One Adam step (beta 0.9 / 0.999) on the mean cross-entropy of the samples;
+ * loss (host, may be NULL) is taken before the step and synchronizes. */
+la_status la_mlp_train_step(la_mlp mlp, const float* d_x, const int* d_y, int count, float lr,
+                            float* loss);
+/* Class probabilities (d_probs [count][3], may be NULL) and argmax classes
+ * (d_class, may be NULL); asynchronous on the context's stream. */
+la_status la_mlp_predict(la_mlp mlp, const float* d_x, int count, float* d_probs, int* d_class);
 
 /* ---- allocation-free factorization (no reference counterpart) ------------ */
 

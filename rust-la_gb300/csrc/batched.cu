@@ -1,34 +1,82 @@
 // Batched solves of many small, unevenly sized systems (not in the reference;
 // each system is LUDecomposition::new + solve, lu.rs:104-278, on its own).
 //
-// One persistent kernel per precision: every CTA takes the next system from an
-// atomic work queue (descriptors sorted by decreasing n^3 on the host, so
-// the largest systems start first and the tail is short), then
-//   loads A_i (FP64 in HBM) into its working matrix: shared memory when it fits,
-//   else the CTA's slice of a global scratch buffer (L2-resident at these sizes);
-//   factors it with partial pivoting (the reference's first-maximum pivot rule)
-//   by right-looking rank-1 updates over a 16 x 16 thread grid;
+// One persistent kernel per pass: every CTA takes the next system from an
+// atomic work queue (descriptors sorted by decreasing n, i.e. by cost, so the
+// largest systems start first and the tail is short), then
+//   loads A_i (FP64 in HBM) into its working matrix: shared memory when the
+//   system's whole layout fits the CTA's budget, else the CTA's slice of a
+//   global scratch buffer;
+//   factors it by a blocked right-looking LU with partial pivoting (the
+//   reference's first-maximum pivot rule, lu.rs:132-137) with implicit row
+//   swaps: a row map sends logical rows to physical rows, so a swap moves two
+//   integers and the final map is the permutation P (lu.rs:245-254);
 //   solves for B_i and writes X_i.
-// MIXED factors in FP32 and then refines in FP64 per system: r = b - A x
-// with A_i read again in FP64, d = LU32 \ r, x += d, until the normwise
-// backward error <= tol or max_iters; systems that do not converge are flagged
-// for the FP64 pass, which the same graph runs afterwards over flagged systems
-// only. All state is per CTA; no CTA waits on another.
+// Per 16-column panel: the panel is staged in shared memory in the arithmetic
+// type, factored column by column (each thread owns rows, two barriers per
+// column), written back; U12 = L11^-1 A12 is solved with each column in
+// registers; A22 -= L21 U12 is register-tiled (a thread holds 4x4 of A22 and
+// its rows of L21, all loads of a tile are issued before its FMAs).
+// The working matrix is stored in the system's factor precision: FP64 (plain
+// pass), FP32, BF16 or FP8 e4m3 (mixed pass; FP8 with a power-of-two scale of
+// A_i), with FP32 arithmetic for the low precisions. Narrower storage keeps
+// larger systems in shared memory but gives less accurate factors. The mixed
+// pass then refines each system in FP64 (r = b - A x with A_i read again in
+// FP64, d = LU \ r, x += d) until its normwise backward error <= tol or
+// max_iters; systems that do not converge are flagged and the FP64 pass, run
+// after it in the same CUDA graph, redoes only those. All state is per CTA; no
+// CTA waits on another.
+#include <cuda_fp8.h>
+
 #include "la_internal.cuh"
 
 namespace {
 
-constexpr int BT = 256;  // threads per CTA (16 x 16 update grid)
+constexpr int BT_MAX = 256;  // threads per CTA (one system per CTA): 64, 128 or 256
+constexpr int NW_MAX = BT_MAX / 32;
+constexpr int NMAX = 512;  // largest system
+constexpr int PBW = 16;    // panel width of the per-system LU
+constexpr int SP = 17;     // pitch of the staged panel (odd: rows fall in distinct banks)
 
 struct SysDesc {
-  long long a;     // offset of A_i (n x n, row-major) in the A buffer, elements
-  long long b;     // offset of B_i / X_i (n x nrhs, row-major), elements
-  int n, nrhs;
+  long long a;  // offset of A_i (n x n, row-major) in the A buffer, elements
+  long long b;  // offset of B_i / X_i (n x nrhs, row-major), elements
+  int n, nrhs, cls, pad;
 };
 
-template <typename T>
-__device__ __forceinline__ unsigned long long bkey(T v, int pos, int j) {
-  if (sizeof(T) == 8) {
+// Storage policies: element type in memory, arithmetic type, conversions.
+struct StF64 {
+  using S = double;
+  using R = double;
+  static __device__ __forceinline__ R ld(const S* p) { return *p; }
+  static __device__ __forceinline__ S cv(R v) { return v; }
+  static __device__ __forceinline__ R up(S v) { return v; }
+};
+struct StF32 {
+  using S = float;
+  using R = float;
+  static __device__ __forceinline__ R ld(const S* p) { return *p; }
+  static __device__ __forceinline__ S cv(R v) { return v; }
+  static __device__ __forceinline__ R up(S v) { return v; }
+};
+struct StBF16 {
+  using S = __nv_bfloat16;
+  using R = float;
+  static __device__ __forceinline__ R ld(const S* p) { return __bfloat162float(*p); }
+  static __device__ __forceinline__ S cv(R v) { return __float2bfloat16_rn(v); }
+  static __device__ __forceinline__ R up(S v) { return __bfloat162float(v); }
+};
+struct StFP8 {
+  using S = __nv_fp8_e4m3;
+  using R = float;
+  static __device__ __forceinline__ R ld(const S* p) { return static_cast<float>(*p); }
+  static __device__ __forceinline__ S cv(R v) { return __nv_fp8_e4m3(v); }
+  static __device__ __forceinline__ R up(S v) { return static_cast<float>(v); }
+};
+
+template <typename R>
+__device__ __forceinline__ unsigned long long bkey(R v, int pos, int j) {
+  if (sizeof(R) == 8) {
     const unsigned long long a = (unsigned long long)__double_as_longlong((double)v) &
                                  0x7fffffffffffffffull;
     if (a > 0x7ff0000000000000ull) return pos == j ? ~0ull : 0ull;
@@ -47,185 +95,285 @@ __device__ __forceinline__ bool bbetter(unsigned long long ka, int pa, unsigned 
   return ka > kb || (ka == kb && pa < pb);
 }
 
-// Blocked right-looking LU with partial pivoting of M (n x n, pitch p), panel
-// width pb (<= 16): piv[j] = the row swapped with j at step j.
-//   panel  : columns [j0, j1) over rows >= j0, rank-1 updates inside the
-//            panel; each pivot swap moves the whole row (lu.rs:140-145)
-//   U12    : rows [j0, j1), columns >= j1, one thread per column
-//   A22   -= L21 U12 with K = pb: each thread keeps its row's L21 entries in
-//            registers and reads U12 from shared memory, so every element of
-//            A22 is read and written once per panel (matters when M lives in
-//            global scratch).
-// stage points at shared memory for L21 / U12 when M is in global memory
-// (nullptr: read them from M itself).
-template <typename T>
-__device__ void block_lu(T* M, int p, int n, int pb, int* piv, unsigned long long* rk, int* rp,
-                         int* s_int, T* stage) {
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int tx = tid & 15, ty = tid >> 4;
-  for (int j0 = 0; j0 < n; j0 += pb) {
-    const int jb = min(pb, n - j0), j1 = j0 + jb;
-    // The panel's rows as (R, pitch rp_, column offset co, columns swapped sw):
-    // M itself when it is in shared memory, else a staged copy of the panel,
-    // so that the pivot steps never wait on L2.
-    T* R;
-    int rpit, co, sw;
-    if (stage) {
-      R = stage;  // [rows][17]
-      rpit = 17;
-      co = 0;
-      sw = jb;
-      for (int idx = tid; idx < (n - j0) * jb; idx += BT) {
-        const int r = idx / jb, c = idx % jb;
-        R[r * 17 + c] = M[(j0 + r) * p + j0 + c];
-      }
-      __syncthreads();
-    } else {
-      R = M + j0 * p;
-      rpit = p;
-      co = j0;
-      sw = n;
-    }
-    for (int j = j0; j < j1; j++) {
-      const int jr = j - j0, jc = co + j - j0;  // row / column of step j in R
-      unsigned long long bk = 0ull;
-      int bp = -1;
-      for (int r = j + tid; r < n; r += BT) {
-        const unsigned long long k = bkey<T>(R[(r - j0) * rpit + jc], r, j);
-        if (bbetter(k, r, bk, bp)) { bk = k; bp = r; }
-      }
-      for (int off = 16; off > 0; off >>= 1) {
-        unsigned long long ok = __shfl_down_sync(0xffffffffu, bk, off);
-        int op = __shfl_down_sync(0xffffffffu, bp, off);
-        if (bbetter(ok, op, bk, bp)) { bk = ok; bp = op; }
-      }
-      if (lane == 0) { rk[warp] = bk; rp[warp] = bp; }
-      __syncthreads();
-      if (tid == 0) {
-        for (int w = 1; w < BT / 32; w++)
-          if (bbetter(rk[w], rp[w], bk, bp)) { bk = rk[w]; bp = rp[w]; }
-        s_int[0] = bp;
-        piv[j] = bp;
-      }
-      __syncthreads();
-      const int pr = s_int[0] - j0;
-      if (pr != jr)
-        for (int c = tid; c < sw; c += BT) {
-          T t = R[jr * rpit + c];
-          R[jr * rpit + c] = R[pr * rpit + c];
-          R[pr * rpit + c] = t;
-        }
-      __syncthreads();
-      const T d = R[jr * rpit + jc];
-      const T sc = d != T(0) ? T(1) / d : T(1);
-      for (int r = jr + 1 + tid; r < n - j0; r += BT) {
-        const T v = R[r * rpit + jc];
-        R[r * rpit + jc] = d != T(0) ? v * sc : v;
-      }
-      __syncthreads();
-      const int w = j1 - j - 1;  // remaining panel columns
-      if (w > 0)
-        for (int idx = tid; idx < (n - j - 1) * w; idx += BT) {
-          const int r = jr + 1 + idx / w, c = jc + 1 + idx % w;
-          R[r * rpit + c] = fma(-R[r * rpit + jc], R[jr * rpit + c], R[r * rpit + c]);
-        }
-      __syncthreads();
-    }
-    if (stage) {
-      // Panel back to M, and its row swaps (in order) on the other columns.
-      for (int idx = tid; idx < (n - j0) * jb; idx += BT) {
-        const int r = idx / jb, c = idx % jb;
-        M[(j0 + r) * p + j0 + c] = R[r * 17 + c];
-      }
-      for (int c = tid; c < n; c += BT) {
-        if (c >= j0 && c < j1) continue;
-        for (int k = j0; k < j1; k++) {
-          const int q = piv[k];
-          if (q != k) {
-            T t = M[k * p + c];
-            M[k * p + c] = M[q * p + c];
-            M[q * p + c] = t;
-          }
-        }
-      }
-      __syncthreads();
-    }
-    if (j1 >= n) break;
-    // U12 = L11^-1 A12: each thread owns whole columns.
-    for (int c = j1 + tid; c < n; c += BT)
-      for (int k = 0; k < jb; k++) {
-        const T u = M[(j0 + k) * p + c];
-        for (int i = k + 1; i < jb; i++)
-          M[(j0 + i) * p + c] = fma(-M[(j0 + i) * p + j0 + k], u, M[(j0 + i) * p + c]);
-      }
-    __syncthreads();
-    const int nr = n - j1;  // trailing size
-    const T* Lb;
-    const T* Ub;
-    int ldl, ldu;
-    if (stage) {
-      T* ls = stage;               // [256][16] (reuses the panel staging area)
-      T* us = stage + 256 * 17;    // [16][256]
-      for (int idx = tid; idx < nr * jb; idx += BT) {
-        const int r = idx / jb, k = idx % jb;
-        ls[r * 16 + k] = M[(j1 + r) * p + j0 + k];
-      }
-      for (int idx = tid; idx < jb * nr; idx += BT) {
-        const int k = idx / nr, c = idx % nr;
-        us[k * 256 + c] = M[(j0 + k) * p + j1 + c];
-      }
-      __syncthreads();
-      Lb = ls; ldl = 16; Ub = us; ldu = 256;
-    } else {
-      Lb = M + j1 * p + j0; ldl = p; Ub = M + j0 * p + j1; ldu = p;
-    }
-    for (int r = ty; r < nr; r += 16) {
-      T l[16];
+struct Shared {
+  unsigned long long rk[NW_MAX];
+  int rp[NW_MAX];
+  // [0] ||A||_inf, [1 + c] max |r_c|, [5 + c] max |x_c|, [9 + c] max |b_c|,
+  // [13] max |a_ij| (FP8 scaling)
+  double norm[14];
+};
+
+__host__ __device__ constexpr size_t al16(size_t x) { return (x + 15) / 16 * 16; }
+
+// Shared-memory layout of one system (byte offsets into the dynamic shared
+// memory): [M if resident][staged panel][U12][row map][x FP64][d FP32].
+struct Lay {
+  size_t stage, us, rmap, x, d, total;
+};
+template <typename S, typename R>
+__host__ __device__ Lay lay(int n, int nrhs, bool resident, bool mixed) {
+  Lay L;
+  size_t o = resident ? al16((size_t)n * n * sizeof(S)) : 0;
+  L.stage = o;
+  o += al16((size_t)n * SP * sizeof(R));
+  L.us = o;
+  o += al16((size_t)PBW * n * sizeof(R));
+  L.rmap = o;
+  o += al16((size_t)n * sizeof(int));
+  L.x = o;
+  o += al16((size_t)n * nrhs * sizeof(double));
+  L.d = o;
+  o += mixed ? al16((size_t)n * nrhs * sizeof(float)) : 0;
+  L.total = o;
+  return L;
+}
+
+// A22 -= L21 U12 for the trailing nr x nr block (logical rows/columns >= j1):
+// warp w, lane l computes rows rb + w + NW t (t < TR) and columns
+// cb + l + 32 q (q < QN), with its L21 rows (staged rows PBW + i) in
+// registers; all loads of a tile are issued before its FMAs. QN is picked
+// from nr so that narrow trailing blocks do not run idle columns.
+template <typename P, int TR, int QN>
+__device__ __forceinline__ void trailing_update(typename P::S* M, int p, const int* rmap, int j1,
+                                                int nr, const typename P::R* st,
+                                                const typename P::R* us) {
+  const int BT = blockDim.x, NW = BT >> 5;
+  using S = typename P::S;
+  using R = typename P::R;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int rb = 0; rb < nr; rb += NW * TR) {
+    R lr[TR][PBW];
+    S* crow[TR];
 #pragma unroll
-      for (int k = 0; k < 16; k++) l[k] = k < jb ? Lb[r * ldl + k] : T(0);
-      T* mrow = M + (j1 + r) * p + j1;
-      for (int c = tx; c < nr; c += 16) {
-        T acc = mrow[c];
+    for (int t = 0; t < TR; t++) {
+      const int i = rb + warp + NW * t;
+      const bool ok = i < nr;
+      crow[t] = ok ? M + (size_t)rmap[j1 + i] * p + j1 : nullptr;
 #pragma unroll
-        for (int k = 0; k < 16; k++)
-          if (k < jb) acc = fma(-l[k], Ub[k * ldu + c], acc);
-        mrow[c] = acc;
-      }
+      for (int k = 0; k < PBW; k++) lr[t][k] = ok ? st[(PBW + i) * SP + k] : R(0);
     }
-    __syncthreads();
+    for (int cb = 0; cb < nr; cb += 32 * QN) {
+      R acc[TR][QN];
+#pragma unroll
+      for (int t = 0; t < TR; t++)
+#pragma unroll
+        for (int q = 0; q < QN; q++) {
+          const int c = cb + lane + 32 * q;
+          acc[t][q] = (crow[t] && c < nr) ? P::ld(&crow[t][c]) : R(0);
+        }
+#pragma unroll
+      for (int k = 0; k < PBW; k++) {
+        R uv[QN];
+#pragma unroll
+        for (int q = 0; q < QN; q++) {
+          const int c = cb + lane + 32 * q;
+          uv[q] = c < nr ? us[k * nr + c] : R(0);
+        }
+#pragma unroll
+        for (int t = 0; t < TR; t++)
+#pragma unroll
+          for (int q = 0; q < QN; q++) acc[t][q] = fma(-lr[t][k], uv[q], acc[t][q]);
+      }
+#pragma unroll
+      for (int t = 0; t < TR; t++)
+#pragma unroll
+        for (int q = 0; q < QN; q++) {
+          const int c = cb + lane + 32 * q;
+          if (crow[t] && c < nr) crow[t][c] = P::cv(acc[t][q]);
+        }
+    }
   }
 }
 
-// X (n x nrhs, pitch px) <- U^-1 L^-1 P X with the factors in M (rows in
-// parallel over the CTA, one step per row).
-template <typename T, typename TX>
-__device__ void block_solve(const T* M, int p, int n, const int* piv, TX* X, int px, int nrhs) {
-  const int tid = threadIdx.x;
-  // Row swaps in order (the swap list replayed in order is the reference's
-  // permutation, lu.rs:245-254).
-  if (tid < nrhs)
-    for (int j = 0; j < n; j++) {
-      const int q = piv[j];
-      if (q != j) {
-        TX t = X[j * px + tid];
-        X[j * px + tid] = X[q * px + tid];
-        X[q * px + tid] = t;
+// Blocked right-looking LU with partial pivoting of M (n x n, pitch p, rows
+// addressed through rmap: logical row i is physical row rmap[i]). On return
+// rmap[i] = the original row now at position i (the reference's piv).
+//   panel : columns [j0, j1) of logical rows >= j0 staged in st (pitch SP);
+//           thread t owns staged rows t, t + BT; per column: pivot search
+//           over own rows, barrier, swap (two staged rows, two map entries),
+//           barrier, scale + rank-1 update of own rows (a thread then reads
+//           only its own rows until the next barrier).
+//   U12   : rows [j0, j1), columns >= j1, each column solved in registers.
+//   A22  -= L21 U12 (trailing_update).
+// Values written back to M are rounded to the storage type, and the staged
+// copies used by later steps are those rounded values.
+template <typename P>
+__device__ void block_lu(typename P::S* M, int p, int n, int* rmap, typename P::R* st,
+                         typename P::R* us, Shared& sh) {
+  const int BT = blockDim.x, NW = BT >> 5;
+  using S = typename P::S;
+  using R = typename P::R;
+  constexpr int TR = 2;  // rows per thread in the A22 tile
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int i = tid; i < n; i += BT) rmap[i] = i;
+  __syncthreads();
+  for (int j0 = 0; j0 < n; j0 += PBW) {
+    const int jb = min(PBW, n - j0), j1 = j0 + jb, prow = n - j0;
+    for (int idx = tid; idx < prow * jb; idx += BT) {
+      const int r = idx / jb, c = idx - r * jb;
+      st[r * SP + c] = P::ld(&M[(size_t)rmap[j0 + r] * p + j0 + c]);
+    }
+    __syncthreads();
+    for (int jj = 0; jj < jb; jj++) {
+      unsigned long long bk = 0ull;
+      int bp = -1;
+      for (int r = tid; r < prow; r += BT)
+        if (r >= jj) {
+          const unsigned long long k = bkey<R>(st[r * SP + jj], r, jj);
+          if (bbetter(k, r, bk, bp)) { bk = k; bp = r; }
+        }
+      for (int off = 16; off > 0; off >>= 1) {
+        const unsigned long long ok = __shfl_down_sync(0xffffffffu, bk, off);
+        const int op = __shfl_down_sync(0xffffffffu, bp, off);
+        if (bbetter(ok, op, bk, bp)) { bk = ok; bp = op; }
+      }
+      if (lane == 0) { sh.rk[warp] = bk; sh.rp[warp] = bp; }
+      __syncthreads();
+      bk = sh.rk[0];
+      bp = sh.rp[0];
+#pragma unroll
+      for (int w = 1; w < NW; w++)
+        if (bbetter(sh.rk[w], sh.rp[w], bk, bp)) { bk = sh.rk[w]; bp = sh.rp[w]; }
+      if (bp != jj) {  // bp >= jj: row jj itself always has a key
+        if (tid < jb) {
+          const R t = st[jj * SP + tid];
+          st[jj * SP + tid] = st[bp * SP + tid];
+          st[bp * SP + tid] = t;
+        }
+        if (tid == 0) {
+          const int t = rmap[j0 + jj];
+          rmap[j0 + jj] = rmap[j0 + bp];
+          rmap[j0 + bp] = t;
+        }
+      }
+      __syncthreads();
+      const R d = st[jj * SP + jj];
+      const R sc = d != R(0) ? R(1) / d : R(1);
+      for (int r = tid; r < prow; r += BT)
+        if (r > jj) {
+          R* row = st + r * SP;
+          const R l = d != R(0) ? row[jj] * sc : row[jj];
+          row[jj] = l;
+          for (int c = jj + 1; c < jb; c++) row[c] = fma(-l, st[jj * SP + c], row[c]);
+        }
+    }
+    __syncthreads();
+    for (int idx = tid; idx < prow * jb; idx += BT) {
+      const int r = idx / jb, c = idx - r * jb;
+      const S v = P::cv(st[r * SP + c]);
+      M[(size_t)rmap[j0 + r] * p + j0 + c] = v;
+      st[r * SP + c] = P::up(v);
+    }
+    if (j1 >= n) break;  // uniform; jb == PBW below
+    const int nr = n - j1;
+    for (int idx = tid; idx < PBW * nr; idx += BT) {
+      const int k = idx / nr, c = idx - k * nr;
+      us[k * nr + c] = P::ld(&M[(size_t)rmap[j0 + k] * p + j1 + c]);
+    }
+    __syncthreads();
+    for (int c = tid; c < nr; c += BT) {
+      R u[PBW];
+#pragma unroll
+      for (int k = 0; k < PBW; k++) u[k] = us[k * nr + c];
+#pragma unroll
+      for (int k = 0; k < PBW; k++)
+#pragma unroll
+        for (int i = k + 1; i < PBW; i++) u[i] = fma(-st[i * SP + k], u[k], u[i]);
+#pragma unroll
+      for (int k = 0; k < PBW; k++) {
+        const S v = P::cv(u[k]);
+        M[(size_t)rmap[j0 + k] * p + j1 + c] = v;
+        us[k * nr + c] = P::up(v);
       }
     }
-  __syncthreads();
-  for (int k = 0; k < n; k++) {
-    for (int idx = tid; idx < (n - k - 1) * nrhs; idx += BT) {
-      const int i = k + 1 + idx / nrhs, c = idx % nrhs;
-      X[i * px + c] = fma(-(TX)M[i * p + k], X[k * px + c], X[i * px + c]);
+    __syncthreads();
+    switch (min(4, (nr + 31) / 32)) {
+      case 1: trailing_update<P, TR, 1>(M, p, rmap, j1, nr, st, us); break;
+      case 2: trailing_update<P, TR, 2>(M, p, rmap, j1, nr, st, us); break;
+      case 3: trailing_update<P, TR, 3>(M, p, rmap, j1, nr, st, us); break;
+      default: trailing_update<P, TR, 4>(M, p, rmap, j1, nr, st, us); break;
     }
     __syncthreads();
   }
-  for (int k = n - 1; k >= 0; k--) {
-    if (tid < nrhs) X[k * px + tid] = X[k * px + tid] / (TX)M[k * p + k];
+  __syncthreads();
+}
+
+// X (n x nrhs, pitch nrhs, already in the factor's row order, i.e. P b)
+// <- U^-1 L^-1 X with the stored factors in M. 16-row blocks: warp 0 solves
+// the diagonal block (lanes = rows, two right-hand sides per pass, values
+// passed by shuffles), then all threads update the remaining rows.
+template <typename P, typename TX>
+__device__ void block_solve(const typename P::S* M, int p, int n, const int* rmap, TX* X,
+                            int nrhs) {
+  const int BT = blockDim.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int li = lane & 15, half = lane >> 4;
+  for (int kb = 0; kb < n; kb += 16) {
+    const int kbn = min(16, n - kb);
+    if (warp == 0) {
+      // lane's row of the diagonal block in registers (16 loads in flight)
+      const typename P::S* lrow = M + (size_t)rmap[kb + min(li, kbn - 1)] * p + kb;
+      TX lv[16];
+#pragma unroll
+      for (int k = 0; k < 16; k++) lv[k] = k < kbn ? (TX)P::ld(&lrow[k]) : TX(0);
+      for (int c0 = 0; c0 < nrhs; c0 += 2) {
+        const int c = c0 + half;
+        const bool act = li < kbn && c < nrhs;
+        TX xi = act ? X[(kb + li) * nrhs + c] : TX(0);
+#pragma unroll
+        for (int k = 0; k < 15; k++) {
+          if (k + 1 < kbn) {
+            const TX xk = __shfl_sync(0xffffffffu, xi, (lane & 16) | k);
+            if (act && li > k) xi = fma(-lv[k], xk, xi);
+          }
+        }
+        if (act) X[(kb + li) * nrhs + c] = xi;
+      }
+    }
     __syncthreads();
-    for (int idx = tid; idx < k * nrhs; idx += BT) {
+    const int rest = n - kb - kbn;
+    for (int idx = tid; idx < rest * nrhs; idx += BT) {
+      const int i = kb + kbn + idx / nrhs, c = idx % nrhs;
+      const typename P::S* lrow = M + (size_t)rmap[i] * p + kb;
+      TX s = X[i * nrhs + c];
+#pragma unroll
+      for (int k = 0; k < 16; k++)
+        if (k < kbn) s = fma(-(TX)P::ld(&lrow[k]), X[(kb + k) * nrhs + c], s);
+      X[i * nrhs + c] = s;
+    }
+    __syncthreads();
+  }
+  for (int kb = (n - 1) / 16 * 16; kb >= 0; kb -= 16) {
+    const int kbn = min(16, n - kb);
+    if (warp == 0) {
+      const typename P::S* urow = M + (size_t)rmap[kb + min(li, kbn - 1)] * p + kb;
+      TX uv[16];
+#pragma unroll
+      for (int k = 0; k < 16; k++) uv[k] = k < kbn ? (TX)P::ld(&urow[k]) : TX(1);
+      for (int c0 = 0; c0 < nrhs; c0 += 2) {
+        const int c = c0 + half;
+        const bool act = li < kbn && c < nrhs;
+        TX xi = act ? X[(kb + li) * nrhs + c] : TX(0);
+#pragma unroll
+        for (int k = 15; k >= 0; k--) {
+          if (k < kbn) {
+            if (act && li == k) xi = xi / uv[k];
+            const TX xk = __shfl_sync(0xffffffffu, xi, (lane & 16) | k);
+            if (act && li < k) xi = fma(-uv[k], xk, xi);
+          }
+        }
+        if (act) X[(kb + li) * nrhs + c] = xi;
+      }
+    }
+    __syncthreads();
+    for (int idx = tid; idx < kb * nrhs; idx += BT) {
       const int i = idx / nrhs, c = idx % nrhs;
-      X[i * px + c] = fma(-(TX)M[i * p + k], X[k * px + c], X[i * px + c]);
+      const typename P::S* urow = M + (size_t)rmap[i] * p + kb;
+      TX s = X[i * nrhs + c];
+#pragma unroll
+      for (int k = 0; k < 16; k++)
+        if (k < kbn) s = fma(-(TX)P::ld(&urow[k]), X[(kb + k) * nrhs + c], s);
+      X[i * nrhs + c] = s;
     }
     __syncthreads();
   }
@@ -239,186 +387,316 @@ struct BatchArgs {
   int count;
   int* queue;        // work counter (zeroed before the launch)
   int* status;       // per system (sorted order): iterations, < 0 = not converged
-  double* eta;       // per system: final backward error (MIXED) or -1
+  double* eta;       // per system: final backward error (mixed pass) or -1
   void* scratch;     // per-CTA global working matrices for systems that do not fit
-  size_t scratch_elems;  // elements per CTA slice
-  int smem_n;        // largest n whose working matrix fits in shared memory
+  size_t scratch_bytes;  // bytes per CTA slice
+  size_t smem_budget;    // dynamic shared memory of each CTA
   int max_iters;
   double tol;
   int only_flagged;  // FP64 pass: process only systems with status < 0
-  int panel;         // panel width of the per-system blocked LU (<= 16)
+  long long* cycles; // per system: SM cycles spent on it, summed over the passes
+  unsigned long long* phase;  // [8]: load, factor, solves, residuals of the first pass,
+                              // then the same for the FP64 redo pass (summed over CTAs)
 };
 
-template <typename T, bool MIXED>
-__global__ void __launch_bounds__(BT) batched_kernel(BatchArgs a) {
+// Per-CTA phase clock: thread 0 adds the cycles since the last mark to a slot.
+struct PhaseClock {
+  long long last;
+  unsigned long long acc[4];
+  __device__ void start() {
+    last = clock64();
+    acc[0] = acc[1] = acc[2] = acc[3] = 0ull;
+  }
+  __device__ void mark(int k) {
+    const long long t = clock64();
+    acc[k] += (unsigned long long)(t - last);
+    last = t;
+  }
+  __device__ void flush(unsigned long long* out) {
+    for (int k = 0; k < 4; k++) atomicAdd(&out[k], acc[k]);
+  }
+};
+
+// atomicMax on a non-negative double held in shared memory.
+__device__ __forceinline__ void amax_pos(double* p, double v) {
+  atomicMax(reinterpret_cast<unsigned long long*>(p), (unsigned long long)__double_as_longlong(v));
+}
+
+// out[c] = max over the CTA of |v[i nrhs + c]| (c < nrhs, n rows): per-thread
+// maxima, then a warp reduction, then one shared atomic per warp and column.
+// out must be zero on entry; no barrier inside.
+__device__ __forceinline__ void col_absmax(const double* v, int n, int nrhs, double* out) {
+  const int BT = blockDim.x;
+  double m[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int idx = threadIdx.x; idx < n * nrhs; idx += BT) {
+    const int c = idx % nrhs;
+    const double a = fabs(v[idx]);
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      if (q == c) m[q] = fmax(m[q], a);
+  }
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    for (int off = 16; off > 0; off >>= 1) m[q] = fmax(m[q], __shfl_xor_sync(0xffffffffu, m[q], off));
+    if ((threadIdx.x & 31) == 0 && q < nrhs) amax_pos(&out[q], m[q]);
+  }
+}
+
+// One halving step of a warp reduction of 2H values per lane: lanes with
+// bit s set keep the upper H values, the others the lower H, each adding its
+// partner's copy (partner = lane ^ s).
+template <int H>
+__device__ __forceinline__ void halve(double* v, int lane, int s) {
+  const bool up = lane & s;
+#pragma unroll
+  for (int j = 0; j < H; j++) {
+    const double send = up ? v[j] : v[j + H];
+    const double keep = up ? v[j + H] : v[j];
+    v[j] = keep + __shfl_xor_sync(0xffffffffu, send, s);
+  }
+}
+
+// R = B - A x (FP64) for rows [0, n) with NR right-hand sides: each warp takes
+// four rows at a time, lanes stride the columns (coalesced rows of A, x from
+// shared memory), and the 4 x 4 partial sums are reduced across the warp by
+// recursive halving (16 adds per lane instead of 5 per value).
+template <int NR>
+__device__ void residual_rows(const double* __restrict__ Ai, int n, const double* xv,
+                              const double* __restrict__ Bi, double* Ri) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, NW = blockDim.x >> 5;
+  for (int r0 = 4 * warp; r0 < n; r0 += 4 * NW) {
+    double v[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) v[j] = 0.0;
+#pragma unroll 2
+    for (int k0 = 0; k0 < n; k0 += 32) {
+      const int k = k0 + lane;
+      const bool kin = k < n;
+      double a[4], xk[NR];
+#pragma unroll
+      for (int i = 0; i < 4; i++) a[i] = (kin && r0 + i < n) ? Ai[(size_t)(r0 + i) * n + k] : 0.0;
+#pragma unroll
+      for (int c = 0; c < NR; c++) xk[c] = kin ? xv[k * NR + c] : 0.0;
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int c = 0; c < NR; c++) v[i * 4 + c] = fma(a[i], xk[c], v[i * 4 + c]);
+    }
+    halve<8>(v, lane, 16);
+    halve<4>(v, lane, 8);
+    halve<2>(v, lane, 4);
+    halve<1>(v, lane, 2);
+    v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+    // lane now holds value q = 4 i + c with q's bits = lane bits 4..1
+    const int q = ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 +
+                  ((lane >> 1) & 1);
+    const int i = q >> 2, c = q & 3;
+    if ((lane & 1) == 0 && c < NR && r0 + i < n)
+      Ri[(size_t)(r0 + i) * NR + c] = Bi[(size_t)(r0 + i) * NR + c] - v[0];
+  }
+}
+
+// One system on the whole CTA: factor in storage P, then (mixed) refine.
+template <typename P, bool MIXED>
+__device__ void process_system(const BatchArgs& a, int sidx, const SysDesc& d, Shared& sh,
+                               char* smem) {
+  const int BT = blockDim.x, NW = BT >> 5;
+  using S = typename P::S;
+  using R = typename P::R;
+  const int tid = threadIdx.x;
+  const int n = d.n, nrhs = d.nrhs;
+  const Lay Lres = lay<S, R>(n, nrhs, true, MIXED);
+  const bool resident = Lres.total <= a.smem_budget;
+  const Lay L = resident ? Lres : lay<S, R>(n, nrhs, false, MIXED);
+  S* M = resident ? reinterpret_cast<S*>(smem)
+                  : reinterpret_cast<S*>(static_cast<char*>(a.scratch) +
+                                         (size_t)blockIdx.x * a.scratch_bytes);
+  R* st = reinterpret_cast<R*>(smem + L.stage);
+  R* us = reinterpret_cast<R*>(smem + L.us);
+  int* rmap = reinterpret_cast<int*>(smem + L.rmap);
+  double* xv = reinterpret_cast<double*>(smem + L.x);
+  float* dv = reinterpret_cast<float*>(smem + L.d);
+  const double* Ai = a.A + d.a;
+  const double* Bi = a.B + d.b;
+  double* Xi = a.X + d.b;
+  PhaseClock pc;
+  if (tid == 0) pc.start();
+  unsigned long long* const phase = a.phase + (a.only_flagged ? 4 : 0);
+
+  // Storage scale (a power of two): the largest |a_ij| goes to 16 for FP8, so
+  // the factors (|l| <= 1, modest growth in U) stay inside e4m3's range.
+  if (tid == 0) { sh.norm[0] = 0.0; sh.norm[13] = 0.0; }
+  __syncthreads();
+  float scale = 1.f;
+  if (sizeof(S) == 1) {
+    double m = 0.0;
+    for (int idx = tid; idx < n * n; idx += BT) m = fmax(m, fabs(Ai[idx]));
+    for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, off));
+    if ((tid & 31) == 0) amax_pos(&sh.norm[13], m);
+    __syncthreads();
+    int e = 0;
+    if (sh.norm[13] > 0.0 && sh.norm[13] < INFINITY) {
+      frexp(sh.norm[13], &e);
+      scale = ldexpf(1.f, 4 - e);
+    }
+  }
+  // Load A_i (one warp per row, coalesced) in the storage type; the mixed pass
+  // also takes ||A||_inf (largest row sum of |a_ij|) on the way.
+  {
+    const int lane = tid & 31, warp = tid >> 5;
+    double rmax = 0.0;
+    for (int r = warp; r < n; r += NW) {
+      const double* ar = Ai + (size_t)r * n;
+      S* mr = M + (size_t)r * n;
+      double rs = 0.0;
+      for (int k = lane; k < n; k += 32) {
+        const double v = ar[k];
+        if (MIXED) rs += fabs(v);
+        mr[k] = P::cv((R)(v * (double)scale));
+      }
+      if (MIXED) {
+        for (int off = 16; off > 0; off >>= 1) rs += __shfl_xor_sync(0xffffffffu, rs, off);
+        rmax = fmax(rmax, rs);
+      }
+    }
+    if (MIXED && lane == 0) amax_pos(&sh.norm[0], rmax);
+  }
+  __syncthreads();
+  if (tid == 0) pc.mark(0);
+  block_lu<P>(M, n, n, rmap, st, us, sh);
+  if (tid == 0) pc.mark(1);
+
+  if (!MIXED) {
+    for (int idx = tid; idx < n * nrhs; idx += BT) {
+      const int i = idx / nrhs, c = idx - i * nrhs;
+      xv[idx] = Bi[(size_t)rmap[i] * nrhs + c];
+    }
+    __syncthreads();
+    block_solve<P, double>(M, n, n, rmap, xv, nrhs);
+    for (int idx = tid; idx < n * nrhs; idx += BT) Xi[idx] = xv[idx];
+    if (tid == 0) {
+      a.status[sidx] = 0;
+      a.eta[sidx] = -1.0;
+      pc.mark(2);
+      if (a.phase) pc.flush(phase);
+    }
+    return;
+  }
+  // ---- FP64 refinement with the stored factors (of scale * A) ----
+  // The residual r = B - A x lives in X_i (global) until the final x is written.
+  if (tid == 0) for (int q = 1; q < 13; q++) sh.norm[q] = 0.0;
+  __syncthreads();
+  col_absmax(Bi, n, nrhs, &sh.norm[1 + 2 * 4]);
+  for (int idx = tid; idx < n * nrhs; idx += BT) xv[idx] = 0.0;
+  __syncthreads();
+  const double* rv = Bi;  // x = 0: r = B
+  int it = 0;
+  double eta = INFINITY, prev = INFINITY;
+  bool ok = false;
+  for (;;) {
+    if (tid < 8) sh.norm[1 + tid] = 0.0;
+    __syncthreads();
+    col_absmax(rv, n, nrhs, &sh.norm[1]);
+    col_absmax(xv, n, nrhs, &sh.norm[1 + 4]);
+    __syncthreads();
+    eta = 0.0;
+    for (int c = 0; c < nrhs; c++) {
+      const double den = sh.norm[0] * sh.norm[1 + 4 + c] + sh.norm[1 + 8 + c];
+      const double v = den > 0 ? sh.norm[1 + c] / den : (sh.norm[1 + c] > 0 ? INFINITY : 0.0);
+      if (!(v <= eta)) eta = v;
+    }
+    if (eta <= a.tol) { ok = true; break; }
+    if (it >= a.max_iters || !(eta < 0.9 * prev)) break;
+    prev = eta;
+    it++;
+    // d = P r / rmax (the factor's row order)
+    {
+      double inv[4];
+#pragma unroll
+      for (int c = 0; c < 4; c++) inv[c] = sh.norm[1 + c] > 0 ? 1.0 / sh.norm[1 + c] : 0.0;
+      for (int idx = tid; idx < n * nrhs; idx += BT) {
+        const int i = idx / nrhs, c = idx - i * nrhs;
+        const double ic = c == 0 ? inv[0] : c == 1 ? inv[1] : c == 2 ? inv[2] : inv[3];
+        dv[idx] = (float)(rv[(size_t)rmap[i] * nrhs + c] * ic);
+      }
+    }
+    __syncthreads();
+    if (tid == 0) pc.mark(3);
+    block_solve<P, float>(M, n, n, rmap, dv, nrhs);
+    if (tid == 0) pc.mark(2);
+    // (scale A) d = r / rmax  =>  A (scale d rmax) = r
+    for (int idx = tid; idx < n * nrhs; idx += BT)
+      xv[idx] += (double)dv[idx] * sh.norm[1 + idx % nrhs] * (double)scale;
+    __syncthreads();
+    switch (nrhs) {
+      case 1: residual_rows<1>(Ai, n, xv, Bi, Xi); break;
+      case 2: residual_rows<2>(Ai, n, xv, Bi, Xi); break;
+      case 3: residual_rows<3>(Ai, n, xv, Bi, Xi); break;
+      default: residual_rows<4>(Ai, n, xv, Bi, Xi); break;
+    }
+    rv = Xi;
+    __syncthreads();
+  }
+  __syncthreads();
+  for (int idx = tid; idx < n * nrhs; idx += BT) Xi[idx] = xv[idx];
+  if (tid == 0) {
+    a.status[sidx] = ok ? it : -1 - it;
+    a.eta[sidx] = eta;
+    pc.mark(3);
+    if (a.phase) pc.flush(phase);
+  }
+}
+
+// Storage classes of the mixed pass.
+enum { CLS_F64 = 0, CLS_F32 = 1, CLS_BF16 = 2, CLS_FP8 = 3 };
+
+template <bool MIXED>
+__global__ void __launch_bounds__(BT_MAX, MIXED ? 2 : 1) batched_kernel(BatchArgs a) {
   extern __shared__ __align__(16) double bsm[];
-  __shared__ unsigned long long rk[BT / 32];
-  __shared__ int rp[BT / 32];
-  __shared__ int s_int[2];
-  __shared__ T s_t[2];
+  __shared__ Shared sh;
   __shared__ int s_sys;
-  __shared__ double s_norm[1 + 3 * 4];
-  __shared__ int s_done;
   const int tid = threadIdx.x;
   for (;;) {
     if (tid == 0) s_sys = atomicAdd(a.queue, 1);
     __syncthreads();
     const int sidx = s_sys;
+    __syncthreads();
     if (sidx >= a.count) return;
-    if (a.only_flagged && a.status[sidx] >= 0) { __syncthreads(); continue; }
+    if (a.only_flagged && a.status[sidx] >= 0) continue;
     const SysDesc d = a.desc[sidx];
-    const int n = d.n, nrhs = d.nrhs;
-    const int p = n + 1;  // padded pitch
-    const bool in_smem = n <= a.smem_n;
-    T* M = in_smem ? reinterpret_cast<T*>(bsm)
-                   : reinterpret_cast<T*>(a.scratch) + (size_t)blockIdx.x * a.scratch_elems;
-    // Shared-memory layout after the matrix (sized for n <= 256, nrhs <= 4):
-    // piv (256 int), then vectors.
-    char* tail = reinterpret_cast<char*>(bsm) + (in_smem ? ((size_t)n * p * sizeof(T) + 15) / 16 * 16 : 0);
-    int* piv = reinterpret_cast<int*>(tail);
-    double* xv = reinterpret_cast<double*>(tail + 256 * sizeof(int));  // n x 4 FP64 (solution)
-    double* rv = xv + 256 * 4;                                          // n x 4 FP64 (residual)
-    float* dv = reinterpret_cast<float*>(rv + 256 * 4);                 // n x 4 FP32 (correction)
-    const double* Ai = a.A + d.a;
-    const double* Bi = a.B + d.b;
-    double* Xi = a.X + d.b;
-
-    for (int idx = tid; idx < n * n; idx += BT) M[(idx / n) * p + idx % n] = (T)Ai[idx];
-    for (int idx = tid; idx < n * nrhs; idx += BT) xv[idx] = Bi[idx];
-    __syncthreads();
-    // L21/U12 staging for global-resident matrices: after the vectors.
-    T* stage = in_smem ? nullptr : reinterpret_cast<T*>(dv + 256 * 4);
-    block_lu<T>(M, p, n, a.panel, piv, rk, rp, s_int, stage);
-
+    char* smem = reinterpret_cast<char*>(bsm);
+    const long long t0 = clock64();
     if (!MIXED) {
-      block_solve<T, double>(M, p, n, piv, xv, nrhs, nrhs);
-      for (int idx = tid; idx < n * nrhs; idx += BT) Xi[idx] = xv[idx];
-      if (tid == 0) { a.status[sidx] = 0; a.eta[sidx] = -1.0; }
-      __syncthreads();
-      continue;
-    }
-    // ---- FP64 refinement with the FP32 factors ----
-    // ||A||_inf (row sums, one warp per row), ||b_j||_inf
-    if (tid == 0) for (int q = 0; q < 1 + 3 * 4; q++) s_norm[q] = 0.0;
-    __syncthreads();
-    {
-      const int lane = tid & 31, warp = tid >> 5;
-      for (int r = warp; r < n; r += BT / 32) {
-        double s = 0.0;
-        for (int k = lane; k < n; k += 32) s += fabs(Ai[(size_t)r * n + k]);
-        for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
-        if (lane == 0)
-          atomicMax(reinterpret_cast<unsigned long long*>(&s_norm[0]),
-                    (unsigned long long)__double_as_longlong(s));
-      }
-    }
-    for (int idx = tid; idx < n * nrhs; idx += BT) {
-      atomicMax(reinterpret_cast<unsigned long long*>(&s_norm[1 + 2 * 4 + idx % nrhs]),
-                (unsigned long long)__double_as_longlong(fabs(Bi[idx])));
-      rv[idx] = Bi[idx];
-      xv[idx] = 0.0;
+      process_system<StF64, false>(a, sidx, d, sh, smem);
+    } else if (d.cls == CLS_FP8) {
+      process_system<StFP8, true>(a, sidx, d, sh, smem);
+    } else if (d.cls == CLS_BF16) {
+      process_system<StBF16, true>(a, sidx, d, sh, smem);
+    } else {
+      process_system<StF32, true>(a, sidx, d, sh, smem);
     }
     __syncthreads();
-    int it = 0;
-    double eta = INFINITY, prev = INFINITY;
-    bool ok = false;
-    for (;;) {
-      // eta from r (rmax in s_norm[1..4]) and x (xmax in s_norm[5..8])
-      if (tid < 8) s_norm[1 + tid] = 0.0;
-      __syncthreads();
-      for (int idx = tid; idx < n * nrhs; idx += BT) {
-        const int c = idx % nrhs;
-        atomicMax(reinterpret_cast<unsigned long long*>(&s_norm[1 + c]),
-                  (unsigned long long)__double_as_longlong(fabs(rv[idx])));
-        atomicMax(reinterpret_cast<unsigned long long*>(&s_norm[1 + 4 + c]),
-                  (unsigned long long)__double_as_longlong(fabs(xv[idx])));
-      }
-      __syncthreads();
-      eta = 0.0;
-      for (int c = 0; c < nrhs; c++) {
-        const double den = s_norm[0] * s_norm[1 + 4 + c] + s_norm[1 + 8 + c];
-        const double v = den > 0 ? s_norm[1 + c] / den : (s_norm[1 + c] > 0 ? INFINITY : 0.0);
-        if (!(v <= eta)) eta = v;
-      }
-      if (eta <= a.tol) { ok = true; break; }
-      if (it >= a.max_iters || !(eta < 0.9 * prev)) break;
-      prev = eta;
-      it++;
-      // d = LU32 \ (r / rmax), in FP32
-      for (int idx = tid; idx < n * nrhs; idx += BT) {
-        const double s = s_norm[1 + idx % nrhs];
-        dv[idx] = s > 0 ? (float)(rv[idx] / s) : 0.f;
-      }
-      __syncthreads();
-      block_solve<T, float>(M, p, n, piv, dv, nrhs, nrhs);
-      for (int idx = tid; idx < n * nrhs; idx += BT) xv[idx] += (double)dv[idx] * s_norm[1 + idx % nrhs];
-      __syncthreads();
-      // r = b - A x in FP64: one warp per row, lanes along the row (coalesced)
-      {
-        const int lane = tid & 31, warp = tid >> 5;
-        for (int r = warp; r < n; r += BT / 32) {
-          const double* ar = Ai + (size_t)r * n;
-          double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-          for (int k = lane; k < n; k += 32) {
-            const double av = ar[k];
-            const double* xk = xv + k * nrhs;
-            s0 = fma(av, xk[0], s0);
-            if (nrhs > 1) s1 = fma(av, xk[1], s1);
-            if (nrhs > 2) s2 = fma(av, xk[2], s2);
-            if (nrhs > 3) s3 = fma(av, xk[3], s3);
-          }
-          for (int off = 16; off > 0; off >>= 1) {
-            s0 += __shfl_down_sync(0xffffffffu, s0, off);
-            s1 += __shfl_down_sync(0xffffffffu, s1, off);
-            s2 += __shfl_down_sync(0xffffffffu, s2, off);
-            s3 += __shfl_down_sync(0xffffffffu, s3, off);
-          }
-          if (lane == 0) {
-            rv[r * nrhs] = Bi[(size_t)r * nrhs] - s0;
-            if (nrhs > 1) rv[r * nrhs + 1] = Bi[(size_t)r * nrhs + 1] - s1;
-            if (nrhs > 2) rv[r * nrhs + 2] = Bi[(size_t)r * nrhs + 2] - s2;
-            if (nrhs > 3) rv[r * nrhs + 3] = Bi[(size_t)r * nrhs + 3] - s3;
-          }
-        }
-      }
-      __syncthreads();
-    }
-    for (int idx = tid; idx < n * nrhs; idx += BT) Xi[idx] = xv[idx];
-    if (tid == 0) {
-      a.status[sidx] = ok ? it : -1 - it;
-      a.eta[sidx] = eta;
-    }
-    __syncthreads();
-    (void)s_done;
+    if (tid == 0) a.cycles[sidx] += clock64() - t0;
   }
 }
 
-// Upper bound of the kernel's static shared memory (reductions, norms, ids).
-constexpr size_t batch_static_smem() { return 1024; }
-
-// Shared memory of the vectors after the matrix: pivots, x, r (FP64), d (FP32).
-constexpr size_t tail_bytes() {
-  return 256 * sizeof(int) + 2 * 256 * 4 * sizeof(double) + 256 * 4 * sizeof(float);
+// desc[i].cls from the selector's class (0 FP8, 1 BF16, 2 FP32) of the caller's
+// system perm[i].
+__global__ void select_kernel(SysDesc* desc, const int* __restrict__ perm,
+                              const int* __restrict__ sel, int count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const int c = sel[perm[i]];
+  desc[i].cls = c == 0 ? CLS_FP8 : (c == 1 ? CLS_BF16 : CLS_F32);
 }
 
-template <typename T, bool MIXED>
-size_t smem_for(int n) {
-  const size_t mat = ((size_t)n * (n + 1) * sizeof(T) + 15) / 16 * 16;
-  return mat + tail_bytes();
-}
-
-// Staging for the panel (256 x 17), then L21 / U12 (global-resident matrices)
-// after the vectors.
-template <typename T>
-size_t stage_bytes() {
-  return (256 * 17 + 16 * 256) * sizeof(T);
-}
+constexpr size_t BATCH_STATIC_SMEM = 1024;  // bound of the kernel's static shared memory
 
 }  // namespace
 
 struct la_batch_plan_s {
   la_ctx ctx;
-  int count = 0, mode = 0, threads = BT, ctas_per_sm = 1;
+  int count = 0, mode = 0, ctas_per_sm = 1, threads = BT_MAX;
   double tol = 1e-14;
   int max_iters = 10;
   const double *A = nullptr, *B = nullptr;
@@ -427,20 +705,41 @@ struct la_batch_plan_s {
   int* d_queue = nullptr;
   int* d_status = nullptr;
   double* d_eta = nullptr;
+  long long* d_cycles = nullptr;
+  unsigned long long* d_phase = nullptr;
+  int* d_perm = nullptr;
   void* d_scratch = nullptr;
-  int* d_perm = nullptr;  // sorted position -> caller's system index (host copy below)
-  std::vector<int> perm;
-  size_t smem = 0, scratch_elems = 0;
-  int smem_n = 0, grid = 0;
+  std::vector<int> perm;  // sorted position -> caller's system index
+  size_t smem = 0, smem_fp64 = 0, scratch_bytes = 0;
+  int grid = 0, grid_fp64 = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
 };
 
 namespace {
 
-template <typename T, bool MIXED>
-la_status launch_batch(la_batch_plan_s* pl, int* queue, int only_flagged, size_t smem, int smem_n,
-                       void* scratch, size_t scratch_elems) {
+template <bool MIXED>
+la_status set_kernel_smem(la_ctx ctx) {
+  cudaError_t e = cudaFuncSetAttribute(batched_kernel<MIXED>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(ctx->smem_optin - BATCH_STATIC_SMEM));
+  return e == cudaSuccess ? LA_OK : la_cuda_fail(ctx, e, "cudaFuncSetAttribute(batched)");
+}
+
+// CTAs of batched_kernel<MIXED> that fit on one SM with `threads` threads and
+// `smem` bytes of dynamic shared memory each.
+template <bool MIXED>
+int resident_ctas(int threads, size_t smem) {
+  int blocks = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, batched_kernel<MIXED>, threads,
+                                                    smem) != cudaSuccess)
+    return 0;
+  return blocks;
+}
+
+template <bool MIXED>
+la_status launch_pass(la_batch_plan_s* pl, int* queue, int only_flagged, size_t smem, int grid,
+                      int threads) {
   la_ctx ctx = pl->ctx;
   BatchArgs a;
   a.A = pl->A;
@@ -451,53 +750,42 @@ la_status launch_batch(la_batch_plan_s* pl, int* queue, int only_flagged, size_t
   a.queue = queue;
   a.status = pl->d_status;
   a.eta = pl->d_eta;
-  a.scratch = scratch;
-  a.scratch_elems = scratch_elems;
-  a.smem_n = smem_n;
+  a.scratch = pl->d_scratch;
+  a.scratch_bytes = pl->scratch_bytes;
+  a.smem_budget = smem;
   a.max_iters = pl->max_iters;
   a.tol = pl->tol;
   a.only_flagged = only_flagged;
-  a.panel = 16;
-  static bool configured = false;  // outside any stream capture (first plan run)
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(batched_kernel<T, MIXED>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(ctx->smem_optin - batch_static_smem()));
-    if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaFuncSetAttribute(batched)");
-    configured = true;
-  }
-  batched_kernel<T, MIXED><<<pl->grid, BT, smem, ctx->stream>>>(a);
+  a.cycles = pl->d_cycles;
+  a.phase = pl->d_phase;
+  batched_kernel<MIXED><<<grid, threads, smem, ctx->stream>>>(a);
   ctx->launches++;
   return la_check_launch(ctx, "batched_kernel");
 }
 
-// Largest n whose working matrix and vectors fit `budget` bytes of shared memory.
-template <typename T, bool MIXED>
-int fit_n(size_t budget) {
-  int n = 0;
-  for (int t = 1; t <= 256; t++)
-    if (smem_for<T, MIXED>(t) <= budget) n = t;
-  return n;
-}
-
-// The whole pipeline (both passes) on the context's stream.
+// The whole pipeline on the context's stream.
 la_status enqueue_plan(la_batch_plan_s* pl) {
   la_ctx ctx = pl->ctx;
   LA_CUDA(ctx, cudaMemsetAsync(pl->d_queue, 0, 2 * sizeof(int), ctx->stream));
-  // The per-CTA budget keeps ctas_per_sm CTAs resident per SM.
+  LA_CUDA(ctx, cudaMemsetAsync(pl->d_cycles, 0, pl->count * sizeof(long long), ctx->stream));
+  LA_CUDA(ctx, cudaMemsetAsync(pl->d_phase, 0, 8 * sizeof(unsigned long long), ctx->stream));
   if (pl->mode == LA_BATCH_FP64) {
-    LA_TRY((launch_batch<double, false>(pl, pl->d_queue, 0, pl->smem, pl->smem_n, pl->d_scratch,
-                                        pl->scratch_elems)));
+    LA_TRY(launch_pass<false>(pl, pl->d_queue, 0, pl->smem, pl->grid, pl->threads));
   } else {
-    LA_TRY((launch_batch<float, true>(pl, pl->d_queue, 0, pl->smem, pl->smem_n, pl->d_scratch,
-                                      pl->scratch_elems)));
-    // FP64 pass over systems whose refinement did not converge.
-    const size_t budget = pl->smem;
-    LA_TRY((launch_batch<double, false>(pl, pl->d_queue + 1, 1, budget,
-                                        fit_n<double, false>(budget), pl->d_scratch,
-                                        pl->scratch_elems)));
+    LA_TRY(launch_pass<true>(pl, pl->d_queue, 0, pl->smem, pl->grid, pl->threads));
+    // FP64 pass over systems whose refinement did not converge: one
+    // 256-thread CTA per SM with all of its shared memory.
+    LA_TRY(launch_pass<false>(pl, pl->d_queue + 1, 1, pl->smem_fp64, pl->grid_fp64, BT_MAX));
   }
   return LA_OK;
+}
+
+int class_of(int prec) {
+  switch (prec) {
+    case LA_PREC_FP8: return CLS_FP8;
+    case LA_PREC_BF16: return CLS_BF16;
+    default: return CLS_F32;
+  }
 }
 
 }  // namespace
@@ -506,25 +794,53 @@ extern "C" {
 
 la_status la_batch_plan_create(la_ctx ctx, const double* d_a, const double* d_b, double* d_x,
                                const la_batch_system* systems, int count, int mode,
-                               int ctas_per_sm, double tol, int max_iters, la_batch_plan* out) {
+                               int ctas_per_sm, int warps_per_system, double tol, int max_iters,
+                               la_batch_plan* out) {
   if (!ctx || !d_a || !d_b || !d_x || !systems || !out || count <= 0) return LA_INVALID;
   if (mode != LA_BATCH_FP64 && mode != LA_BATCH_MIXED) return LA_INVALID;
-  if (ctas_per_sm < 1 || ctas_per_sm > 4) return LA_INVALID;
+  if (warps_per_system == 0) warps_per_system = NW_MAX;
+  if (ctas_per_sm < 1 || ctas_per_sm > 8) return LA_INVALID;
+  if (warps_per_system != 2 && warps_per_system != 4 && warps_per_system != 8) return LA_INVALID;
   LA_CUDA(ctx, cudaSetDevice(ctx->device));
-  for (int i = 0; i < count; i++)
-    if (systems[i].n < 1 || systems[i].n > 256 || systems[i].nrhs < 1 || systems[i].nrhs > 4)
+  int nmax = 0;
+  for (int i = 0; i < count; i++) {
+    if (systems[i].n < 1 || systems[i].n > NMAX || systems[i].nrhs < 1 || systems[i].nrhs > 4)
       return LA_UNSUPPORTED;
+    nmax = std::max(nmax, systems[i].n);
+  }
+  LA_TRY(set_kernel_smem<true>(ctx));
+  LA_TRY(set_kernel_smem<false>(ctx));
+  // Per-CTA budget: ctas_per_sm CTAs share an SM's shared memory. Every system
+  // of the batch must fit with its matrix in global scratch; the FP64 redo
+  // pass of a mixed plan has a whole SM per CTA.
+  const size_t optin = (size_t)ctx->smem_optin - BATCH_STATIC_SMEM;
+  const size_t budget =
+      std::min(optin, (size_t)(228 * 1024) / ctas_per_sm - 1024 - BATCH_STATIC_SMEM);
+  const int threads = 32 * warps_per_system;
+  const size_t need = mode == LA_BATCH_FP64 ? lay<double, double>(nmax, 4, false, false).total
+                                            : lay<float, float>(nmax, 4, false, true).total;
+  if (budget < need) return LA_UNSUPPORTED;
+  if (lay<double, double>(NMAX, 4, false, false).total > optin) return LA_UNSUPPORTED;
+  const int fit = mode == LA_BATCH_FP64 ? resident_ctas<false>(threads, budget)
+                                        : resident_ctas<true>(threads, budget);
+  if (fit < ctas_per_sm) return LA_UNSUPPORTED;
   la_batch_plan_s* pl = new (std::nothrow) la_batch_plan_s();
   if (!pl) return LA_NOMEM;
   pl->ctx = ctx;
   pl->count = count;
   pl->mode = mode;
   pl->ctas_per_sm = ctas_per_sm;
+  pl->threads = threads;
   pl->tol = tol;
   pl->max_iters = max_iters;
   pl->A = d_a;
   pl->B = d_b;
   pl->X = d_x;
+  pl->smem = budget;
+  pl->smem_fp64 = optin;
+  pl->grid = ctx->sm_count * ctas_per_sm;
+  pl->grid_fp64 = ctx->sm_count;
+  pl->scratch_bytes = al16((size_t)NMAX * NMAX * sizeof(double));
   // Work queue order: decreasing n (cost ~ n^3), ties by index.
   pl->perm.resize(count);
   for (int i = 0; i < count; i++) pl->perm[i] = i;
@@ -537,39 +853,29 @@ la_status la_batch_plan_create(la_ctx ctx, const double* d_a, const double* d_b,
     h[i].b = (long long)s.b_offset;
     h[i].n = s.n;
     h[i].nrhs = s.nrhs;
+    h[i].cls = class_of(s.precision);
+    h[i].pad = 0;
   }
-  // Shared memory per CTA for the requested residency.
-  // Per CTA: the opt-in limit less the static part, or the SM's 228 KB shared
-  // among ctas_per_sm CTAs (1 KB reserved per CTA).
-  const size_t per_cta = (size_t)ctx->smem_optin - batch_static_smem();
-  size_t budget = std::min(per_cta, (size_t)(228 * 1024) / ctas_per_sm - 1024 - batch_static_smem());
-  // A CTA also needs room for the L21 / U12 staging when a system works in
-  // global scratch.
-  const size_t need = tail_bytes() + (mode == LA_BATCH_FP64 ? stage_bytes<double>()
-                                                             : stage_bytes<double>());
-  if (budget < need) {
-    delete pl;
-    return LA_UNSUPPORTED;
-  }
-  pl->smem = budget;
-  pl->smem_n = mode == LA_BATCH_FP64 ? fit_n<double, false>(budget) : fit_n<float, true>(budget);
-  pl->grid = ctx->sm_count * ctas_per_sm;
-  pl->scratch_elems = (size_t)256 * 257;
+  const int slices = std::max(pl->grid, pl->grid_fp64);
   la_status s = la_device_alloc(ctx, reinterpret_cast<void**>(&pl->d_desc), count * sizeof(SysDesc));
   if (s == LA_OK) s = la_device_alloc(ctx, reinterpret_cast<void**>(&pl->d_queue), 64);
   if (s == LA_OK) s = la_device_alloc(ctx, reinterpret_cast<void**>(&pl->d_status), count * sizeof(int));
   if (s == LA_OK) s = la_device_alloc(ctx, reinterpret_cast<void**>(&pl->d_eta), count * sizeof(double));
-  if (s == LA_OK)
-    s = la_device_alloc(ctx, &pl->d_scratch, (size_t)pl->grid * pl->scratch_elems * sizeof(double));
+  if (s == LA_OK) s = la_device_alloc(ctx, reinterpret_cast<void**>(&pl->d_cycles), count * sizeof(long long));
+  if (s == LA_OK) s = la_device_alloc(ctx, reinterpret_cast<void**>(&pl->d_perm), count * sizeof(int));
+  if (s == LA_OK) s = la_device_alloc(ctx, reinterpret_cast<void**>(&pl->d_phase), 8 * sizeof(unsigned long long));
+  if (s == LA_OK) s = la_device_alloc(ctx, &pl->d_scratch, (size_t)slices * pl->scratch_bytes);
   if (s == LA_OK) {
     cudaError_t e = cudaMemcpyAsync(pl->d_desc, h.data(), count * sizeof(SysDesc),
                                     cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(pl->d_perm, pl->perm.data(), count * sizeof(int), cudaMemcpyHostToDevice,
+                          ctx->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(pl->d_status, 0, count * sizeof(int), ctx->stream);
     if (e != cudaSuccess) s = la_cuda_fail(ctx, e, "batch plan upload");
   }
   if (s == LA_OK) s = la_sync_and_check(ctx, "batch plan");
-  // Capture the pipeline in a CUDA graph (attributes are set by a first
-  // uncaptured run so capture only records launches).
+  // One uncaptured run, then the graph.
   if (s == LA_OK) s = enqueue_plan(pl);
   if (s == LA_OK) s = la_sync_and_check(ctx, "batch warm run");
   if (s == LA_OK) {
@@ -620,11 +926,43 @@ la_status la_batch_plan_stats(la_batch_plan pl, int* iterations, double* eta, in
   LA_TRY(la_sync_and_check(ctx, "batch stats"));
   for (int i = 0; i < pl->count; i++) {
     const int orig = pl->perm[i];
-    // FP64 pass results carry status 0 and eta -1; refinement keeps its count.
     if (iterations) iterations[orig] = st[i] >= 0 ? st[i] : -1 - st[i];
     if (eta) eta[orig] = et[i];
+    // The FP64 pass leaves eta = -1 on the systems it redid.
     if (fell_back) fell_back[orig] = (pl->mode == LA_BATCH_MIXED && et[i] < 0.0) ? 1 : 0;
   }
+  return LA_OK;
+}
+
+la_status la_batch_plan_select_device(la_batch_plan pl, const int* d_class) {
+  if (!pl || !d_class) return LA_INVALID;
+  if (pl->mode != LA_BATCH_MIXED) return LA_INVALID;
+  la_ctx ctx = pl->ctx;
+  LA_CUDA(ctx, cudaSetDevice(ctx->device));
+  select_kernel<<<(pl->count + 255) / 256, 256, 0, ctx->stream>>>(pl->d_desc, pl->d_perm, d_class,
+                                                                  pl->count);
+  ctx->launches++;
+  return la_check_launch(ctx, "select_kernel");
+}
+
+la_status la_batch_plan_phase_cycles(la_batch_plan pl, long long* phase) {
+  if (!pl || !phase) return LA_INVALID;
+  la_ctx ctx = pl->ctx;
+  LA_CUDA(ctx, cudaSetDevice(ctx->device));
+  LA_CUDA(ctx, cudaMemcpyAsync(phase, pl->d_phase, 8 * sizeof(long long), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  return la_sync_and_check(ctx, "batch phase cycles");
+}
+
+la_status la_batch_plan_cycles(la_batch_plan pl, long long* cycles) {
+  if (!pl || !cycles) return LA_INVALID;
+  la_ctx ctx = pl->ctx;
+  LA_CUDA(ctx, cudaSetDevice(ctx->device));
+  std::vector<long long> c(pl->count);
+  LA_CUDA(ctx, cudaMemcpyAsync(c.data(), pl->d_cycles, pl->count * sizeof(long long),
+                               cudaMemcpyDeviceToHost, ctx->stream));
+  LA_TRY(la_sync_and_check(ctx, "batch cycles"));
+  for (int i = 0; i < pl->count; i++) cycles[pl->perm[i]] = c[i];
   return LA_OK;
 }
 
@@ -638,60 +976,67 @@ void la_batch_plan_destroy(la_batch_plan pl) {
   la_device_free(ctx, pl->d_queue);
   la_device_free(ctx, pl->d_status);
   la_device_free(ctx, pl->d_eta);
+  la_device_free(ctx, pl->d_cycles);
+  la_device_free(ctx, pl->d_perm);
+  la_device_free(ctx, pl->d_phase);
   la_device_free(ctx, pl->d_scratch);
   cudaStreamSynchronize(ctx->stream);
   delete pl;
 }
 
-}  // extern "C"
-
-extern "C" la_status la_batch_autotune(la_ctx ctx, const double* d_a, const double* d_b,
-                                       double* d_x, const la_batch_system* systems, int count,
-                                       int mode, double tol, int max_iters,
-                                       const char* table_path, int* best_ctas_per_sm,
-                                       double* best_ms) {
-  if (!ctx || !best_ctas_per_sm) return LA_INVALID;
+la_status la_batch_autotune(la_ctx ctx, const double* d_a, const double* d_b, double* d_x,
+                            const la_batch_system* systems, int count, int mode, double tol,
+                            int max_iters, const char* table_path, int* best_ctas_per_sm,
+                            int* best_warps_per_system, double* best_ms) {
+  if (!ctx || !best_ctas_per_sm || !systems || count <= 0) return LA_INVALID;
   double mean_n = 0;
   for (int i = 0; i < count; i++) mean_n += systems[i].n;
-  mean_n /= std::max(count, 1);
-  int best = 1;
+  mean_n /= count;
+  int best_c = 0, best_w = 0;
   double best_t = INFINITY;
-  std::vector<std::pair<int, double>> rows;
-  for (int c = 1; c <= 4; c++) {
-    la_batch_plan pl = nullptr;
-    la_status s = la_batch_plan_create(ctx, d_a, d_b, d_x, systems, count, mode, c, tol,
-                                       max_iters, &pl);
-    if (s != LA_OK) continue;
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    double t = INFINITY;
-    for (int rep = 0; rep < 3; rep++) {
-      cudaEventRecord(e0, ctx->stream);
-      la_batch_plan_run(pl);
-      cudaEventRecord(e1, ctx->stream);
-      if (cudaEventSynchronize(e1) != cudaSuccess) break;
-      float ms = 0;
-      cudaEventElapsedTime(&ms, e0, e1);
-      t = std::min(t, (double)ms);
+  struct Row { int c, w; double ms; };
+  std::vector<Row> rows;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  LA_CUDA(ctx, cudaEventCreate(&e0));
+  LA_CUDA(ctx, cudaEventCreate(&e1));
+  const int warps[3] = {8, 4, 2};
+  const int ctas[4] = {1, 2, 4, 8};
+  for (int w : warps)
+    for (int c : ctas) {
+      la_batch_plan pl = nullptr;
+      if (la_batch_plan_create(ctx, d_a, d_b, d_x, systems, count, mode, c, w, tol, max_iters,
+                               &pl) != LA_OK)
+        continue;
+      double t = INFINITY;
+      for (int rep = 0; rep < 3; rep++) {
+        cudaEventRecord(e0, ctx->stream);
+        la_batch_plan_run(pl);
+        cudaEventRecord(e1, ctx->stream);
+        if (cudaEventSynchronize(e1) != cudaSuccess) break;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        t = std::min(t, (double)ms);
+      }
+      la_batch_plan_destroy(pl);
+      rows.push_back({c, w, t});
+      if (t < best_t) { best_t = t; best_c = c; best_w = w; }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    la_batch_plan_destroy(pl);
-    rows.push_back({c, t});
-    if (t < best_t) { best_t = t; best = c; }
-  }
-  if (rows.empty()) return LA_CUDA_ERROR;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rows.empty()) return LA_UNSUPPORTED;
   if (table_path) {
     FILE* f = fopen(table_path, "a");
     if (f) {
       for (auto& r : rows)
-        fprintf(f, "%s %d %.1f %d %.4f\n", mode == LA_BATCH_FP64 ? "fp64" : "mixed", count,
-                mean_n, r.first, r.second);
+        fprintf(f, "%s %d %.1f %d %d %.4f\n", mode == LA_BATCH_FP64 ? "fp64" : "mixed", count,
+                mean_n, r.c, r.w, r.ms);
       fclose(f);
     }
   }
-  *best_ctas_per_sm = best;
+  *best_ctas_per_sm = best_c;
+  if (best_warps_per_system) *best_warps_per_system = best_w;
   if (best_ms) *best_ms = best_t;
   return la_sync_and_check(ctx, "batch autotune");
 }
+
+}  // extern "C"

@@ -1,0 +1,625 @@
+// Learned precision selector for batched solves (not in the reference).
+//
+// Per system, a feature kernel computes 16 cheap features (norms, diagonal
+// dominance, row/column scaling spread, a few-step Lanczos estimate of the
+// condition number); a small MLP (16 -> 64 -> 64 -> 3, ReLU, softmax, FP32)
+// proposes the storage precision of the system's LU factors (FP8, BF16, FP32);
+// the FP64 pass of the batched solver stays the fallback and the judge.
+//
+// The network is trained on the GPU by the kernels below: forward (one thread
+// per sample), per-sample deltas, parameter gradients (one thread per
+// parameter summing over the samples in a fixed order, so a step is
+// deterministic) and Adam. A generator kernel builds the Householder-
+// conditioned training and test systems A = H1 diag(s) H2 on the device.
+#include <new>
+
+#include "la_internal.cuh"
+
+namespace {
+
+constexpr int NF = 16, H1 = 64, H2 = 64, NC = 3;
+constexpr int OFF_W1 = 0;                   // [H1][NF]
+constexpr int OFF_B1 = OFF_W1 + H1 * NF;    // [H1]
+constexpr int OFF_W2 = OFF_B1 + H1;         // [H2][H1]
+constexpr int OFF_B2 = OFF_W2 + H2 * H1;    // [H2]
+constexpr int OFF_W3 = OFF_B2 + H2;         // [NC][H2]
+constexpr int OFF_B3 = OFF_W3 + NC * H2;    // [NC]
+constexpr int NPARAM = OFF_B3 + NC;         // 5443
+constexpr int ACT = NF + H1 + H2 + NC;      // per-sample activations kept for backprop
+
+struct SysRec {
+  long long a, b;
+  int n, nrhs;
+};
+
+// ---- counter-based random numbers (splitmix64) -----------------------------
+__host__ __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ double u01(unsigned long long key, unsigned long long i) {
+  return ((mix64(key ^ mix64(i)) >> 11) + 0.5) * (1.0 / 9007199254740992.0);  // (0, 1)
+}
+__device__ __forceinline__ double gauss(unsigned long long key, unsigned long long i) {
+  const double u1 = u01(key, 2 * i), u2 = u01(key, 2 * i + 1);
+  return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+}
+
+// A_i = H1 diag(s) H2, s_k = kappa_i^(-k/(n-1)), log10 kappa_i uniform in
+// [lk0, lk1]; H = product of 4 reflectors I - 2 v v^T / v^T v, v iid N(0,1);
+// B_i iid N(0,1). One CTA per system; A_i is built in place in global memory.
+__global__ void __launch_bounds__(256)
+gen_hh_kernel(const SysRec* __restrict__ sys, int count, double* A, double* B, double lk0,
+              double lk1, unsigned long long seed, double* kappa_out) {
+  __shared__ double v[512];
+  __shared__ double w[512];
+  __shared__ double s_vv;
+  const int tid = threadIdx.x;
+  for (int i = blockIdx.x; i < count; i += gridDim.x) {
+    const SysRec d = sys[i];
+    const int n = d.n;
+    double* a = A + d.a;
+    const unsigned long long key = mix64(seed ^ (0xA5A5A5A5ull * (unsigned long long)(i + 1)));
+    const double lk = lk0 + (lk1 - lk0) * u01(key, 0x7fffffffull);
+    const double kappa = pow(10.0, lk);
+    if (tid == 0 && kappa_out) kappa_out[i] = kappa;
+    for (int idx = tid; idx < n * n; idx += blockDim.x) {
+      const int r = idx / n, c = idx % n;
+      a[idx] = (r == c) ? (n > 1 ? pow(kappa, -(double)r / (n - 1)) : 1.0) : 0.0;
+    }
+    for (int idx = tid; idx < n * d.nrhs; idx += blockDim.x)
+      B[d.b + idx] = gauss(key, 0x100000000ull + idx);
+    __syncthreads();
+    for (int h = 0; h < 8; h++) {
+      const bool right = h < 4;
+      for (int k = tid; k < n; k += blockDim.x) v[k] = gauss(key, ((unsigned long long)(h + 1) << 40) + k);
+      __syncthreads();
+      if (tid == 0) {
+        double s = 0.0;
+        for (int k = 0; k < n; k++) s += v[k] * v[k];
+        s_vv = s;
+      }
+      __syncthreads();
+      const double f = 2.0 / s_vv;
+      // right: A -= f (A v) v^T ; left: A -= f v (v^T A)
+      if (right) {  // w = A v: one warp per row
+        const int lane = tid & 31;
+        for (int r = tid >> 5; r < n; r += blockDim.x >> 5) {
+          double s = 0.0;
+          for (int k = lane; k < n; k += 32) s += a[(size_t)r * n + k] * v[k];
+          for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+          if (lane == 0) w[r] = s;
+        }
+      } else {  // w = A^T v: one thread per column
+        for (int c = tid; c < n; c += blockDim.x) {
+          double s = 0.0;
+          for (int k = 0; k < n; k++) s += v[k] * a[(size_t)k * n + c];
+          w[c] = s;
+        }
+      }
+      __syncthreads();
+      for (int idx = tid; idx < n * n; idx += blockDim.x) {
+        const int r = idx / n, c = idx % n;
+        a[idx] -= right ? f * w[r] * v[c] : f * v[r] * w[c];
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// ---- features -----------------------------------------------------------------
+__device__ double block_sum(double v, double* red) {
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+  __syncthreads();
+  return t;
+}
+__device__ double block_max(double v, double* red) {
+  for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, off));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); w++) t = fmax(t, red[w]);
+  __syncthreads();
+  return t;
+}
+__device__ double block_min(double v, double* red) {
+  for (int off = 16; off > 0; off >>= 1) v = fmin(v, __shfl_down_sync(0xffffffffu, v, off));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = INFINITY;
+  for (int w = 0; w < (int)(blockDim.x >> 5); w++) t = fmin(t, red[w]);
+  __syncthreads();
+  return t;
+}
+
+__device__ __forceinline__ float lg(double x) { return (float)log10(fmax(x, 1e-300)); }
+
+// Smallest eigenvalue of the symmetric tridiagonal (alpha, beta) of order k
+// by bisection on the Sturm count.
+__device__ double tridiag_min_eig(const double* al, const double* be, int k) {
+  double lo = INFINITY, hi = -INFINITY;
+  for (int i = 0; i < k; i++) {
+    const double r = (i > 0 ? fabs(be[i - 1]) : 0.0) + (i + 1 < k ? fabs(be[i]) : 0.0);
+    lo = fmin(lo, al[i] - r);
+    hi = fmax(hi, al[i] + r);
+  }
+  for (int it = 0; it < 100; it++) {
+    const double mid = 0.5 * (lo + hi);
+    int cnt = 0;
+    double q = al[0] - mid;
+    if (q < 0) cnt++;
+    for (int i = 1; i < k; i++) {
+      q = al[i] - mid - be[i - 1] * be[i - 1] / (q != 0.0 ? q : 1e-300);
+      if (q < 0) cnt++;
+    }
+    if (cnt >= 1) hi = mid; else lo = mid;
+  }
+  return 0.5 * (lo + hi);
+}
+
+constexpr int LK = 8;  // Lanczos steps
+
+// 16 features per system (one CTA per system). The last two come from LK steps
+// of Lanczos on A^T A with full reorthogonalisation: the largest and the
+// smallest Ritz values bound sigma_max^2 from below and sigma_min^2 from above.
+__global__ void __launch_bounds__(256)
+features_kernel(const double* __restrict__ A, const SysRec* __restrict__ sys, int count,
+                float* __restrict__ F) {
+  __shared__ double red[8];
+  __shared__ double q[LK + 1][512];
+  __shared__ double t1[512];
+  __shared__ double t2[512];
+  __shared__ double al[LK], be[LK];
+  const int tid = threadIdx.x;
+  for (int i = blockIdx.x; i < count; i += gridDim.x) {
+    const SysRec d = sys[i];
+    const int n = d.n;
+    const double* a = A + d.a;
+    // norms and dominance
+    double rmax = 0, rmin = INFINITY, dmin = INFINITY, dsum = 0, ddom = 0, amax = 0, fro = 0,
+           diag_min = INFINITY;
+    const int lane = tid & 31;
+    for (int r = tid >> 5; r < n; r += blockDim.x >> 5) {  // one warp per row
+      double rs = 0, f2 = 0, am = 0;
+      for (int k = lane; k < n; k += 32) {
+        const double x = fabs(a[(size_t)r * n + k]);
+        rs += x;
+        f2 += x * x;
+        am = fmax(am, x);
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        rs += __shfl_xor_sync(0xffffffffu, rs, o);
+        f2 += __shfl_xor_sync(0xffffffffu, f2, o);
+        am = fmax(am, __shfl_xor_sync(0xffffffffu, am, o));
+      }
+      if (lane == 0) {
+        const double di = fabs(a[(size_t)r * n + r]);
+        const double off = rs - di;
+        fro += f2;
+        amax = fmax(amax, am);
+        rmax = fmax(rmax, rs);
+        rmin = fmin(rmin, rs);
+        const double ratio = di / fmax(off, 1e-300);
+        dmin = fmin(dmin, ratio);
+        dsum += log10(fmax(ratio, 1e-300));
+        ddom += ratio > 1.0 ? 1.0 : 0.0;
+        diag_min = fmin(diag_min, di);
+      }
+    }
+    double cmax = 0, cmin = INFINITY, asym = 0;
+    for (int c = tid; c < n; c += blockDim.x) {
+      double cs = 0;
+      for (int k = 0; k < n; k++) {
+        cs += fabs(a[(size_t)k * n + c]);
+        const double dd = a[(size_t)c * n + k] - a[(size_t)k * n + c];
+        asym += dd * dd;
+      }
+      cmax = fmax(cmax, cs);
+      cmin = fmin(cmin, cs);
+    }
+    rmax = block_max(rmax, red);
+    rmin = block_min(rmin, red);
+    dmin = block_min(dmin, red);
+    dsum = block_sum(dsum, red);
+    ddom = block_sum(ddom, red);
+    amax = block_max(amax, red);
+    fro = block_sum(fro, red);
+    diag_min = block_min(diag_min, red);
+    cmax = block_max(cmax, red);
+    cmin = block_min(cmin, red);
+    asym = block_sum(asym, red);
+    // Lanczos on A^T A from a fixed start vector
+    for (int k = tid; k < n; k += blockDim.x) q[0][k] = 1.0 + 0.5 * sin(1.0 + k);
+    double nrm = sqrt(block_sum([&] {
+      double s = 0;
+      for (int k = tid; k < n; k += blockDim.x) s += q[0][k] * q[0][k];
+      return s;
+    }(), red));
+    for (int k = tid; k < n; k += blockDim.x) q[0][k] /= nrm;
+    __syncthreads();
+    int kk = 0;
+    for (int j = 0; j < LK && j < n; j++) {
+      // t2 = A^T (A q_j)
+      for (int r = tid >> 5; r < n; r += blockDim.x >> 5) {
+        double s = 0;
+        for (int k = lane; k < n; k += 32) s += a[(size_t)r * n + k] * q[j][k];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) t1[r] = s;
+      }
+      __syncthreads();
+      for (int c = tid; c < n; c += blockDim.x) {
+        double s = 0;
+        for (int k = 0; k < n; k++) s += a[(size_t)k * n + c] * t1[k];
+        t2[c] = s;
+      }
+      __syncthreads();
+      double aj = 0;
+      for (int k = tid; k < n; k += blockDim.x) aj += q[j][k] * t2[k];
+      aj = block_sum(aj, red);
+      // full reorthogonalisation against q_0..q_j
+      for (int p = 0; p <= j; p++) {
+        double c = 0;
+        for (int k = tid; k < n; k += blockDim.x) c += q[p][k] * t2[k];
+        c = block_sum(c, red);
+        for (int k = tid; k < n; k += blockDim.x) t2[k] -= c * q[p][k];
+        __syncthreads();
+      }
+      double bj = 0;
+      for (int k = tid; k < n; k += blockDim.x) bj += t2[k] * t2[k];
+      bj = sqrt(block_sum(bj, red));
+      if (tid == 0) { al[j] = aj; be[j] = bj; }
+      kk = j + 1;
+      if (!(bj > 1e-12 * fabs(aj)) || j + 1 >= LK) break;
+      for (int k = tid; k < n; k += blockDim.x) q[j + 1][k] = t2[k] / bj;
+      __syncthreads();
+    }
+    __syncthreads();
+    if (tid == 0) {
+      double smax2 = 0;
+      for (int j = 0; j < kk; j++) smax2 = fmax(smax2, al[j] + (j > 0 ? fabs(be[j - 1]) : 0.0));
+      // largest Ritz value: bisection on the negated matrix
+      double nal[LK], nbe[LK];
+      for (int j = 0; j < kk; j++) { nal[j] = -al[j]; nbe[j] = be[j]; }
+      const double emax = -tridiag_min_eig(nal, nbe, kk);
+      const double emin = fmax(tridiag_min_eig(al, be, kk), emax * 1e-32);
+      float* f = F + (size_t)i * NF;
+      f[0] = (float)(log2((double)n) / 9.0);
+      f[1] = (float)d.nrhs / 4.f;
+      f[2] = lg(rmax);
+      f[3] = lg(cmax);
+      f[4] = lg(sqrt(fro));
+      f[5] = lg(amax);
+      f[6] = lg(sqrt(fmax(emax, 0.0)));
+      f[7] = lg(sqrt(fro) / sqrt(fmax(emax, 1e-300)));
+      f[8] = lg(dmin);
+      f[9] = (float)(dsum / n);
+      f[10] = (float)(ddom / n);
+      f[11] = lg(rmax / fmax(rmin, 1e-300));
+      f[12] = lg(cmax / fmax(cmin, 1e-300));
+      f[13] = (float)(sqrt(asym) / fmax(sqrt(fro), 1e-300));
+      f[14] = lg(diag_min / fmax(amax, 1e-300));
+      f[15] = lg(sqrt(fmax(emax, 1e-300) / emin));
+    }
+    __syncthreads();
+  }
+}
+
+// ---- MLP ------------------------------------------------------------------------
+// Forward for one sample: x normalised -> h1 -> h2 -> logits -> softmax.
+__device__ void mlp_fwd(const float* __restrict__ P, const float* x, float* h1, float* h2,
+                        float* pr) {
+  for (int o = 0; o < H1; o++) {
+    float s = P[OFF_B1 + o];
+    for (int k = 0; k < NF; k++) s = fmaf(P[OFF_W1 + o * NF + k], x[k], s);
+    h1[o] = fmaxf(s, 0.f);
+  }
+  for (int o = 0; o < H2; o++) {
+    float s = P[OFF_B2 + o];
+    for (int k = 0; k < H1; k++) s = fmaf(P[OFF_W2 + o * H1 + k], h1[k], s);
+    h2[o] = fmaxf(s, 0.f);
+  }
+  float lg3[NC], mx = -INFINITY;
+  for (int o = 0; o < NC; o++) {
+    float s = P[OFF_B3 + o];
+    for (int k = 0; k < H2; k++) s = fmaf(P[OFF_W3 + o * H2 + k], h2[k], s);
+    lg3[o] = s;
+    mx = fmaxf(mx, s);
+  }
+  float z = 0.f;
+  for (int o = 0; o < NC; o++) { lg3[o] = expf(lg3[o] - mx); z += lg3[o]; }
+  for (int o = 0; o < NC; o++) pr[o] = lg3[o] / z;
+}
+
+// One thread per sample: normalise, forward, keep activations; with labels,
+// also the per-sample output delta and loss.
+__global__ void mlp_forward_kernel(const float* __restrict__ P, const float* __restrict__ mean,
+                                   const float* __restrict__ stdv, const float* __restrict__ X,
+                                   int count, float* __restrict__ act, float* __restrict__ probs,
+                                   int* __restrict__ cls, const int* __restrict__ y,
+                                   float* __restrict__ loss) {
+  __shared__ float Ps[NPARAM];
+  for (int i = threadIdx.x; i < NPARAM; i += blockDim.x) Ps[i] = P[i];
+  __syncthreads();
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= count) return;
+  float x[NF], h1[H1], h2[H2], pr[NC];
+  for (int k = 0; k < NF; k++) x[k] = (X[(size_t)s * NF + k] - mean[k]) / stdv[k];
+  mlp_fwd(Ps, x, h1, h2, pr);
+  if (act) {
+    float* a = act + (size_t)s * ACT;
+    for (int k = 0; k < NF; k++) a[k] = x[k];
+    for (int k = 0; k < H1; k++) a[NF + k] = h1[k];
+    for (int k = 0; k < H2; k++) a[NF + H1 + k] = h2[k];
+    for (int k = 0; k < NC; k++) a[NF + H1 + H2 + k] = pr[k] - ((y && y[s] == k) ? 1.f : 0.f);
+  }
+  if (probs)
+    for (int k = 0; k < NC; k++) probs[(size_t)s * NC + k] = pr[k];
+  if (cls) {
+    int best = 0;
+    for (int k = 1; k < NC; k++)
+      if (pr[k] > pr[best]) best = k;
+    cls[s] = best;
+  }
+  if (loss && y) loss[s] = -logf(fmaxf(pr[y[s]], 1e-30f));
+}
+
+// Hidden-layer deltas per sample: d2 = (W3^T d3) . [h2 > 0], d1 = (W2^T d2) . [h1 > 0].
+__global__ void mlp_delta_kernel(const float* __restrict__ P, const float* __restrict__ act,
+                                 int count, float* __restrict__ delta) {
+  __shared__ float Ps[NPARAM];
+  for (int i = threadIdx.x; i < NPARAM; i += blockDim.x) Ps[i] = P[i];
+  __syncthreads();
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= count) return;
+  const float* a = act + (size_t)s * ACT;
+  const float* h1 = a + NF;
+  const float* h2 = a + NF + H1;
+  const float* d3 = a + NF + H1 + H2;
+  float d2[H2];
+  float* out = delta + (size_t)s * (H1 + H2);
+  for (int k = 0; k < H2; k++) {
+    float t = 0.f;
+    for (int o = 0; o < NC; o++) t = fmaf(Ps[OFF_W3 + o * H2 + k], d3[o], t);
+    d2[k] = h2[k] > 0.f ? t : 0.f;
+    out[H1 + k] = d2[k];
+  }
+  for (int k = 0; k < H1; k++) {
+    float t = 0.f;
+    for (int o = 0; o < H2; o++) t = fmaf(Ps[OFF_W2 + o * H1 + k], d2[o], t);
+    out[k] = h1[k] > 0.f ? t : 0.f;
+  }
+}
+
+// Mean gradient of the cross-entropy: one thread per parameter, samples summed
+// in index order (deterministic).
+__global__ void mlp_grad_kernel(const float* __restrict__ act, const float* __restrict__ delta,
+                                int count, float* __restrict__ G) {
+  const int pidx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pidx >= NPARAM) return;
+  float g = 0.f;
+  for (int s = 0; s < count; s++) {
+    const float* a = act + (size_t)s * ACT;
+    const float* dl = delta + (size_t)s * (H1 + H2);
+    float v;
+    if (pidx < OFF_B1) { const int o = pidx / NF, k = pidx % NF; v = dl[o] * a[k]; }
+    else if (pidx < OFF_W2) { v = dl[pidx - OFF_B1]; }
+    else if (pidx < OFF_B2) { const int q = pidx - OFF_W2, o = q / H1, k = q % H1; v = dl[H1 + o] * a[NF + k]; }
+    else if (pidx < OFF_W3) { v = dl[H1 + pidx - OFF_B2]; }
+    else if (pidx < OFF_B3) { const int q = pidx - OFF_W3, o = q / H2, k = q % H2; v = a[NF + H1 + H2 + o] * a[NF + H1 + k]; }
+    else { v = a[NF + H1 + H2 + (pidx - OFF_B3)]; }
+    g += v;
+  }
+  G[pidx] = g / (float)count;
+}
+
+// Adam (beta1 0.9, beta2 0.999, eps 1e-8), t = step number from 1.
+__global__ void adam_kernel(float* __restrict__ P, const float* __restrict__ G, float* __restrict__ m,
+                            float* __restrict__ v, float lr, int t) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= NPARAM) return;
+  const float b1 = 0.9f, b2 = 0.999f;
+  m[i] = b1 * m[i] + (1.f - b1) * G[i];
+  v[i] = b2 * v[i] + (1.f - b2) * G[i] * G[i];
+  const float mh = m[i] / (1.f - powf(b1, (float)t));
+  const float vh = v[i] / (1.f - powf(b2, (float)t));
+  P[i] -= lr * mh / (sqrtf(vh) + 1e-8f);
+}
+
+}  // namespace
+
+struct la_mlp_s {
+  la_ctx ctx;
+  float* d_params = nullptr;  // NPARAM + 2 * NF (mean, std) + 2 * NPARAM (Adam) + NPARAM (grad)
+  int step = 0;
+  float* P() { return d_params; }
+  float* mean() { return d_params + NPARAM; }
+  float* stdv() { return d_params + NPARAM + NF; }
+  float* am() { return d_params + NPARAM + 2 * NF; }
+  float* av() { return am() + NPARAM; }
+  float* grad() { return av() + NPARAM; }
+};
+
+extern "C" {
+
+int la_mlp_param_count(void) { return NPARAM; }
+
+la_status la_mlp_create(la_ctx ctx, unsigned long long seed, la_mlp* out) {
+  if (!ctx || !out) return LA_INVALID;
+  LA_CUDA(ctx, cudaSetDevice(ctx->device));
+  la_mlp m = new (std::nothrow) la_mlp_s();
+  if (!m) return LA_NOMEM;
+  m->ctx = ctx;
+  const size_t total = NPARAM + 2 * NF + 3 * (size_t)NPARAM;
+  la_status s = la_device_alloc(ctx, reinterpret_cast<void**>(&m->d_params), total * sizeof(float));
+  if (s != LA_OK) { delete m; return s; }
+  // He-style uniform init from a seeded splitmix64 stream; normalisation 0/1.
+  std::vector<float> h(total, 0.f);
+  unsigned long long st = seed;
+  auto uni = [&]() { st = mix64(st); return (float)((st >> 11) * (1.0 / 9007199254740992.0)) * 2.f - 1.f; };
+  for (int i = 0; i < H1 * NF; i++) h[OFF_W1 + i] = uni() * sqrtf(6.f / NF);
+  for (int i = 0; i < H2 * H1; i++) h[OFF_W2 + i] = uni() * sqrtf(6.f / H1);
+  for (int i = 0; i < NC * H2; i++) h[OFF_W3 + i] = uni() * sqrtf(6.f / H2);
+  for (int k = 0; k < NF; k++) h[NPARAM + NF + k] = 1.f;
+  cudaError_t e = cudaMemcpyAsync(m->d_params, h.data(), total * sizeof(float),
+                                  cudaMemcpyHostToDevice, ctx->stream);
+  if (e != cudaSuccess) { s = la_cuda_fail(ctx, e, "mlp init"); la_device_free(ctx, m->d_params); delete m; return s; }
+  s = la_sync_and_check(ctx, "mlp init");
+  if (s != LA_OK) { la_device_free(ctx, m->d_params); delete m; return s; }
+  *out = m;
+  return LA_OK;
+}
+
+void la_mlp_destroy(la_mlp m) {
+  if (!m) return;
+  cudaSetDevice(m->ctx->device);
+  la_device_free(m->ctx, m->d_params);
+  cudaStreamSynchronize(m->ctx->stream);
+  delete m;
+}
+
+// params: NPARAM weights then NF means and NF standard deviations (host).
+la_status la_mlp_get_params(la_mlp m, float* params) {
+  if (!m || !params) return LA_INVALID;
+  LA_CUDA(m->ctx, cudaMemcpyAsync(params, m->d_params, (NPARAM + 2 * NF) * sizeof(float),
+                                  cudaMemcpyDeviceToHost, m->ctx->stream));
+  return la_sync_and_check(m->ctx, "mlp params");
+}
+
+la_status la_mlp_set_params(la_mlp m, const float* params) {
+  if (!m || !params) return LA_INVALID;
+  LA_CUDA(m->ctx, cudaMemcpyAsync(m->d_params, params, (NPARAM + 2 * NF) * sizeof(float),
+                                  cudaMemcpyHostToDevice, m->ctx->stream));
+  LA_CUDA(m->ctx, cudaMemsetAsync(m->am(), 0, 3 * (size_t)NPARAM * sizeof(float), m->ctx->stream));
+  m->step = 0;
+  return la_sync_and_check(m->ctx, "mlp params");
+}
+
+// Mean cross-entropy gradient for labels y over count samples (device X, y),
+// without updating; grad (host, NPARAM) may be NULL.
+static la_status mlp_backprop(la_mlp m, const float* d_x, const int* d_y, int count, float* loss) {
+  la_ctx ctx = m->ctx;
+  float *act = nullptr, *delta = nullptr, *dl = nullptr;
+  la_status s = la_device_alloc(ctx, reinterpret_cast<void**>(&act), (size_t)count * ACT * 4);
+  if (s == LA_OK) s = la_device_alloc(ctx, reinterpret_cast<void**>(&delta), (size_t)count * (H1 + H2) * 4);
+  if (s == LA_OK) s = la_device_alloc(ctx, reinterpret_cast<void**>(&dl), (size_t)count * 4);
+  if (s == LA_OK) {
+    const int g = (count + 127) / 128;
+    mlp_forward_kernel<<<g, 128, 0, ctx->stream>>>(m->P(), m->mean(), m->stdv(), d_x, count, act,
+                                                   nullptr, nullptr, d_y, dl);
+    mlp_delta_kernel<<<g, 128, 0, ctx->stream>>>(m->P(), act, count, delta);
+    mlp_grad_kernel<<<(NPARAM + 127) / 128, 128, 0, ctx->stream>>>(act, delta, count, m->grad());
+    ctx->launches += 3;
+    s = la_check_launch(ctx, "mlp backprop");
+  }
+  if (s == LA_OK && loss) {
+    std::vector<float> h(count);
+    cudaError_t e = cudaMemcpyAsync(h.data(), dl, count * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) s = la_cuda_fail(ctx, e, "loss");
+    double t = 0;
+    for (float v : h) t += v;
+    *loss = (float)(t / count);
+  }
+  la_device_free(ctx, act);
+  la_device_free(ctx, delta);
+  la_device_free(ctx, dl);
+  return s;
+}
+
+la_status la_mlp_gradients(la_mlp m, const float* d_x, const int* d_y, int count, float* grad,
+                           float* loss) {
+  if (!m || !d_x || !d_y || count <= 0) return LA_INVALID;
+  LA_CUDA(m->ctx, cudaSetDevice(m->ctx->device));
+  LA_TRY(mlp_backprop(m, d_x, d_y, count, loss));
+  if (grad) {
+    LA_CUDA(m->ctx, cudaMemcpyAsync(grad, m->grad(), NPARAM * sizeof(float),
+                                    cudaMemcpyDeviceToHost, m->ctx->stream));
+  }
+  return la_sync_and_check(m->ctx, "mlp gradients");
+}
+
+la_status la_mlp_train_step(la_mlp m, const float* d_x, const int* d_y, int count, float lr,
+                            float* loss) {
+  if (!m || !d_x || !d_y || count <= 0) return LA_INVALID;
+  LA_CUDA(m->ctx, cudaSetDevice(m->ctx->device));
+  LA_TRY(mlp_backprop(m, d_x, d_y, count, loss));
+  m->step++;
+  adam_kernel<<<(NPARAM + 127) / 128, 128, 0, m->ctx->stream>>>(m->P(), m->grad(), m->am(),
+                                                                 m->av(), lr, m->step);
+  m->ctx->launches++;
+  return la_check_launch(m->ctx, "adam");
+}
+
+la_status la_mlp_predict(la_mlp m, const float* d_x, int count, float* d_probs, int* d_class) {
+  if (!m || !d_x || count <= 0) return LA_INVALID;
+  LA_CUDA(m->ctx, cudaSetDevice(m->ctx->device));
+  mlp_forward_kernel<<<(count + 127) / 128, 128, 0, m->ctx->stream>>>(
+      m->P(), m->mean(), m->stdv(), d_x, count, nullptr, d_probs, d_class, nullptr, nullptr);
+  m->ctx->launches++;
+  return la_check_launch(m->ctx, "mlp predict");
+}
+
+la_status la_batch_features_device(la_ctx ctx, const double* d_a, const la_batch_system* systems,
+                                   int count, float* d_features) {
+  if (!ctx || !d_a || !systems || !d_features || count <= 0) return LA_INVALID;
+  LA_CUDA(ctx, cudaSetDevice(ctx->device));
+  std::vector<SysRec> h(count);
+  for (int i = 0; i < count; i++) {
+    if (systems[i].n < 1 || systems[i].n > 512) return LA_UNSUPPORTED;
+    h[i] = {(long long)systems[i].a_offset, (long long)systems[i].b_offset, systems[i].n,
+            systems[i].nrhs};
+  }
+  SysRec* d = nullptr;
+  LA_TRY(la_device_alloc(ctx, reinterpret_cast<void**>(&d), count * sizeof(SysRec)));
+  cudaError_t e = cudaMemcpyAsync(d, h.data(), count * sizeof(SysRec), cudaMemcpyHostToDevice,
+                                  ctx->stream);
+  la_status s = e == cudaSuccess ? LA_OK : la_cuda_fail(ctx, e, "features upload");
+  if (s == LA_OK) {
+    features_kernel<<<std::min(count, ctx->sm_count * 8), 256, 0, ctx->stream>>>(d_a, d, count,
+                                                                                 d_features);
+    ctx->launches++;
+    s = la_check_launch(ctx, "features_kernel");
+  }
+  la_device_free(ctx, d);
+  if (s == LA_OK) s = la_sync_and_check(ctx, "features");
+  return s;
+}
+
+la_status la_generate_conditioned_batch(la_ctx ctx, const la_batch_system* systems, int count,
+                                        double log10_kappa_min, double log10_kappa_max,
+                                        unsigned long long seed, double* d_a, double* d_b,
+                                        double* d_kappa) {
+  if (!ctx || !systems || !d_a || !d_b || count <= 0) return LA_INVALID;
+  LA_CUDA(ctx, cudaSetDevice(ctx->device));
+  std::vector<SysRec> h(count);
+  for (int i = 0; i < count; i++) {
+    if (systems[i].n < 1 || systems[i].n > 512) return LA_UNSUPPORTED;
+    h[i] = {(long long)systems[i].a_offset, (long long)systems[i].b_offset, systems[i].n,
+            systems[i].nrhs};
+  }
+  SysRec* d = nullptr;
+  LA_TRY(la_device_alloc(ctx, reinterpret_cast<void**>(&d), count * sizeof(SysRec)));
+  cudaError_t e = cudaMemcpyAsync(d, h.data(), count * sizeof(SysRec), cudaMemcpyHostToDevice,
+                                  ctx->stream);
+  la_status s = e == cudaSuccess ? LA_OK : la_cuda_fail(ctx, e, "generator upload");
+  if (s == LA_OK) {
+    gen_hh_kernel<<<std::min(count, ctx->sm_count * 8), 256, 0, ctx->stream>>>(
+        d, count, d_a, d_b, log10_kappa_min, log10_kappa_max, seed, d_kappa);
+    ctx->launches++;
+    s = la_check_launch(ctx, "gen_hh_kernel");
+  }
+  la_device_free(ctx, d);
+  if (s == LA_OK) s = la_sync_and_check(ctx, "generator");
+  return s;
+}
+
+}  // extern "C"

@@ -42,10 +42,10 @@ def main():
     db = torch.from_numpy(b).cuda()
     dx = torch.zeros_like(db)
     for mode in modes:
-        best, ms = la_gpu.batch_autotune(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems,
-                                         mode)
+        best, warps, ms = la_gpu.batch_autotune(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(),
+                                                systems, mode)
         plan = la_gpu.BatchPlan(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems, mode,
-                                ctas_per_sm=best)
+                                ctas_per_sm=best, warps_per_system=warps)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(5):
@@ -53,8 +53,9 @@ def main():
         ctx.synchronize()
         dt = (time.perf_counter() - t0) / 5
         its, eta, fb = plan.stats()
-        print("mode=%d ctas/SM=%d %.2f ms/batch %.0f solves/s fell_back=%d max_iters=%d"
-              % (mode, best, dt * 1e3, count / dt, int(fb.sum()), int(its.max())))
+        print("mode=%d ctas/SM=%d warps/system=%d %.2f ms/batch %.0f solves/s fell_back=%d "
+              "max_iters=%d" % (mode, best, warps, dt * 1e3, count / dt, int(fb.sum()),
+                                int(its.max())))
         plan.free()
 
 

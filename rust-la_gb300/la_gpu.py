@@ -84,11 +84,24 @@ SIGNATURES = {
     "la_lu_mixed_new_device": ([_P, _P, _S, _S, _I, _P], _I),
     "la_lu_solve_refined_device": ([_P, _P, _S, _S, _P, _S, _I, _D, _P], _I),
     "la_lowp_update_device": ([_P, _I, _S, _S, _S, _P, _S, _P, _S, _P, _S, ctypes.c_float], _I),
-    "la_batch_plan_create": ([_P, _P, _P, _P, _P, _I, _I, _I, _D, _I, _P], _I),
+    "la_batch_plan_create": ([_P, _P, _P, _P, _P, _I, _I, _I, _I, _D, _I, _P], _I),
     "la_batch_plan_run": ([_P], _I),
     "la_batch_plan_stats": ([_P, _P, _P, _P], _I),
     "la_batch_plan_destroy": ([_P], None),
-    "la_batch_autotune": ([_P, _P, _P, _P, _P, _I, _I, _D, _I, ctypes.c_char_p, _P, _P], _I),
+    "la_batch_autotune": ([_P, _P, _P, _P, _P, _I, _I, _D, _I, ctypes.c_char_p, _P, _P, _P], _I),
+    "la_batch_plan_cycles": ([_P, _P], _I),
+    "la_batch_plan_select_device": ([_P, _P], _I),
+    "la_batch_plan_phase_cycles": ([_P, _P], _I),
+    "la_batch_features_device": ([_P, _P, _P, _I, _P], _I),
+    "la_generate_conditioned_batch": ([_P, _P, _I, _D, _D, ctypes.c_ulonglong, _P, _P, _P], _I),
+    "la_mlp_param_count": ([], _I),
+    "la_mlp_create": ([_P, ctypes.c_ulonglong, _P], _I),
+    "la_mlp_destroy": ([_P], None),
+    "la_mlp_get_params": ([_P, _P], _I),
+    "la_mlp_set_params": ([_P, _P], _I),
+    "la_mlp_gradients": ([_P, _P, _P, _I, _P, _P], _I),
+    "la_mlp_train_step": ([_P, _P, _P, _I, ctypes.c_float, _P], _I),
+    "la_mlp_predict": ([_P, _P, _I, _P, _P], _I),
 }
 
 BATCH_FP64, BATCH_MIXED = 0, 1
@@ -96,9 +109,10 @@ BATCH_FP64, BATCH_MIXED = 0, 1
 
 class BatchSystem(ctypes.Structure):
     _fields_ = [("a_offset", ctypes.c_size_t), ("b_offset", ctypes.c_size_t),
-                ("n", ctypes.c_int), ("nrhs", ctypes.c_int)]
+                ("n", ctypes.c_int), ("nrhs", ctypes.c_int), ("precision", ctypes.c_int),
+                ("reserved", ctypes.c_int)]
 
-PREC_BF16, PREC_FP16, PREC_FP32 = 1, 2, 3
+PREC_BF16, PREC_FP16, PREC_FP32, PREC_FP8 = 1, 2, 3, 4
 
 
 class RefineStats(ctypes.Structure):
@@ -449,28 +463,36 @@ def lowp_update_device(ctx, fmt, m_, n, k, a_ptr, lda, b_ptr, ldb, c_ptr, ldc, a
     return _check(ctx, st)
 
 
-def batch_systems(ns, nrhss):
-    """Packs per-system sizes into la_batch_system records with dense offsets."""
+def batch_systems(ns, nrhss, precisions=None):
+    """Packs per-system sizes (and factor precisions) into la_batch_system
+    records with dense offsets."""
     arr = (BatchSystem * len(ns))()
     ao = bo = 0
     for i, (n, r) in enumerate(zip(ns, nrhss)):
         arr[i].a_offset, arr[i].b_offset, arr[i].n, arr[i].nrhs = ao, bo, int(n), int(r)
+        arr[i].precision = int(precisions[i]) if precisions is not None else 0
         ao += int(n) * int(n)
         bo += int(n) * int(r)
     return arr, ao, bo
 
 
+def set_precisions(systems, precisions):
+    for i, p in enumerate(precisions):
+        systems[i].precision = int(p)
+
+
 class BatchPlan:
     """A captured batched factor + solve (la_batch_plan)."""
 
-    def __init__(self, ctx, a_ptr, b_ptr, x_ptr, systems, mode, ctas_per_sm=1, tol=1e-14,
-                 max_iters=10):
+    def __init__(self, ctx, a_ptr, b_ptr, x_ptr, systems, mode, ctas_per_sm=1, warps_per_system=8,
+                 tol=1e-14, max_iters=10):
         self.ctx = ctx
         self.count = len(systems)
         self.h = ctypes.c_void_p()
         _check(ctx, lib().la_batch_plan_create(ctx.h, ctypes.c_void_p(a_ptr), ctypes.c_void_p(b_ptr),
                                                ctypes.c_void_p(x_ptr), systems, self.count, mode,
-                                               ctas_per_sm, tol, max_iters, ctypes.byref(self.h)))
+                                               ctas_per_sm, warps_per_system, tol, max_iters,
+                                               ctypes.byref(self.h)))
 
     def run(self):
         _check(self.ctx, lib().la_batch_plan_run(self.h))
@@ -481,6 +503,21 @@ class BatchPlan:
         fb = np.empty(self.count, dtype=np.int32)
         _check(self.ctx, lib().la_batch_plan_stats(self.h, _ptr(its), _ptr(eta), _ptr(fb)))
         return its, eta, fb
+
+    def select_device(self, class_ptr):
+        """Per-system factor storage from selector classes (device int32, 0/1/2)."""
+        _check(self.ctx, lib().la_batch_plan_select_device(self.h, ctypes.c_void_p(class_ptr)))
+
+    def phase_cycles(self):
+        """[load, factor, solves, residuals] cycles of the first pass, then of the FP64 redo."""
+        c = np.empty(8, dtype=np.int64)
+        _check(self.ctx, lib().la_batch_plan_phase_cycles(self.h, _ptr(c)))
+        return c
+
+    def cycles(self):
+        c = np.empty(self.count, dtype=np.int64)
+        _check(self.ctx, lib().la_batch_plan_cycles(self.h, _ptr(c)))
+        return c
 
     def free(self):
         if self.h:
@@ -496,13 +533,87 @@ class BatchPlan:
 
 def batch_autotune(ctx, a_ptr, b_ptr, x_ptr, systems, mode, tol=1e-14, max_iters=10,
                    table_path=None):
+    """Returns (ctas_per_sm, warps_per_system, ms) of the fastest plan shape."""
     best = ctypes.c_int()
+    warps = ctypes.c_int()
     ms = ctypes.c_double()
     _check(ctx, lib().la_batch_autotune(ctx.h, ctypes.c_void_p(a_ptr), ctypes.c_void_p(b_ptr),
                                         ctypes.c_void_p(x_ptr), systems, len(systems), mode, tol,
                                         max_iters, table_path.encode() if table_path else None,
-                                        ctypes.byref(best), ctypes.byref(ms)))
-    return best.value, ms.value
+                                        ctypes.byref(best), ctypes.byref(warps), ctypes.byref(ms)))
+    return best.value, warps.value, ms.value
+
+
+def batch_features_device(ctx, a_ptr, systems, f_ptr):
+    """16 selector features per system into the device buffer f_ptr ([count][16] FP32)."""
+    _check(ctx, lib().la_batch_features_device(ctx.h, ctypes.c_void_p(a_ptr), systems,
+                                               len(systems), ctypes.c_void_p(f_ptr)))
+
+
+def generate_conditioned_batch(ctx, systems, log10_kappa_min, log10_kappa_max, seed, a_ptr, b_ptr,
+                               kappa_ptr=None):
+    """Householder-conditioned systems A = H1 diag(s) H2 written on the device."""
+    _check(ctx, lib().la_generate_conditioned_batch(
+        ctx.h, systems, len(systems), log10_kappa_min, log10_kappa_max, seed,
+        ctypes.c_void_p(a_ptr), ctypes.c_void_p(b_ptr),
+        ctypes.c_void_p(kappa_ptr) if kappa_ptr else None))
+
+
+SELECTOR_CLASSES = (PREC_FP8, PREC_BF16, PREC_FP32)  # MLP class index -> factor precision
+
+
+class Mlp:
+    """The selector network (la_mlp): 16 -> 64 -> 64 -> 3, FP32, trained on the GPU."""
+
+    N_FEATURES = 16
+
+    def __init__(self, ctx, seed=0):
+        self.ctx = ctx
+        self.h = ctypes.c_void_p()
+        _check(ctx, lib().la_mlp_create(ctx.h, ctypes.c_ulonglong(seed), ctypes.byref(self.h)))
+        self.nparam = lib().la_mlp_param_count()
+
+    def get_params(self):
+        p = np.empty(self.nparam + 32, dtype=np.float32)
+        _check(self.ctx, lib().la_mlp_get_params(self.h, _ptr(p)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        if p.size != self.nparam + 32:
+            raise ValueError("expected %d floats" % (self.nparam + 32))
+        _check(self.ctx, lib().la_mlp_set_params(self.h, _ptr(p)))
+
+    def gradients(self, x_ptr, y_ptr, count):
+        g = np.empty(self.nparam, dtype=np.float32)
+        loss = ctypes.c_float()
+        _check(self.ctx, lib().la_mlp_gradients(self.h, ctypes.c_void_p(x_ptr),
+                                                ctypes.c_void_p(y_ptr), count, _ptr(g),
+                                                ctypes.byref(loss)))
+        return g, loss.value
+
+    def train_step(self, x_ptr, y_ptr, count, lr, want_loss=False):
+        loss = ctypes.c_float()
+        _check(self.ctx, lib().la_mlp_train_step(self.h, ctypes.c_void_p(x_ptr),
+                                                 ctypes.c_void_p(y_ptr), count, ctypes.c_float(lr),
+                                                 ctypes.byref(loss) if want_loss else None))
+        return loss.value if want_loss else None
+
+    def predict(self, x_ptr, count, probs_ptr=None, class_ptr=None):
+        _check(self.ctx, lib().la_mlp_predict(self.h, ctypes.c_void_p(x_ptr), count,
+                                              ctypes.c_void_p(probs_ptr) if probs_ptr else None,
+                                              ctypes.c_void_p(class_ptr) if class_ptr else None))
+
+    def free(self):
+        if self.h:
+            lib().la_mlp_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 def matrix_mul_device(ctx, a_ptr, lda, b_ptr, ldb, c_ptr, ldc, m_, k, n):

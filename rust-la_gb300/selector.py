@@ -1,0 +1,158 @@
+"""Learned precision selector for batched mixed-precision solves.
+
+Each system of a batch is factored in FP32 arithmetic with its LU factors
+stored in FP8 (e4m3), BF16 or FP32, then refined in FP64; systems whose
+refinement stalls are redone by the plan's FP64 pass, which is also the judge
+of every answer (backward error <= tol or FP64). Narrow storage lets larger
+systems factor in shared memory, but converges only for well-conditioned
+systems: the best class depends on n and on the conditioning.
+
+``PrecisionSelector`` picks the class per system from 16 cheap features
+(la_batch_features_device) with a 16 -> 64 -> 64 -> 3 MLP trained on the GPU
+(la_mlp_*). Labels come from running the batch once per class and taking, per
+system, the class with the fewest measured SM cycles including the FP64 redo
+(``measure_costs``). Everything runs through the C ABI of liblagpu.so; torch
+only provides device memory.
+"""
+import numpy as np
+import torch
+
+import la_gpu
+
+CLASS_NAMES = ("fp8", "bf16", "fp32")
+CLASS_PREC = la_gpu.SELECTOR_CLASSES
+
+
+def conditioned_batch(ctx, count, seed, n_range=(16, 512), nrhs_range=(1, 4),
+                      log10_kappa=(1.0, 12.0)):
+    """count Householder-conditioned systems on the device: n uniform in
+    n_range, nrhs uniform in nrhs_range, log10 kappa_2 uniform in log10_kappa.
+    Returns (systems, dA, dB, dX, kappa) with dA/dB/dX torch FP64 tensors."""
+    rng = np.random.default_rng(seed)
+    ns = rng.integers(n_range[0], n_range[1] + 1, size=count)
+    rs = rng.integers(nrhs_range[0], nrhs_range[1] + 1, size=count)
+    systems, na, nb = la_gpu.batch_systems(ns, rs)
+    da = torch.empty(na, dtype=torch.float64, device="cuda")
+    db = torch.empty(nb, dtype=torch.float64, device="cuda")
+    dx = torch.zeros(nb, dtype=torch.float64, device="cuda")
+    dk = torch.empty(count, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    la_gpu.generate_conditioned_batch(ctx, systems, log10_kappa[0], log10_kappa[1],
+                                      int(seed) * 7919 + 17, da.data_ptr(), db.data_ptr(),
+                                      dk.data_ptr())
+    return systems, da, db, dx, dk.cpu().numpy()
+
+
+def features(ctx, systems, da):
+    """[count, 16] FP32 features on the device."""
+    f = torch.empty((len(systems), 16), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    la_gpu.batch_features_device(ctx, da.data_ptr(), systems, f.data_ptr())
+    return f
+
+
+def measure_costs(ctx, systems, da, db, dx, ctas_per_sm=1, tol=1e-14, max_iters=10, reps=1):
+    """Runs the mixed plan with every system in each class in turn. Returns
+    (cycles [count, 3] int64, converged [count, 3] bool): SM cycles spent per
+    system (mixed attempt plus FP64 redo) and whether refinement converged."""
+    count = len(systems)
+    cyc = np.zeros((count, 3), dtype=np.int64)
+    conv = np.zeros((count, 3), dtype=bool)
+    plan = la_gpu.BatchPlan(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems,
+                            la_gpu.BATCH_MIXED, ctas_per_sm=ctas_per_sm, tol=tol,
+                            max_iters=max_iters)
+    try:
+        sel = torch.empty(count, dtype=torch.int32, device="cuda")
+        for c in range(3):
+            sel.fill_(c)
+            torch.cuda.synchronize()
+            plan.select_device(sel.data_ptr())
+            best = None
+            for _ in range(reps):
+                plan.run()
+                cur = plan.cycles()
+                best = cur if best is None else np.minimum(best, cur)
+            cyc[:, c] = best
+            _, _, fb = plan.stats()
+            conv[:, c] = fb == 0
+    finally:
+        plan.free()
+    return cyc, conv
+
+
+def labels_from_costs(cycles):
+    """Cheapest class per system."""
+    return np.argmin(cycles, axis=1).astype(np.int32)
+
+
+class PrecisionSelector:
+    """MLP precision selector (la_mlp) with feature normalisation."""
+
+    def __init__(self, ctx, seed=0):
+        self.ctx = ctx
+        self.mlp = la_gpu.Mlp(ctx, seed)
+
+    def fit(self, feats, labels, steps=1500, lr=3e-3, batch=4096, seed=0, log_every=0):
+        """Adam on minibatches of (feats [m,16] FP32 device, labels [m] int32).
+        Sets the input normalisation from feats. Returns the loss log."""
+        feats = feats.contiguous()
+        labels = torch.as_tensor(labels, dtype=torch.int32, device="cuda").contiguous()
+        m = feats.shape[0]
+        p = self.mlp.get_params()
+        npar = self.mlp.nparam
+        mean = feats.double().mean(0)
+        std = feats.double().std(0).clamp_min(1e-3)
+        p[npar:npar + 16] = mean.cpu().numpy()
+        p[npar + 16:npar + 32] = std.cpu().numpy()
+        self.mlp.set_params(p)
+        rng = np.random.default_rng(seed)
+        batch = min(batch, m)
+        log = []
+        perm = torch.from_numpy(rng.permutation(m)).cuda()
+        pos = 0
+        for step in range(steps):
+            if pos + batch > m:
+                perm = torch.from_numpy(rng.permutation(m)).cuda()
+                pos = 0
+            idx = perm[pos:pos + batch]
+            pos += batch
+            xb = feats.index_select(0, idx).contiguous()
+            yb = labels.index_select(0, idx).contiguous()
+            torch.cuda.synchronize()
+            want = bool(log_every) and (step % log_every == 0 or step == steps - 1)
+            loss = self.mlp.train_step(xb.data_ptr(), yb.data_ptr(), batch, lr, want_loss=want)
+            if want:
+                log.append((step, loss))
+        self.ctx.synchronize()
+        return log
+
+    def predict(self, feats, out=None, sync=True):
+        """Class per system (device int32 tensor). With sync=False the result
+        is ordered on the context's stream only (e.g. for a plan's
+        select_device)."""
+        cls = out if out is not None else torch.empty(feats.shape[0], dtype=torch.int32,
+                                                      device="cuda")
+        self.mlp.predict(feats.data_ptr(), feats.shape[0], None, cls.data_ptr())
+        if sync:
+            self.ctx.synchronize()
+        return cls
+
+    def loss(self, feats, labels):
+        labels = torch.as_tensor(labels, dtype=torch.int32, device="cuda").contiguous()
+        torch.cuda.synchronize()
+        return self.mlp.gradients(feats.data_ptr(), labels.data_ptr(), feats.shape[0])[1]
+
+    def params(self):
+        return self.mlp.get_params()
+
+    def load(self, params):
+        self.mlp.set_params(np.asarray(params, dtype=np.float32))
+
+    def save(self, path):
+        np.save(path, self.params())
+
+    @classmethod
+    def from_file(cls, ctx, path):
+        s = cls(ctx)
+        s.load(np.load(path))
+        return s

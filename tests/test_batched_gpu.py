@@ -30,14 +30,14 @@ def make_batch(count, seed, nmax=256, shift_even=True):
     return ns, rs, mats, rhss
 
 
-def run_batch(lagpu, torch, ctx, ns, rs, mats, rhss, mode, ctas=1):
-    systems, na, nb = lagpu.batch_systems(ns, rs)
+def run_batch(lagpu, torch, ctx, ns, rs, mats, rhss, mode, ctas=1, precisions=None, warps=8):
+    systems, na, nb = lagpu.batch_systems(ns, rs, precisions)
     a = torch.from_numpy(np.concatenate([m.ravel() for m in mats])).cuda()
     b = torch.from_numpy(np.concatenate([r.ravel() for r in rhss])).cuda()
     x = torch.zeros(nb, dtype=torch.float64, device="cuda")
     torch.cuda.synchronize()
     plan = lagpu.BatchPlan(ctx, a.data_ptr(), b.data_ptr(), x.data_ptr(), systems, mode,
-                           ctas_per_sm=ctas, tol=5e-15, max_iters=10)
+                           ctas_per_sm=ctas, warps_per_system=warps, tol=5e-15, max_iters=10)
     x.zero_()
     plan.run()
     its, eta, fb = plan.stats()
@@ -49,15 +49,88 @@ def run_batch(lagpu, torch, ctx, ns, rs, mats, rhss, mode, ctas=1):
     return out, its, eta, fb
 
 
-@pytest.mark.parametrize("mode", [0, 1], ids=["fp64", "mixed"])
-@pytest.mark.parametrize("ctas", [1, 2])
-def test_batched_backward_error(lagpu, ctx_fast, torch, mode, ctas):
-    ns, rs, mats, rhss = make_batch(160, 11 + ctas)
-    xs, its, eta, fb = run_batch(lagpu, torch, ctx_fast, ns, rs, mats, rhss, mode, ctas)
+@pytest.mark.parametrize("mode,ctas,warps,nmax", [
+    (0, 1, 8, 256), (0, 2, 4, 256), (0, 4, 2, 128), (1, 1, 8, 256), (1, 2, 8, 256),
+    (1, 4, 4, 256), (1, 8, 2, 128)],
+    ids=["fp64-1x8", "fp64-2x4", "fp64-4x2", "mixed-1x8", "mixed-2x8", "mixed-4x4", "mixed-8x2"])
+def test_batched_backward_error(lagpu, ctx_fast, torch, mode, ctas, warps, nmax):
+    # every supported (CTAs per SM, warps per system) shape gives eta <= 1e-14
+    ns, rs, mats, rhss = make_batch(160, 11 + ctas + warps, nmax=nmax)
+    xs, its, eta, fb = run_batch(lagpu, torch, ctx_fast, ns, rs, mats, rhss, mode, ctas,
+                                 warps=warps)
     worst = max(oracle.backward_error(m, x, r) for m, x, r in zip(mats, xs, rhss))
     assert worst <= ETA_MAX
     if mode == 1:
         assert (its >= 0).all()
+
+
+def test_batched_plan_rejects_shapes_that_do_not_fit(lagpu, ctx_fast, torch):
+    # n = 512 in FP64 needs a whole SM's shared memory per CTA
+    rng = np.random.default_rng(2)
+    ns, rs = [512, 8], [1, 1]
+    mats = [rng.standard_normal((n, n)) + n * np.eye(n) for n in ns]
+    rhss = [rng.standard_normal((n, r)) for n, r in zip(ns, rs)]
+    with pytest.raises(lagpu.LaError) as e:
+        run_batch(lagpu, torch, ctx_fast, ns, rs, mats, rhss, 0, ctas=2, warps=4)
+    assert e.value.status == lagpu.UNSUPPORTED
+    xs, _, _, _ = run_batch(lagpu, torch, ctx_fast, ns, rs, mats, rhss, 0, ctas=1)
+    for m, x, r in zip(mats, xs, rhss):
+        assert oracle.backward_error(m, x, r) <= ETA_MAX
+
+
+@pytest.mark.parametrize("prec", ["fp8", "bf16", "fp32", "mixed"])
+def test_batched_storage_classes_up_to_512(lagpu, ctx_fast, torch, prec):
+    # n up to 512 (global-scratch systems included); every storage class ends at
+    # eta <= 1e-14, by refinement or by the FP64 pass.
+    rng = np.random.default_rng(21)
+    ns = np.concatenate([rng.integers(1, 513, size=40), [512, 511, 300, 1]])
+    rs = rng.integers(1, 5, size=len(ns))
+    mats, rhss = [], []
+    for i, (n, r) in enumerate(zip(ns, rs)):
+        a = rng.standard_normal((n, n))
+        if i % 3 != 2:
+            a += (1.0 + n) * np.eye(n)   # well conditioned: refinement converges
+        mats.append(a)
+        rhss.append(rng.standard_normal((n, r)))
+    code = {"fp8": lagpu.PREC_FP8, "bf16": lagpu.PREC_BF16, "fp32": lagpu.PREC_FP32}
+    if prec == "mixed":
+        precs = [(lagpu.PREC_FP8, lagpu.PREC_BF16, lagpu.PREC_FP32)[i % 3] for i in range(len(ns))]
+    else:
+        precs = [code[prec]] * len(ns)
+    xs, its, eta, fb = run_batch(lagpu, torch, ctx_fast, ns, rs, mats, rhss, 1, 1, precs)
+    for i, (m, x, r) in enumerate(zip(mats, xs, rhss)):
+        assert oracle.backward_error(m, x, r) <= ETA_MAX, (i, ns[i], precs[i], fb[i])
+    shifted = [i for i in range(len(ns)) if i % 3 != 2]
+    if prec == "fp32":
+        assert (fb[shifted] == 0).all()   # FP32 factors of shifted systems refine to tol
+    if prec == "bf16":
+        assert (fb[shifted] == 0).mean() >= 0.8
+
+
+def test_batched_select_device_and_cycles(lagpu, ctx_fast, torch):
+    ns, rs, mats, rhss = make_batch(50, 8, nmax=512)
+    systems, na, nb = lagpu.batch_systems(ns, rs)
+    a = torch.from_numpy(np.concatenate([m.ravel() for m in mats])).cuda()
+    b = torch.from_numpy(np.concatenate([r.ravel() for r in rhss])).cuda()
+    x = torch.zeros(nb, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    plan = lagpu.BatchPlan(ctx_fast, a.data_ptr(), b.data_ptr(), x.data_ptr(), systems, 1,
+                           tol=5e-15)
+    for c in range(3):
+        sel = torch.full((len(ns),), c, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        plan.select_device(sel.data_ptr())
+        x.zero_()
+        torch.cuda.synchronize()
+        plan.run()
+        cyc = plan.cycles()
+        its, eta, fb = plan.stats()
+        assert (cyc > 0).all()
+        xs = x.cpu().numpy()
+        for s, m, r in zip(systems, mats, rhss):
+            xi = xs[s.b_offset:s.b_offset + s.n * s.nrhs].reshape(s.n, s.nrhs)
+            assert oracle.backward_error(m, xi, r) <= ETA_MAX
+    plan.free()
 
 
 def test_batched_fp64_pivots_match_reference_solution(lagpu, ctx_fast, torch):
@@ -94,9 +167,9 @@ def test_batch_autotune_writes_table(lagpu, ctx_fast, torch, tmp_path):
     b = torch.from_numpy(np.concatenate([r.ravel() for r in rhss])).cuda()
     x = torch.zeros(nb, dtype=torch.float64, device="cuda")
     path = str(tmp_path / "tune.txt")
-    best, ms = lagpu.batch_autotune(ctx_fast, a.data_ptr(), b.data_ptr(), x.data_ptr(), systems, 1,
-                                    table_path=path)
-    assert 1 <= best <= 4 and ms > 0
+    best, warps, ms = lagpu.batch_autotune(ctx_fast, a.data_ptr(), b.data_ptr(), x.data_ptr(),
+                                           systems, 1, table_path=path)
+    assert best in (1, 2, 4, 8) and warps in (2, 4, 8) and ms > 0
     lines = open(path).read().strip().splitlines()
-    assert 1 <= len(lines) <= 4 and all(l.startswith("mixed") for l in lines)
-    assert str(best) in [l.split()[3] for l in lines]
+    assert 1 <= len(lines) <= 12 and all(l.startswith("mixed") for l in lines)
+    assert (str(best), str(warps)) in [(l.split()[3], l.split()[4]) for l in lines]

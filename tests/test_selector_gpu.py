@@ -1,0 +1,198 @@
+"""Learned precision selector on the GPU: the generator's singular values, the
+feature kernel and the hand-written MLP kernels (forward, gradients, Adam)
+against the CPU oracle, and the gain of selector-chosen factor precisions over
+always-FP32 factors on a seeded Householder-conditioned batch."""
+import time
+
+import numpy as np
+import pytest
+
+import oracle
+from oracle import selector_ref as sr
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    return pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def sel_mod(lagpu, torch):
+    import selector
+    return selector
+
+
+def _system(lagpu, systems, da, i):
+    s = systems[i]
+    return da[s.a_offset:s.a_offset + s.n * s.n].reshape(s.n, s.n)
+
+
+def test_generator_singular_values(lagpu, ctx_fast, torch, sel_mod):
+    systems, da, db, dx, kappa = sel_mod.conditioned_batch(ctx_fast, 12, seed=3, n_range=(2, 96),
+                                                           log10_kappa=(1.0, 6.0))
+    a = da.cpu().numpy()
+    for i, s in enumerate(systems):
+        sv = np.linalg.svd(_system(lagpu, systems, a, i), compute_uv=False)
+        want = kappa[i] ** (-np.arange(s.n) / (s.n - 1))
+        assert 10.0 <= kappa[i] <= 1e6
+        assert np.allclose(sv, want, rtol=1e-9, atol=1e-12), i
+
+
+def test_generator_is_reproducible(lagpu, ctx_fast, torch, sel_mod):
+    r1 = sel_mod.conditioned_batch(ctx_fast, 5, seed=8, n_range=(16, 64))
+    r2 = sel_mod.conditioned_batch(ctx_fast, 5, seed=8, n_range=(16, 64))
+    assert torch.equal(r1[1], r2[1]) and torch.equal(r1[2], r2[2])
+
+
+def test_features_match_oracle(lagpu, ctx_fast, torch, sel_mod):
+    systems, da, db, dx, kappa = sel_mod.conditioned_batch(ctx_fast, 24, seed=4, n_range=(1, 512))
+    f = sel_mod.features(ctx_fast, systems, da).cpu().numpy()
+    a = da.cpu().numpy()
+    for i, s in enumerate(systems):
+        want = sr.features(_system(lagpu, systems, a, i), s.nrhs)
+        assert np.allclose(f[i], want, rtol=1e-4, atol=2e-4), (i, s.n, f[i] - want)
+
+
+def _random_mlp_data(torch, m, seed):
+    rng = np.random.default_rng(seed)
+    X = rng.standard_normal((m, 16)).astype(np.float32) * 2 + 1
+    y = rng.integers(0, 3, size=m).astype(np.int32)
+    return X, y, torch.from_numpy(X).cuda(), torch.from_numpy(y).cuda()
+
+
+def _set_random_params(lagpu, mlp, seed):
+    rng = np.random.default_rng(seed)
+    p = (rng.standard_normal(mlp.nparam + 32) * 0.2).astype(np.float32)
+    p[mlp.nparam:mlp.nparam + 16] = 1.0
+    p[mlp.nparam + 16:] = 2.0
+    mlp.set_params(p)
+    return p
+
+
+def test_mlp_gradients_match_oracle(lagpu, ctx_fast, torch):
+    mlp = lagpu.Mlp(ctx_fast, seed=1)
+    p = _set_random_params(lagpu, mlp, 2)
+    X, y, dX, dy = _random_mlp_data(torch, 777, 3)
+    torch.cuda.synchronize()
+    g, loss = mlp.gradients(dX.data_ptr(), dy.data_ptr(), len(y))
+    want_loss, want = sr.mlp_loss_grad(p.astype(np.float64), X, y)
+    assert abs(loss - want_loss) <= 1e-5 * max(1.0, abs(want_loss))
+    assert np.allclose(g, want, rtol=2e-4, atol=2e-6)
+    # and both agree with central differences of the oracle's loss
+    idx = np.arange(0, sr.NPARAM, 97)
+    assert np.allclose(g[idx], sr.numeric_grad(p.astype(np.float64), X, y, idx), rtol=2e-3,
+                       atol=1e-5)
+    mlp.free()
+
+
+def test_mlp_predict_matches_oracle(lagpu, ctx_fast, torch):
+    mlp = lagpu.Mlp(ctx_fast, seed=5)
+    p = _set_random_params(lagpu, mlp, 6)
+    X, y, dX, dy = _random_mlp_data(torch, 1000, 7)
+    probs = torch.empty((1000, 3), dtype=torch.float32, device="cuda")
+    cls = torch.empty(1000, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    mlp.predict(dX.data_ptr(), 1000, probs.data_ptr(), cls.data_ptr())
+    ctx_fast.synchronize()
+    want = sr.mlp_forward(p.astype(np.float64), X)
+    assert np.allclose(probs.cpu().numpy(), want, atol=1e-5)
+    c = cls.cpu().numpy()
+    sure = np.sort(want, 1)[:, -1] - np.sort(want, 1)[:, -2] > 1e-4
+    assert (c[sure] == want.argmax(1)[sure]).all()
+    mlp.free()
+
+
+def test_adam_step_matches_oracle(lagpu, ctx_fast, torch):
+    mlp = lagpu.Mlp(ctx_fast, seed=9)
+    p = _set_random_params(lagpu, mlp, 10).astype(np.float64)
+    X, y, dX, dy = _random_mlp_data(torch, 300, 11)
+    torch.cuda.synchronize()
+    lr = 1e-2
+    m = np.zeros(sr.NPARAM)
+    v = np.zeros(sr.NPARAM)
+    w = p[:sr.NPARAM].copy()
+    for t in range(1, 4):
+        _, g = sr.mlp_loss_grad(np.concatenate([w, p[sr.NPARAM:]]), X, y)
+        m = 0.9 * m + 0.1 * g
+        v = 0.999 * v + 0.001 * g * g
+        w = w - lr * (m / (1 - 0.9 ** t)) / (np.sqrt(v / (1 - 0.999 ** t)) + 1e-8)
+        mlp.train_step(dX.data_ptr(), dy.data_ptr(), 300, lr)
+    got = mlp.get_params()[:sr.NPARAM]
+    assert np.abs(got - w).max() <= 2e-4
+    mlp.free()
+
+
+def test_training_learns_a_separable_rule(lagpu, ctx_fast, torch, sel_mod):
+    rng = np.random.default_rng(12)
+    X = rng.standard_normal((6000, 16)).astype(np.float32)
+    y = np.where(X[:, 15] < -0.4, 0, np.where(X[:, 15] < 0.6, 1, 2)).astype(np.int32)
+    dX = torch.from_numpy(X).cuda()
+    s = sel_mod.PrecisionSelector(ctx_fast, seed=13)
+    log = s.fit(dX, y, steps=400, lr=3e-3, batch=1024, log_every=100)
+    assert log[-1][1] < 0.5 * log[0][1]
+    acc = (s.predict(dX).cpu().numpy() == y).mean()
+    assert acc >= 0.95
+
+
+def test_selector_gain_over_fp32_factors(lagpu, ctx_fast, torch, sel_mod):
+    """Train on measured labels, then solve a fresh batch: every system ends at
+    eta <= 1e-14 (refinement or the FP64 pass) and the selector's choice,
+    features and inference included, is faster than FP32 factors for all."""
+    tol = 1e-14
+    n_range = (16, 512)
+    tr = sel_mod.conditioned_batch(ctx_fast, 3000, seed=101, n_range=n_range)
+    cyc, conv = sel_mod.measure_costs(ctx_fast, *tr[:4], tol=tol)
+    labels = sel_mod.labels_from_costs(cyc)
+    feats = sel_mod.features(ctx_fast, tr[0], tr[1])
+    s = sel_mod.PrecisionSelector(ctx_fast, seed=1)
+    s.fit(feats, labels, steps=800, lr=3e-3, batch=1024)
+    del tr, feats
+
+    systems, da, db, dx, kappa = sel_mod.conditioned_batch(ctx_fast, 3000, seed=202,
+                                                           n_range=n_range)
+    plan = lagpu.BatchPlan(ctx_fast, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems, 1,
+                           tol=tol)
+    count = len(systems)
+    f = torch.empty((count, 16), dtype=torch.float32, device="cuda")
+    cls = torch.empty(count, dtype=torch.int32, device="cuda")
+    fp32 = torch.full((count,), 2, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+
+    def run_fixed():
+        plan.select_device(fp32.data_ptr())
+        plan.run()
+
+    def run_selected():
+        lagpu.batch_features_device(ctx_fast, da.data_ptr(), systems, f.data_ptr())
+        s.predict(f, out=cls, sync=False)
+        plan.select_device(cls.data_ptr())
+        plan.run()
+
+    def timed(fn, reps=3):
+        best = np.inf
+        for _ in range(reps):
+            ctx_fast.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            ctx_fast.synchronize()
+            best = min(best, time.perf_counter() - t0)
+        return best
+
+    t_fixed = timed(run_fixed)
+    t_sel = timed(run_selected)
+    its, eta, fb = plan.stats()
+    x = dx.cpu().numpy()
+    a = da.cpu().numpy()
+    b = db.cpu().numpy()
+    rng = np.random.default_rng(0)
+    for i in rng.choice(count, 60, replace=False):
+        si = systems[int(i)]
+        xi = x[si.b_offset:si.b_offset + si.n * si.nrhs].reshape(si.n, si.nrhs)
+        bi = b[si.b_offset:si.b_offset + si.n * si.nrhs].reshape(si.n, si.nrhs)
+        assert oracle.backward_error(_system(lagpu, systems, a, int(i)), xi, bi) <= tol
+    plan.free()
+    print("selector %.2f ms vs fp32 %.2f ms (gain %.2fx)" % (t_sel * 1e3, t_fixed * 1e3,
+                                                            t_fixed / t_sel))
+    assert t_sel < t_fixed
