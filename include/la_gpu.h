@@ -79,7 +79,15 @@ typedef enum la_option {
   LA_OPT_LOOKAHEAD = 5,
   /* 1 (default): the FP32 panels of the mixed LU run on one thread-block
    * cluster (distributed shared memory); 0: the cooperative multi-CTA kernel. */
-  LA_OPT_CLUSTER_PANEL = 6
+  LA_OPT_CLUSTER_PANEL = 6,
+  /* Batch plans (read when a plan is built): largest Krylov basis (0-20) of
+   * the GMRES-IR stage that a LA_BATCH_MIXED plan runs on a system whose
+   * LU-IR reached a backward error below 1e-6 and then stalled, before the
+   * FP64 pass; 0 (default) turns the stage off. It pays off for factors whose
+   * LU-IR contracts but slowly (BF16 / FP8 storage of well-conditioned
+   * systems); with FP32 factors the stalled systems have kappa u_32 near 1 and
+   * need more Krylov steps than the FP64 redo costs. */
+  LA_OPT_BATCH_GMRES = 7
 } la_option;
 
 #define LA_ARITH_FAST 0
@@ -259,10 +267,11 @@ la_status la_batch_plan_cycles(la_batch_plan plan, long long* cycles);
 
 /* 16 features per system (row-major FP32 [count][16]) for the precision
  * selector: log2 n / 9, nrhs / 4, log10 of the max row and column sums, of the
- * Frobenius norm, of max |a_ij|, of the 8-step Lanczos estimate of sigma_max,
+ * Frobenius norm, of max |a_ij|, of the 6-step Lanczos estimate of sigma_max,
  * of ||A||_F / sigma_max, of the smallest diagonal-dominance ratio, the mean
  * log10 dominance ratio, the fraction of dominant rows, log10 of the row-sum
- * and column-sum spreads, the relative asymmetry ||A - A^T||_F / ||A||_F,
+ * and column-sum spreads, the asymmetry probe ||A q - A^T q|| / ||A q|| (q the
+ * fixed Lanczos start vector),
  * log10 min|a_ii| / max|a_ij|, and log10 of the Lanczos estimate of
  * sigma_max / sigma_min (a lower bound on kappa_2). Systems as in a batch
  * plan (1 <= n <= 512); synchronizes. */

@@ -8,9 +8,10 @@ rust-la_gb300/csrc/selector.cu compute, so that tests can check them:
 * ``mlp_forward`` / ``mlp_loss_grad``: the 16 -> 64 -> 64 -> 3 ReLU/softmax
   network and the analytic gradient of its mean cross-entropy (float64), with
   ``numeric_grad`` (central differences) to pin the analytic gradient itself;
-* ``features``: the 16 per-system features, with the same 8-step Lanczos on
-  A^T A (fixed start vector, full reorthogonalisation) and the same bisection
-  for the extreme Ritz values.
+* ``features``: the 16 per-system features, with the same 6-step Lanczos on
+  A^T A (fixed start vector, full reorthogonalisation), the same bisection for
+  the extreme Ritz values and the same asymmetry probe ||A q0 - A^T q0|| /
+  ||A q0||.
 
 Nothing here is on the product path.
 """
@@ -20,7 +21,7 @@ NF, H1, H2, NC = 16, 64, 64, 3
 SHAPES = [("W1", (H1, NF)), ("b1", (H1,)), ("W2", (H2, H1)), ("b2", (H2,)), ("W3", (NC, H2)),
           ("b3", (NC,))]
 NPARAM = sum(int(np.prod(s)) for _, s in SHAPES)  # 5443
-LK = 8
+LK = 6
 
 
 def unpack(p):
@@ -90,7 +91,7 @@ def _tridiag_min_eig(al, be):
     for i in range(k):
         r = (abs(be[i - 1]) if i > 0 else 0.0) + (abs(be[i]) if i + 1 < k else 0.0)
         lo, hi = min(lo, al[i] - r), max(hi, al[i] + r)
-    for _ in range(100):
+    for _ in range(80):
         mid = 0.5 * (lo + hi)
         cnt = 0
         q = al[0] - mid
@@ -121,9 +122,10 @@ def features(A, nrhs):
     ratio = di / np.maximum(off, 1e-300)
     fro = np.sqrt((aa * aa).sum())
     amax = aa.max()
-    asym = np.sqrt(((A - A.T) ** 2).sum())
     q = [1.0 + 0.5 * np.sin(1.0 + np.arange(n))]
     q[0] = q[0] / np.linalg.norm(q[0])
+    aq0 = A @ q[0]
+    asym = np.linalg.norm(aq0 - A.T @ q[0]) / max(np.linalg.norm(aq0), 1e-300)
     al, be = [], []
     for j in range(min(LK, n)):
         t2 = A.T @ (A @ q[j])
@@ -143,6 +145,6 @@ def features(A, nrhs):
         _lg(np.sqrt(max(emax, 0.0))), _lg(fro / np.sqrt(max(emax, 1e-300))), _lg(ratio.min()),
         np.mean(np.log10(np.maximum(ratio, 1e-300))), np.mean(ratio > 1.0),
         _lg(rs.max() / max(rs.min(), 1e-300)), _lg(cs.max() / max(cs.min(), 1e-300)),
-        asym / max(fro, 1e-300), _lg(di.min() / max(amax, 1e-300)),
+        asym, _lg(di.min() / max(amax, 1e-300)),
         _lg(np.sqrt(max(emax, 1e-300) / emin)),
     ])

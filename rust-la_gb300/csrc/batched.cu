@@ -37,6 +37,15 @@ constexpr int NW_MAX = BT_MAX / 32;
 constexpr int NMAX = 512;  // largest system
 constexpr int PBW = 16;    // panel width of the per-system LU
 constexpr int SP = 17;     // pitch of the staged panel (odd: rows fall in distinct banks)
+constexpr int GM_M = 20;     // largest Krylov basis of one GMRES correction
+constexpr int GM_OUTER = 2;  // GMRES-IR steps after LU-IR stalls
+constexpr double GM_TOL = 1e-12;  // relative preconditioned residual of a GMRES correction
+constexpr double GM_TRIGGER = 1e-6;  // LU-IR must have reached this backward error
+// Hessenberg matrix [GM_M + 1][GM_M], right-hand side g, rotations cs, sn
+constexpr size_t GM_SMALL = (size_t)((GM_M + 1) * GM_M + 3 * (GM_M + 1)) * sizeof(double);
+// The Krylov basis lives in the CTA's global scratch slice, after the space of
+// an FP32 working matrix of NMAX x NMAX.
+constexpr size_t GM_V_OFFSET = (size_t)NMAX * NMAX * sizeof(float);
 
 struct SysDesc {
   long long a;  // offset of A_i (n x n, row-major) in the A buffer, elements
@@ -101,6 +110,8 @@ struct Shared {
   // [0] ||A||_inf, [1 + c] max |r_c|, [5 + c] max |x_c|, [9 + c] max |b_c|,
   // [13] max |a_ij| (FP8 scaling)
   double norm[14];
+  double red[NW_MAX];  // block reductions
+  double gres;         // GMRES residual estimate (broadcast)
 };
 
 __host__ __device__ constexpr size_t al16(size_t x) { return (x + 15) / 16 * 16; }
@@ -108,7 +119,7 @@ __host__ __device__ constexpr size_t al16(size_t x) { return (x + 15) / 16 * 16;
 // Shared-memory layout of one system (byte offsets into the dynamic shared
 // memory): [M if resident][staged panel][U12][row map][x FP64][d FP32].
 struct Lay {
-  size_t stage, us, rmap, x, d, total;
+  size_t stage, us, rmap, x, d, gm, total;
 };
 template <typename S, typename R>
 __host__ __device__ Lay lay(int n, int nrhs, bool resident, bool mixed) {
@@ -124,6 +135,8 @@ __host__ __device__ Lay lay(int n, int nrhs, bool resident, bool mixed) {
   o += al16((size_t)n * nrhs * sizeof(double));
   L.d = o;
   o += mixed ? al16((size_t)n * nrhs * sizeof(float)) : 0;
+  L.gm = o;  // GMRES: work vector w (n FP64), then the small arrays
+  o += mixed ? al16((size_t)n * sizeof(double) + GM_SMALL) : 0;
   L.total = o;
   return L;
 }
@@ -394,6 +407,7 @@ struct BatchArgs {
   int max_iters;
   double tol;
   int only_flagged;  // FP64 pass: process only systems with status < 0
+  int gmres_m;       // largest Krylov basis of the GMRES-IR stage (0: no GMRES-IR)
   long long* cycles; // per system: SM cycles spent on it, summed over the passes
   unsigned long long* phase;  // [8]: load, factor, solves, residuals of the first pass,
                               // then the same for the FP64 redo pass (summed over CTAs)
@@ -456,11 +470,12 @@ __device__ __forceinline__ void halve(double* v, int lane, int s) {
   }
 }
 
-// R = B - A x (FP64) for rows [0, n) with NR right-hand sides: each warp takes
+// R = B - A x (or R = A x when MV) in FP64 for rows [0, n) with NR right-hand
+// sides: each warp takes
 // four rows at a time, lanes stride the columns (coalesced rows of A, x from
 // shared memory), and the 4 x 4 partial sums are reduced across the warp by
 // recursive halving (16 adds per lane instead of 5 per value).
-template <int NR>
+template <int NR, bool MV = false>
 __device__ void residual_rows(const double* __restrict__ Ai, int n, const double* xv,
                               const double* __restrict__ Bi, double* Ri) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, NW = blockDim.x >> 5;
@@ -492,7 +507,152 @@ __device__ void residual_rows(const double* __restrict__ Ai, int n, const double
                   ((lane >> 1) & 1);
     const int i = q >> 2, c = q & 3;
     if ((lane & 1) == 0 && c < NR && r0 + i < n)
-      Ri[(size_t)(r0 + i) * NR + c] = Bi[(size_t)(r0 + i) * NR + c] - v[0];
+      Ri[(size_t)(r0 + i) * NR + c] = MV ? v[0] : Bi[(size_t)(r0 + i) * NR + c] - v[0];
+  }
+}
+
+__device__ __forceinline__ double block_sum_d(double s, double* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, NW = blockDim.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) red[warp] = s;
+  __syncthreads();
+  double t = 0.0;
+  for (int w = 0; w < NW; w++) t += red[w];
+  __syncthreads();
+  return t;
+}
+
+__device__ __forceinline__ double block_max_d(double s, double* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, NW = blockDim.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) s = fmax(s, __shfl_xor_sync(0xffffffffu, s, o));
+  if (lane == 0) red[warp] = s;
+  __syncthreads();
+  double t = 0.0;
+  for (int w = 0; w < NW; w++) t = fmax(t, red[w]);
+  __syncthreads();
+  return t;
+}
+
+// Normwise backward error max_c ||r_c||_inf / (||A||_inf ||x_c||_inf + ||b_c||_inf)
+// of the current (x, r); leaves max |r_c| in sh.norm[1 + c].
+__device__ double refine_eta(const double* rv, const double* xv, int n, int nrhs, Shared& sh) {
+  if (threadIdx.x < 8) sh.norm[1 + threadIdx.x] = 0.0;
+  __syncthreads();
+  col_absmax(rv, n, nrhs, &sh.norm[1]);
+  col_absmax(xv, n, nrhs, &sh.norm[1 + 4]);
+  __syncthreads();
+  double eta = 0.0;
+  for (int c = 0; c < nrhs; c++) {
+    const double den = sh.norm[0] * sh.norm[1 + 4 + c] + sh.norm[1 + 8 + c];
+    const double v = den > 0 ? sh.norm[1 + c] / den : (sh.norm[1 + c] > 0 ? INFINITY : 0.0);
+    if (!(v <= eta)) eta = v;
+  }
+  return eta;
+}
+
+// w <- A^-1 w through the stored factors of scale * A: an FP32 solve of
+// P w / max|w| (the preconditioner of GMRES-IR).
+template <typename P>
+__device__ void precondition(const typename P::S* M, int n, const int* rmap, double* w, float* dv,
+                             float scale, Shared& sh) {
+  const int BT = blockDim.x;
+  double m = 0.0;
+  for (int i = threadIdx.x; i < n; i += BT) m = fmax(m, fabs(w[i]));
+  m = block_max_d(m, sh.red);
+  const double inv = m > 0 ? 1.0 / m : 0.0;
+  for (int i = threadIdx.x; i < n; i += BT) dv[i] = (float)(w[rmap[i]] * inv);
+  __syncthreads();
+  block_solve<P, float>(M, n, n, rmap, dv, 1);
+  for (int i = threadIdx.x; i < n; i += BT) w[i] = (double)dv[i] * m * (double)scale;
+  __syncthreads();
+}
+
+// One GMRES-IR correction of column c: solves (LU)^-1 A d = (LU)^-1 r_c by
+// GMRES (FP64 Arnoldi with modified Gram-Schmidt and Givens rotations,
+// basis V in global scratch, at most mcap steps, stopping when the estimated
+// preconditioned residual falls below GM_TOL times its start), then x_c += d.
+// Returns the steps taken.
+template <typename P>
+__device__ int gmres_column(const double* __restrict__ Ai, int n, int nrhs, int c,
+                            const typename P::S* M, const int* rmap, const double* rv, double* xv,
+                            float* dv, float scale, double* w, double* H, double* V, int mcap,
+                            Shared& sh) {
+  const int tid = threadIdx.x, BT = blockDim.x;
+  double* g = H + (GM_M + 1) * GM_M;
+  double* cs = g + GM_M + 1;
+  double* sn = cs + GM_M + 1;
+  for (int i = tid; i < n; i += BT) w[i] = rv[(size_t)i * nrhs + c];
+  __syncthreads();
+  precondition<P>(M, n, rmap, w, dv, scale, sh);
+  double s = 0.0;
+  for (int i = tid; i < n; i += BT) s += w[i] * w[i];
+  const double beta = sqrt(block_sum_d(s, sh.red));
+  if (!(beta > 0.0) || !(beta < INFINITY)) return 0;
+  for (int i = tid; i < n; i += BT) V[i] = w[i] / beta;
+  if (tid == 0) g[0] = beta;
+  __syncthreads();
+  int k = 0;
+  for (int j = 0; j < mcap; j++) {
+    residual_rows<1, true>(Ai, n, V + (size_t)j * n, nullptr, w);  // w = A v_j
+    __syncthreads();
+    precondition<P>(M, n, rmap, w, dv, scale, sh);
+    for (int i = 0; i <= j; i++) {
+      const double* vi = V + (size_t)i * n;
+      double hs = 0.0;
+      for (int t = tid; t < n; t += BT) hs += vi[t] * w[t];
+      const double h = block_sum_d(hs, sh.red);
+      for (int t = tid; t < n; t += BT) w[t] -= h * vi[t];
+      if (tid == 0) H[i * GM_M + j] = h;
+    }
+    double hs = 0.0;
+    for (int t = tid; t < n; t += BT) hs += w[t] * w[t];
+    const double hn = sqrt(block_sum_d(hs, sh.red));
+    double* vn = V + (size_t)(j + 1) * n;
+    for (int t = tid; t < n; t += BT) vn[t] = hn > 0 ? w[t] / hn : 0.0;
+    if (tid == 0) {
+      for (int i = 0; i < j; i++) {
+        const double h0 = H[i * GM_M + j], h1 = H[(i + 1) * GM_M + j];
+        H[i * GM_M + j] = cs[i] * h0 + sn[i] * h1;
+        H[(i + 1) * GM_M + j] = -sn[i] * h0 + cs[i] * h1;
+      }
+      const double h0 = H[j * GM_M + j];
+      const double r = hypot(h0, hn);
+      const double cj = r > 0 ? h0 / r : 1.0, sj = r > 0 ? hn / r : 0.0;
+      cs[j] = cj;
+      sn[j] = sj;
+      H[j * GM_M + j] = r;
+      g[j + 1] = -sj * g[j];
+      g[j] = cj * g[j];
+      sh.gres = fabs(g[j + 1]);
+    }
+    __syncthreads();
+    k = j + 1;
+    if (!(sh.gres > GM_TOL * beta) || !(hn > 0)) break;
+  }
+  if (tid == 0) {  // H(0:k, 0:k) y = g, y over g
+    for (int i = k - 1; i >= 0; i--) {
+      double t = g[i];
+      for (int l = i + 1; l < k; l++) t -= H[i * GM_M + l] * g[l];
+      g[i] = H[i * GM_M + i] != 0.0 ? t / H[i * GM_M + i] : 0.0;
+    }
+  }
+  __syncthreads();
+  for (int t = tid; t < n; t += BT) {
+    double d = 0.0;
+    for (int i = 0; i < k; i++) d += g[i] * V[(size_t)i * n + t];
+    xv[(size_t)t * nrhs + c] += d;
+  }
+  __syncthreads();
+  return k;
+}
+
+__device__ __forceinline__ void residual_all(const double* Ai, int n, int nrhs, const double* xv,
+                                             const double* Bi, double* Ri) {
+  switch (nrhs) {
+    case 1: residual_rows<1>(Ai, n, xv, Bi, Ri); break;
+    case 2: residual_rows<2>(Ai, n, xv, Bi, Ri); break;
+    case 3: residual_rows<3>(Ai, n, xv, Bi, Ri); break;
+    default: residual_rows<4>(Ai, n, xv, Bi, Ri); break;
   }
 }
 
@@ -593,18 +753,9 @@ __device__ void process_system(const BatchArgs& a, int sidx, const SysDesc& d, S
   int it = 0;
   double eta = INFINITY, prev = INFINITY;
   bool ok = false;
+  // LU-IR: x += LU \ r while the backward error drops by 10% per step.
   for (;;) {
-    if (tid < 8) sh.norm[1 + tid] = 0.0;
-    __syncthreads();
-    col_absmax(rv, n, nrhs, &sh.norm[1]);
-    col_absmax(xv, n, nrhs, &sh.norm[1 + 4]);
-    __syncthreads();
-    eta = 0.0;
-    for (int c = 0; c < nrhs; c++) {
-      const double den = sh.norm[0] * sh.norm[1 + 4 + c] + sh.norm[1 + 8 + c];
-      const double v = den > 0 ? sh.norm[1 + c] / den : (sh.norm[1 + c] > 0 ? INFINITY : 0.0);
-      if (!(v <= eta)) eta = v;
-    }
+    eta = refine_eta(rv, xv, n, nrhs, sh);
     if (eta <= a.tol) { ok = true; break; }
     if (it >= a.max_iters || !(eta < 0.9 * prev)) break;
     prev = eta;
@@ -628,19 +779,36 @@ __device__ void process_system(const BatchArgs& a, int sidx, const SysDesc& d, S
     for (int idx = tid; idx < n * nrhs; idx += BT)
       xv[idx] += (double)dv[idx] * sh.norm[1 + idx % nrhs] * (double)scale;
     __syncthreads();
-    switch (nrhs) {
-      case 1: residual_rows<1>(Ai, n, xv, Bi, Xi); break;
-      case 2: residual_rows<2>(Ai, n, xv, Bi, Xi); break;
-      case 3: residual_rows<3>(Ai, n, xv, Bi, Xi); break;
-      default: residual_rows<4>(Ai, n, xv, Bi, Xi); break;
-    }
+    residual_all(Ai, n, nrhs, xv, Bi, Xi);
     rv = Xi;
     __syncthreads();
+  }
+  // GMRES-IR when LU-IR made progress (its best backward error went below
+  // GM_TRIGGER) and then stalled: the same factors precondition GMRES in FP64,
+  // as long as its matrix-vector products (steps x nrhs x n^2) stay below
+  // half of what the FP64 redo would cost (n^3 / 3). Systems on which LU-IR
+  // diverged from the start (kappa u_factor >> 1) go straight to the FP64 pass.
+  int gsteps = 0;
+  const int mcap = min(a.gmres_m, n / (2 * nrhs));
+  if (!ok && mcap >= 4 && fmin(eta, prev) < GM_TRIGGER) {
+    double* w = reinterpret_cast<double*>(smem + L.gm);
+    double* H = w + n;
+    double* V = reinterpret_cast<double*>(static_cast<char*>(a.scratch) +
+                                          (size_t)blockIdx.x * a.scratch_bytes + GM_V_OFFSET);
+    for (int outer = 0; outer < GM_OUTER && !ok; outer++) {
+      for (int c = 0; c < nrhs; c++)
+        gsteps += gmres_column<P>(Ai, n, nrhs, c, M, rmap, rv, xv, dv, scale, w, H, V, mcap, sh);
+      residual_all(Ai, n, nrhs, xv, Bi, Xi);
+      rv = Xi;
+      __syncthreads();
+      eta = refine_eta(rv, xv, n, nrhs, sh);
+      if (eta <= a.tol) ok = true;
+    }
   }
   __syncthreads();
   for (int idx = tid; idx < n * nrhs; idx += BT) Xi[idx] = xv[idx];
   if (tid == 0) {
-    a.status[sidx] = ok ? it : -1 - it;
+    a.status[sidx] = ok ? it + gsteps : -1 - (it + gsteps);
     a.eta[sidx] = eta;
     pc.mark(3);
     if (a.phase) pc.flush(phase);
@@ -696,7 +864,7 @@ constexpr size_t BATCH_STATIC_SMEM = 1024;  // bound of the kernel's static shar
 
 struct la_batch_plan_s {
   la_ctx ctx;
-  int count = 0, mode = 0, ctas_per_sm = 1, threads = BT_MAX;
+  int count = 0, mode = 0, ctas_per_sm = 1, threads = BT_MAX, gmres_m = 0;
   double tol = 1e-14;
   int max_iters = 10;
   const double *A = nullptr, *B = nullptr;
@@ -756,6 +924,7 @@ la_status launch_pass(la_batch_plan_s* pl, int* queue, int only_flagged, size_t 
   a.max_iters = pl->max_iters;
   a.tol = pl->tol;
   a.only_flagged = only_flagged;
+  a.gmres_m = pl->gmres_m;
   a.cycles = pl->d_cycles;
   a.phase = pl->d_phase;
   batched_kernel<MIXED><<<grid, threads, smem, ctx->stream>>>(a);
@@ -831,6 +1000,7 @@ la_status la_batch_plan_create(la_ctx ctx, const double* d_a, const double* d_b,
   pl->mode = mode;
   pl->ctas_per_sm = ctas_per_sm;
   pl->threads = threads;
+  pl->gmres_m = mode == LA_BATCH_MIXED ? std::min(ctx->batch_gmres, GM_M) : 0;
   pl->tol = tol;
   pl->max_iters = max_iters;
   pl->A = d_a;

@@ -231,6 +231,10 @@ la_status la_ctx_set_option(la_ctx ctx, int option, int64_t value) {
     case LA_OPT_CLUSTER_PANEL:
       ctx->cluster_panels = value ? 1 : 0;
       return LA_OK;
+    case LA_OPT_BATCH_GMRES:
+      if (value < 0 || value > 20) return LA_INVALID;
+      ctx->batch_gmres = (int)value;
+      return LA_OK;
   }
   return LA_INVALID;
 }
@@ -244,6 +248,7 @@ la_status la_ctx_get_option(la_ctx ctx, int option, int64_t* value) {
     case LA_OPT_PROFILE: *value = ctx->profile; return LA_OK;
     case LA_OPT_LOOKAHEAD: *value = ctx->lookahead; return LA_OK;
     case LA_OPT_CLUSTER_PANEL: *value = ctx->cluster_panels; return LA_OK;
+    case LA_OPT_BATCH_GMRES: *value = ctx->batch_gmres; return LA_OK;
   }
   return LA_INVALID;
 }

@@ -52,6 +52,7 @@ struct la_context {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int lookahead = 1;
   int cluster_panels = 1;                // FP32 panels on one thread-block cluster
+  int batch_gmres = 0;                   // Krylov steps per GMRES correction in batch plans (0: off)
   int sm_count = 0;
   size_t smem_optin = 0;
   int arith = LA_ARITH_FAST;

@@ -152,7 +152,7 @@ __device__ double tridiag_min_eig(const double* al, const double* be, int k) {
     lo = fmin(lo, al[i] - r);
     hi = fmax(hi, al[i] + r);
   }
-  for (int it = 0; it < 100; it++) {
+  for (int it = 0; it < 80; it++) {
     const double mid = 0.5 * (lo + hi);
     int cnt = 0;
     double q = al[0] - mid;
@@ -166,11 +166,14 @@ __device__ double tridiag_min_eig(const double* al, const double* be, int k) {
   return 0.5 * (lo + hi);
 }
 
-constexpr int LK = 8;  // Lanczos steps
+constexpr int LK = 6;  // Lanczos steps
 
-// 16 features per system (one CTA per system). The last two come from LK steps
-// of Lanczos on A^T A with full reorthogonalisation: the largest and the
-// smallest Ritz values bound sigma_max^2 from below and sigma_min^2 from above.
+// 16 features per system (one CTA per system). A is read only in coalesced
+// passes: rows by warps (A q, row statistics) and columns by threads
+// (A^T t, column statistics). The condition estimate is LK steps of Lanczos
+// on A^T A from a fixed start vector q0 with full reorthogonalisation: the
+// extreme Ritz values bound sigma_max^2 from below and sigma_min^2 from above.
+// The asymmetry feature is the probe ||A q0 - A^T q0|| / ||A q0||.
 __global__ void __launch_bounds__(256)
 features_kernel(const double* __restrict__ A, const SysRec* __restrict__ sys, int count,
                 float* __restrict__ F) {
@@ -179,52 +182,100 @@ features_kernel(const double* __restrict__ A, const SysRec* __restrict__ sys, in
   __shared__ double t1[512];
   __shared__ double t2[512];
   __shared__ double al[LK], be[LK];
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int NWp = blockDim.x >> 5;
   for (int i = blockIdx.x; i < count; i += gridDim.x) {
     const SysRec d = sys[i];
     const int n = d.n;
     const double* a = A + d.a;
-    // norms and dominance
+    for (int k = tid; k < n; k += blockDim.x) q[0][k] = 1.0 + 0.5 * sin(1.0 + k);
+    double nrm = 0;
+    for (int k = tid; k < n; k += blockDim.x) nrm += q[0][k] * q[0][k];
+    nrm = sqrt(block_sum(nrm, red));
+    for (int k = tid; k < n; k += blockDim.x) q[0][k] /= nrm;
+    __syncthreads();
     double rmax = 0, rmin = INFINITY, dmin = INFINITY, dsum = 0, ddom = 0, amax = 0, fro = 0,
-           diag_min = INFINITY;
-    const int lane = tid & 31;
-    for (int r = tid >> 5; r < n; r += blockDim.x >> 5) {  // one warp per row
-      double rs = 0, f2 = 0, am = 0;
-      for (int k = lane; k < n; k += 32) {
-        const double x = fabs(a[(size_t)r * n + k]);
-        rs += x;
-        f2 += x * x;
-        am = fmax(am, x);
+           diag_min = INFINITY, cmax = 0, cmin = INFINITY, asym = 0, aq = 0;
+    int kk = 0;
+    for (int j = 0; j < LK && j < n; j++) {
+      // t1 = A q_j (one warp per row); row statistics on the first pass
+      for (int r = tid >> 5; r < n; r += NWp) {
+        double s = 0, rs = 0, f2 = 0, am = 0;
+        for (int k = lane; k < n; k += 32) {
+          const double x = a[(size_t)r * n + k];
+          s += x * q[j][k];
+          if (j == 0) {
+            rs += fabs(x);
+            f2 += x * x;
+            am = fmax(am, fabs(x));
+          }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+          s += __shfl_xor_sync(0xffffffffu, s, o);
+          if (j == 0) {
+            rs += __shfl_xor_sync(0xffffffffu, rs, o);
+            f2 += __shfl_xor_sync(0xffffffffu, f2, o);
+            am = fmax(am, __shfl_xor_sync(0xffffffffu, am, o));
+          }
+        }
+        if (lane == 0) {
+          t1[r] = s;
+          if (j == 0) {
+            const double di = fabs(a[(size_t)r * n + r]);
+            const double off = rs - di;
+            fro += f2;
+            amax = fmax(amax, am);
+            rmax = fmax(rmax, rs);
+            rmin = fmin(rmin, rs);
+            const double ratio = di / fmax(off, 1e-300);
+            dmin = fmin(dmin, ratio);
+            dsum += log10(fmax(ratio, 1e-300));
+            ddom += ratio > 1.0 ? 1.0 : 0.0;
+            diag_min = fmin(diag_min, di);
+          }
+        }
       }
-      for (int o = 16; o > 0; o >>= 1) {
-        rs += __shfl_xor_sync(0xffffffffu, rs, o);
-        f2 += __shfl_xor_sync(0xffffffffu, f2, o);
-        am = fmax(am, __shfl_xor_sync(0xffffffffu, am, o));
+      __syncthreads();
+      // t2 = A^T t1 (one thread per column); column statistics and the
+      // asymmetry probe on the first pass
+      for (int c = tid; c < n; c += blockDim.x) {
+        double s = 0, cs = 0, sq = 0;
+        for (int k = 0; k < n; k++) {
+          const double x = a[(size_t)k * n + c];
+          s += x * t1[k];
+          if (j == 0) {
+            cs += fabs(x);
+            sq += x * q[0][k];
+          }
+        }
+        t2[c] = s;
+        if (j == 0) {
+          cmax = fmax(cmax, cs);
+          cmin = fmin(cmin, cs);
+          const double dd = t1[c] - sq;  // (A q0)_c - (A^T q0)_c
+          asym += dd * dd;
+          aq += t1[c] * t1[c];
+        }
       }
-      if (lane == 0) {
-        const double di = fabs(a[(size_t)r * n + r]);
-        const double off = rs - di;
-        fro += f2;
-        amax = fmax(amax, am);
-        rmax = fmax(rmax, rs);
-        rmin = fmin(rmin, rs);
-        const double ratio = di / fmax(off, 1e-300);
-        dmin = fmin(dmin, ratio);
-        dsum += log10(fmax(ratio, 1e-300));
-        ddom += ratio > 1.0 ? 1.0 : 0.0;
-        diag_min = fmin(diag_min, di);
+      __syncthreads();
+      double aj = 0;
+      for (int k = tid; k < n; k += blockDim.x) aj += q[j][k] * t2[k];
+      aj = block_sum(aj, red);
+      for (int pq = 0; pq <= j; pq++) {  // full reorthogonalisation
+        double c = 0;
+        for (int k = tid; k < n; k += blockDim.x) c += q[pq][k] * t2[k];
+        c = block_sum(c, red);
+        for (int k = tid; k < n; k += blockDim.x) t2[k] -= c * q[pq][k];
+        __syncthreads();
       }
-    }
-    double cmax = 0, cmin = INFINITY, asym = 0;
-    for (int c = tid; c < n; c += blockDim.x) {
-      double cs = 0;
-      for (int k = 0; k < n; k++) {
-        cs += fabs(a[(size_t)k * n + c]);
-        const double dd = a[(size_t)c * n + k] - a[(size_t)k * n + c];
-        asym += dd * dd;
-      }
-      cmax = fmax(cmax, cs);
-      cmin = fmin(cmin, cs);
+      double bj = 0;
+      for (int k = tid; k < n; k += blockDim.x) bj += t2[k] * t2[k];
+      bj = sqrt(block_sum(bj, red));
+      if (tid == 0) { al[j] = aj; be[j] = bj; }
+      kk = j + 1;
+      if (!(bj > 1e-12 * fabs(aj)) || j + 1 >= LK) break;
+      for (int k = tid; k < n; k += blockDim.x) q[j + 1][k] = t2[k] / bj;
+      __syncthreads();
     }
     rmax = block_max(rmax, red);
     rmin = block_min(rmin, red);
@@ -237,56 +288,8 @@ features_kernel(const double* __restrict__ A, const SysRec* __restrict__ sys, in
     cmax = block_max(cmax, red);
     cmin = block_min(cmin, red);
     asym = block_sum(asym, red);
-    // Lanczos on A^T A from a fixed start vector
-    for (int k = tid; k < n; k += blockDim.x) q[0][k] = 1.0 + 0.5 * sin(1.0 + k);
-    double nrm = sqrt(block_sum([&] {
-      double s = 0;
-      for (int k = tid; k < n; k += blockDim.x) s += q[0][k] * q[0][k];
-      return s;
-    }(), red));
-    for (int k = tid; k < n; k += blockDim.x) q[0][k] /= nrm;
-    __syncthreads();
-    int kk = 0;
-    for (int j = 0; j < LK && j < n; j++) {
-      // t2 = A^T (A q_j)
-      for (int r = tid >> 5; r < n; r += blockDim.x >> 5) {
-        double s = 0;
-        for (int k = lane; k < n; k += 32) s += a[(size_t)r * n + k] * q[j][k];
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        if (lane == 0) t1[r] = s;
-      }
-      __syncthreads();
-      for (int c = tid; c < n; c += blockDim.x) {
-        double s = 0;
-        for (int k = 0; k < n; k++) s += a[(size_t)k * n + c] * t1[k];
-        t2[c] = s;
-      }
-      __syncthreads();
-      double aj = 0;
-      for (int k = tid; k < n; k += blockDim.x) aj += q[j][k] * t2[k];
-      aj = block_sum(aj, red);
-      // full reorthogonalisation against q_0..q_j
-      for (int p = 0; p <= j; p++) {
-        double c = 0;
-        for (int k = tid; k < n; k += blockDim.x) c += q[p][k] * t2[k];
-        c = block_sum(c, red);
-        for (int k = tid; k < n; k += blockDim.x) t2[k] -= c * q[p][k];
-        __syncthreads();
-      }
-      double bj = 0;
-      for (int k = tid; k < n; k += blockDim.x) bj += t2[k] * t2[k];
-      bj = sqrt(block_sum(bj, red));
-      if (tid == 0) { al[j] = aj; be[j] = bj; }
-      kk = j + 1;
-      if (!(bj > 1e-12 * fabs(aj)) || j + 1 >= LK) break;
-      for (int k = tid; k < n; k += blockDim.x) q[j + 1][k] = t2[k] / bj;
-      __syncthreads();
-    }
-    __syncthreads();
+    aq = block_sum(aq, red);
     if (tid == 0) {
-      double smax2 = 0;
-      for (int j = 0; j < kk; j++) smax2 = fmax(smax2, al[j] + (j > 0 ? fabs(be[j - 1]) : 0.0));
-      // largest Ritz value: bisection on the negated matrix
       double nal[LK], nbe[LK];
       for (int j = 0; j < kk; j++) { nal[j] = -al[j]; nbe[j] = be[j]; }
       const double emax = -tridiag_min_eig(nal, nbe, kk);
@@ -305,7 +308,7 @@ features_kernel(const double* __restrict__ A, const SysRec* __restrict__ sys, in
       f[10] = (float)(ddom / n);
       f[11] = lg(rmax / fmax(rmin, 1e-300));
       f[12] = lg(cmax / fmax(cmin, 1e-300));
-      f[13] = (float)(sqrt(asym) / fmax(sqrt(fro), 1e-300));
+      f[13] = (float)(sqrt(asym) / fmax(sqrt(aq), 1e-300));
       f[14] = lg(diag_min / fmax(amax, 1e-300));
       f[15] = lg(sqrt(fmax(emax, 1e-300) / emin));
     }

@@ -51,7 +51,7 @@ def run_batch(lagpu, torch, ctx, ns, rs, mats, rhss, mode, ctas=1, precisions=No
 
 @pytest.mark.parametrize("mode,ctas,warps,nmax", [
     (0, 1, 8, 256), (0, 2, 4, 256), (0, 4, 2, 128), (1, 1, 8, 256), (1, 2, 8, 256),
-    (1, 4, 4, 256), (1, 8, 2, 128)],
+    (1, 4, 4, 256), (1, 8, 2, 100)],
     ids=["fp64-1x8", "fp64-2x4", "fp64-4x2", "mixed-1x8", "mixed-2x8", "mixed-4x4", "mixed-8x2"])
 def test_batched_backward_error(lagpu, ctx_fast, torch, mode, ctas, warps, nmax):
     # every supported (CTAs per SM, warps per system) shape gives eta <= 1e-14
@@ -173,3 +173,49 @@ def test_batch_autotune_writes_table(lagpu, ctx_fast, torch, tmp_path):
     lines = open(path).read().strip().splitlines()
     assert 1 <= len(lines) <= 12 and all(l.startswith("mixed") for l in lines)
     assert (str(best), str(warps)) in [(l.split()[3], l.split()[4]) for l in lines]
+
+
+def _conditioned(lagpu, ctx, torch, count, seed, n_range, lk):
+    import selector
+    return selector.conditioned_batch(ctx, count, seed, n_range=n_range, nrhs_range=(1, 2),
+                                      log10_kappa=lk)
+
+
+def _check_all(lagpu, systems, da, db, dx, tol):
+    a, b, x = da.cpu().numpy(), db.cpu().numpy(), dx.cpu().numpy()
+    for s in systems:
+        A = a[s.a_offset:s.a_offset + s.n * s.n].reshape(s.n, s.n)
+        B = b[s.b_offset:s.b_offset + s.n * s.nrhs].reshape(s.n, s.nrhs)
+        X = x[s.b_offset:s.b_offset + s.n * s.nrhs].reshape(s.n, s.nrhs)
+        assert oracle.backward_error(A, X, B) <= tol
+
+
+def test_batched_gmres_ir_rescues_stalled_refinement(lagpu, torch):
+    # BF16 factors on kappa_2 in [1e1, 1e2] with at most 4 LU-IR steps: LU-IR
+    # gets below 1e-6 but not to 1e-14; GMRES-IR preconditioned by the same
+    # factors finishes and saves FP64 redos. With the stage off the FP64 pass redoes every stalled system.
+    # Every answer ends at eta <= 1e-14 either way.
+    fbs = {}
+    for gmres in (20, 0):
+        ctx = lagpu.Context()
+        ctx.set_option(lagpu.OPT_BATCH_GMRES, gmres)
+        systems, da, db, dx, kappa = _conditioned(lagpu, ctx, torch, 24, 31, (120, 300),
+                                                  (1.0, 2.0))
+        lagpu.set_precisions(systems, [lagpu.PREC_BF16] * len(systems))
+        plan = lagpu.BatchPlan(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems, 1,
+                               ctas_per_sm=2, tol=1e-14, max_iters=4)
+        its, eta, fbs[gmres] = plan.stats()
+        plan.free()
+        _check_all(lagpu, systems, da, db, dx, 1e-14)
+        ctx.close()
+    assert fbs[0].sum() > 0
+    assert fbs[20].sum() < fbs[0].sum()
+
+
+def test_batched_gmres_option_bounds(lagpu):
+    ctx = lagpu.Context()
+    with pytest.raises(lagpu.LaError):
+        ctx.set_option(lagpu.OPT_BATCH_GMRES, 21)
+    ctx.set_option(lagpu.OPT_BATCH_GMRES, 5)
+    assert ctx.get_option(lagpu.OPT_BATCH_GMRES) == 5
+    ctx.close()

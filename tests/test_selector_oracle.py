@@ -40,7 +40,7 @@ def test_features_of_diagonal_matrix():
     assert np.isclose(f[0], np.log2(5) / 9) and np.isclose(f[1], 0.5)
     assert np.isclose(f[2], np.log10(4.0)) and np.isclose(f[5], np.log10(4.0))
     assert np.isclose(f[6], np.log10(4.0), atol=1e-9)          # sigma_max exactly
-    assert np.isclose(f[15], np.log10(16.0), atol=1e-9)        # kappa_2 exactly (n <= 8 steps)
+    assert np.isclose(f[15], np.log10(16.0), atol=1e-9)        # kappa_2 exactly (n <= 6 steps)
     assert f[10] == 1.0 and f[13] == 0.0
 
 
