@@ -267,7 +267,7 @@ la_status la_batch_plan_cycles(la_batch_plan plan, long long* cycles);
 
 /* 16 features per system (row-major FP32 [count][16]) for the precision
  * selector: log2 n / 9, nrhs / 4, log10 of the max row and column sums, of the
- * Frobenius norm, of max |a_ij|, of the 6-step Lanczos estimate of sigma_max,
+ * Frobenius norm, of max |a_ij|, of the 4-step Lanczos estimate of sigma_max,
  * of ||A||_F / sigma_max, of the smallest diagonal-dominance ratio, the mean
  * log10 dominance ratio, the fraction of dominant rows, log10 of the row-sum
  * and column-sum spreads, the asymmetry probe ||A q - A^T q|| / ||A q|| (q the

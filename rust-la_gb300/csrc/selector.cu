@@ -166,48 +166,76 @@ __device__ double tridiag_min_eig(const double* al, const double* be, int k) {
   return 0.5 * (lo + hi);
 }
 
-constexpr int LK = 6;  // Lanczos steps
+constexpr int LK = 4;  // Lanczos steps
+constexpr int FEAT_CTAS_PER_SM = 2;
 
-// 16 features per system (one CTA per system). A is read only in coalesced
-// passes: rows by warps (A q, row statistics) and columns by threads
-// (A^T t, column statistics). The condition estimate is LK steps of Lanczos
-// on A^T A from a fixed start vector q0 with full reorthogonalisation: the
-// extreme Ritz values bound sigma_max^2 from below and sigma_min^2 from above.
-// The asymmetry feature is the probe ||A q0 - A^T q0|| / ||A q0||.
+// 16 features per system (one CTA per system). FP64 arithmetic is slow on
+// this GPU, so A_i is read in FP64 once and rounded to an FP32 copy in the
+// CTA's global scratch slice; every statistic and matrix-vector product works
+// in FP32 on that copy (dot products of length n accumulate in FP64). One
+// Lanczos step on A^T A is one pass over A: a warp loads a whole row (16
+// independent loads per lane), takes t_r = a_r . q, and adds a_r t_r into
+// per-lane column accumulators, which are summed across warps in shared
+// memory; so both A q and A^T (A q) come from a single read of each element.
+// The first pass also reads A in FP64, writes the FP32 copy and takes the row
+// and column statistics. LK steps from a fixed start vector q0 with full
+// reorthogonalisation; the extreme Ritz values bound sigma_max^2 from below and
+// sigma_min^2 from above. The asymmetry feature is the probe
+// ||A q0 - A^T q0|| / ||A q0||.
 __global__ void __launch_bounds__(256)
 features_kernel(const double* __restrict__ A, const SysRec* __restrict__ sys, int count,
-                float* __restrict__ F) {
+                float* __restrict__ F, float* __restrict__ scratch) {
   __shared__ double red[8];
-  __shared__ double q[LK + 1][512];
-  __shared__ double t1[512];
-  __shared__ double t2[512];
+  __shared__ float q[LK + 1][512];
+  __shared__ float t1[512];
+  __shared__ float t2[512];
+  __shared__ float part[8][512];  // per-warp column partial sums
   __shared__ double al[LK], be[LK];
-  const int tid = threadIdx.x, lane = tid & 31;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int NWp = blockDim.x >> 5;
+  float* af = scratch + (size_t)blockIdx.x * 512 * 512;
   for (int i = blockIdx.x; i < count; i += gridDim.x) {
     const SysRec d = sys[i];
     const int n = d.n;
     const double* a = A + d.a;
-    for (int k = tid; k < n; k += blockDim.x) q[0][k] = 1.0 + 0.5 * sin(1.0 + k);
     double nrm = 0;
-    for (int k = tid; k < n; k += blockDim.x) nrm += q[0][k] * q[0][k];
+    for (int k = tid; k < n; k += blockDim.x) {
+      const float v = 1.0f + 0.5f * sinf(1.0f + (float)k);
+      q[0][k] = v;
+      nrm += (double)v * v;
+    }
     nrm = sqrt(block_sum(nrm, red));
-    for (int k = tid; k < n; k += blockDim.x) q[0][k] /= nrm;
+    for (int k = tid; k < n; k += blockDim.x) q[0][k] = (float)(q[0][k] / nrm);
     __syncthreads();
-    double rmax = 0, rmin = INFINITY, dmin = INFINITY, dsum = 0, ddom = 0, amax = 0, fro = 0,
-           diag_min = INFINITY, cmax = 0, cmin = INFINITY, asym = 0, aq = 0;
+    float rmax = 0, rmin = INFINITY, dmin = INFINITY, amax = 0, diag_min = INFINITY, cmax = 0,
+          cmin = INFINITY;
+    double dsum = 0, ddom = 0, fro = 0, asym = 0, aq = 0;
     int kk = 0;
     for (int j = 0; j < LK && j < n; j++) {
-      // t1 = A q_j (one warp per row); row statistics on the first pass
-      for (int r = tid >> 5; r < n; r += NWp) {
-        double s = 0, rs = 0, f2 = 0, am = 0;
-        for (int k = lane; k < n; k += 32) {
-          const double x = a[(size_t)r * n + k];
-          s += x * q[j][k];
-          if (j == 0) {
-            rs += fabs(x);
-            f2 += x * x;
-            am = fmax(am, fabs(x));
+      float acc[16], cs[16], sq[16];
+#pragma unroll
+      for (int m = 0; m < 16; m++) { acc[m] = 0.f; cs[m] = 0.f; sq[m] = 0.f; }
+      for (int r = warp; r < n; r += NWp) {
+        float x[16];
+        float* fr = af + (size_t)r * n;
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+          const int k = lane + 32 * m;
+          if (j == 0) x[m] = k < n ? (float)a[(size_t)r * n + k] : 0.f;
+          else x[m] = k < n ? fr[k] : 0.f;
+        }
+        float s = 0, rs = 0, f2 = 0, am = 0;
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+          const int k = lane + 32 * m;
+          if (k < n) {
+            s = fmaf(x[m], q[j][k], s);
+            if (j == 0) {
+              fr[k] = x[m];
+              rs += fabsf(x[m]);
+              f2 = fmaf(x[m], x[m], f2);
+              am = fmaxf(am, fabsf(x[m]));
+            }
           }
         }
         for (int o = 16; o > 0; o >>= 1) {
@@ -215,78 +243,98 @@ features_kernel(const double* __restrict__ A, const SysRec* __restrict__ sys, in
           if (j == 0) {
             rs += __shfl_xor_sync(0xffffffffu, rs, o);
             f2 += __shfl_xor_sync(0xffffffffu, f2, o);
-            am = fmax(am, __shfl_xor_sync(0xffffffffu, am, o));
+            am = fmaxf(am, __shfl_xor_sync(0xffffffffu, am, o));
+          }
+        }
+        const float q0r = q[0][r];
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+          acc[m] = fmaf(x[m], s, acc[m]);
+          if (j == 0) {
+            cs[m] += fabsf(x[m]);
+            sq[m] = fmaf(x[m], q0r, sq[m]);
           }
         }
         if (lane == 0) {
           t1[r] = s;
           if (j == 0) {
-            const double di = fabs(a[(size_t)r * n + r]);
-            const double off = rs - di;
+            const float di = fabsf((float)a[(size_t)r * n + r]);
+            const float off = rs - di;
             fro += f2;
-            amax = fmax(amax, am);
-            rmax = fmax(rmax, rs);
-            rmin = fmin(rmin, rs);
-            const double ratio = di / fmax(off, 1e-300);
-            dmin = fmin(dmin, ratio);
-            dsum += log10(fmax(ratio, 1e-300));
-            ddom += ratio > 1.0 ? 1.0 : 0.0;
-            diag_min = fmin(diag_min, di);
+            amax = fmaxf(amax, am);
+            rmax = fmaxf(rmax, rs);
+            rmin = fminf(rmin, rs);
+            const float ratio = di / fmaxf(off, 1e-30f);
+            dmin = fminf(dmin, ratio);
+            dsum += log10f(fmaxf(ratio, 1e-30f));
+            ddom += ratio > 1.f ? 1.0 : 0.0;
+            diag_min = fminf(diag_min, di);
           }
         }
       }
+      // t2 = A^T t1: sum the warps' column partials
+#pragma unroll
+      for (int m = 0; m < 16; m++)
+        if (lane + 32 * m < n) part[warp][lane + 32 * m] = acc[m];
       __syncthreads();
-      // t2 = A^T t1 (one thread per column); column statistics and the
-      // asymmetry probe on the first pass
       for (int c = tid; c < n; c += blockDim.x) {
-        double s = 0, cs = 0, sq = 0;
-        for (int k = 0; k < n; k++) {
-          const double x = a[(size_t)k * n + c];
-          s += x * t1[k];
-          if (j == 0) {
-            cs += fabs(x);
-            sq += x * q[0][k];
-          }
-        }
-        t2[c] = s;
-        if (j == 0) {
-          cmax = fmax(cmax, cs);
-          cmin = fmin(cmin, cs);
-          const double dd = t1[c] - sq;  // (A q0)_c - (A^T q0)_c
-          asym += dd * dd;
-          aq += t1[c] * t1[c];
-        }
+        float t = 0.f;
+        for (int w = 0; w < NWp; w++) t += part[w][c];
+        t2[c] = t;
       }
       __syncthreads();
+      if (j == 0) {  // column sums of |A| and A^T q0, the same way
+#pragma unroll
+        for (int m = 0; m < 16; m++)
+          if (lane + 32 * m < n) part[warp][lane + 32 * m] = cs[m];
+        __syncthreads();
+        for (int c = tid; c < n; c += blockDim.x) {
+          float t = 0.f;
+          for (int w = 0; w < NWp; w++) t += part[w][c];
+          cmax = fmaxf(cmax, t);
+          cmin = fminf(cmin, t);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int m = 0; m < 16; m++)
+          if (lane + 32 * m < n) part[warp][lane + 32 * m] = sq[m];
+        __syncthreads();
+        for (int c = tid; c < n; c += blockDim.x) {
+          float t = 0.f;
+          for (int w = 0; w < NWp; w++) t += part[w][c];
+          const double dd = (double)t1[c] - t;  // (A q0)_c - (A^T q0)_c
+          asym += dd * dd;
+          aq += (double)t1[c] * t1[c];
+        }
+        __syncthreads();
+      }
       double aj = 0;
-      for (int k = tid; k < n; k += blockDim.x) aj += q[j][k] * t2[k];
+      for (int k = tid; k < n; k += blockDim.x) aj += (double)q[j][k] * t2[k];
       aj = block_sum(aj, red);
       for (int pq = 0; pq <= j; pq++) {  // full reorthogonalisation
         double c = 0;
-        for (int k = tid; k < n; k += blockDim.x) c += q[pq][k] * t2[k];
+        for (int k = tid; k < n; k += blockDim.x) c += (double)q[pq][k] * t2[k];
         c = block_sum(c, red);
-        for (int k = tid; k < n; k += blockDim.x) t2[k] -= c * q[pq][k];
+        for (int k = tid; k < n; k += blockDim.x) t2[k] = (float)(t2[k] - c * q[pq][k]);
         __syncthreads();
       }
       double bj = 0;
-      for (int k = tid; k < n; k += blockDim.x) bj += t2[k] * t2[k];
+      for (int k = tid; k < n; k += blockDim.x) bj += (double)t2[k] * t2[k];
       bj = sqrt(block_sum(bj, red));
       if (tid == 0) { al[j] = aj; be[j] = bj; }
       kk = j + 1;
-      if (!(bj > 1e-12 * fabs(aj)) || j + 1 >= LK) break;
-      for (int k = tid; k < n; k += blockDim.x) q[j + 1][k] = t2[k] / bj;
+      if (!(bj > 1e-6 * fabs(aj)) || j + 1 >= LK) break;
+      for (int k = tid; k < n; k += blockDim.x) q[j + 1][k] = (float)(t2[k] / bj);
       __syncthreads();
     }
-    rmax = block_max(rmax, red);
-    rmin = block_min(rmin, red);
-    dmin = block_min(dmin, red);
+    const double rmax_b = block_max(rmax, red), rmin_b = block_min(rmin, red);
+    const double dmin_b = block_min(dmin, red);
     dsum = block_sum(dsum, red);
     ddom = block_sum(ddom, red);
-    amax = block_max(amax, red);
+    const double amax_b = block_max(amax, red);
     fro = block_sum(fro, red);
-    diag_min = block_min(diag_min, red);
-    cmax = block_max(cmax, red);
-    cmin = block_min(cmin, red);
+    const double diag_b = block_min(diag_min, red);
+    const double cmax_b = block_max(cmax, red), cmin_b = block_min(cmin, red);
     asym = block_sum(asym, red);
     aq = block_sum(aq, red);
     if (tid == 0) {
@@ -297,19 +345,19 @@ features_kernel(const double* __restrict__ A, const SysRec* __restrict__ sys, in
       float* f = F + (size_t)i * NF;
       f[0] = (float)(log2((double)n) / 9.0);
       f[1] = (float)d.nrhs / 4.f;
-      f[2] = lg(rmax);
-      f[3] = lg(cmax);
+      f[2] = lg(rmax_b);
+      f[3] = lg(cmax_b);
       f[4] = lg(sqrt(fro));
-      f[5] = lg(amax);
+      f[5] = lg(amax_b);
       f[6] = lg(sqrt(fmax(emax, 0.0)));
       f[7] = lg(sqrt(fro) / sqrt(fmax(emax, 1e-300)));
-      f[8] = lg(dmin);
+      f[8] = lg(dmin_b);
       f[9] = (float)(dsum / n);
       f[10] = (float)(ddom / n);
-      f[11] = lg(rmax / fmax(rmin, 1e-300));
-      f[12] = lg(cmax / fmax(cmin, 1e-300));
+      f[11] = lg(rmax_b / fmax(rmin_b, 1e-300));
+      f[12] = lg(cmax_b / fmax(cmin_b, 1e-300));
       f[13] = (float)(sqrt(asym) / fmax(sqrt(aq), 1e-300));
-      f[14] = lg(diag_min / fmax(amax, 1e-300));
+      f[14] = lg(diag_b / fmax(amax_b, 1e-300));
       f[15] = lg(sqrt(fmax(emax, 1e-300) / emin));
     }
     __syncthreads();
@@ -582,17 +630,23 @@ la_status la_batch_features_device(la_ctx ctx, const double* d_a, const la_batch
             systems[i].nrhs};
   }
   SysRec* d = nullptr;
+  float* scr = nullptr;
+  const int grid = std::min(count, ctx->sm_count * FEAT_CTAS_PER_SM);
   LA_TRY(la_device_alloc(ctx, reinterpret_cast<void**>(&d), count * sizeof(SysRec)));
-  cudaError_t e = cudaMemcpyAsync(d, h.data(), count * sizeof(SysRec), cudaMemcpyHostToDevice,
-                                  ctx->stream);
-  la_status s = e == cudaSuccess ? LA_OK : la_cuda_fail(ctx, e, "features upload");
+  la_status s = la_device_alloc(ctx, reinterpret_cast<void**>(&scr),
+                                (size_t)grid * 512 * 512 * sizeof(float));
   if (s == LA_OK) {
-    features_kernel<<<std::min(count, ctx->sm_count * 8), 256, 0, ctx->stream>>>(d_a, d, count,
-                                                                                 d_features);
+    cudaError_t e = cudaMemcpyAsync(d, h.data(), count * sizeof(SysRec), cudaMemcpyHostToDevice,
+                                    ctx->stream);
+    if (e != cudaSuccess) s = la_cuda_fail(ctx, e, "features upload");
+  }
+  if (s == LA_OK) {
+    features_kernel<<<grid, 256, 0, ctx->stream>>>(d_a, d, count, d_features, scr);
     ctx->launches++;
     s = la_check_launch(ctx, "features_kernel");
   }
   la_device_free(ctx, d);
+  la_device_free(ctx, scr);
   if (s == LA_OK) s = la_sync_and_check(ctx, "features");
   return s;
 }

@@ -51,7 +51,8 @@ def features(ctx, systems, da):
     return f
 
 
-def measure_costs(ctx, systems, da, db, dx, ctas_per_sm=1, tol=1e-14, max_iters=10, reps=1):
+def measure_costs(ctx, systems, da, db, dx, ctas_per_sm=2, warps_per_system=8, tol=1e-14,
+                  max_iters=10, reps=1):
     """Runs the mixed plan with every system in each class in turn. Returns
     (cycles [count, 3] int64, converged [count, 3] bool): SM cycles spent per
     system (mixed attempt plus FP64 redo) and whether refinement converged."""
@@ -59,8 +60,8 @@ def measure_costs(ctx, systems, da, db, dx, ctas_per_sm=1, tol=1e-14, max_iters=
     cyc = np.zeros((count, 3), dtype=np.int64)
     conv = np.zeros((count, 3), dtype=bool)
     plan = la_gpu.BatchPlan(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems,
-                            la_gpu.BATCH_MIXED, ctas_per_sm=ctas_per_sm, tol=tol,
-                            max_iters=max_iters)
+                            la_gpu.BATCH_MIXED, ctas_per_sm=ctas_per_sm,
+                            warps_per_system=warps_per_system, tol=tol, max_iters=max_iters)
     try:
         sel = torch.empty(count, dtype=torch.int32, device="cuda")
         for c in range(3):

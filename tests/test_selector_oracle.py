@@ -35,12 +35,12 @@ def test_mlp_forward_is_a_distribution():
 
 
 def test_features_of_diagonal_matrix():
-    d = np.array([4.0, 2.0, 1.0, 0.5, 0.25])
+    d = np.array([4.0, 2.0, 1.0, 0.25])
     f = sr.features(np.diag(d), 2)
-    assert np.isclose(f[0], np.log2(5) / 9) and np.isclose(f[1], 0.5)
+    assert np.isclose(f[0], np.log2(4) / 9) and np.isclose(f[1], 0.5)
     assert np.isclose(f[2], np.log10(4.0)) and np.isclose(f[5], np.log10(4.0))
     assert np.isclose(f[6], np.log10(4.0), atol=1e-9)          # sigma_max exactly
-    assert np.isclose(f[15], np.log10(16.0), atol=1e-9)        # kappa_2 exactly (n <= 6 steps)
+    assert np.isclose(f[15], np.log10(16.0), atol=1e-9)        # kappa_2 exactly (n <= 4 steps)
     assert f[10] == 1.0 and f[13] == 0.0
 
 
