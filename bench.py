@@ -19,6 +19,19 @@ count 2/3 n^3 + 2 n^2 nrhs (factor + solve).
           left-looking LUDecomposition::new) timed on a bounded prefix of the
           same factorization on this host.
 
+Further sections of the same JSON line (skipped with --no-mixed,
+--no-batched, --no-selector):
+  mixed_ir : mixed-precision LU (tcgen05 BF16/FP16 or FP32 trailing updates)
+          + FP64 refinement at n=16384, kappa in {1e2, 1e6, 1e10}, 4 RHS,
+          against the plain FP64 LU at the same size.
+  batched_uneven : 20,000 systems, n uniform in [8, 256], 1-4 RHS, half of them
+          shifted by 0.5 n I; solves/s of the mixed plan against the plain FP64
+          plan, each with its autotuned shape.
+  learned_selector : 50,000 held-out Householder-conditioned systems, n in
+          [16, 512], log10 kappa uniform in [1, 12]; plain FP64 plan, mixed plan
+          with FP32 factors everywhere, and the selector's per-system choice
+          (features + inference included).
+
 `--impl reference` times the reference's CPU algorithm (the oracle's
 multi-threaded form, bit-identical results) on the same workload instead.
 Multi-GPU runs are independent replicas (the single LU does not shard).
@@ -240,6 +253,139 @@ def run_mixed(la_gpu, torch, ctx, n, nrhs=4, kappas=(1e2, 1e6, 1e10), precs=(1, 
             "speedup_vs_plain_fp64": speed}
 
 
+def _wall_ms(ctx, torch, fn, reps=3):
+    """Best of reps wall-clock runs of fn, synchronised on both sides (the
+    batches below run for tens to hundreds of milliseconds, so launch and
+    synchronisation overheads are negligible)."""
+    best = float("inf")
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        fn()
+        ctx.synchronize()
+        best = min(best, time.perf_counter() - t0)
+    return best * 1e3
+
+
+def _sample_eta(la_gpu, ctx, systems, da, db, dx, count=64, seed=0):
+    """Largest normwise backward error over a seeded sample of the systems,
+    by the library's compensated FP64 residual."""
+    rng = np.random.default_rng(seed)
+    worst = 0.0
+    for i in rng.choice(len(systems), min(count, len(systems)), replace=False):
+        s = systems[int(i)]
+        e = la_gpu.backward_error_device(ctx, da.data_ptr() + 8 * s.a_offset, s.n,
+                                         dx.data_ptr() + 8 * s.b_offset, s.nrhs,
+                                         db.data_ptr() + 8 * s.b_offset, s.nrhs, s.n, s.nrhs)
+        worst = max(worst, e)
+    return worst
+
+
+def run_batched(la_gpu, torch, ctx, count=20000, seed=4):
+    """Uneven batch: count systems, n uniform in [8, 256], 1-4 RHS, A iid N(0,1)
+    plus 0.5 n I on even-indexed systems, B iid N(0,1) (generated on the device,
+    seeded). Each arm runs its autotuned plan shape (CTAs per SM x warps per
+    system) from a captured CUDA graph; solves/s = count / batch time."""
+    rng = np.random.default_rng(seed)
+    ns = rng.integers(8, 257, size=count)
+    rs = rng.integers(1, 5, size=count)
+    systems, na, nb = la_gpu.batch_systems(ns, rs)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    da = torch.randn(na, dtype=torch.float64, device="cuda", generator=gen)
+    db = torch.randn(nb, dtype=torch.float64, device="cuda", generator=gen)
+    dx = torch.zeros(nb, dtype=torch.float64, device="cuda")
+    idx = np.concatenate([s.a_offset + np.arange(s.n) * (s.n + 1)
+                          for i, s in enumerate(systems) if i % 2 == 0])
+    shift = np.concatenate([np.full(s.n, 0.5 * s.n) for i, s in enumerate(systems) if i % 2 == 0])
+    da[torch.from_numpy(idx).cuda()] += torch.from_numpy(shift).cuda()
+    torch.cuda.synchronize()
+    out = {"workload": "uneven batch: %d systems, n uniform in [8, 256], 1-4 RHS, A iid N(0,1) "
+                       "+ 0.5 n I on even systems" % count, "count": count}
+    for mode, name in ((la_gpu.BATCH_FP64, "plain_fp64"), (la_gpu.BATCH_MIXED, "mixed_ir")):
+        c, w, _ = la_gpu.batch_autotune(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems,
+                                        mode)
+        plan = la_gpu.BatchPlan(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems, mode,
+                                ctas_per_sm=c, warps_per_system=w)
+        ms = _wall_ms(ctx, torch, plan.run, reps=5)
+        its, eta, fb = plan.stats()
+        out[name] = {"ms": ms, "solves_per_s": count / (ms * 1e-3), "ctas_per_sm": c,
+                     "warps_per_system": w, "fell_back": int(fb.sum()),
+                     "max_eta_sample": _sample_eta(la_gpu, ctx, systems, da, db, dx)}
+        plan.free()
+    out["speedup_solves_per_s"] = (out["mixed_ir"]["solves_per_s"] /
+                                   out["plain_fp64"]["solves_per_s"])
+    del da, db, dx
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_selector(la_gpu, torch, ctx, count=50000, seed=7):
+    """Learned precision selector on a held-out Householder-conditioned batch:
+    count systems, n uniform in [16, 512], 1-4 RHS, log10 kappa_2 uniform in
+    [1, 12] (seed 7; the committed weights were trained on 200,000 systems with
+    seeds 1000+). Times, per batch: the plain FP64 plan; the mixed plan with
+    FP32 factors for every system (the method without the selector); and the
+    selector path (features + MLP inference + per-system class choice + the
+    same mixed plan), everything on the device."""
+    import selector as S
+    weights = os.path.join(ROOT, "rust-la_gb300", "selector_weights.npy")
+    systems, da, db, dx, kappa = S.conditioned_batch(ctx, count, seed)
+    sel = S.PrecisionSelector.from_file(ctx, weights)
+    out = {"workload": "learned selector: %d systems, n uniform in [16, 512], 1-4 RHS, "
+                       "A = H1 diag(s) H2, log10 kappa uniform in [1, 12]" % count,
+           "count": count}
+    c64, w64, _ = la_gpu.batch_autotune(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems,
+                                        la_gpu.BATCH_FP64)
+    p64 = la_gpu.BatchPlan(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems,
+                           la_gpu.BATCH_FP64, ctas_per_sm=c64, warps_per_system=w64)
+    t64 = _wall_ms(ctx, torch, p64.run)
+    out["plain_fp64"] = {"ms": t64, "solves_per_s": count / (t64 * 1e-3), "ctas_per_sm": c64,
+                         "warps_per_system": w64,
+                         "max_eta_sample": _sample_eta(la_gpu, ctx, systems, da, db, dx)}
+    p64.free()
+    plan = la_gpu.BatchPlan(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems,
+                            la_gpu.BATCH_MIXED, ctas_per_sm=2, warps_per_system=8)
+    fp32 = torch.full((count,), 2, dtype=torch.int32, device="cuda")
+    cls = torch.empty(count, dtype=torch.int32, device="cuda")
+    fbuf = torch.empty((count, 16), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+
+    def fixed():
+        plan.select_device(fp32.data_ptr())
+        plan.run()
+
+    def choose():
+        la_gpu.batch_features_device(ctx, da.data_ptr(), systems, fbuf.data_ptr())
+        sel.predict(fbuf, out=cls, sync=False)
+
+    def selected():
+        choose()
+        plan.select_device(cls.data_ptr())
+        plan.run()
+
+    t32 = _wall_ms(ctx, torch, fixed)
+    its, eta, fb = plan.stats()
+    out["mixed_fp32_factors"] = {"ms": t32, "solves_per_s": count / (t32 * 1e-3),
+                                 "fell_back": int(fb.sum()),
+                                 "max_eta_sample": _sample_eta(la_gpu, ctx, systems, da, db, dx)}
+    tf = _wall_ms(ctx, torch, choose)
+    ts = _wall_ms(ctx, torch, selected)
+    its, eta, fb = plan.stats()
+    counts = np.bincount(cls.cpu().numpy(), minlength=3).tolist()
+    out["mixed_selector"] = {"ms": ts, "solves_per_s": count / (ts * 1e-3),
+                             "features_inference_ms": tf, "fell_back": int(fb.sum()),
+                             "class_counts_fp8_bf16_fp32": counts,
+                             "max_eta_sample": _sample_eta(la_gpu, ctx, systems, da, db, dx)}
+    plan.free()
+    out["speedup_selector_vs_plain_fp64"] = t64 / ts
+    out["speedup_selector_vs_fp32_factors"] = t32 / ts
+    del da, db, dx
+    torch.cuda.empty_cache()
+    return out
+
+
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -431,6 +577,12 @@ def run_ours(args):
     mixed = None
     if not args.no_mixed:
         mixed = run_mixed(la_gpu, torch, ctx, args.mixed_n)
+    batched = None
+    if not args.no_batched:
+        batched = run_batched(la_gpu, torch, ctx, args.batched_count)
+    selected = None
+    if not args.no_selector:
+        selected = run_selector(la_gpu, torch, ctx, args.selector_count)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -454,6 +606,8 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "gemm_8192": gemm,
             "mixed_ir": mixed,
+            "batched_uneven": batched,
+            "learned_selector": selected,
             "fp64_peak_tflops": fp64_peak,
         }
         print(json.dumps(line))
@@ -474,6 +628,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--mixed-n", type=int, default=16384)
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batched-count", type=int, default=20000)
+    ap.add_argument("--no-selector", action="store_true")
+    ap.add_argument("--selector-count", type=int, default=50000)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
     args = ap.parse_args()
