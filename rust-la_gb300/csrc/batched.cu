@@ -28,6 +28,7 @@
 // CTA waits on another.
 #include <cuda_fp8.h>
 
+#include "f64conv.h"
 #include "la_internal.cuh"
 
 namespace {
@@ -311,6 +312,28 @@ __device__ void block_lu(typename P::S* M, int p, int n, int* rmap, typename P::
   __syncthreads();
 }
 
+// One row of a block step of the triangular solves: x_i -= f * X_blk over all
+// nrhs right-hand sides, with the row's kbn (<= 16) factor entries f loaded
+// once (16 independent loads in flight) and the block's solved values X_blk
+// read from shared memory (the same address across the warp: a broadcast).
+template <typename P, typename TX>
+__device__ __forceinline__ void solve_row_update(const typename P::S* frow, int kbn, TX* xi,
+                                                 const TX* xblk, int nrhs) {
+  TX f[16];
+#pragma unroll
+  for (int k = 0; k < 16; k++) f[k] = k < kbn ? (TX)P::ld(&frow[k]) : TX(0);
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    if (c < nrhs) {
+      TX s = xi[c];
+#pragma unroll
+      for (int k = 0; k < 16; k++)
+        if (k < kbn) s = fma(-f[k], xblk[k * nrhs + c], s);
+      xi[c] = s;
+    }
+  }
+}
+
 // X (n x nrhs, pitch nrhs, already in the factor's row order, i.e. P b)
 // <- U^-1 L^-1 X with the stored factors in M. 16-row blocks: warp 0 solves
 // the diagonal block (lanes = rows, two right-hand sides per pass, values
@@ -345,15 +368,9 @@ __device__ void block_solve(const typename P::S* M, int p, int n, const int* rma
     }
     __syncthreads();
     const int rest = n - kb - kbn;
-    for (int idx = tid; idx < rest * nrhs; idx += BT) {
-      const int i = kb + kbn + idx / nrhs, c = idx % nrhs;
-      const typename P::S* lrow = M + (size_t)rmap[i] * p + kb;
-      TX s = X[i * nrhs + c];
-#pragma unroll
-      for (int k = 0; k < 16; k++)
-        if (k < kbn) s = fma(-(TX)P::ld(&lrow[k]), X[(kb + k) * nrhs + c], s);
-      X[i * nrhs + c] = s;
-    }
+    for (int r = tid; r < rest; r += BT)
+      solve_row_update<P, TX>(M + (size_t)rmap[kb + kbn + r] * p + kb, kbn,
+                              X + (size_t)(kb + kbn + r) * nrhs, X + (size_t)kb * nrhs, nrhs);
     __syncthreads();
   }
   for (int kb = (n - 1) / 16 * 16; kb >= 0; kb -= 16) {
@@ -379,15 +396,9 @@ __device__ void block_solve(const typename P::S* M, int p, int n, const int* rma
       }
     }
     __syncthreads();
-    for (int idx = tid; idx < kb * nrhs; idx += BT) {
-      const int i = idx / nrhs, c = idx % nrhs;
-      const typename P::S* urow = M + (size_t)rmap[i] * p + kb;
-      TX s = X[i * nrhs + c];
-#pragma unroll
-      for (int k = 0; k < 16; k++)
-        if (k < kbn) s = fma(-(TX)P::ld(&urow[k]), X[(kb + k) * nrhs + c], s);
-      X[i * nrhs + c] = s;
-    }
+    for (int r = tid; r < kb; r += BT)
+      solve_row_update<P, TX>(M + (size_t)rmap[r] * p + kb, kbn, X + (size_t)r * nrhs,
+                              X + (size_t)kb * nrhs, nrhs);
     __syncthreads();
   }
 }
@@ -438,21 +449,29 @@ __device__ __forceinline__ void amax_pos(double* p, double v) {
 
 // out[c] = max over the CTA of |v[i nrhs + c]| (c < nrhs, n rows): per-thread
 // maxima, then a warp reduction, then one shared atomic per warp and column.
-// out must be zero on entry; no barrier inside.
+// The maxima are taken on the magnitudes' bit patterns with integer
+// instructions (they order like the values, and a NaN orders above every
+// number, so a NaN residual can never pass the convergence test); the FP64
+// pipe stays free for the residual. out must be zero on entry; no barrier
+// inside.
 __device__ __forceinline__ void col_absmax(const double* v, int n, int nrhs, double* out) {
   const int BT = blockDim.x;
-  double m[4] = {0.0, 0.0, 0.0, 0.0};
+  unsigned long long m[4] = {0ull, 0ull, 0ull, 0ull};
   for (int idx = threadIdx.x; idx < n * nrhs; idx += BT) {
     const int c = idx % nrhs;
-    const double a = fabs(v[idx]);
+    const unsigned long long a = la_absbits_f64(v[idx]);
 #pragma unroll
     for (int q = 0; q < 4; q++)
-      if (q == c) m[q] = fmax(m[q], a);
+      if (q == c) m[q] = a > m[q] ? a : m[q];
   }
 #pragma unroll
   for (int q = 0; q < 4; q++) {
-    for (int off = 16; off > 0; off >>= 1) m[q] = fmax(m[q], __shfl_xor_sync(0xffffffffu, m[q], off));
-    if ((threadIdx.x & 31) == 0 && q < nrhs) amax_pos(&out[q], m[q]);
+    for (int off = 16; off > 0; off >>= 1) {
+      const unsigned long long o = __shfl_xor_sync(0xffffffffu, m[q], off);
+      m[q] = o > m[q] ? o : m[q];
+    }
+    if ((threadIdx.x & 31) == 0 && q < nrhs)
+      atomicMax(reinterpret_cast<unsigned long long*>(&out[q]), m[q]);
   }
 }
 
@@ -471,18 +490,21 @@ __device__ __forceinline__ void halve(double* v, int lane, int s) {
 }
 
 // R = B - A x (or R = A x when MV) in FP64 for rows [0, n) with NR right-hand
-// sides: each warp takes
-// four rows at a time, lanes stride the columns (coalesced rows of A, x from
-// shared memory), and the 4 x 4 partial sums are reduced across the warp by
-// recursive halving (16 adds per lane instead of 5 per value).
+// sides: each warp takes four rows at a time, lanes stride the columns
+// (coalesced rows of A, x from shared memory), and the V = 4 CW partial sums
+// (CW = NR rounded up to a power of two) are reduced across the warp by
+// recursive halving, V - 1 adds per lane, followed by 5 - log2 V butterfly
+// adds: 6, 9 and 16 FP64 adds per lane for 1, 2 and 4 right-hand sides.
 template <int NR, bool MV = false>
 __device__ void residual_rows(const double* __restrict__ Ai, int n, const double* xv,
                               const double* __restrict__ Bi, double* Ri) {
+  constexpr int CW = NR == 1 ? 1 : (NR == 2 ? 2 : 4);
+  constexpr int V = 4 * CW;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, NW = blockDim.x >> 5;
   for (int r0 = 4 * warp; r0 < n; r0 += 4 * NW) {
-    double v[16];
+    double v[V];
 #pragma unroll
-    for (int j = 0; j < 16; j++) v[j] = 0.0;
+    for (int j = 0; j < V; j++) v[j] = 0.0;
 #pragma unroll 2
     for (int k0 = 0; k0 < n; k0 += 32) {
       const int k = k0 + lane;
@@ -495,18 +517,26 @@ __device__ void residual_rows(const double* __restrict__ Ai, int n, const double
 #pragma unroll
       for (int i = 0; i < 4; i++)
 #pragma unroll
-        for (int c = 0; c < NR; c++) v[i * 4 + c] = fma(a[i], xk[c], v[i * 4 + c]);
+        for (int c = 0; c < NR; c++) v[i * CW + c] = fma(a[i], xk[c], v[i * CW + c]);
     }
-    halve<8>(v, lane, 16);
-    halve<4>(v, lane, 8);
-    halve<2>(v, lane, 4);
-    halve<1>(v, lane, 2);
-    v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
-    // lane now holds value q = 4 i + c with q's bits = lane bits 4..1
-    const int q = ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 +
-                  ((lane >> 1) & 1);
-    const int i = q >> 2, c = q & 3;
-    if ((lane & 1) == 0 && c < NR && r0 + i < n)
+    // Halving: after the step with lane bit s, a lane keeps the half of its
+    // values selected by that bit. The value index q = i CW + c ends up with
+    // its top bit chosen by lane bit 16, the next by lane bit 8, and so on.
+    if constexpr (V == 16) halve<8>(v, lane, 16);
+    if constexpr (V >= 8) halve<4>(v, lane, V == 16 ? 8 : 16);
+    halve<2>(v, lane, V == 16 ? 4 : (V == 8 ? 8 : 16));
+    halve<1>(v, lane, V == 16 ? 2 : (V == 8 ? 4 : 8));
+    // Butterfly over the lane bits below the ones used for halving.
+    constexpr int LB = V == 16 ? 4 : (V == 8 ? 3 : 2);  // lane bits used by halving
+#pragma unroll
+    for (int s = (16 >> LB); s >= 1; s >>= 1) v[0] += __shfl_xor_sync(0xffffffffu, v[0], s);
+    // q's bits (most significant first) are lane bits 16, 8, ... (LB of them).
+    int q = 0;
+#pragma unroll
+    for (int t = 0; t < LB; t++) q = q * 2 + ((lane >> (4 - t)) & 1);
+    const int i = q / CW, c = q % CW;
+    const bool leader = (lane & ((32 >> LB) - 1)) == 0;
+    if (leader && c < NR && r0 + i < n)
       Ri[(size_t)(r0 + i) * NR + c] = MV ? v[0] : Bi[(size_t)(r0 + i) * NR + c] - v[0];
   }
 }
@@ -683,43 +713,63 @@ __device__ void process_system(const BatchArgs& a, int sidx, const SysDesc& d, S
   if (tid == 0) pc.start();
   unsigned long long* const phase = a.phase + (a.only_flagged ? 4 : 0);
 
-  // Storage scale (a power of two): the largest |a_ij| goes to 16 for FP8, so
-  // the factors (|l| <= 1, modest growth in U) stay inside e4m3's range.
+  // Storage scale (a power of two): the largest finite |a_ij| goes to 16 for
+  // FP8, so the factors (|l| <= 1, modest growth in U) stay inside e4m3's
+  // range. The maximum is taken on the magnitudes' bit patterns (integer
+  // instructions: the FP64 pipe is GB300's scarcest unit).
   if (tid == 0) { sh.norm[0] = 0.0; sh.norm[13] = 0.0; }
   __syncthreads();
   float scale = 1.f;
   if (sizeof(S) == 1) {
-    double m = 0.0;
-    for (int idx = tid; idx < n * n; idx += BT) m = fmax(m, fabs(Ai[idx]));
-    for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, off));
-    if ((tid & 31) == 0) amax_pos(&sh.norm[13], m);
+    unsigned long long m = 0ull;
+    for (int idx = tid; idx < n * n; idx += BT) {
+      const unsigned long long a = la_absbits_f64(Ai[idx]);
+      if (a < 0x7ff0000000000000ull && a > m) m = a;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      const unsigned long long o = __shfl_down_sync(0xffffffffu, m, off);
+      m = o > m ? o : m;
+    }
+    if ((tid & 31) == 0) atomicMax(reinterpret_cast<unsigned long long*>(&sh.norm[13]), m);
     __syncthreads();
-    int e = 0;
-    if (sh.norm[13] > 0.0 && sh.norm[13] < INFINITY) {
-      frexp(sh.norm[13], &e);
-      scale = ldexpf(1.f, 4 - e);
+    const unsigned long long mb = reinterpret_cast<const unsigned long long&>(sh.norm[13]);
+    if (mb > 0ull) {
+      // 2^(4 - e) with mb = 0.f * 2^e (0.5 <= f < 1), from the biased
+      // exponent; subnormal maxima (e <= -1022) clamp to the FP32 range.
+      const int e = (int)(mb >> 52) - 1022;
+      scale = ldexpf(1.f, max(-126, min(127, 4 - e)));
     }
   }
-  // Load A_i (one warp per row, coalesced) in the storage type; the mixed pass
-  // also takes ||A||_inf (largest row sum of |a_ij|) on the way.
+  // Load A_i (one warp per row, coalesced) in the storage type. The low
+  // precisions convert with integer instructions (la_f64_to_f32), and the
+  // mixed pass takes ||A||_inf (largest row sum of |a_ij|) in FP32 on the way:
+  // each row sum is a lower bound of the exact one after the factor
+  // (1 - 2^-19), which covers the conversion and FP32 summation errors, so the
+  // backward error computed with it never understates the exact one.
   {
     const int lane = tid & 31, warp = tid >> 5;
-    double rmax = 0.0;
+    float rmax = 0.f;
     for (int r = warp; r < n; r += NW) {
       const double* ar = Ai + (size_t)r * n;
       S* mr = M + (size_t)r * n;
-      double rs = 0.0;
+      float rs = 0.f;
       for (int k = lane; k < n; k += 32) {
-        const double v = ar[k];
-        if (MIXED) rs += fabs(v);
-        mr[k] = P::cv((R)(v * (double)scale));
+        if constexpr (sizeof(S) == 8) {
+          mr[k] = ar[k];
+        } else {
+          float v = la_f64_to_f32(ar[k]);
+          if (MIXED) rs += fabsf(v);
+          if (sizeof(S) == 1) v *= scale;
+          mr[k] = P::cv(v);
+        }
       }
       if (MIXED) {
         for (int off = 16; off > 0; off >>= 1) rs += __shfl_xor_sync(0xffffffffu, rs, off);
-        rmax = fmax(rmax, rs);
+        rmax = fmaxf(rmax, rs);
       }
     }
-    if (MIXED && lane == 0) amax_pos(&sh.norm[0], rmax);
+    if (MIXED && lane == 0)
+      amax_pos(&sh.norm[0], la_f32_to_f64(rmax) * (1.0 - 0x1p-19));
   }
   __syncthreads();
   if (tid == 0) pc.mark(0);
@@ -768,7 +818,7 @@ __device__ void process_system(const BatchArgs& a, int sidx, const SysDesc& d, S
       for (int idx = tid; idx < n * nrhs; idx += BT) {
         const int i = idx / nrhs, c = idx - i * nrhs;
         const double ic = c == 0 ? inv[0] : c == 1 ? inv[1] : c == 2 ? inv[2] : inv[3];
-        dv[idx] = (float)(rv[(size_t)rmap[i] * nrhs + c] * ic);
+        dv[idx] = la_f64_to_f32(rv[(size_t)rmap[i] * nrhs + c] * ic);
       }
     }
     __syncthreads();
@@ -777,7 +827,7 @@ __device__ void process_system(const BatchArgs& a, int sidx, const SysDesc& d, S
     if (tid == 0) pc.mark(2);
     // (scale A) d = r / rmax  =>  A (scale d rmax) = r
     for (int idx = tid; idx < n * nrhs; idx += BT)
-      xv[idx] += (double)dv[idx] * sh.norm[1 + idx % nrhs] * (double)scale;
+      xv[idx] = fma(la_f32_to_f64(dv[idx]), sh.norm[1 + idx % nrhs] * (double)scale, xv[idx]);
     __syncthreads();
     residual_all(Ai, n, nrhs, xv, Bi, Xi);
     rv = Xi;

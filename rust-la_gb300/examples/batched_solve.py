@@ -1,10 +1,13 @@
 """Example: batched uneven solves through a captured plan.
 
-    python rust-la_gb300/examples/batched_solve.py [count] [mode]
+    python rust-la_gb300/examples/batched_solve.py [count] [mode] [ctas_per_sm warps_per_system]
 
 count systems (default 20000) with n uniform in [8, 256] and 1-4 right-hand
 sides; A iid N(0,1), plus 0.5 n I on even-indexed systems (seed 4). mode 0 =
-plain FP64, 1 = FP32 + FP64 refinement (default both). Prints solves/s.
+plain FP64, 1 = FP32 + FP64 refinement (default both). The plan shape is
+autotuned unless ctas_per_sm and warps_per_system are given (then the plan
+runs once while it is built and five times from its graph, which keeps the
+launch sequence short for a profiler). Prints solves/s.
 """
 import os
 import sys
@@ -41,9 +44,13 @@ def main():
     da = torch.from_numpy(a).cuda()
     db = torch.from_numpy(b).cuda()
     dx = torch.zeros_like(db)
+    fixed = (int(sys.argv[3]), int(sys.argv[4])) if len(sys.argv) > 4 else None
     for mode in modes:
-        best, warps, ms = la_gpu.batch_autotune(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(),
-                                                systems, mode)
+        if fixed:
+            best, warps = fixed
+        else:
+            best, warps, _ = la_gpu.batch_autotune(ctx, da.data_ptr(), db.data_ptr(),
+                                                   dx.data_ptr(), systems, mode)
         plan = la_gpu.BatchPlan(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems, mode,
                                 ctas_per_sm=best, warps_per_system=warps)
         torch.cuda.synchronize()
