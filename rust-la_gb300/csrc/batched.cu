@@ -106,8 +106,10 @@ __device__ __forceinline__ bool bbetter(unsigned long long ka, int pa, unsigned 
 }
 
 struct Shared {
-  unsigned long long rk[NW_MAX];
-  int rp[NW_MAX];
+  // per-warp pivot candidates (key, logical position, staged row), by column parity
+  unsigned long long rk[2][NW_MAX];
+  int rp[2][NW_MAX];
+  int rs[2][NW_MAX];
   // [0] ||A||_inf, [1 + c] max |r_c|, [5 + c] max |x_c|, [9 + c] max |b_c|,
   // [13] max |a_ij| (FP8 scaling)
   double norm[14];
@@ -130,8 +132,8 @@ __host__ __device__ Lay lay(int n, int nrhs, bool resident, bool mixed) {
   o += al16((size_t)n * SP * sizeof(R));
   L.us = o;
   o += al16((size_t)PBW * n * sizeof(R));
-  L.rmap = o;
-  o += al16((size_t)n * sizeof(int));
+  L.rmap = o;  // rmap, then the panel's perm and spos (block_lu)
+  o += al16((size_t)3 * n * sizeof(int));
   L.x = o;
   o += al16((size_t)n * nrhs * sizeof(double));
   L.d = o;
@@ -144,13 +146,13 @@ __host__ __device__ Lay lay(int n, int nrhs, bool resident, bool mixed) {
 
 // A22 -= L21 U12 for the trailing nr x nr block (logical rows/columns >= j1):
 // warp w, lane l computes rows rb + w + NW t (t < TR) and columns
-// cb + l + 32 q (q < QN), with its L21 rows (staged rows PBW + i) in
+// cb + l + 32 q (q < QN), with its L21 rows (staged rows perm[PBW + i]) in
 // registers; all loads of a tile are issued before its FMAs. QN is picked
 // from nr so that narrow trailing blocks do not run idle columns.
 template <typename P, int TR, int QN>
 __device__ __forceinline__ void trailing_update(typename P::S* M, int p, const int* rmap, int j1,
                                                 int nr, const typename P::R* st,
-                                                const typename P::R* us) {
+                                                const typename P::R* us, const int* perm) {
   const int BT = blockDim.x, NW = BT >> 5;
   using S = typename P::S;
   using R = typename P::R;
@@ -163,8 +165,9 @@ __device__ __forceinline__ void trailing_update(typename P::S* M, int p, const i
       const int i = rb + warp + NW * t;
       const bool ok = i < nr;
       crow[t] = ok ? M + (size_t)rmap[j1 + i] * p + j1 : nullptr;
+      const R* lrow = ok ? st + perm[PBW + i] * SP : st;
 #pragma unroll
-      for (int k = 0; k < PBW; k++) lr[t][k] = ok ? st[(PBW + i) * SP + k] : R(0);
+      for (int k = 0; k < PBW; k++) lr[t][k] = ok ? lrow[k] : R(0);
     }
     for (int cb = 0; cb < nr; cb += 32 * QN) {
       R acc[TR][QN];
@@ -202,11 +205,19 @@ __device__ __forceinline__ void trailing_update(typename P::S* M, int p, const i
 // Blocked right-looking LU with partial pivoting of M (n x n, pitch p, rows
 // addressed through rmap: logical row i is physical row rmap[i]). On return
 // rmap[i] = the original row now at position i (the reference's piv).
-//   panel : columns [j0, j1) of logical rows >= j0 staged in st (pitch SP);
-//           thread t owns staged rows t, t + BT; per column: pivot search
-//           over own rows, barrier, swap (two staged rows, two map entries),
-//           barrier, scale + rank-1 update of own rows (a thread then reads
-//           only its own rows until the next barrier).
+//   panel : columns [j0, j1) of logical rows >= j0 staged in st (pitch SP).
+//           Staged rows never move: perm[r] is the staged row at logical
+//           position j0 + r and spos[s] the logical position (relative to j0)
+//           of staged row s. Thread t owns staged rows t, t + BT, ... Per
+//           column jj: pivot search over own rows still at positions >= jj
+//           (the reference's first-maximum rule, ties to the lowest logical
+//           position, lu.rs:132-137), one barrier, then every thread picks the
+//           winner from the warps' candidates, reads the pivot row in place,
+//           and scales and updates its own rows; the row that was at position
+//           jj takes the winner's position. Only thread 0 touches perm and
+//           rmap, and the pivot row is never written after it is chosen, so
+//           one barrier per column suffices (the candidate slots are
+//           double-buffered by column parity).
 //   U12   : rows [j0, j1), columns >= j1, each column solved in registers.
 //   A22  -= L21 U12 (trailing_update).
 // Values written back to M are rounded to the storage type, and the staged
@@ -219,6 +230,8 @@ __device__ void block_lu(typename P::S* M, int p, int n, int* rmap, typename P::
   using R = typename P::R;
   constexpr int TR = 2;  // rows per thread in the A22 tile
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  int* perm = rmap + n;
+  int* spos = rmap + 2 * n;
   for (int i = tid; i < n; i += BT) rmap[i] = i;
   __syncthreads();
   for (int j0 = 0; j0 < n; j0 += PBW) {
@@ -227,56 +240,74 @@ __device__ void block_lu(typename P::S* M, int p, int n, int* rmap, typename P::
       const int r = idx / jb, c = idx - r * jb;
       st[r * SP + c] = P::ld(&M[(size_t)rmap[j0 + r] * p + j0 + c]);
     }
+    for (int r = tid; r < prow; r += BT) {
+      perm[r] = r;
+      spos[r] = r;
+    }
     __syncthreads();
     for (int jj = 0; jj < jb; jj++) {
+      const int par = jj & 1;
       unsigned long long bk = 0ull;
-      int bp = -1;
-      for (int r = tid; r < prow; r += BT)
-        if (r >= jj) {
-          const unsigned long long k = bkey<R>(st[r * SP + jj], r, jj);
-          if (bbetter(k, r, bk, bp)) { bk = k; bp = r; }
+      int bp = -1, bs = -1;
+      for (int s = tid; s < prow; s += BT) {
+        const int ps = spos[s];
+        if (ps >= jj) {
+          const unsigned long long k = bkey<R>(st[s * SP + jj], ps, jj);
+          if (bbetter(k, ps, bk, bp)) { bk = k; bp = ps; bs = s; }
         }
+      }
       for (int off = 16; off > 0; off >>= 1) {
         const unsigned long long ok = __shfl_down_sync(0xffffffffu, bk, off);
         const int op = __shfl_down_sync(0xffffffffu, bp, off);
-        if (bbetter(ok, op, bk, bp)) { bk = ok; bp = op; }
+        const int os = __shfl_down_sync(0xffffffffu, bs, off);
+        if (bbetter(ok, op, bk, bp)) { bk = ok; bp = op; bs = os; }
       }
-      if (lane == 0) { sh.rk[warp] = bk; sh.rp[warp] = bp; }
+      if (lane == 0) { sh.rk[par][warp] = bk; sh.rp[par][warp] = bp; sh.rs[par][warp] = bs; }
       __syncthreads();
-      bk = sh.rk[0];
-      bp = sh.rp[0];
-#pragma unroll
+      bk = sh.rk[par][0];
+      bp = sh.rp[par][0];
+      bs = sh.rs[par][0];
       for (int w = 1; w < NW; w++)
-        if (bbetter(sh.rk[w], sh.rp[w], bk, bp)) { bk = sh.rk[w]; bp = sh.rp[w]; }
-      if (bp != jj) {  // bp >= jj: row jj itself always has a key
-        if (tid < jb) {
-          const R t = st[jj * SP + tid];
-          st[jj * SP + tid] = st[bp * SP + tid];
-          st[bp * SP + tid] = t;
+        if (bbetter(sh.rk[par][w], sh.rp[par][w], bk, bp)) {
+          bk = sh.rk[par][w]; bp = sh.rp[par][w]; bs = sh.rs[par][w];
         }
-        if (tid == 0) {
-          const int t = rmap[j0 + jj];
-          rmap[j0 + jj] = rmap[j0 + bp];
-          rmap[j0 + bp] = t;
-        }
-      }
-      __syncthreads();
-      const R d = st[jj * SP + jj];
+      // bp >= jj: the row at position jj always has a key.
+      const R* prow_v = st + bs * SP;
+      const R d = prow_v[jj];
       const R sc = d != R(0) ? R(1) / d : R(1);
-      for (int r = tid; r < prow; r += BT)
-        if (r > jj) {
-          R* row = st + r * SP;
+      for (int s = tid; s < prow; s += BT) {
+        int ps = spos[s];
+        if (s == bs) {
+          spos[s] = jj;
+          continue;
+        }
+        if (ps == jj) {  // the row displaced from position jj goes to bp
+          ps = bp;
+          spos[s] = bp;
+        }
+        if (ps > jj) {
+          R* row = st + s * SP;
           const R l = d != R(0) ? row[jj] * sc : row[jj];
           row[jj] = l;
-          for (int c = jj + 1; c < jb; c++) row[c] = fma(-l, st[jj * SP + c], row[c]);
+          for (int c = jj + 1; c < jb; c++) row[c] = fma(-l, prow_v[c], row[c]);
         }
+      }
+      if (tid == 0 && bp != jj) {
+        const int t = perm[jj];
+        perm[jj] = perm[bp];
+        perm[bp] = t;
+        const int u = rmap[j0 + jj];
+        rmap[j0 + jj] = rmap[j0 + bp];
+        rmap[j0 + bp] = u;
+      }
     }
     __syncthreads();
     for (int idx = tid; idx < prow * jb; idx += BT) {
       const int r = idx / jb, c = idx - r * jb;
-      const S v = P::cv(st[r * SP + c]);
+      R* sv = st + perm[r] * SP + c;
+      const S v = P::cv(*sv);
       M[(size_t)rmap[j0 + r] * p + j0 + c] = v;
-      st[r * SP + c] = P::up(v);
+      *sv = P::up(v);
     }
     if (j1 >= n) break;  // uniform; jb == PBW below
     const int nr = n - j1;
@@ -285,27 +316,32 @@ __device__ void block_lu(typename P::S* M, int p, int n, int* rmap, typename P::
       us[k * nr + c] = P::ld(&M[(size_t)rmap[j0 + k] * p + j1 + c]);
     }
     __syncthreads();
-    for (int c = tid; c < nr; c += BT) {
-      R u[PBW];
+    {
+      const R* l11[PBW];
 #pragma unroll
-      for (int k = 0; k < PBW; k++) u[k] = us[k * nr + c];
+      for (int i = 0; i < PBW; i++) l11[i] = st + perm[i] * SP;
+      for (int c = tid; c < nr; c += BT) {
+        R u[PBW];
 #pragma unroll
-      for (int k = 0; k < PBW; k++)
+        for (int k = 0; k < PBW; k++) u[k] = us[k * nr + c];
 #pragma unroll
-        for (int i = k + 1; i < PBW; i++) u[i] = fma(-st[i * SP + k], u[k], u[i]);
+        for (int k = 0; k < PBW; k++)
 #pragma unroll
-      for (int k = 0; k < PBW; k++) {
-        const S v = P::cv(u[k]);
-        M[(size_t)rmap[j0 + k] * p + j1 + c] = v;
-        us[k * nr + c] = P::up(v);
+          for (int i = k + 1; i < PBW; i++) u[i] = fma(-l11[i][k], u[k], u[i]);
+#pragma unroll
+        for (int k = 0; k < PBW; k++) {
+          const S v = P::cv(u[k]);
+          M[(size_t)rmap[j0 + k] * p + j1 + c] = v;
+          us[k * nr + c] = P::up(v);
+        }
       }
     }
     __syncthreads();
     switch (min(4, (nr + 31) / 32)) {
-      case 1: trailing_update<P, TR, 1>(M, p, rmap, j1, nr, st, us); break;
-      case 2: trailing_update<P, TR, 2>(M, p, rmap, j1, nr, st, us); break;
-      case 3: trailing_update<P, TR, 3>(M, p, rmap, j1, nr, st, us); break;
-      default: trailing_update<P, TR, 4>(M, p, rmap, j1, nr, st, us); break;
+      case 1: trailing_update<P, TR, 1>(M, p, rmap, j1, nr, st, us, perm); break;
+      case 2: trailing_update<P, TR, 2>(M, p, rmap, j1, nr, st, us, perm); break;
+      case 3: trailing_update<P, TR, 3>(M, p, rmap, j1, nr, st, us, perm); break;
+      default: trailing_update<P, TR, 4>(M, p, rmap, j1, nr, st, us, perm); break;
     }
     __syncthreads();
   }
@@ -753,14 +789,27 @@ __device__ void process_system(const BatchArgs& a, int sidx, const SysDesc& d, S
       const double* ar = Ai + (size_t)r * n;
       S* mr = M + (size_t)r * n;
       float rs = 0.f;
-      for (int k = lane; k < n; k += 32) {
-        if constexpr (sizeof(S) == 8) {
-          mr[k] = ar[k];
-        } else {
-          float v = la_f64_to_f32(ar[k]);
-          if (MIXED) rs += fabsf(v);
-          if (sizeof(S) == 1) v *= scale;
-          mr[k] = P::cv(v);
+      // Eight loads per lane are issued before any conversion or store.
+      for (int k0 = 0; k0 < n; k0 += 256) {
+        double v8[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          const int k = k0 + lane + 32 * q;
+          v8[q] = k < n ? __ldg(ar + k) : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          const int k = k0 + lane + 32 * q;
+          if (k < n) {
+            if constexpr (sizeof(S) == 8) {
+              mr[k] = v8[q];
+            } else {
+              float v = la_f64_to_f32(v8[q]);
+              if (MIXED) rs += fabsf(v);
+              if (sizeof(S) == 1) v *= scale;
+              mr[k] = P::cv(v);
+            }
+          }
         }
       }
       if (MIXED) {
@@ -938,7 +987,14 @@ namespace {
 
 template <bool MIXED>
 la_status set_kernel_smem(la_ctx ctx) {
-  cudaError_t e = cudaFuncSetAttribute(batched_kernel<MIXED>,
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, batched_kernel<MIXED>);
+  if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaFuncGetAttributes(batched)");
+  if (fa.sharedSizeBytes > BATCH_STATIC_SMEM) {
+    ctx->last_error = "batched_kernel static shared memory exceeds its reserved bound";
+    return LA_UNSUPPORTED;
+  }
+  e = cudaFuncSetAttribute(batched_kernel<MIXED>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)(ctx->smem_optin - BATCH_STATIC_SMEM));
   return e == cudaSuccess ? LA_OK : la_cuda_fail(ctx, e, "cudaFuncSetAttribute(batched)");
@@ -1036,8 +1092,9 @@ la_status la_batch_plan_create(la_ctx ctx, const double* d_a, const double* d_b,
   const size_t budget =
       std::min(optin, (size_t)(228 * 1024) / ctas_per_sm - 1024 - BATCH_STATIC_SMEM);
   const int threads = 32 * warps_per_system;
-  const size_t need = mode == LA_BATCH_FP64 ? lay<double, double>(nmax, 4, false, false).total
-                                            : lay<float, float>(nmax, 4, false, true).total;
+  const size_t need = mode == LA_BATCH_FP64
+                          ? lay<double, double>(nmax, 4, false, false).total
+                          : lay<float, float>(nmax, 4, false, true).total;
   if (budget < need) return LA_UNSUPPORTED;
   if (lay<double, double>(NMAX, 4, false, false).total > optin) return LA_UNSUPPORTED;
   const int fit = mode == LA_BATCH_FP64 ? resident_ctas<false>(threads, budget)
