@@ -13,6 +13,7 @@
 // conditioned training and test systems A = H1 diag(s) H2 on the device.
 #include <new>
 
+#include "f64conv.h"
 #include "la_internal.cuh"
 
 namespace {
@@ -110,63 +111,102 @@ gen_hh_kernel(const SysRec* __restrict__ sys, int count, double* A, double* B, d
 }
 
 // ---- features -----------------------------------------------------------------
-__device__ double block_sum(double v, double* red) {
+// Sum of v over the CTA with one barrier: warp sums go to red[par][warp],
+// the slots alternating between calls (par flips on every call, in every
+// thread alike), so a slot is rewritten only two calls later, after a barrier
+// that every reader of its previous contents has passed.
+__device__ double block_sum(double v, double (*red)[8], int& par) {
   for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  double t = 0.0;
-  for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
-  __syncthreads();
-  return t;
-}
-__device__ double block_max(double v, double* red) {
-  for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, off));
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  if ((threadIdx.x & 31) == 0) red[par][threadIdx.x >> 5] = v;
   __syncthreads();
   double t = 0.0;
-  for (int w = 0; w < (int)(blockDim.x >> 5); w++) t = fmax(t, red[w]);
-  __syncthreads();
-  return t;
-}
-__device__ double block_min(double v, double* red) {
-  for (int off = 16; off > 0; off >>= 1) v = fmin(v, __shfl_down_sync(0xffffffffu, v, off));
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  double t = INFINITY;
-  for (int w = 0; w < (int)(blockDim.x >> 5); w++) t = fmin(t, red[w]);
-  __syncthreads();
+  for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[par][w];
+  par ^= 1;
   return t;
 }
 
-__device__ __forceinline__ float lg(double x) { return (float)log10(fmax(x, 1e-300)); }
-
-// Smallest eigenvalue of the symmetric tridiagonal (alpha, beta) of order k
-// by bisection on the Sturm count.
-__device__ double tridiag_min_eig(const double* al, const double* be, int k) {
-  double lo = INFINITY, hi = -INFINITY;
-  for (int i = 0; i < k; i++) {
-    const double r = (i > 0 ? fabs(be[i - 1]) : 0.0) + (i + 1 < k ? fabs(be[i]) : 0.0);
-    lo = fmin(lo, al[i] - r);
-    hi = fmax(hi, al[i] + r);
-  }
-  for (int it = 0; it < 80; it++) {
-    const double mid = 0.5 * (lo + hi);
-    int cnt = 0;
-    double q = al[0] - mid;
-    if (q < 0) cnt++;
-    for (int i = 1; i < k; i++) {
-      q = al[i] - mid - be[i - 1] * be[i - 1] / (q != 0.0 ? q : 1e-300);
-      if (q < 0) cnt++;
-    }
-    if (cnt >= 1) hi = mid; else lo = mid;
-  }
-  return 0.5 * (lo + hi);
+// log10(max(x, 1e-300)) as a float, from the binary exponent and an FP32 log2
+// of the mantissa (x = m 2^e, 1 <= m < 2): the feature is FP32 anyway, and a
+// double-precision log10 would occupy GB300's slow FP64 pipe.
+__device__ __forceinline__ float lg(double x) {
+  x = fmax(x, 1e-300);
+  const uint64_t b = la_bits_f64(x);
+  const int eb = (int)((b >> 52) & 0x7ff);
+  if (eb == 0 || eb == 0x7ff) return (float)log10(x);  // subnormal, infinity, NaN
+  const float m = la_f64_to_f32(la_f64_from_bits((b & 0x000fffffffffffffull) |
+                                                 0x3ff0000000000000ull));
+  return ((float)(eb - 1023) + log2f(m)) * 0.30102999566398120f;
 }
 
 constexpr int LK = 4;  // Lanczos steps
+
+// Smallest eigenvalue of the symmetric tridiagonal (alpha, beta) of order
+// k <= LK, computed by one full warp (every lane returns it). Multisection on
+// the Gershgorin interval: per round, lane l counts the eigenvalues below
+// x_l = lo + (hi - lo) (l + 1) / 33 with the division-free Sturm sequence
+// p_0 = 1, p_i = (alpha_i - x) p_(i-1) - beta_(i-1)^2 p_(i-2) (the count is
+// the number of sign changes; the values stay far inside the FP64 range for
+// k <= 4), and a ballot keeps the sub-interval where the count first reaches
+// one. Sixteen rounds shrink the interval by 33^16 > 2^80, the resolution of
+// 80 bisection steps, with 32 times fewer dependent FP64 operations.
+__device__ double tridiag_min_eig_warp(const double* al, const double* be, int k, double sgn) {
+  const int lane = threadIdx.x & 31;
+  // the tridiagonal sgn * T in registers (compile-time indices, k <= LK)
+  double as[LK], bb[LK];
+#pragma unroll
+  for (int i = 0; i < LK; i++) {
+    as[i] = i < k ? sgn * al[i] : 0.0;
+    bb[i] = i + 1 < k ? be[i] : 0.0;
+  }
+  double lo = INFINITY, hi = -INFINITY;
+#pragma unroll
+  for (int i = 0; i < LK; i++)
+    if (i < k) {
+      const double r = (i > 0 ? fabs(bb[i - 1]) : 0.0) + fabs(bb[i]);
+      lo = fmin(lo, as[i] - r);
+      hi = fmax(hi, as[i] + r);
+    }
+  // Work on T / 2^s with 2^s >= the Gershgorin bound (exact scaling), so the
+  // Sturm values stay below 3^k in magnitude whatever the scale of T.
+  const double gb = fmax(fabs(lo), fabs(hi));
+  int sexp = 0;
+  if (gb > 0.0 && gb < INFINITY) frexp(gb, &sexp);
+  double bs2[LK];
+#pragma unroll
+  for (int i = 0; i < LK; i++) {
+    as[i] = ldexp(as[i], -sexp);
+    const double t = ldexp(bb[i], -sexp);
+    bs2[i] = t * t;
+  }
+  lo = ldexp(lo, -sexp);
+  hi = ldexp(hi, -sexp);
+  for (int round = 0; round < 16; round++) {
+    const double x = lo + (hi - lo) * ((double)(lane + 1) / 33.0);
+    double pm2 = 1.0, pm1 = as[0] - x;
+    int cnt = pm1 < 0.0 ? 1 : 0;
+#pragma unroll
+    for (int i = 1; i < LK; i++)
+      if (i < k) {
+        const double pi = (as[i] - x) * pm1 - bs2[i - 1] * pm2;
+        if ((pi < 0.0) != (pm1 < 0.0)) cnt++;
+        pm2 = pm1;
+        pm1 = pi;
+      }
+    const unsigned mask = __ballot_sync(0xffffffffu, cnt >= 1);
+    const double xl = lo + (hi - lo) * ((double)lane / 33.0);  // lane's left end
+    if (mask) {
+      const int f = __ffs(mask) - 1;
+      const double nlo = __shfl_sync(0xffffffffu, xl, f);
+      const double nhi = __shfl_sync(0xffffffffu, x, f);
+      lo = nlo;
+      hi = nhi;
+    } else {
+      lo = __shfl_sync(0xffffffffu, x, 31);
+    }
+  }
+  return ldexp(0.5 * (lo + hi), sexp);
+}
+
 constexpr int FEAT_CTAS_PER_SM = 2;
 
 // 16 features per system (one CTA per system). FP64 arithmetic is slow on
@@ -185,12 +225,17 @@ constexpr int FEAT_CTAS_PER_SM = 2;
 __global__ void __launch_bounds__(256)
 features_kernel(const double* __restrict__ A, const SysRec* __restrict__ sys, int count,
                 float* __restrict__ F, float* __restrict__ scratch) {
-  __shared__ double red[8];
+  __shared__ double red[2][8];
+  int rpar = 0;
   __shared__ float q[LK + 1][512];
   __shared__ float t1[512];
   __shared__ float t2[512];
   __shared__ float part[8][512];  // per-warp column partial sums
   __shared__ double al[LK], be[LK];
+  __shared__ float finf[8][7];   // per-warp extrema
+  __shared__ double find[8][5];  // per-warp sums
+  __shared__ float totf[7];      // combined extrema
+  __shared__ double totd[7];     // combined sums, then the extreme Ritz values
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int NWp = blockDim.x >> 5;
   float* af = scratch + (size_t)blockIdx.x * 512 * 512;
@@ -204,7 +249,7 @@ features_kernel(const double* __restrict__ A, const SysRec* __restrict__ sys, in
       q[0][k] = v;
       nrm += (double)v * v;
     }
-    nrm = sqrt(block_sum(nrm, red));
+    nrm = sqrt(block_sum(nrm, red, rpar));
     for (int k = tid; k < n; k += blockDim.x) q[0][k] = (float)(q[0][k] / nrm);
     __syncthreads();
     float rmax = 0, rmin = INFINITY, dmin = INFINITY, amax = 0, diag_min = INFINITY, cmax = 0,
@@ -221,7 +266,7 @@ features_kernel(const double* __restrict__ A, const SysRec* __restrict__ sys, in
 #pragma unroll
         for (int m = 0; m < 16; m++) {
           const int k = lane + 32 * m;
-          if (j == 0) x[m] = k < n ? (float)a[(size_t)r * n + k] : 0.f;
+          if (j == 0) x[m] = k < n ? la_f64_to_f32(a[(size_t)r * n + k]) : 0.f;
           else x[m] = k < n ? fr[k] : 0.f;
         }
         float s = 0, rs = 0, f2 = 0, am = 0;
@@ -258,7 +303,7 @@ features_kernel(const double* __restrict__ A, const SysRec* __restrict__ sys, in
         if (lane == 0) {
           t1[r] = s;
           if (j == 0) {
-            const float di = fabsf((float)a[(size_t)r * n + r]);
+            const float di = fabsf(la_f64_to_f32(a[(size_t)r * n + r]));
             const float off = rs - di;
             fro += f2;
             amax = fmaxf(amax, am);
@@ -302,46 +347,87 @@ features_kernel(const double* __restrict__ A, const SysRec* __restrict__ sys, in
         for (int c = tid; c < n; c += blockDim.x) {
           float t = 0.f;
           for (int w = 0; w < NWp; w++) t += part[w][c];
-          const double dd = (double)t1[c] - t;  // (A q0)_c - (A^T q0)_c
+          const double dd = la_f32_to_f64(t1[c]) - la_f32_to_f64(t);  // (A q0)_c - (A^T q0)_c
           asym += dd * dd;
-          aq += (double)t1[c] * t1[c];
+          aq = fma(la_f32_to_f64(t1[c]), la_f32_to_f64(t1[c]), aq);
         }
         __syncthreads();
       }
       double aj = 0;
-      for (int k = tid; k < n; k += blockDim.x) aj += (double)q[j][k] * t2[k];
-      aj = block_sum(aj, red);
+      for (int k = tid; k < n; k += blockDim.x)
+        aj = fma(la_f32_to_f64(q[j][k]), la_f32_to_f64(t2[k]), aj);
+      aj = block_sum(aj, red, rpar);
       for (int pq = 0; pq <= j; pq++) {  // full reorthogonalisation
         double c = 0;
-        for (int k = tid; k < n; k += blockDim.x) c += (double)q[pq][k] * t2[k];
-        c = block_sum(c, red);
-        for (int k = tid; k < n; k += blockDim.x) t2[k] = (float)(t2[k] - c * q[pq][k]);
-        __syncthreads();
+        for (int k = tid; k < n; k += blockDim.x)
+          c = fma(la_f32_to_f64(q[pq][k]), la_f32_to_f64(t2[k]), c);
+        c = block_sum(c, red, rpar);
+        // each thread updates and later reads only its own entries of t2
+        for (int k = tid; k < n; k += blockDim.x)
+          t2[k] = la_f64_to_f32(fma(-c, la_f32_to_f64(q[pq][k]), la_f32_to_f64(t2[k])));
       }
       double bj = 0;
-      for (int k = tid; k < n; k += blockDim.x) bj += (double)t2[k] * t2[k];
-      bj = sqrt(block_sum(bj, red));
+      for (int k = tid; k < n; k += blockDim.x)
+        bj = fma(la_f32_to_f64(t2[k]), la_f32_to_f64(t2[k]), bj);
+      bj = sqrt(block_sum(bj, red, rpar));
       if (tid == 0) { al[j] = aj; be[j] = bj; }
       kk = j + 1;
       if (!(bj > 1e-6 * fabs(aj)) || j + 1 >= LK) break;
-      for (int k = tid; k < n; k += blockDim.x) q[j + 1][k] = (float)(t2[k] / bj);
+      const double ibj = 1.0 / bj;
+      for (int k = tid; k < n; k += blockDim.x)
+        q[j + 1][k] = la_f64_to_f32(la_f32_to_f64(t2[k]) * ibj);
       __syncthreads();
     }
-    const double rmax_b = block_max(rmax, red), rmin_b = block_min(rmin, red);
-    const double dmin_b = block_min(dmin, red);
-    dsum = block_sum(dsum, red);
-    ddom = block_sum(ddom, red);
-    const double amax_b = block_max(amax, red);
-    fro = block_sum(fro, red);
-    const double diag_b = block_min(diag_min, red);
-    const double cmax_b = block_max(cmax, red), cmin_b = block_min(cmin, red);
-    asym = block_sum(asym, red);
-    aq = block_sum(aq, red);
+    // The twelve statistics: a warp reduction each, one barrier, then lane l
+    // of warp 0 combines statistic l over the warps.
+    {
+      // FP32 extrema (max: rmax, amax, cmax; min: rmin, dmin, diag_min, cmin)
+      // and FP64 sums (dsum, ddom, fro, asym, aq).
+      float v[7] = {rmax, amax, cmax, rmin, dmin, diag_min, cmin};
+      double w[5] = {dsum, ddom, fro, asym, aq};
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+        for (int t = 0; t < 3; t++) v[t] = fmaxf(v[t], __shfl_xor_sync(0xffffffffu, v[t], off));
+#pragma unroll
+        for (int t = 3; t < 7; t++) v[t] = fminf(v[t], __shfl_xor_sync(0xffffffffu, v[t], off));
+#pragma unroll
+        for (int t = 0; t < 5; t++) w[t] += __shfl_xor_sync(0xffffffffu, w[t], off);
+      }
+      if (lane == 0) {
+#pragma unroll
+        for (int t = 0; t < 7; t++) finf[warp][t] = v[t];
+#pragma unroll
+        for (int t = 0; t < 5; t++) find[warp][t] = w[t];
+      }
+      __syncthreads();
+      if (warp == 0) {
+        if (lane < 7) {
+          float acc = finf[0][lane];
+          for (int ww = 1; ww < NWp; ww++)
+            acc = lane < 3 ? fmaxf(acc, finf[ww][lane]) : fminf(acc, finf[ww][lane]);
+          totf[lane] = acc;
+        } else if (lane < 12) {
+          double acc = find[0][lane - 7];
+          for (int ww = 1; ww < NWp; ww++) acc += find[ww][lane - 7];
+          totd[lane - 7] = acc;
+        }
+        // extreme Ritz values of the Lanczos tridiagonal
+        const double emax = -tridiag_min_eig_warp(al, be, kk, -1.0);
+        const double emin = fmax(tridiag_min_eig_warp(al, be, kk, 1.0), emax * 1e-32);
+        if (lane == 0) { totd[5] = emax; totd[6] = emin; }
+      }
+      __syncthreads();
+    }
+    const double rmax_b = totf[0], amax_b = totf[1], cmax_b = totf[2];
+    const double rmin_b = totf[3], dmin_b = totf[4], diag_b = totf[5], cmin_b = totf[6];
+    dsum = totd[0];
+    ddom = totd[1];
+    fro = totd[2];
+    asym = totd[3];
+    aq = totd[4];
+    const double emax = totd[5], emin = totd[6];
     if (tid == 0) {
-      double nal[LK], nbe[LK];
-      for (int j = 0; j < kk; j++) { nal[j] = -al[j]; nbe[j] = be[j]; }
-      const double emax = -tridiag_min_eig(nal, nbe, kk);
-      const double emin = fmax(tridiag_min_eig(al, be, kk), emax * 1e-32);
       float* f = F + (size_t)i * NF;
       f[0] = (float)(log2((double)n) / 9.0);
       f[1] = (float)d.nrhs / 4.f;
