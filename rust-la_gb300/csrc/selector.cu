@@ -12,6 +12,7 @@
 // deterministic) and Adam. A generator kernel builds the Householder-
 // conditioned training and test systems A = H1 diag(s) H2 on the device.
 #include <new>
+#include <type_traits>
 
 #include "f64conv.h"
 #include "la_internal.cuh"
@@ -140,6 +141,128 @@ __device__ __forceinline__ float lg(double x) {
 
 constexpr int LK = 4;  // Lanczos steps
 
+struct RowStats {
+  float rmax, rmin, dmin, amax, diag_min;
+  double fro, dsum, ddom;
+};
+
+template <int PF>
+__device__ __forceinline__ void load_row_f64(double (&x)[PF], const double* __restrict__ row, int n,
+                                             int lane);
+__device__ __forceinline__ void load_row_f32(float (&x)[16], const float* row, int n, int lane);
+
+// One Lanczos pass over the rows of warp `warp` (rows warp, warp + NWp, ...):
+// t1[r] = a_r . qj and acc += a_r t1[r] (this lane's columns). FIRST: the rows
+// come from A in FP64 (converted to FP32 and stored in af), and the row and
+// column statistics of pass 0 are taken on the way. The next row's loads are
+// issued before the current row is reduced.
+template <bool FIRST>
+__device__ __forceinline__ void feature_rows(const double* __restrict__ a, float* af, int n,
+                                             const float* qj, const float* q0, float* t1,
+                                             float (&acc)[16], float (&cs)[16], float (&sq)[16],
+                                             RowStats& st, int warp, int lane, int NWp) {
+  // Prefetched slots per lane: all 16 from the FP32 copy; 8 (columns < 256)
+  // from A in FP64, whose wider raw values would not fit the register budget.
+  // The rest of a wider FP64 row is loaded when it is used.
+  constexpr int PF = FIRST ? 8 : 16;
+  using L = typename std::conditional<FIRST, double, float>::type;
+  L xn[PF];
+  if (warp < n) {
+    if constexpr (FIRST) load_row_f64<PF>(xn, a + (size_t)warp * n, n, lane);
+    else load_row_f32(xn, af + (size_t)warp * n, n, lane);
+  }
+  for (int r = warp; r < n; r += NWp) {
+    float x[16];
+#pragma unroll
+    for (int m = 0; m < 16; m++) {
+      if constexpr (FIRST) {
+        const int k = lane + 32 * m;
+        x[m] = m < PF ? la_f64_to_f32(xn[m < PF ? m : 0])
+                      : (k < n ? la_f64_to_f32(__ldg(a + (size_t)r * n + k)) : 0.f);
+      } else {
+        x[m] = xn[m];
+      }
+    }
+    if (r + NWp < n) {
+      if constexpr (FIRST) load_row_f64<PF>(xn, a + (size_t)(r + NWp) * n, n, lane);
+      else load_row_f32(xn, af + (size_t)(r + NWp) * n, n, lane);
+    }
+    float* fr = af + (size_t)r * n;
+    float s = 0, rs = 0, f2 = 0, am = 0;
+#pragma unroll
+    for (int m = 0; m < 16; m++) {
+      const int k = lane + 32 * m;
+      if (k < n) {
+        s = fmaf(x[m], qj[k], s);
+        if (FIRST) {
+          fr[k] = x[m];
+          rs += fabsf(x[m]);
+          f2 = fmaf(x[m], x[m], f2);
+          am = fmaxf(am, fabsf(x[m]));
+        }
+      }
+    }
+    float di = 0.f;
+    if (FIRST) {  // the diagonal a_rr: slot r / 32 of lane r % 32
+      float xdg = x[0];
+#pragma unroll
+      for (int m = 1; m < 16; m++) xdg = m == (r >> 5) ? x[m] : xdg;
+      di = fabsf(__shfl_sync(0xffffffffu, xdg, r & 31));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (FIRST) {
+        rs += __shfl_xor_sync(0xffffffffu, rs, o);
+        f2 += __shfl_xor_sync(0xffffffffu, f2, o);
+        am = fmaxf(am, __shfl_xor_sync(0xffffffffu, am, o));
+      }
+    }
+    const float q0r = q0[r];
+#pragma unroll
+    for (int m = 0; m < 16; m++) {
+      acc[m] = fmaf(x[m], s, acc[m]);
+      if (FIRST) {
+        cs[m] += fabsf(x[m]);
+        sq[m] = fmaf(x[m], q0r, sq[m]);
+      }
+    }
+    if (lane == 0) {
+      t1[r] = s;
+      if (FIRST) {
+        const float off = rs - di;
+        st.fro += f2;
+        st.amax = fmaxf(st.amax, am);
+        st.rmax = fmaxf(st.rmax, rs);
+        st.rmin = fminf(st.rmin, rs);
+        const float ratio = di / fmaxf(off, 1e-30f);
+        st.dmin = fminf(st.dmin, ratio);
+        st.dsum += log10f(fmaxf(ratio, 1e-30f));
+        st.ddom += ratio > 1.f ? 1.0 : 0.0;
+        st.diag_min = fminf(st.diag_min, di);
+      }
+    }
+  }
+}
+
+// A row's entries k = lane + 32 m (m < PF resp. 16, k < n; zero beyond n)
+// into registers, all loads issued before any is used.
+template <int PF>
+__device__ __forceinline__ void load_row_f64(double (&x)[PF], const double* __restrict__ row, int n,
+                                             int lane) {
+#pragma unroll
+  for (int m = 0; m < PF; m++) {
+    const int k = lane + 32 * m;
+    x[m] = k < n ? __ldg(row + k) : 0.0;
+  }
+}
+__device__ __forceinline__ void load_row_f32(float (&x)[16], const float* row, int n, int lane) {
+#pragma unroll
+  for (int m = 0; m < 16; m++) {
+    const int k = lane + 32 * m;
+    x[m] = k < n ? row[k] : 0.f;
+  }
+}
+
 // Smallest eigenvalue of the symmetric tridiagonal (alpha, beta) of order
 // k <= LK, computed by one full warp (every lane returns it). Multisection on
 // the Gershgorin interval: per round, lane l counts the eigenvalues below
@@ -222,7 +345,7 @@ constexpr int FEAT_CTAS_PER_SM = 2;
 // reorthogonalisation; the extreme Ritz values bound sigma_max^2 from below and
 // sigma_min^2 from above. The asymmetry feature is the probe
 // ||A q0 - A^T q0|| / ||A q0||.
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 2)
 features_kernel(const double* __restrict__ A, const SysRec* __restrict__ sys, int count,
                 float* __restrict__ F, float* __restrict__ scratch) {
   __shared__ double red[2][8];
@@ -252,71 +375,21 @@ features_kernel(const double* __restrict__ A, const SysRec* __restrict__ sys, in
     nrm = sqrt(block_sum(nrm, red, rpar));
     for (int k = tid; k < n; k += blockDim.x) q[0][k] = (float)(q[0][k] / nrm);
     __syncthreads();
-    float rmax = 0, rmin = INFINITY, dmin = INFINITY, amax = 0, diag_min = INFINITY, cmax = 0,
-          cmin = INFINITY;
-    double dsum = 0, ddom = 0, fro = 0, asym = 0, aq = 0;
+    RowStats st = {0.f, INFINITY, INFINITY, 0.f, INFINITY, 0.0, 0.0, 0.0};
+    float cmax = 0, cmin = INFINITY;
+    double asym = 0, aq = 0;
     int kk = 0;
     for (int j = 0; j < LK && j < n; j++) {
       float acc[16], cs[16], sq[16];
 #pragma unroll
       for (int m = 0; m < 16; m++) { acc[m] = 0.f; cs[m] = 0.f; sq[m] = 0.f; }
-      for (int r = warp; r < n; r += NWp) {
-        float x[16];
-        float* fr = af + (size_t)r * n;
-#pragma unroll
-        for (int m = 0; m < 16; m++) {
-          const int k = lane + 32 * m;
-          if (j == 0) x[m] = k < n ? la_f64_to_f32(a[(size_t)r * n + k]) : 0.f;
-          else x[m] = k < n ? fr[k] : 0.f;
-        }
-        float s = 0, rs = 0, f2 = 0, am = 0;
-#pragma unroll
-        for (int m = 0; m < 16; m++) {
-          const int k = lane + 32 * m;
-          if (k < n) {
-            s = fmaf(x[m], q[j][k], s);
-            if (j == 0) {
-              fr[k] = x[m];
-              rs += fabsf(x[m]);
-              f2 = fmaf(x[m], x[m], f2);
-              am = fmaxf(am, fabsf(x[m]));
-            }
-          }
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-          s += __shfl_xor_sync(0xffffffffu, s, o);
-          if (j == 0) {
-            rs += __shfl_xor_sync(0xffffffffu, rs, o);
-            f2 += __shfl_xor_sync(0xffffffffu, f2, o);
-            am = fmaxf(am, __shfl_xor_sync(0xffffffffu, am, o));
-          }
-        }
-        const float q0r = q[0][r];
-#pragma unroll
-        for (int m = 0; m < 16; m++) {
-          acc[m] = fmaf(x[m], s, acc[m]);
-          if (j == 0) {
-            cs[m] += fabsf(x[m]);
-            sq[m] = fmaf(x[m], q0r, sq[m]);
-          }
-        }
-        if (lane == 0) {
-          t1[r] = s;
-          if (j == 0) {
-            const float di = fabsf(la_f64_to_f32(a[(size_t)r * n + r]));
-            const float off = rs - di;
-            fro += f2;
-            amax = fmaxf(amax, am);
-            rmax = fmaxf(rmax, rs);
-            rmin = fminf(rmin, rs);
-            const float ratio = di / fmaxf(off, 1e-30f);
-            dmin = fminf(dmin, ratio);
-            dsum += log10f(fmaxf(ratio, 1e-30f));
-            ddom += ratio > 1.f ? 1.0 : 0.0;
-            diag_min = fminf(diag_min, di);
-          }
-        }
-      }
+      // Rows are software-pipelined per warp (feature_rows): the next row's
+      // loads are issued before the current row's reduction, so the memory
+      // latency overlaps the shuffles.
+      if (j == 0)
+        feature_rows<true>(a, af, n, q[0], q[0], t1, acc, cs, sq, st, warp, lane, NWp);
+      else
+        feature_rows<false>(a, af, n, q[j], q[0], t1, acc, cs, sq, st, warp, lane, NWp);
       // t2 = A^T t1: sum the warps' column partials
 #pragma unroll
       for (int m = 0; m < 16; m++)
@@ -383,8 +456,8 @@ features_kernel(const double* __restrict__ A, const SysRec* __restrict__ sys, in
     {
       // FP32 extrema (max: rmax, amax, cmax; min: rmin, dmin, diag_min, cmin)
       // and FP64 sums (dsum, ddom, fro, asym, aq).
-      float v[7] = {rmax, amax, cmax, rmin, dmin, diag_min, cmin};
-      double w[5] = {dsum, ddom, fro, asym, aq};
+      float v[7] = {st.rmax, st.amax, cmax, st.rmin, st.dmin, st.diag_min, cmin};
+      double w[5] = {st.dsum, st.ddom, st.fro, asym, aq};
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) {
 #pragma unroll
@@ -421,9 +494,7 @@ features_kernel(const double* __restrict__ A, const SysRec* __restrict__ sys, in
     }
     const double rmax_b = totf[0], amax_b = totf[1], cmax_b = totf[2];
     const double rmin_b = totf[3], dmin_b = totf[4], diag_b = totf[5], cmin_b = totf[6];
-    dsum = totd[0];
-    ddom = totd[1];
-    fro = totd[2];
+    const double dsum = totd[0], ddom = totd[1], fro = totd[2];
     asym = totd[3];
     aq = totd[4];
     const double emax = totd[5], emin = totd[6];
