@@ -15,6 +15,18 @@
 // One cluster barrier per column and no global-memory round trips; the FP32
 // update work per column is small. A last cluster barrier keeps every CTA's
 // shared memory alive until all remote reads are done.
+//
+// panel_cluster_reg_kernel (used when each thread holds at most 4 rows) keeps
+// the rows in registers instead: thread t of CTA g owns rows row0 + t + 256 q
+// with their 32 panel values and their current positions. Rows never move
+// between threads; a pivot exchange swaps two position registers, and each
+// row is written to its final position at the end. Per column: the warp's
+// best (key, position) is one 64-bit word (key high, bit-inverted position
+// low, so the integer maximum is the reference's first maximum), the winning
+// lane of each warp publishes its row, one CTA barrier, warp 0 publishes the
+// CTA's candidate and row, one cluster barrier, and then every warp reads the
+// C candidates and the winner's row over distributed shared memory and
+// scales and updates its rows in registers.
 #include "la_internal.cuh"
 
 namespace {
@@ -68,6 +80,33 @@ struct ClusterPanelArgs {
   int* ipiv;
   int* swaps;
 };
+
+// The panel's row moves as one list for the row-swap kernel: swaps[0] = k,
+// swaps[1 + i] = destination row, swaps[1 + 2 MAX_PANEL_W + i] = source row
+// (the composition of the swaps (j0 + c, pivs[c]), c < jb).
+__device__ void build_swap_list(const ClusterPanelArgs& p, const int* pivs) {
+  int cnt = 0;
+  int* dst = p.swaps + 1;
+  int* src = p.swaps + 1 + 2 * MAX_PANEL_W;
+  auto find_or_add = [&](int pos) {
+    for (int q = 0; q < cnt; q++)
+      if (dst[q] == pos) return q;
+    dst[cnt] = pos;
+    src[cnt] = pos;
+    return cnt++;
+  };
+  for (int c = 0; c < p.jb; c++) {
+    int a = find_or_add(p.j0 + c);
+    int b = find_or_add(pivs[c]);
+    int t = src[a];
+    src[a] = src[b];
+    src[b] = t;
+  }
+  int k = 0;
+  for (int q = 0; q < cnt; q++)
+    if (src[q] != dst[q]) { dst[k] = dst[q]; src[k] = src[q]; k++; }
+  p.swaps[0] = k;
+}
 
 __global__ void __launch_bounds__(CT, 1) panel_cluster_kernel(ClusterPanelArgs p) {
   extern __shared__ __align__(16) float csm[];
@@ -196,32 +235,223 @@ __global__ void __launch_bounds__(CT, 1) panel_cluster_kernel(ClusterPanelArgs p
     int r = idx / CW, c = idx % CW;
     if (c < jb) p.A[(size_t)(row0 + r) * p.ld + p.j0 + c] = va[r * CP + c];
   }
-  if (g == 0 && tid == 0) {
-    int cnt = 0;
-    int* dst = p.swaps + 1;
-    int* src = p.swaps + 1 + 2 * MAX_PANEL_W;
-    auto find_or_add = [&](int pos) {
-      for (int q = 0; q < cnt; q++)
-        if (dst[q] == pos) return q;
-      dst[cnt] = pos;
-      src[cnt] = pos;
-      return cnt++;
-    };
-    for (int c = 0; c < jb; c++) {
-      int a = find_or_add(p.j0 + c);
-      int b = find_or_add(s_pivs[c]);
-      int t = src[a];
-      src[a] = src[b];
-      src[b] = t;
+  if (g == 0 && tid == 0) build_swap_list(p, s_pivs);
+}
+
+__device__ __forceinline__ unsigned long long ld_remote_u64(uint32_t addr) {
+  unsigned long long v;
+  asm volatile("ld.shared::cluster.u64 %0, [%1];" : "=l"(v) : "r"(addr) : "memory");
+  return v;
+}
+
+// x = v[c] for a runtime c with compile-time register indices.
+__device__ __forceinline__ float pick(const float (&v)[CW], int c) {
+  float x = v[0];
+#pragma unroll
+  for (int k = 1; k < CW; k++) x = k == c ? v[k] : x;
+  return x;
+}
+
+template <int RPT>
+__global__ void __launch_bounds__(CT, 1) panel_cluster_reg_kernel(ClusterPanelArgs p) {
+  constexpr int NW = CT / 32;
+  __shared__ __align__(16) float wrow[2][NW][CW];
+  __shared__ unsigned long long wkey[2][NW];
+  __shared__ __align__(16) float s_crow[2][CW];
+  __shared__ unsigned long long s_key[2];
+  __shared__ int s_pivs[CW];
+
+  const int g = (int)cta_rank();
+  const int C = (int)gridDim.x;  // one cluster per launch
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int rpc = p.rpc, jb = p.jb;
+  const int row0 = p.j0 + g * rpc;
+  const int nrows = max(0, min(rpc, p.m - row0));
+  const bool vec = (p.ld % 4 == 0) && (p.j0 % 4 == 0) &&
+                   (reinterpret_cast<uintptr_t>(p.A) % 16 == 0);
+
+  float v[RPT][CW];
+  int pos[RPT];
+#pragma unroll
+  for (int q = 0; q < RPT; q++) {
+    const int lr = q * CT + tid;
+    pos[q] = lr < nrows ? row0 + lr : -1;
+    const float* src = p.A + (size_t)(lr < nrows ? row0 + lr : 0) * p.ld + p.j0;
+    if (pos[q] >= 0 && vec && jb == CW) {
+#pragma unroll
+      for (int c4 = 0; c4 < CW / 4; c4++) {
+        const float4 t = reinterpret_cast<const float4*>(src)[c4];
+        v[q][4 * c4] = t.x;
+        v[q][4 * c4 + 1] = t.y;
+        v[q][4 * c4 + 2] = t.z;
+        v[q][4 * c4 + 3] = t.w;
+      }
+    } else {
+#pragma unroll
+      for (int c = 0; c < CW; c++) v[q][c] = (pos[q] >= 0 && c < jb) ? src[c] : 0.f;
     }
-    int k = 0;
-    for (int q = 0; q < cnt; q++)
-      if (src[q] != dst[q]) { dst[k] = dst[q]; src[k] = src[q]; k++; }
-    p.swaps[0] = k;
   }
+
+  for (int c = 0; c < jb; c++) {
+    const int j = p.j0 + c, par = c & 1;
+    // 1. this thread's and this warp's best candidate
+    unsigned long long best = 0ull;
+    int bq = 0;
+#pragma unroll
+    for (int q = 0; q < RPT; q++)
+      if (pos[q] >= j) {
+        const unsigned long long pk =
+            ((unsigned long long)ckey(pick(v[q], c), pos[q], j) << 32) | (unsigned)(~pos[q]);
+        if (pk > best) { best = pk; bq = q; }
+      }
+    unsigned long long wb = best;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const unsigned long long o = __shfl_xor_sync(0xffffffffu, wb, off);
+      wb = o > wb ? o : wb;
+    }
+    const unsigned wmask = __ballot_sync(0xffffffffu, wb != 0ull && best == wb);
+    if (wmask && lane == __ffs(wmask) - 1) {
+      float* dst = wrow[par][warp];
+#pragma unroll
+      for (int q = 0; q < RPT; q++)
+        if (q == bq) {
+#pragma unroll
+          for (int k = 0; k < CW; k++) dst[k] = v[q][k];
+        }
+    }
+    if (lane == 0) wkey[par][warp] = wb;
+    __syncthreads();
+    // 2. the CTA's candidate (warp 0) for the cluster
+    if (warp == 0) {
+      const unsigned long long k = lane < NW ? wkey[par][lane] : 0ull;
+      unsigned long long km = k;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const unsigned long long o = __shfl_xor_sync(0xffffffffu, km, off);
+        km = o > km ? o : km;
+      }
+      const unsigned cm = __ballot_sync(0xffffffffu, km != 0ull && k == km);
+      if (cm) s_crow[par][lane] = wrow[par][__ffs(cm) - 1][lane];
+      if (lane == 0) s_key[par] = km;
+    }
+    cluster_sync();
+    // 3. the cluster's winner and its row, read by every warp
+    const unsigned long long gk =
+        lane < C ? ld_remote_u64(remote_addr(&s_key[par], (uint32_t)lane)) : 0ull;
+    unsigned long long gm = gk;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const unsigned long long o = __shfl_xor_sync(0xffffffffu, gm, off);
+      gm = o > gm ? o : gm;
+    }
+    const unsigned gmask = __ballot_sync(0xffffffffu, lane < C && gk == gm);
+    const int gsrc = __ffs(gmask) - 1;  // the row at position j is a candidate: gm != 0
+    const int piv = (int)(~(unsigned)(gm & 0xffffffffull));
+    const float u = ld_remote_f32(remote_addr(&s_crow[par][lane], (uint32_t)gsrc));
+    float uu[CW];
+#pragma unroll
+    for (int k = 0; k < CW; k++) uu[k] = __shfl_sync(0xffffffffu, u, k);
+    const float d = pick(uu, c);
+    const float sc = d != 0.f ? 1.f / d : 1.f;
+#pragma unroll
+    for (int q = 0; q < RPT; q++) {
+      if (pos[q] == piv) {
+        pos[q] = j;  // the pivot row; it keeps its values
+      } else {
+        if (pos[q] == j) pos[q] = piv;  // the displaced row takes the pivot's place
+        if (pos[q] > j) {
+          const float x = pick(v[q], c);
+          const float l = d != 0.f ? x * sc : x;
+#pragma unroll
+          for (int k = 0; k < CW; k++)
+            v[q][k] = k == c ? l : (k > c ? fmaf(-l, uu[k], v[q][k]) : v[q][k]);
+        }
+      }
+    }
+    if (g == 0 && tid == 0) {
+      p.ipiv[j] = piv;
+      s_pivs[c] = piv;
+    }
+  }
+  cluster_sync();  // remote reads of the last column are done everywhere
+
+  // each row to its final position
+#pragma unroll
+  for (int q = 0; q < RPT; q++)
+    if (pos[q] >= 0) {
+      float* dst = p.A + (size_t)pos[q] * p.ld + p.j0;
+      if (vec && jb == CW) {
+#pragma unroll
+        for (int c4 = 0; c4 < CW / 4; c4++)
+          reinterpret_cast<float4*>(dst)[c4] =
+              make_float4(v[q][4 * c4], v[q][4 * c4 + 1], v[q][4 * c4 + 2], v[q][4 * c4 + 3]);
+      } else {
+#pragma unroll
+        for (int c = 0; c < CW; c++)
+          if (c < jb) dst[c] = v[q][c];
+      }
+    }
+  if (g == 0 && tid == 0) build_swap_list(p, s_pivs);
 }
 
 }  // namespace
+
+// Launches panel_cluster_reg_kernel<RPT> as one cluster of `cluster` CTAs;
+// LA_UNSUPPORTED (nothing launched) when such a cluster cannot be resident.
+template <int RPT>
+la_status launch_reg(la_ctx ctx, float* A, size_t ld, int m, int j0, int jb, int* d_ipiv,
+                     int cluster, int rpc) {
+  static int ok_for = -1;  // cluster size checked once per instantiation (0: none)
+  if (ok_for < 0) {
+    ok_for = 0;
+    if (cudaFuncSetAttribute(panel_cluster_reg_kernel<RPT>,
+                             cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(cluster);
+      cfg.blockDim = dim3(CT);
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = cluster;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int nclusters = 0;
+      if (cudaOccupancyMaxActiveClusters(&nclusters, panel_cluster_reg_kernel<RPT>, &cfg) ==
+              cudaSuccess &&
+          nclusters >= 1)
+        ok_for = cluster;
+    }
+    cudaGetLastError();
+  }
+  if (ok_for != cluster) return LA_UNSUPPORTED;
+  ClusterPanelArgs a;
+  a.A = A;
+  a.ld = ld;
+  a.m = m;
+  a.j0 = j0;
+  a.jb = jb;
+  a.rpc = rpc;
+  a.ipiv = d_ipiv;
+  a.swaps = ctx->d_swaps;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(cluster);
+  cfg.blockDim = dim3(CT);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = ctx->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = cluster;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaError_t e = cudaLaunchKernelEx(&cfg, panel_cluster_reg_kernel<RPT>, a);
+  if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaLaunchKernelEx(panel_cluster_reg)");
+  ctx->launches++;
+  return LA_OK;
+}
 
 // Returns LA_UNSUPPORTED (without launching) when the panel does not fit one
 // cluster; the caller then uses the cooperative kernel.
@@ -266,6 +496,15 @@ la_status launch_panel_cluster_f32(la_ctx ctx, float* A, size_t ld, int m, int j
   }
   if (cluster == 0) return LA_UNSUPPORTED;
   const int rpc = (R + cluster - 1) / cluster;
+  {
+    // Register rows: at most 4 rows per thread.
+    const int rpt = (rpc + CT - 1) / CT;
+    la_status rs = LA_UNSUPPORTED;
+    if (rpt <= 1) rs = launch_reg<1>(ctx, A, ld, m, j0, jb, d_ipiv, cluster, rpc);
+    else if (rpt <= 2) rs = launch_reg<2>(ctx, A, ld, m, j0, jb, d_ipiv, cluster, rpc);
+    else if (rpt <= 4) rs = launch_reg<4>(ctx, A, ld, m, j0, jb, d_ipiv, cluster, rpc);
+    if (rs != LA_UNSUPPORTED) return rs;
+  }
   const size_t smem = (size_t)rpc * (CP + 1) * sizeof(float);
   if (smem > max_smem) return LA_UNSUPPORTED;
 

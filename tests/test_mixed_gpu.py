@@ -113,9 +113,11 @@ def test_ill_conditioned_refinement_converges(lagpu, ctx_fast, torch, prec, kapp
     assert eta <= ETA_MAX
 
 
-def test_cluster_and_cooperative_fp32_panels_agree(lagpu, torch):
-    # The two FP32 panel kernels implement the same pivoting: identical factors.
-    n = 1500
+@pytest.mark.parametrize("n", [1500, 6000, 12000], ids=["rows1", "rows2", "rows4"])
+def test_cluster_and_cooperative_fp32_panels_agree(lagpu, torch, n):
+    # The FP32 panel kernels implement the same pivoting: identical pivots from
+    # the cluster panel (1, 2 and 4 rows per thread held in registers at these
+    # sizes) and the cooperative multi-CTA panel.
     rng = np.random.default_rng(44)
     a = torch.from_numpy(rng.standard_normal((n, n))).cuda()
     outs = []
