@@ -23,7 +23,9 @@ Further sections of the same JSON line (skipped with --no-mixed,
 --no-batched, --no-selector):
   mixed_ir : mixed-precision LU (tcgen05 BF16/FP16 or FP32 trailing updates)
           + FP64 refinement at n=16384, kappa in {1e2, 1e6, 1e10}, 4 RHS,
-          against the plain FP64 LU at the same size.
+          against the plain FP64 LU at the same size; the headline speed-up is
+          the automatic path (la_lu_solve_auto_device), each fixed precision
+          is reported beside it.
   batched_uneven : 20,000 systems, n uniform in [8, 256], 1-4 RHS, half of them
           shifted by 0.5 n I; solves/s of the mixed plan against the plain FP64
           plan, each with its autotuned shape.
@@ -208,6 +210,7 @@ def run_mixed(la_gpu, torch, ctx, n, nrhs=4, kappas=(1e2, 1e6, 1e10), precs=(1, 
     x = torch.zeros((n, nrhs), dtype=torch.float64, device="cuda")
     results = []
     best_by_kappa = {}
+    auto_by_kappa = {}
     for kappa in kappas:
         a = householder_conditioned(torch, n, kappa, 30 + int(round(np.log10(kappa))))
         torch.cuda.synchronize()
@@ -229,6 +232,19 @@ def run_mixed(la_gpu, torch, ctx, n, nrhs=4, kappas=(1e2, 1e6, 1e10), precs=(1, 
             results.append(r)
             if ok and (kappa not in best_by_kappa or r["ms"] < best_by_kappa[kappa]["ms"]):
                 best_by_kappa[kappa] = r
+        # automatic precision: FP16 factors, then FP32, then the plain FP64 LU
+        for rep in range(2):  # first run warms up
+            t0 = time.perf_counter()
+            code, st = la_gpu.lu_solve_auto_device(ctx, a.data_ptr(), n, n, b.data_ptr(), nrhs,
+                                                   nrhs, x.data_ptr(), nrhs, tol=5e-15)
+            t1 = time.perf_counter()
+        eta = la_gpu.backward_error_device(ctx, a.data_ptr(), n, x.data_ptr(), nrhs,
+                                           b.data_ptr(), nrhs, n, nrhs)
+        auto_by_kappa[kappa] = {"kappa": kappa, "precision_used": {0: "fp64", 2: "fp16",
+                                                                    3: "fp32"}[st.precision],
+                                "ms": (t1 - t0) * 1e3, "gflops": flops / (t1 - t0) / 1e9,
+                                "iterations": st.iterations, "fell_back": st.fell_back,
+                                "converged": eta <= 1e-14, "eta": eta}
         del a
     # plain FP64 LU + solve on the kappa = 1e2 matrix
     a = householder_conditioned(torch, n, 1e2, 32)
@@ -243,14 +259,19 @@ def run_mixed(la_gpu, torch, ctx, n, nrhs=4, kappas=(1e2, 1e6, 1e10), precs=(1, 
                                              b.data_ptr(), nrhs, n, nrhs)
     plain = {"ms": (t1 - t0) * 1e3, "gflops": flops / (t1 - t0) / 1e9, "eta": plain_eta}
     del a
-    speed = {("%.0e" % k): (best_by_kappa[k]["gflops"] / plain["gflops"] if k in best_by_kappa
-                            else None) for k in kappas}
+    speed = {("%.0e" % k): (auto_by_kappa[k]["gflops"] / plain["gflops"]
+                            if auto_by_kappa[k]["converged"] else None) for k in kappas}
     return {"workload": "mixed-precision LU + FP64 iterative refinement, n=%d, %d RHS, "
                         "A = H1 diag(s) H2 (4 Householder reflectors each), s geometric 1 -> "
                         "1/kappa; nominal flops 2/3 n^3 + 2 n^2 nrhs" % (n, nrhs),
-            "runs": results, "plain_fp64": plain,
-            "best_converged_by_kappa": {("%.0e" % k): v for k, v in best_by_kappa.items()},
-            "speedup_vs_plain_fp64": speed}
+            "auto_by_kappa": {("%.0e" % k): v for k, v in auto_by_kappa.items()},
+            "speedup_vs_plain_fp64": speed,
+            "speedup_basis": "la_lu_solve_auto_device (FP16 factors, then FP32, then the plain "
+                             "FP64 LU; precision chosen at run time, not after the fact) against "
+                             "the plain FP64 LU + solve, wall clock of factor + solve",
+            "plain_fp64": plain, "runs": results,
+            "fastest_fixed_precision_by_kappa": {("%.0e" % k): v
+                                                 for k, v in best_by_kappa.items()}}
 
 
 def _wall_ms(ctx, torch, fn, reps=3):

@@ -190,6 +190,22 @@ la_status la_lu_mixed_new_device(la_ctx ctx, const double* d_a, size_t lda, size
 la_status la_lu_solve_refined_device(la_lu lu, const double* d_b, size_t ldb, size_t nrhs,
                                      double* d_x, size_t ldx, int max_iters, double tol,
                                      la_refine_stats* stats);
+/* Solves A X = B (A n x n FP64 on the device, B and X n x nrhs, nrhs <= 16)
+ * to a normwise backward error <= tol with the cheapest factorization that
+ * gets there: (1) the mixed LU with FP16 trailing updates and plain iterative
+ * refinement, at most 10 steps, given up as soon as refinement stalls;
+ * (2) the mixed LU with FP32 trailing updates, refinement and GMRES-IR, at
+ * most 40 steps; (3) the plain FP64 LU and solve (LUDecomposition::new +
+ * solve, lu.rs:104-278), which answers whatever (1) and (2) could not.
+ * stats->precision is LA_PREC_FP16, LA_PREC_FP32 or 0 (plain FP64, then
+ * stats->fell_back = 1), stats->iterations the refinement steps of all stages
+ * and stats->eta the final backward error. LA_SINGULAR only when the plain
+ * FP64 LU has an exact zero pivot (the reference's None). No reference
+ * counterpart: it replaces Matrix::solve (mod.rs:1030-1032) for callers that
+ * accept any factorization whose answer meets tol. */
+la_status la_lu_solve_auto_device(la_ctx ctx, const double* d_a, size_t lda, size_t n,
+                                  const double* d_b, size_t ldb, size_t nrhs, double* d_x,
+                                  size_t ldx, double tol, la_refine_stats* stats);
 /* Tensor-core building block of the mixed LU, exposed for testing:
  * C (m x n f32, pitch ldc) -= alpha * A (m x k) * B^T (B: n x k), A and B 16-bit
  * (fmt 1 = BF16, 2 = FP16) K-major with pitches multiple of 8 elements. */

@@ -375,6 +375,12 @@ la_status mixed_factor(la_ctx ctx, la_lu h, int prec) {
   return LA_OK;
 }
 
+// Iterative refinement with the mixed factors of h (la_lu_solve_refined_device;
+// allow_gmres = false stops when plain refinement stalls).
+la_status refine_impl(la_lu h, const double* d_b, size_t ldb, size_t nrhs, double* d_x,
+                      size_t ldx, int max_iters, double tol, bool allow_gmres,
+                      la_refine_stats* stats);
+
 }  // namespace
 
 extern "C" {
@@ -427,6 +433,64 @@ la_status la_lu_mixed_new_device(la_ctx ctx, const double* d_a, size_t lda, size
 la_status la_lu_solve_refined_device(la_lu h, const double* d_b, size_t ldb, size_t nrhs,
                                      double* d_x, size_t ldx, int max_iters, double tol,
                                      la_refine_stats* stats) {
+  return refine_impl(h, d_b, ldb, nrhs, d_x, ldx, max_iters, tol, true, stats);
+}
+
+la_status la_lu_solve_auto_device(la_ctx ctx, const double* d_a, size_t lda, size_t n,
+                                  const double* d_b, size_t ldb, size_t nrhs, double* d_x,
+                                  size_t ldx, double tol, la_refine_stats* stats) {
+  if (!ctx || !d_a || !d_b || !d_x || lda < n || ldb < nrhs || ldx < nrhs) return LA_INVALID;
+  if (n == 0) return LA_BADSHAPE;
+  if (nrhs == 0 || nrhs > 16) return LA_UNSUPPORTED;
+  la_refine_stats st = {};
+  int its = 0;
+  // 1. FP16 trailing updates (the fastest factorization) with plain refinement
+  //    only: it either contracts quickly or the condition number is too large
+  //    for FP16 factors, and then GMRES steps would cost more than stage 2.
+  // 2. FP32 trailing updates with refinement and, if that stalls, GMRES-IR.
+  const int precs[2] = {LA_PREC_FP16, LA_PREC_FP32};
+  for (int stage = 0; stage < 2; stage++) {
+    la_lu h = nullptr;
+    la_status s = la_lu_mixed_new_device(ctx, d_a, lda, n, precs[stage], &h);
+    if (s != LA_OK) return s;
+    s = refine_impl(h, d_b, ldb, nrhs, d_x, ldx, stage == 0 ? 10 : 40, tol, stage == 1, &st);
+    la_lu_free(h);
+    its += s == LA_SINGULAR ? 0 : st.iterations;
+    if (s == LA_OK) {
+      st.iterations = its;
+      st.fell_back = 0;
+      if (stats) *stats = st;
+      return LA_OK;
+    }
+    if (s != LA_NOT_CONVERGED && s != LA_SINGULAR) return s;
+  }
+  // 3. The plain FP64 LU (the reference's algorithm) answers, and judges: a
+  //    zero pivot there is the reference's None.
+  la_lu lu = nullptr;
+  la_status s = la_lu_new_device(ctx, d_a, lda, n, n, &lu);
+  if (s != LA_OK) return s;
+  s = la_lu_solve_device(lu, d_b, ldb, n, nrhs, d_x, ldx);
+  la_lu_free(lu);
+  if (s != LA_OK) return s;
+  double eta = 0.0;
+  LA_TRY(la_backward_error_device(ctx, d_a, lda, d_x, ldx, d_b, ldb, n, nrhs, &eta));
+  st.iterations = its;
+  st.converged = eta <= tol ? 1 : 0;
+  st.eta = eta;
+  st.fell_back = 1;
+  st.precision = 0;
+  st.gmres_steps = 0;
+  if (stats) *stats = st;
+  return LA_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+la_status refine_impl(la_lu h, const double* d_b, size_t ldb, size_t nrhs, double* d_x,
+                      size_t ldx, int max_iters, double tol, bool allow_gmres,
+                      la_refine_stats* stats) {
   if (!h || !d_b || !d_x || ldb < nrhs || ldx < nrhs || !h->d_lu32) return LA_INVALID;
   if (nrhs == 0 || nrhs > 16) return LA_UNSUPPORTED;
   la_ctx ctx = h->ctx;
@@ -504,7 +568,7 @@ la_status la_lu_solve_refined_device(la_lu h, const double* d_b, size_t ldb, siz
   // GMRES-IR once plain refinement stalls.
   int outer = 0;
   prev = INFINITY;
-  while (!converged && it + outer < max_iters && eta < 0.5 * prev) {
+  while (allow_gmres && !converged && it + outer < max_iters && eta < 0.5 * prev) {
     prev = eta;
     outer++;
     for (int j = 0; j < R; j++) {
@@ -528,4 +592,4 @@ la_status la_lu_solve_refined_device(la_lu h, const double* d_b, size_t ldb, siz
   return converged ? LA_OK : LA_NOT_CONVERGED;
 }
 
-}  // extern "C"
+}  // namespace

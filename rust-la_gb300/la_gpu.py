@@ -84,6 +84,7 @@ SIGNATURES = {
     "la_lu_factor_noalloc": ([_P, _P, _S, _S, _S, _P, _P, _P], _I),
     "la_lu_mixed_new_device": ([_P, _P, _S, _S, _I, _P], _I),
     "la_lu_solve_refined_device": ([_P, _P, _S, _S, _P, _S, _I, _D, _P], _I),
+    "la_lu_solve_auto_device": ([_P, _P, _S, _S, _P, _S, _S, _P, _S, _D, _P], _I),
     "la_lowp_update_device": ([_P, _I, _S, _S, _S, _P, _S, _P, _S, _P, _S, ctypes.c_float], _I),
     "la_batch_plan_create": ([_P, _P, _P, _P, _P, _I, _I, _I, _I, _D, _I, _P], _I),
     "la_batch_plan_run": ([_P], _I),
@@ -454,6 +455,17 @@ def lu_solve_refined_device(lu, b_ptr, ldb, nrhs, x_ptr, ldx, max_iters=50, tol=
                                           ctypes.c_void_p(x_ptr), ldx, max_iters, tol,
                                           ctypes.byref(stats))
     _check(lu.ctx, st, (OK, NOT_CONVERGED, SINGULAR))
+    return st, stats
+
+
+def lu_solve_auto_device(ctx, a_ptr, lda, n, b_ptr, ldb, nrhs, x_ptr, ldx, tol=1e-14):
+    """Automatic precision (la_lu_solve_auto_device): FP16 factors, then FP32,
+    then the plain FP64 LU. Returns (status, RefineStats)."""
+    stats = RefineStats()
+    st = lib().la_lu_solve_auto_device(ctx.h, ctypes.c_void_p(a_ptr), lda, n,
+                                       ctypes.c_void_p(b_ptr), ldb, nrhs, ctypes.c_void_p(x_ptr),
+                                       ldx, ctypes.c_double(tol), ctypes.byref(stats))
+    _check(ctx, st, (OK, SINGULAR))
     return st, stats
 
 

@@ -129,3 +129,41 @@ def test_cluster_and_cooperative_fp32_panels_agree(lagpu, torch, n):
         lu.free()
         ctx.close()
     assert np.array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("kappa,scale,want", [(1e2, 1.0, (2,)), (1e10, 1.0, (2, 3)),
+                                               (1e2, 1e40, (0,))],
+                         ids=["kappa1e2", "kappa1e10", "fp32-overflow"])
+def test_auto_precision_cascade(lagpu, ctx_fast, torch, kappa, scale, want):
+    # FP16 factors where they refine to tol; FP16 or FP32 factors (GMRES-IR)
+    # at kappa 1e10; the plain FP64 LU where no FP32 copy of A exists (entries
+    # 1e40 overflow FP32); every answer at eta <= 1e-14.
+    n = 1024
+    a = _hh(torch, n, kappa, 17) * scale
+    rng = np.random.default_rng(18)
+    b = torch.from_numpy(rng.standard_normal((n, 3))).cuda()
+    x = torch.zeros((n, 3), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    st, stats = lagpu.lu_solve_auto_device(ctx_fast, a.data_ptr(), n, n, b.data_ptr(), 3, 3,
+                                           x.data_ptr(), 3, tol=5e-15)
+    assert st == lagpu.OK
+    assert stats.precision in want, (stats.precision, stats.iterations, stats.eta)
+    assert stats.fell_back == (1 if stats.precision == 0 else 0)
+    eta = oracle.backward_error(a.cpu().numpy(), x.cpu().numpy(), b.cpu().numpy())
+    assert eta <= ETA_MAX
+
+
+def test_auto_precision_singular_and_limits(lagpu, ctx_fast, torch):
+    n = 64
+    a = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+    a[:, :n - 1] = torch.randn((n, n - 1), dtype=torch.float64, device="cuda")
+    b = torch.ones((n, 1), dtype=torch.float64, device="cuda")
+    x = torch.zeros((n, 17), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    st, _ = lagpu.lu_solve_auto_device(ctx_fast, a.data_ptr(), n, n, b.data_ptr(), 1, 1,
+                                       x.data_ptr(), 1)
+    assert st == lagpu.SINGULAR  # a zero column: the reference's None
+    with pytest.raises(lagpu.LaError) as e:
+        lagpu.lu_solve_auto_device(ctx_fast, a.data_ptr(), n, n, x.data_ptr(), 17, 17,
+                                   x.data_ptr(), 17)
+    assert e.value.status == lagpu.UNSUPPORTED
