@@ -330,7 +330,7 @@ __device__ double tridiag_min_eig_warp(const double* al, const double* be, int k
   return ldexp(0.5 * (lo + hi), sexp);
 }
 
-constexpr int FEAT_CTAS_PER_SM = 2;
+constexpr int FEAT_CTAS_PER_SM = 4;  // 4 CTAs of 4 warps: four systems in flight per SM
 
 // 16 features per system (one CTA per system). FP64 arithmetic is slow on
 // this GPU, so A_i is read in FP64 once and rounded to an FP32 copy in the
@@ -345,7 +345,7 @@ constexpr int FEAT_CTAS_PER_SM = 2;
 // reorthogonalisation; the extreme Ritz values bound sigma_max^2 from below and
 // sigma_min^2 from above. The asymmetry feature is the probe
 // ||A q0 - A^T q0|| / ||A q0||.
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(128, 4)
 features_kernel(const double* __restrict__ A, const SysRec* __restrict__ sys, int count,
                 float* __restrict__ F, float* __restrict__ scratch) {
   __shared__ double red[2][8];
@@ -798,7 +798,7 @@ la_status la_batch_features_device(la_ctx ctx, const double* d_a, const la_batch
     if (e != cudaSuccess) s = la_cuda_fail(ctx, e, "features upload");
   }
   if (s == LA_OK) {
-    features_kernel<<<grid, 256, 0, ctx->stream>>>(d_a, d, count, d_features, scr);
+    features_kernel<<<grid, 128, 0, ctx->stream>>>(d_a, d, count, d_features, scr);
     ctx->launches++;
     s = la_check_launch(ctx, "features_kernel");
   }
