@@ -8,11 +8,20 @@
 // keeping every SM's FP64 pipe fed (several resident CTAs, register-blocked
 // 4x4 micro-tiles, cp.async double buffering) rather than at operand reuse.
 //
+// The FMA modes of the FP64 tiles with N > 16 (the LU's trailing update and
+// Matrix * Matrix) stage their operand slabs with TMA (gemm_f64_tma_kernel):
+// thread 0 issues two-dimensional tiled copies of the next A and B slabs into
+// the other half of a two-stage ring while all threads compute on the current
+// one, and the copies complete on an mbarrier. The other modes, narrow N and
+// operands that break TMA's 16-byte alignment rules use cp.async
+// (gemm_f64_kernel).
+//
 // Each output element is accumulated by one thread in a fixed k order, which
 // gives the EXACT modes the reference's summation order: src/matrix/mod.rs:
 // 965-973 (Mul: res = res + a*b from zero, ascending idx) and src/decomp/lu.rs:
 // 124-126 (s = s + l*u, ascending k) and :260/:272 (x = x - x_k*l, per term).
 #include "la_internal.cuh"
+#include "tma_util.cuh"
 
 namespace {
 
@@ -179,7 +188,131 @@ gemm_f64_kernel(int M, int N, int K, const T* __restrict__ A, size_t lda,
     }
 }
 
+// TMA-staged FP64 tile (FMA modes): 64 x 64 output tile per 256-thread CTA,
+// 32-deep K slabs in a two-stage ring. A slab of A is one TMA box of 64 rows x
+// 32 columns (dense [64][32]); a slab of B is two boxes of 32 k-rows x 32
+// columns (dense [2][32][32]), keeping every box row at 256 bytes. Zero fill
+// covers the matrix edges; the last slab applies only its valid k. Each wait
+// is bounded: a CTA that gives up records DERR_GEMM_TIMEOUT, drains its own
+// copies (bounded) and exits with every thread, without writing C.
+constexpr int TMA_BN = 64;
+constexpr int TMA_STAGE_D = BM * BK + BK * TMA_BN;  // doubles per stage
+constexpr uint32_t TMA_STAGE_BYTES = TMA_STAGE_D * sizeof(double);
+constexpr size_t TMA_SMEM = 2 * (size_t)TMA_STAGE_BYTES + 1024;  // + alignment slack
+
+template <int MODE>
+__global__ void __launch_bounds__(THREADS)
+gemm_f64_tma_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
+                    int M, int N, int K, double* __restrict__ C, size_t ldc, int* err) {
+  extern __shared__ __align__(1024) unsigned char tma_raw[];
+  __shared__ __align__(8) uint64_t full[2];
+  double* smem = reinterpret_cast<double*>(
+      (reinterpret_cast<uintptr_t>(tma_raw) + 1023) & ~uintptr_t(1023));
+  const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * TMA_BN;
+  constexpr bool ZERO = MODE == GM_FMA_ZERO;
+
+  double acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int r = m0 + ty + 16 * i, c = n0 + tx + 16 * j;
+      acc[i][j] = (!ZERO && r < M && c < N) ? C[(size_t)r * ldc + c] : 0.0;
+    }
+
+  const int nslab = (K + BK - 1) / BK;
+  if (tid == 0) {
+    la_tma::mbar_init(&full[0], 1);
+    la_tma::mbar_init(&full[1], 1);
+    la_tma::mbar_init_fence();
+  }
+  __syncthreads();
+  auto issue = [&](int stage, int s) {
+    double* st = smem + stage * TMA_STAGE_D;
+    la_tma::mbar_expect_tx(&full[stage], TMA_STAGE_BYTES);
+    la_tma::tma_load_2d(st, &ta, s * BK, m0, &full[stage]);
+    la_tma::tma_load_2d(st + BM * BK, &tb, n0, s * BK, &full[stage]);
+    la_tma::tma_load_2d(st + BM * BK + BK * 32, &tb, n0 + 32, s * BK, &full[stage]);
+  };
+  if (tid == 0 && nslab > 0) issue(0, 0);
+
+  for (int s = 0; s < nslab; s++) {
+    const int buf = s & 1;
+    if (tid == 0 && s + 1 < nslab) issue(buf ^ 1, s + 1);
+    const bool ok =
+        la_tma::mbar_wait(&full[buf], (uint32_t)((s >> 1) & 1), err, (int)DERR_GEMM_TIMEOUT);
+    const double* as = smem + buf * TMA_STAGE_D;
+    const double* bs = as + BM * BK;
+    const int kn = min(BK, K - s * BK);
+    if (ok) {
+#pragma unroll 8
+      for (int k = 0; k < BK; k++) {
+        if (k < kn) {
+          double a[4], b[4];
+#pragma unroll
+          for (int i = 0; i < 4; i++) a[i] = as[(ty + 16 * i) * BK + k];
+#pragma unroll
+          for (int j = 0; j < 4; j++) b[j] = bs[(j >> 1) * BK * 32 + k * 32 + tx + 16 * (j & 1)];
+#pragma unroll
+          for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+              acc[i][j] = ZERO ? fma(a[i], b[j], acc[i][j]) : fma(-a[i], b[j], acc[i][j]);
+        }
+      }
+    }
+    if (__syncthreads_or(!ok)) {
+      // Give up: drain this CTA's copies still in flight, then every thread exits.
+      if (tid == 0) {
+        la_tma::mbar_drain(&full[buf], (uint32_t)((s >> 1) & 1));
+        if (s + 1 < nslab) la_tma::mbar_drain(&full[buf ^ 1], (uint32_t)(((s + 1) >> 1) & 1));
+      }
+      return;
+    }
+  }
+
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int r = m0 + ty + 16 * i, c = n0 + tx + 16 * j;
+      if (r < M && c < N) C[(size_t)r * ldc + c] = acc[i][j];
+    }
+}
+
 constexpr size_t GEMM_SMEM_CAP = 96 * 1024;
+
+// The TMA form of the FMA modes; LA_UNSUPPORTED (nothing launched) when an
+// operand breaks TMA's rules (16-byte aligned bases, pitches of whole 16-byte
+// units) so that the caller uses the cp.async form.
+template <int MODE>
+la_status launch_tma(la_ctx ctx, int M, int N, int K, const double* A, size_t lda,
+                     const double* B, size_t ldb, double* C, size_t ldc, size_t min_smem) {
+  if (K <= 0 || (reinterpret_cast<uintptr_t>(A) % 16) || (reinterpret_cast<uintptr_t>(B) % 16) ||
+      (lda % 2) || (ldb % 2))
+    return LA_UNSUPPORTED;
+  CUtensorMap ta, tb;
+  if (!la_tma::encode_2d(ctx, &ta, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, A, (size_t)M, (size_t)K,
+                         lda, (uint32_t)BK, (uint32_t)BM, CU_TENSOR_MAP_SWIZZLE_NONE) ||
+      !la_tma::encode_2d(ctx, &tb, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, B, (size_t)K, (size_t)N,
+                         ldb, 32u, (uint32_t)BK, CU_TENSOR_MAP_SWIZZLE_NONE))
+    return LA_UNSUPPORTED;
+  static bool configured = false;  // one attribute call per instantiation
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(gemm_f64_tma_kernel<MODE>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)GEMM_SMEM_CAP);
+    if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaFuncSetAttribute(gemm_tma)");
+    configured = true;
+  }
+  const size_t smem = std::min(GEMM_SMEM_CAP, std::max(TMA_SMEM, min_smem));
+  dim3 grid((N + TMA_BN - 1) / TMA_BN, (M + BM - 1) / BM);
+  gemm_f64_tma_kernel<MODE><<<grid, THREADS, smem, ctx->stream>>>(ta, tb, M, N, K, C, ldc,
+                                                                 ctx->d_err);
+  ctx->launches++;
+  return la_check_launch(ctx, "gemm_f64_tma_kernel");
+}
 
 template <int MODE, int BN, typename T = double>
 la_status launch_mode(la_ctx ctx, int M, int N, int K, const T* A, size_t lda, const T* B,
@@ -227,6 +360,13 @@ la_status launch_gemm(la_ctx ctx, int mode, int M, int N, int K, const double* A
   if (M <= 0 || N <= 0) return LA_OK;
   if (K <= 0 && mode != GM_FMA_ZERO && mode != GM_EXACT_ZERO) return LA_OK;
   if (N <= 16) return launch_bn<16>(ctx, mode, M, N, K, A, lda, B, ldb, C, ldc, min_smem);
+  if (mode == GM_FMA_SUB || mode == GM_FMA_ZERO) {
+    const la_status s =
+        mode == GM_FMA_SUB
+            ? launch_tma<GM_FMA_SUB>(ctx, M, N, K, A, lda, B, ldb, C, ldc, min_smem)
+            : launch_tma<GM_FMA_ZERO>(ctx, M, N, K, A, lda, B, ldb, C, ldc, min_smem);
+    if (s != LA_UNSUPPORTED) return s;
+  }
   return launch_bn<64>(ctx, mode, M, N, K, A, lda, B, ldb, C, ldc, min_smem);
 }
 

@@ -17,6 +17,7 @@
 #include <cuda.h>
 
 #include "la_internal.cuh"
+#include "tma_util.cuh"
 
 namespace {
 
@@ -28,58 +29,16 @@ constexpr uint32_t B_BYTES = TN * TK * 2;  // 16 KB
 constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr size_t TC_SMEM = (size_t)STAGES * STAGE_BYTES + 1024;  // + alignment slack
 constexpr uint32_t TMEM_COLS = 128;
-constexpr unsigned long long TC_WAIT_NS = 2000000000ull;
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ unsigned long long gtimer() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
-  return t;
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-               "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
+using la_tma::mbar_expect_tx;
+using la_tma::mbar_init;
+using la_tma::mbar_try_wait;
+using la_tma::smem_u32;
+using la_tma::tma_load_2d;
+
 // Bounded wait on an mbarrier phase. false: gave up (timeout or error word set).
-__device__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err) {
-  unsigned long long t0 = 0;
-  for (unsigned i = 0;; i++) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if ((i & 255u) == 255u) {
-      if (*reinterpret_cast<volatile int*>(err) != 0) return false;
-      unsigned long long now = gtimer();
-      if (t0 == 0) t0 = now;
-      else if (now - t0 > TC_WAIT_NS) {
-        atomicCAS(err, 0, (int)DERR_TC_TIMEOUT);
-        return false;
-      }
-    }
-  }
-}
-
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
-                                            uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
-      : "memory");
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err) {
+  return la_tma::mbar_wait(bar, parity, err, (int)DERR_TC_TIMEOUT);
 }
 
 // Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row
@@ -124,7 +83,7 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tmap_a,
     }
     mbar_init(&done, 1);
     s_fail = 0;
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    la_tma::mbar_init_fence();
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -232,12 +191,8 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tmap_a,
   }
   // On failure: wait (bounded) for this CTA's copies still in flight.
   if (!have && warp == 0 && lane == 0) {
-    for (int kc = 0; kc < issued; kc++) {
-      const int s = kc % STAGES;
-      unsigned long long t0 = gtimer();
-      while (!mbar_try_wait(&full[s], (uint32_t)((kc / STAGES) & 1)))
-        if (gtimer() - t0 > TC_WAIT_NS) break;
-    }
+    for (int kc = 0; kc < issued; kc++)
+      la_tma::mbar_drain(&full[kc % STAGES], (uint32_t)((kc / STAGES) & 1));
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
@@ -246,49 +201,15 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tmap_a,
                  "r"(TMEM_COLS));
 }
 
-// Driver entry point for tensor-map encoding, fetched once through the runtime
-// (no link-time dependency on libcuda).
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
-                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
-                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
-                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn get_encoder(la_ctx ctx) {
-  static EncodeTiledFn fn = nullptr;
-  if (!fn) {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    cudaError_t e =
-        cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
-    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p) {
-      if (ctx) ctx->last_error = "cuTensorMapEncodeTiled unavailable";
-      return nullptr;
-    }
-    fn = reinterpret_cast<EncodeTiledFn>(p);
-  }
-  return fn;
-}
-
 // 2-D K-major operand map: `rows` rows of `k` 16-bit elements, pitch `ld`
 // elements (ld * 2 bytes must be a multiple of 16), box 64 (K) x 128 (rows).
 bool encode_operand(la_ctx ctx, CUtensorMap* map, const void* base, int fmt, size_t rows,
                     size_t k, size_t ld) {
-  EncodeTiledFn enc = get_encoder(ctx);
-  if (!enc) return false;
-  cuuint64_t dims[2] = {(cuuint64_t)k, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
-  cuuint32_t box[2] = {(cuuint32_t)TK, (cuuint32_t)TM};
-  cuuint32_t estr[2] = {1, 1};
-  CUresult r = enc(map, fmt == LA_LOWP_BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
-                                            : CU_TENSOR_MAP_DATA_TYPE_FLOAT16,
-                   2, const_cast<void*>(base), dims, strides, box, estr,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) {
-    if (ctx) ctx->last_error = "cuTensorMapEncodeTiled failed";
-    return false;
-  }
-  return true;
+  return la_tma::encode_2d(ctx, map,
+                           fmt == LA_LOWP_BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
+                                               : CU_TENSOR_MAP_DATA_TYPE_FLOAT16,
+                           2, base, rows, k, ld, (uint32_t)TK, (uint32_t)TM,
+                           CU_TENSOR_MAP_SWIZZLE_128B);
 }
 
 }  // namespace

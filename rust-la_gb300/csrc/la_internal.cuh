@@ -38,7 +38,8 @@ enum DeviceErr : int {
   DERR_PANEL_TIMEOUT = 1,
   DERR_PANEL_CAPACITY = 2,
   DERR_TC_TIMEOUT = 3,
-  DERR_TRSV_TIMEOUT = 4
+  DERR_TRSV_TIMEOUT = 4,
+  DERR_GEMM_TIMEOUT = 5
 };
 
 // 16-bit operand formats of the tensor-core update.
