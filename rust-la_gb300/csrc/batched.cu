@@ -446,6 +446,7 @@ struct BatchArgs {
   const SysDesc* desc;
   int count;
   int* queue;        // work counter (zeroed before the launch)
+  int* redo;         // [0] = count, [1 + k] = k-th system (sorted index) left for the FP64 pass
   int* status;       // per system (sorted order): iterations, < 0 = not converged
   double* eta;       // per system: final backward error (mixed pass) or -1
   void* scratch;     // per-CTA global working matrices for systems that do not fit
@@ -908,6 +909,7 @@ __device__ void process_system(const BatchArgs& a, int sidx, const SysDesc& d, S
   for (int idx = tid; idx < n * nrhs; idx += BT) Xi[idx] = xv[idx];
   if (tid == 0) {
     a.status[sidx] = ok ? it + gsteps : -1 - (it + gsteps);
+    if (!ok) a.redo[1 + atomicAdd(&a.redo[0], 1)] = sidx;
     a.eta[sidx] = eta;
     pc.mark(3);
     if (a.phase) pc.flush(phase);
@@ -923,13 +925,18 @@ __global__ void __launch_bounds__(BT_MAX, MIXED ? 2 : 1) batched_kernel(BatchArg
   __shared__ Shared sh;
   __shared__ int s_sys;
   const int tid = threadIdx.x;
+  // The FP64 pass of a mixed plan works through the list of systems the mixed
+  // pass could not refine, instead of visiting every system.
   for (;;) {
-    if (tid == 0) s_sys = atomicAdd(a.queue, 1);
+    if (tid == 0) {
+      const int q = atomicAdd(a.queue, 1);
+      const int total = a.only_flagged ? a.redo[0] : a.count;
+      s_sys = q < total ? (a.only_flagged ? a.redo[1 + q] : q) : -1;
+    }
     __syncthreads();
     const int sidx = s_sys;
     __syncthreads();
-    if (sidx >= a.count) return;
-    if (a.only_flagged && a.status[sidx] >= 0) continue;
+    if (sidx < 0) return;
     const SysDesc d = a.desc[sidx];
     char* smem = reinterpret_cast<char*>(bsm);
     const long long t0 = clock64();
@@ -970,6 +977,7 @@ struct la_batch_plan_s {
   double* X = nullptr;
   SysDesc* d_desc = nullptr;
   int* d_queue = nullptr;
+  int* d_redo = nullptr;
   int* d_status = nullptr;
   double* d_eta = nullptr;
   long long* d_cycles = nullptr;
@@ -1022,6 +1030,7 @@ la_status launch_pass(la_batch_plan_s* pl, int* queue, int only_flagged, size_t 
   a.desc = pl->d_desc;
   a.count = pl->count;
   a.queue = queue;
+  a.redo = pl->d_redo;
   a.status = pl->d_status;
   a.eta = pl->d_eta;
   a.scratch = pl->d_scratch;
@@ -1042,6 +1051,7 @@ la_status launch_pass(la_batch_plan_s* pl, int* queue, int only_flagged, size_t 
 la_status enqueue_plan(la_batch_plan_s* pl) {
   la_ctx ctx = pl->ctx;
   LA_CUDA(ctx, cudaMemsetAsync(pl->d_queue, 0, 2 * sizeof(int), ctx->stream));
+  LA_CUDA(ctx, cudaMemsetAsync(pl->d_redo, 0, sizeof(int), ctx->stream));
   LA_CUDA(ctx, cudaMemsetAsync(pl->d_cycles, 0, pl->count * sizeof(long long), ctx->stream));
   LA_CUDA(ctx, cudaMemsetAsync(pl->d_phase, 0, 8 * sizeof(unsigned long long), ctx->stream));
   if (pl->mode == LA_BATCH_FP64) {
@@ -1136,6 +1146,8 @@ la_status la_batch_plan_create(la_ctx ctx, const double* d_a, const double* d_b,
   const int slices = std::max(pl->grid, pl->grid_fp64);
   la_status s = la_device_alloc(ctx, reinterpret_cast<void**>(&pl->d_desc), count * sizeof(SysDesc));
   if (s == LA_OK) s = la_device_alloc(ctx, reinterpret_cast<void**>(&pl->d_queue), 64);
+  if (s == LA_OK)
+    s = la_device_alloc(ctx, reinterpret_cast<void**>(&pl->d_redo), (size_t)(count + 1) * sizeof(int));
   if (s == LA_OK) s = la_device_alloc(ctx, reinterpret_cast<void**>(&pl->d_status), count * sizeof(int));
   if (s == LA_OK) s = la_device_alloc(ctx, reinterpret_cast<void**>(&pl->d_eta), count * sizeof(double));
   if (s == LA_OK) s = la_device_alloc(ctx, reinterpret_cast<void**>(&pl->d_cycles), count * sizeof(long long));
@@ -1251,6 +1263,7 @@ void la_batch_plan_destroy(la_batch_plan pl) {
   if (pl->graph) cudaGraphDestroy(pl->graph);
   la_device_free(ctx, pl->d_desc);
   la_device_free(ctx, pl->d_queue);
+  la_device_free(ctx, pl->d_redo);
   la_device_free(ctx, pl->d_status);
   la_device_free(ctx, pl->d_eta);
   la_device_free(ctx, pl->d_cycles);
