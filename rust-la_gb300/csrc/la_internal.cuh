@@ -137,6 +137,8 @@ la_status launch_trsm_rowpanel(la_ctx ctx, bool exact, double* A, double* S, siz
 la_status launch_panel_f32(la_ctx ctx, cudaStream_t stream, float* A, size_t ld, int m, int j0,
                            int jb, int* d_ipiv, unsigned* bar_base);
 la_status launch_laswp_f32(la_ctx ctx, float* A, size_t ld, int n, int j0, int jb);
+la_status launch_laswp_seq_f32(la_ctx ctx, float* A, size_t ld, const int* ipiv, int k0, int k1,
+                               int c0, int c1);
 la_status launch_panel_cluster_f32(la_ctx ctx, float* A, size_t ld, int m, int j0, int jb,
                                    int* d_ipiv);
 la_status launch_trsm_rowpanel_f32(la_ctx ctx, float* A, size_t ld, int j0, int jb, int c_begin,

@@ -35,6 +35,27 @@ laswp_kernel(T* M0, T* M1, T* M2, size_t ld, int b0, int e0, int b1, int e1,
     if (ok) M[(size_t)dst[q] * ld + c] = tmp[q][threadIdx.x % SW_COLS];
 }
 
+// Row interchanges of pivot positions [k0, k1) (ipiv[k] = the row swapped with
+// row k, in order) on columns [c0, c1): one thread per column applies the swaps
+// in sequence (the panel's own composed moves are for the columns next to the
+// panel; this form serves columns whose swaps were deferred).
+template <typename T>
+__global__ void laswp_seq_kernel(T* A, size_t ld, const int* __restrict__ ipiv, int k0, int k1,
+                                 int c0, int c1) {
+  const int c = c0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= c1) return;
+  for (int k = k0; k < k1; k++) {
+    const int p = ipiv[k];
+    if (p != k) {
+      T* a = A + (size_t)k * ld + c;
+      T* b = A + (size_t)p * ld + c;
+      const T t = *a;
+      *a = *b;
+      *b = t;
+    }
+  }
+}
+
 // ---- row-panel triangular update: U12 = L11^{-1} A12 ----------------------
 // Rows [j0, j0+jb), columns [c_begin, c_end), one 32-column strip per CTA.
 // Column sweep over k (one barrier per k): row k is finished, then every row
@@ -240,6 +261,14 @@ la_status launch_laswp(la_ctx ctx, bool exact, double* A, double* S, size_t ld, 
 }
 la_status launch_laswp_f32(la_ctx ctx, float* A, size_t ld, int n, int j0, int jb) {
   return launch_laswp_t<float>(ctx, ctx->stream, false, A, nullptr, ld, n, j0, jb);
+}
+la_status launch_laswp_seq_f32(la_ctx ctx, float* A, size_t ld, const int* ipiv, int k0, int k1,
+                               int c0, int c1) {
+  if (k1 <= k0 || c1 <= c0) return LA_OK;
+  laswp_seq_kernel<float><<<(c1 - c0 + 255) / 256, 256, 0, ctx->stream>>>(A, ld, ipiv, k0, k1, c0,
+                                                                          c1);
+  ctx->launches++;
+  return la_check_launch(ctx, "laswp_seq_kernel");
 }
 
 template <typename T>

@@ -281,96 +281,154 @@ la_status ensure_dinv(la_ctx ctx, la_lu h) {
   return LA_OK;
 }
 
-// Factors h->d_lu32 (m x n, pitch ld32) in place; pivots into h->d_ipiv.
+// Factors h->d_lu32 (n x n, pitch ld32) in place; pivots into h->d_ipiv.
+//
+// Schedule with lookahead (outer panel P = [a, b), next Q = [b, c)):
+//   after P's inner panels: P's row swaps on the columns >= b (deferred, see
+//   below); U12 = L11^-1 A12 for Q's columns; A22 -= L21 U12 on Q's columns;
+//   then Q's inner panels start on the high-priority side stream while the
+//   main stream finishes U12 and A22 -= L21 U12 on the columns >= c. The two
+//   touch disjoint data: Q's panels read and write rows >= b of columns < c
+//   (their row swaps are limited to those columns), the rest of the update
+//   writes columns >= c and reads L21 and U12 through packed copies. Q's swaps
+//   reach the columns >= c after the join, and the update of those columns
+//   saw the rows in the order before Q's swaps, consistently with its packed
+//   L21. Without lookahead the same steps run on one stream.
 la_status mixed_factor(la_ctx ctx, la_lu h, int prec) {
   const int m = (int)h->m, n = (int)h->n;
   const int kmin = std::min(m, n);
   float* A = h->d_lu32;
   const size_t ld = h->ld32;
-  cudaStream_t st = ctx->stream;
-  LA_CUDA(ctx, cudaMemsetAsync(ctx->d_bar, 0, sizeof(unsigned), st));
+  cudaStream_t ms = ctx->stream;
+  const bool look = ctx->lookahead != 0 && ctx->side_stream != nullptr;
+  cudaStream_t ss = look ? ctx->side_stream : ms;
+  LA_CUDA(ctx, cudaMemsetAsync(ctx->d_bar, 0, sizeof(unsigned), ms));
   unsigned bar_base = 0;
   Buf lh(ctx), uh(ctx), stat(ctx);
   const size_t ldk = pad8(WO);
   if (prec != LA_PREC_FP32) {
     LA_TRY(lh.alloc((size_t)m * ldk * 2 + 256));
     LA_TRY(uh.alloc((size_t)n * ldk * 2 + 256));
+  } else {
+    LA_TRY(lh.alloc((size_t)m * ldk * 4 + 256));  // FP32 copy of L21
   }
   LA_TRY(stat.alloc(256));
   float* d_stat = stat.as<float>();
 
-  for (int j0 = 0; j0 < kmin; j0 += WO) {
-    const int jbo = std::min(WO, kmin - j0);
-    const int j1o = j0 + jbo;
-    // Inner blocked LU of the outer panel's columns.
-    for (int i0 = j0; i0 < j1o; i0 += WI) {
+  // Inner panels of the outer panel [j0, j1o) on stream s; row swaps on the
+  // columns < climit only.
+  auto inner = [&](int j0, int j1o, int climit, cudaStream_t s) -> la_status {
+    cudaStream_t saved = ctx->stream;
+    ctx->stream = s;
+    la_status st = LA_OK;
+    for (int i0 = j0; i0 < j1o && st == LA_OK; i0 += WI) {
       const int ib = std::min(WI, j1o - i0);
       const int i1 = i0 + ib;
       // One thread-block cluster holds the panel when it fits; else the
       // cooperative multi-CTA kernel.
-      la_status ps = ctx->cluster_panels ? launch_panel_cluster_f32(ctx, A, ld, m, i0, ib, h->d_ipiv)
-                                         : LA_UNSUPPORTED;
-      if (ps == LA_UNSUPPORTED)
-        ps = launch_panel_f32(ctx, st, A, ld, m, i0, ib, h->d_ipiv, &bar_base);
-      LA_TRY(ps);
-      LA_TRY(launch_laswp_f32(ctx, A, ld, n, i0, ib));
-      if (i1 < j1o) {
-        LA_TRY(launch_trsm_rowpanel_f32(ctx, A, ld, i0, ib, i1, j1o));
-        if (i1 < m)
-          LA_TRY(launch_gemm_f32(ctx, GM_FMA_SUB, m - i1, j1o - i1, ib, A + (size_t)i1 * ld + i0,
-                                 ld, A + (size_t)i0 * ld + i1, ld, A + (size_t)i1 * ld + i1, ld));
+      st = ctx->cluster_panels ? launch_panel_cluster_f32(ctx, A, ld, m, i0, ib, h->d_ipiv)
+                               : LA_UNSUPPORTED;
+      if (st == LA_UNSUPPORTED) st = launch_panel_f32(ctx, s, A, ld, m, i0, ib, h->d_ipiv, &bar_base);
+      if (st == LA_OK) st = launch_laswp_f32(ctx, A, ld, climit, i0, ib);
+      if (st == LA_OK && i1 < j1o) {
+        st = launch_trsm_rowpanel_f32(ctx, A, ld, i0, ib, i1, j1o);
+        if (st == LA_OK && i1 < m)
+          st = launch_gemm_f32(ctx, GM_FMA_SUB, m - i1, j1o - i1, ib, A + (size_t)i1 * ld + i0, ld,
+                               A + (size_t)i0 * ld + i1, ld, A + (size_t)i1 * ld + i1, ld);
       }
     }
-    if (j1o >= n) continue;
-    // Outer row-panel triangular update U12 = L11^-1 A12, blocked by WI.
+    ctx->stream = saved;
+    return st;
+  };
+  // U12 = L11^-1 A12 for rows [j0, j1o) on columns [c0, c1), blocked by WI.
+  auto outer_trsm = [&](int j0, int j1o, int c0, int c1) -> la_status {
     for (int i0 = j0; i0 < j1o; i0 += WI) {
       const int ib = std::min(WI, j1o - i0);
       const int i1 = i0 + ib;
-      LA_TRY(launch_trsm_rowpanel_f32(ctx, A, ld, i0, ib, j1o, n));
+      LA_TRY(launch_trsm_rowpanel_f32(ctx, A, ld, i0, ib, c0, c1));
       if (i1 < j1o)
-        LA_TRY(launch_gemm_f32(ctx, GM_FMA_SUB, j1o - i1, n - j1o, ib, A + (size_t)i1 * ld + i0, ld,
-                               A + (size_t)i0 * ld + j1o, ld, A + (size_t)i1 * ld + j1o, ld));
+        LA_TRY(launch_gemm_f32(ctx, GM_FMA_SUB, j1o - i1, c1 - c0, ib, A + (size_t)i1 * ld + i0, ld,
+                               A + (size_t)i0 * ld + c0, ld, A + (size_t)i1 * ld + c0, ld));
     }
-    if (j1o >= m) continue;
-    // Trailing update A22 -= L21 * U12.
-    const int M = m - j1o, N = n - j1o;
-    float* C = A + (size_t)j1o * ld + j1o;
+    return LA_OK;
+  };
+  // A22 -= L21 U12 for rows >= j1o on columns [c0, c1). L21 is copied once per
+  // outer panel (pack_l) before the next panel's row swaps can permute it:
+  // 16-bit K-major for the tensor cores, FP32 for the SIMT update; U12 is
+  // packed per call (with its own FP16 scale).
+  auto update = [&](int j0, int j1o, int c0, int c1, bool pack_l) -> la_status {
+    if (c1 <= c0 || j1o >= m) return LA_OK;
+    const int jbo = j1o - j0, M = m - j1o, N = c1 - c0;
+    float* C = A + (size_t)j1o * ld + c0;
     if (prec == LA_PREC_FP32) {
-      LA_TRY(launch_gemm_f32(ctx, GM_FMA_SUB, M, N, jbo, A + (size_t)j1o * ld + j0, ld,
-                             A + (size_t)j0 * ld + j1o, ld, C, ld));
-      continue;
+      if (pack_l)
+        LA_CUDA(ctx, cudaMemcpy2DAsync(lh.p, ldk * sizeof(float), A + (size_t)j1o * ld + j0,
+                                       ld * sizeof(float), (size_t)jbo * sizeof(float), (size_t)M,
+                                       cudaMemcpyDeviceToDevice, ms));
+      return launch_gemm_f32(ctx, GM_FMA_SUB, M, N, jbo, lh.as<float>(), ldk,
+                             A + (size_t)j0 * ld + c0, ld, C, ld);
     }
     const int fmt = prec == LA_PREC_BF16 ? LA_LOWP_BF16 : LA_LOWP_FP16;
     const float* L21 = A + (size_t)j1o * ld + j0;
-    const float* U12 = A + (size_t)j0 * ld + j1o;
+    const float* U12 = A + (size_t)j0 * ld + c0;
+    uint16_t* ub = uh.as<uint16_t>() + (size_t)(c0 - j1o) * ldk;
     if (fmt == LA_LOWP_FP16) {
-      LA_CUDA(ctx, cudaMemsetAsync(d_stat, 0, 2 * sizeof(float), st));
-      absmax_kernel<<<grid_for(ctx, (size_t)jbo * N), 256, 0, st>>>(U12, ld, jbo, N, d_stat);
+      LA_CUDA(ctx, cudaMemsetAsync(d_stat, 0, 2 * sizeof(float), ms));
+      absmax_kernel<<<grid_for(ctx, (size_t)jbo * N), 256, 0, ms>>>(U12, ld, jbo, N, d_stat);
       ctx->launches++;
       LA_TRY(la_check_launch(ctx, "absmax_kernel"));
     } else {
-      set_alpha_one<<<1, 1, 0, st>>>(d_stat);
+      set_alpha_one<<<1, 1, 0, ms>>>(d_stat);
       ctx->launches++;
       LA_TRY(la_check_launch(ctx, "set_alpha_one"));
     }
-    if (fmt == LA_LOWP_BF16)
-      pack_l_kernel<LA_LOWP_BF16><<<grid_for(ctx, (size_t)M * ldk), 256, 0, st>>>(
-          L21, ld, lh.as<uint16_t>(), ldk, M, jbo);
-    else
-      pack_l_kernel<LA_LOWP_FP16><<<grid_for(ctx, (size_t)M * ldk), 256, 0, st>>>(
-          L21, ld, lh.as<uint16_t>(), ldk, M, jbo);
-    ctx->launches++;
-    LA_TRY(la_check_launch(ctx, "pack_l_kernel"));
+    if (pack_l) {
+      if (fmt == LA_LOWP_BF16)
+        pack_l_kernel<LA_LOWP_BF16><<<grid_for(ctx, (size_t)M * ldk), 256, 0, ms>>>(
+            L21, ld, lh.as<uint16_t>(), ldk, M, jbo);
+      else
+        pack_l_kernel<LA_LOWP_FP16><<<grid_for(ctx, (size_t)M * ldk), 256, 0, ms>>>(
+            L21, ld, lh.as<uint16_t>(), ldk, M, jbo);
+      ctx->launches++;
+      LA_TRY(la_check_launch(ctx, "pack_l_kernel"));
+    }
     dim3 pg((N + 31) / 32, ((int)ldk + 31) / 32);
     if (fmt == LA_LOWP_BF16)
-      pack_ut_kernel<LA_LOWP_BF16><<<pg, dim3(32, 8), 0, st>>>(U12, ld, uh.as<uint16_t>(), ldk,
-                                                               jbo, N, d_stat);
+      pack_ut_kernel<LA_LOWP_BF16><<<pg, dim3(32, 8), 0, ms>>>(U12, ld, ub, ldk, jbo, N, d_stat);
     else
-      pack_ut_kernel<LA_LOWP_FP16><<<pg, dim3(32, 8), 0, st>>>(U12, ld, uh.as<uint16_t>(), ldk,
-                                                               jbo, N, d_stat);
+      pack_ut_kernel<LA_LOWP_FP16><<<pg, dim3(32, 8), 0, ms>>>(U12, ld, ub, ldk, jbo, N, d_stat);
     ctx->launches++;
     LA_TRY(la_check_launch(ctx, "pack_ut_kernel"));
-    LA_TRY(launch_tc_update(ctx, st, fmt, M, N, jbo, lh.p, ldk, uh.p, ldk, C, ld, d_stat + 1));
+    return launch_tc_update(ctx, ms, fmt, M, N, jbo, lh.p, ldk, ub, ldk, C, ld, d_stat + 1);
+  };
+
+  // The first outer panel on the main stream.
+  LA_TRY(inner(0, std::min(WO, kmin), std::min(WO, kmin), ms));
+  for (int j0 = 0; j0 < kmin; j0 += WO) {
+    const int j1o = std::min(j0 + WO, kmin);
+    if (j1o >= n) break;
+    const int j2o = std::min(j1o + WO, kmin);  // the next outer panel [j1o, j2o)
+    // this panel's swaps on the columns its inner panels left out
+    LA_TRY(launch_laswp_seq_f32(ctx, A, ld, h->d_ipiv, j0, j1o, j1o, n));
+    LA_TRY(outer_trsm(j0, j1o, j1o, j2o));
+    LA_TRY(update(j0, j1o, j1o, j2o, true));
+    bool forked = false;
+    if (j1o < kmin) {
+      if (look) {
+        LA_CUDA(ctx, cudaEventRecord(ctx->ev_fork, ms));
+        LA_CUDA(ctx, cudaStreamWaitEvent(ss, ctx->ev_fork, 0));
+      }
+      LA_TRY(inner(j1o, j2o, j2o, ss));
+      forked = look;
+    }
+    if (j2o < n) {
+      LA_TRY(outer_trsm(j0, j1o, j2o, n));
+      LA_TRY(update(j0, j1o, j2o, n, false));
+    }
+    if (forked) {
+      LA_CUDA(ctx, cudaEventRecord(ctx->ev_join, ss));
+      LA_CUDA(ctx, cudaStreamWaitEvent(ms, ctx->ev_join, 0));
+    }
   }
   return LA_OK;
 }
