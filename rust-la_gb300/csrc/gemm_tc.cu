@@ -9,7 +9,8 @@
 //   warp 1 lane 0 : MMA issuer. 4 x tcgen05.mma (M=128, N=128, K=16) per chunk;
 //                   tcgen05.commit releases the stage
 //   all 4 warps   : epilogue. tcgen05.ld of the warp's 32 TMEM lanes (rows),
-//                   then C -= alpha * acc
+//                   -alpha * acc into swizzled shared-memory boxes, added to C
+//                   by TMA tensor reductions (the SMs never load C)
 // Shared memory is 3 x 32 KB per CTA, so two CTAs share an SM and one CTA's
 // epilogue overlaps the other's MMAs. Every mbarrier wait is bounded (2 s by
 // %globaltimer). On timeout the CTA records an error, waits (bounded) for its
@@ -28,6 +29,8 @@ constexpr uint32_t A_BYTES = TM * TK * 2;  // 16 KB
 constexpr uint32_t B_BYTES = TN * TK * 2;  // 16 KB
 constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr size_t TC_SMEM = (size_t)STAGES * STAGE_BYTES + 1024;  // + alignment slack
+constexpr uint32_t C_BOX_BYTES = TM * 32 * 4;  // one 128 x 32 FP32 box of the epilogue
+static_assert((TN / 32) * C_BOX_BYTES <= STAGES * STAGE_BYTES, "epilogue boxes reuse the stages");
 constexpr uint32_t TMEM_COLS = 128;
 
 using la_tma::mbar_expect_tx;
@@ -62,9 +65,9 @@ __host__ __device__ constexpr uint32_t idesc_f16(uint32_t ab_fmt) {
 
 __global__ void __launch_bounds__(TC_THREADS, 1)
 tc_update_kernel(const __grid_constant__ CUtensorMap tmap_a,
-                 const __grid_constant__ CUtensorMap tmap_b, float* __restrict__ C, size_t ldc,
-                 int M, int N, int K, const float* __restrict__ alpha_ptr, uint32_t idesc,
-                 int* err) {
+                 const __grid_constant__ CUtensorMap tmap_b,
+                 const __grid_constant__ CUtensorMap tmap_c, int N, int K,
+                 const float* __restrict__ alpha_ptr, uint32_t idesc, int* err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], done;
   __shared__ uint32_t tmem_holder;
@@ -146,14 +149,21 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tmap_a,
   }
   __syncwarp();
 
-  // Epilogue: every thread owns one accumulator row (TMEM lane). The decision
-  // is block-uniform so the warp-collective tcgen05.ld runs on full warps.
+  // Epilogue: every thread owns one accumulator row (TMEM lane). It writes
+  // -alpha * acc, 32 columns at a time, into the freed pipeline buffers as
+  // four 128 x 32 FP32 boxes in the 128-byte swizzled layout (row r's 16-byte
+  // group q at r * 128 + ((q ^ (r & 7)) << 4): a warp's float4 stores are
+  // conflict-free), and one thread adds the boxes to C with TMA tensor
+  // reductions (cp.reduce.async.bulk.tensor .add): the read-modify-write of C
+  // happens in L2, the SMs never load C, and the TMA unit clips the tile at
+  // the matrix edges. The decision is block-uniform so the warp-collective
+  // tcgen05.ld runs on full warps.
   const bool waited = mbar_wait(&done, 0, err);
   const bool have = __syncthreads_and(waited ? 1 : 0) && !s_fail;
   asm volatile("tcgen05.fence::after_thread_sync;");
   if (have) {
-    const float alpha = *alpha_ptr;
-    const int row = m0 + warp * 32 + lane;
+    const float nalpha = -*alpha_ptr;
+    const int rl = warp * 32 + lane;
 #pragma unroll 1
     for (int cc = 0; cc < TN / 32; cc++) {
       uint32_t r[32];
@@ -169,25 +179,30 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tmap_a,
             "=r"(r[31])
           : "r"(taddr));
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      const int c0 = n0 + cc * 32;
-      if (row < M) {
-        float* crow = C + (size_t)row * ldc + c0;
-        if (c0 + 32 <= N) {
+      unsigned char* box = smem + (size_t)cc * C_BOX_BYTES;
 #pragma unroll
-          for (int j = 0; j < 32; j += 4) {
-            float4 v = *reinterpret_cast<float4*>(crow + j);
-            v.x -= alpha * __uint_as_float(r[j]);
-            v.y -= alpha * __uint_as_float(r[j + 1]);
-            v.z -= alpha * __uint_as_float(r[j + 2]);
-            v.w -= alpha * __uint_as_float(r[j + 3]);
-            *reinterpret_cast<float4*>(crow + j) = v;
-          }
-        } else {
-          for (int j = 0; j < 32; j++)
-            if (c0 + j < N) crow[j] -= alpha * __uint_as_float(r[j]);
-        }
+      for (int q = 0; q < 8; q++) {
+        const float4 v = make_float4(nalpha * __uint_as_float(r[4 * q]),
+                                     nalpha * __uint_as_float(r[4 * q + 1]),
+                                     nalpha * __uint_as_float(r[4 * q + 2]),
+                                     nalpha * __uint_as_float(r[4 * q + 3]));
+        *reinterpret_cast<float4*>(box + rl * 128 + ((q ^ (rl & 7)) << 4)) = v;
       }
     }
+    // the boxes, written through the generic proxy, are read by the TMA unit
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  if (have && tid == 0) {
+    for (int cc = 0; cc < TN / 32; cc++)
+      if (n0 + cc * 32 < N)
+        asm volatile(
+            "cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.tile.bulk_group"
+            " [%0, {%1, %2}], [%3];" ::"l"(reinterpret_cast<uint64_t>(&tmap_c)),
+            "r"(n0 + cc * 32), "r"(m0), "r"(smem_u32(smem + (size_t)cc * C_BOX_BYTES))
+            : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
   }
   // On failure: wait (bounded) for this CTA's copies still in flight.
   if (!have && warp == 0 && lane == 0) {
@@ -224,9 +239,14 @@ la_status launch_tc_update(la_ctx ctx, cudaStream_t stream, int fmt, int M, int 
   if ((lda % 8) || (ldb % 8) || (ldc % 4) || (reinterpret_cast<uintptr_t>(A) % 16) ||
       (reinterpret_cast<uintptr_t>(B) % 16) || (reinterpret_cast<uintptr_t>(C) % 16))
     return LA_INVALID;
-  CUtensorMap ta, tb;
+  CUtensorMap ta, tb, tc;
   if (!encode_operand(ctx, &ta, A, fmt, (size_t)M, (size_t)K, lda)) return LA_CUDA_ERROR;
   if (!encode_operand(ctx, &tb, B, fmt, (size_t)N, (size_t)K, ldb)) return LA_CUDA_ERROR;
+  // C (M x N FP32, pitch ldc) in 128 x 32 boxes, 128-byte swizzle: the epilogue's
+  // reduction target.
+  if (!la_tma::encode_2d(ctx, &tc, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, C, (size_t)M, (size_t)N,
+                         ldc, 32u, (uint32_t)TM, CU_TENSOR_MAP_SWIZZLE_128B))
+    return LA_CUDA_ERROR;
   static bool configured = false;
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(tc_update_kernel,
@@ -236,7 +256,7 @@ la_status launch_tc_update(la_ctx ctx, cudaStream_t stream, int fmt, int M, int 
   }
   dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM);
   const uint32_t idesc = idesc_f16(fmt == LA_LOWP_BF16 ? 1u : 0u);
-  tc_update_kernel<<<grid, TC_THREADS, TC_SMEM, stream>>>(ta, tb, C, ldc, M, N, K, d_alpha, idesc,
+  tc_update_kernel<<<grid, TC_THREADS, TC_SMEM, stream>>>(ta, tb, tc, N, K, d_alpha, idesc,
                                                            ctx->d_err);
   ctx->launches++;
   return la_check_launch(ctx, "tc_update_kernel");
