@@ -23,10 +23,16 @@
 // row is written to its final position at the end. Per column: the warp's
 // best (key, position) is one 64-bit word (key high, bit-inverted position
 // low, so the integer maximum is the reference's first maximum), the winning
-// lane of each warp publishes its row, one CTA barrier, warp 0 publishes the
-// CTA's candidate and row, one cluster barrier, and then every warp reads the
-// C candidates and the winner's row over distributed shared memory and
-// scales and updates its rows in registers.
+// lane of each warp publishes its row, one CTA barrier, and warp 0 pushes the
+// CTA's candidate (key and row, 144 bytes) into slot g of every CTA's receive
+// buffer with st.async, which completes the bytes on the receiving CTA's
+// mbarrier. Each CTA waits on its own mbarrier for the C candidates (bounded)
+// and then reads the winner's row locally. The receive buffers and barriers
+// alternate by column parity; a CTA can push column c + 2 only after every
+// CTA has pushed column c + 1, which each does after reading its column-c
+// slots, so no slot is overwritten before it is read. Cluster barriers remain
+// only at the start (barriers initialised) and the end (no CTA leaves while
+// pushes into it may be in flight).
 #include "la_internal.cuh"
 
 namespace {
@@ -79,6 +85,7 @@ struct ClusterPanelArgs {
   int m, j0, jb, rpc;
   int* ipiv;
   int* swaps;
+  int* err;  // the context's error word (bounded waits)
 };
 
 // The panel's row moves as one list for the row-swap kernel: swaps[0] = k,
@@ -238,10 +245,45 @@ __global__ void __launch_bounds__(CT, 1) panel_cluster_kernel(ClusterPanelArgs p
   if (g == 0 && tid == 0) build_swap_list(p, s_pivs);
 }
 
-__device__ __forceinline__ unsigned long long ld_remote_u64(uint32_t addr) {
-  unsigned long long v;
-  asm volatile("ld.shared::cluster.u64 %0, [%1];" : "=l"(v) : "r"(addr) : "memory");
-  return v;
+__device__ __forceinline__ unsigned long long gtimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+// Wait for the phase `parity` of a local mbarrier that remote CTAs complete
+// (acquire at cluster scope); gives up after 2 s or when the error word is
+// set, recording DERR_PANEL_TIMEOUT.
+__device__ bool cluster_mbar_wait(uint64_t* bar, uint32_t parity, int* err) {
+  const uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
+  unsigned long long t0 = 0;
+  for (unsigned i = 0;; i++) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((i & 63u) == 63u) {
+      if (*reinterpret_cast<volatile int*>(err) != 0) return false;
+      const unsigned long long now = gtimer_ns();
+      if (t0 == 0) t0 = now;
+      else if (now - t0 > 2000000000ull) {
+        atomicCAS(err, 0, (int)DERR_PANEL_TIMEOUT);
+        return false;
+      }
+    }
+  }
+}
+// 16-byte asynchronous store into another CTA's shared memory that completes
+// `bytes` on that CTA's mbarrier (both addresses from mapa).
+__device__ __forceinline__ void st_async_v4(uint32_t dst, uint32_t bar, uint32_t x, uint32_t y,
+                                            uint32_t z, uint32_t w) {
+  asm volatile(
+      "st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.b32 [%0], {%1, %2, %3, %4}, [%5];" ::
+          "r"(dst), "r"(x), "r"(y), "r"(z), "r"(w), "r"(bar)
+      : "memory");
 }
 
 // x = v[c] for a runtime c with compile-time register indices.
@@ -255,20 +297,30 @@ __device__ __forceinline__ float pick(const float (&v)[CW], int c) {
 template <int RPT>
 __global__ void __launch_bounds__(CT, 1) panel_cluster_reg_kernel(ClusterPanelArgs p) {
   constexpr int NW = CT / 32;
+  constexpr int SLOT = 36;  // words per pushed candidate: key (2), padding (2), row (32)
+  constexpr uint32_t SLOT_BYTES = SLOT * 4;
   __shared__ __align__(16) float wrow[2][NW][CW];
   __shared__ unsigned long long wkey[2][NW];
-  __shared__ __align__(16) float s_crow[2][CW];
-  __shared__ unsigned long long s_key[2];
+  __shared__ __align__(16) uint32_t recv[2][16][SLOT];
+  __shared__ __align__(8) uint64_t rbar[2];
   __shared__ int s_pivs[CW];
 
   const int g = (int)cta_rank();
-  const int C = (int)gridDim.x;  // one cluster per launch
+  const int C = (int)gridDim.x;  // one cluster per launch, C <= 16
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int rpc = p.rpc, jb = p.jb;
   const int row0 = p.j0 + g * rpc;
   const int nrows = max(0, min(rpc, p.m - row0));
   const bool vec = (p.ld % 4 == 0) && (p.j0 % 4 == 0) &&
                    (reinterpret_cast<uintptr_t>(p.A) % 16 == 0);
+
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(
+                     static_cast<uint32_t>(__cvta_generic_to_shared(&rbar[0]))));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(
+                     static_cast<uint32_t>(__cvta_generic_to_shared(&rbar[1]))));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
 
   float v[RPT][CW];
   int pos[RPT];
@@ -291,7 +343,9 @@ __global__ void __launch_bounds__(CT, 1) panel_cluster_reg_kernel(ClusterPanelAr
       for (int c = 0; c < CW; c++) v[q][c] = (pos[q] >= 0 && c < jb) ? src[c] : 0.f;
     }
   }
+  cluster_sync();  // every CTA's receive barriers are initialised before any push
 
+  bool ok = true;
   for (int c = 0; c < jb; c++) {
     const int j = p.j0 + c, par = c & 1;
     // 1. this thread's and this warp's best candidate
@@ -322,7 +376,8 @@ __global__ void __launch_bounds__(CT, 1) panel_cluster_reg_kernel(ClusterPanelAr
     }
     if (lane == 0) wkey[par][warp] = wb;
     __syncthreads();
-    // 2. the CTA's candidate (warp 0) for the cluster
+    // 2. warp 0 pushes the CTA's candidate (key and row) into slot g of every
+    //    CTA's receive buffer (the slots alternate by column parity).
     if (warp == 0) {
       const unsigned long long k = lane < NW ? wkey[par][lane] : 0ull;
       unsigned long long km = k;
@@ -332,13 +387,33 @@ __global__ void __launch_bounds__(CT, 1) panel_cluster_reg_kernel(ClusterPanelAr
         km = o > km ? o : km;
       }
       const unsigned cm = __ballot_sync(0xffffffffu, km != 0ull && k == km);
-      if (cm) s_crow[par][lane] = wrow[par][__ffs(cm) - 1][lane];
-      if (lane == 0) s_key[par] = km;
+      const float* crow = wrow[par][cm ? __ffs(cm) - 1 : 0];
+      if (lane < C) {
+        const uint32_t dst = remote_addr(&recv[par][g][0], (uint32_t)lane);
+        const uint32_t bar = remote_addr(&rbar[par], (uint32_t)lane);
+        st_async_v4(dst, bar, (uint32_t)km, (uint32_t)(km >> 32), 0u, 0u);
+#pragma unroll
+        for (int q = 0; q < CW / 4; q++) {
+          const float4 t = reinterpret_cast<const float4*>(crow)[q];
+          st_async_v4(dst + 16 + 16 * q, bar, __float_as_uint(t.x), __float_as_uint(t.y),
+                      __float_as_uint(t.z), __float_as_uint(t.w));
+        }
+      }
+      if (lane == 0)
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                         static_cast<uint32_t>(__cvta_generic_to_shared(&rbar[par]))),
+                     "r"((uint32_t)C * SLOT_BYTES)
+                     : "memory");
     }
-    cluster_sync();
-    // 3. the cluster's winner and its row, read by every warp
+    // 3. every CTA's candidate has landed here (or the wait gave up)
+    const bool got = cluster_mbar_wait(&rbar[par], (uint32_t)((c >> 1) & 1), p.err);
+    if (!__syncthreads_and(got ? 1 : 0)) {
+      ok = false;
+      break;
+    }
+    // 4. the winner and its row, from local shared memory
     const unsigned long long gk =
-        lane < C ? ld_remote_u64(remote_addr(&s_key[par], (uint32_t)lane)) : 0ull;
+        lane < C ? *reinterpret_cast<const unsigned long long*>(&recv[par][lane][0]) : 0ull;
     unsigned long long gm = gk;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -348,10 +423,10 @@ __global__ void __launch_bounds__(CT, 1) panel_cluster_reg_kernel(ClusterPanelAr
     const unsigned gmask = __ballot_sync(0xffffffffu, lane < C && gk == gm);
     const int gsrc = __ffs(gmask) - 1;  // the row at position j is a candidate: gm != 0
     const int piv = (int)(~(unsigned)(gm & 0xffffffffull));
-    const float u = ld_remote_f32(remote_addr(&s_crow[par][lane], (uint32_t)gsrc));
+    const float* urow = reinterpret_cast<const float*>(&recv[par][gsrc][4]);
     float uu[CW];
 #pragma unroll
-    for (int k = 0; k < CW; k++) uu[k] = __shfl_sync(0xffffffffu, u, k);
+    for (int k = 0; k < CW; k++) uu[k] = urow[k];
     const float d = pick(uu, c);
     const float sc = d != 0.f ? 1.f / d : 1.f;
 #pragma unroll
@@ -374,7 +449,8 @@ __global__ void __launch_bounds__(CT, 1) panel_cluster_reg_kernel(ClusterPanelAr
       s_pivs[c] = piv;
     }
   }
-  cluster_sync();  // remote reads of the last column are done everywhere
+  cluster_sync();  // no CTA leaves while pushes into its shared memory may be in flight
+  if (!ok) return;
 
   // each row to its final position
 #pragma unroll
@@ -435,6 +511,7 @@ la_status launch_reg(la_ctx ctx, float* A, size_t ld, int m, int j0, int jb, int
   a.rpc = rpc;
   a.ipiv = d_ipiv;
   a.swaps = ctx->d_swaps;
+  a.err = ctx->d_err;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(cluster);
   cfg.blockDim = dim3(CT);
@@ -517,6 +594,7 @@ la_status launch_panel_cluster_f32(la_ctx ctx, float* A, size_t ld, int m, int j
   a.rpc = rpc;
   a.ipiv = d_ipiv;
   a.swaps = ctx->d_swaps;
+  a.err = ctx->d_err;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(cluster);
   cfg.blockDim = dim3(CT);
