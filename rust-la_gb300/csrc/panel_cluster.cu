@@ -20,7 +20,13 @@
 // the rows in registers instead: thread t of CTA g owns rows row0 + t + 256 q
 // with their 32 panel values and their current positions. Rows never move
 // between threads; a pivot exchange swaps two position registers, and each
-// row is written to its final position at the end. Per column: the warp's
+// row is written to its final position at the end. With up to 2 rows per
+// thread each row's registers rotate left by one slot per column, so the
+// current column is always slot 0 and the update is 31 FMAs with fixed
+// register indices; the finished values collect at the end of the window, and
+// the published pivot row carries zeros there so that the update leaves them
+// unchanged (with 4 rows the rotation would not fit the register budget, and
+// the current column is picked by selects). Per column: the warp's
 // best (key, position) is one 64-bit word (key high, bit-inverted position
 // low, so the integer maximum is the reference's first maximum), the winning
 // lane of each warp publishes its row, one CTA barrier, and warp 0 pushes the
@@ -345,9 +351,14 @@ __global__ void __launch_bounds__(CT, 1) panel_cluster_reg_kernel(ClusterPanelAr
   }
   cluster_sync();  // every CTA's receive barriers are initialised before any push
 
+  // Register windows rotate for up to 2 rows per thread; with 4 the rotation
+  // would exceed the register budget, so the current column is picked by
+  // selects and the update is predicated per slot.
+  constexpr bool ROT = RPT <= 2;
   bool ok = true;
   for (int c = 0; c < jb; c++) {
     const int j = p.j0 + c, par = c & 1;
+    const int cur = ROT ? 0 : c;  // slot of the current column
     // 1. this thread's and this warp's best candidate
     unsigned long long best = 0ull;
     int bq = 0;
@@ -355,7 +366,8 @@ __global__ void __launch_bounds__(CT, 1) panel_cluster_reg_kernel(ClusterPanelAr
     for (int q = 0; q < RPT; q++)
       if (pos[q] >= j) {
         const unsigned long long pk =
-            ((unsigned long long)ckey(pick(v[q], c), pos[q], j) << 32) | (unsigned)(~pos[q]);
+            ((unsigned long long)ckey(ROT ? v[q][0] : pick(v[q], c), pos[q], j) << 32) |
+            (unsigned)(~pos[q]);
         if (pk > best) { best = pk; bq = q; }
       }
     unsigned long long wb = best;
@@ -366,12 +378,14 @@ __global__ void __launch_bounds__(CT, 1) panel_cluster_reg_kernel(ClusterPanelAr
     }
     const unsigned wmask = __ballot_sync(0xffffffffu, wb != 0ull && best == wb);
     if (wmask && lane == __ffs(wmask) - 1) {
+      // published without its finished slots (zeros: the update leaves the
+      // other rows' finished slots as they are)
       float* dst = wrow[par][warp];
 #pragma unroll
       for (int q = 0; q < RPT; q++)
         if (q == bq) {
 #pragma unroll
-          for (int k = 0; k < CW; k++) dst[k] = v[q][k];
+          for (int k = 0; k < CW; k++) dst[k] = (!ROT || k < CW - c) ? v[q][k] : 0.f;
         }
     }
     if (lane == 0) wkey[par][warp] = wb;
@@ -427,7 +441,7 @@ __global__ void __launch_bounds__(CT, 1) panel_cluster_reg_kernel(ClusterPanelAr
     float uu[CW];
 #pragma unroll
     for (int k = 0; k < CW; k++) uu[k] = urow[k];
-    const float d = pick(uu, c);
+    const float d = ROT ? uu[0] : pick(uu, cur);
     const float sc = d != 0.f ? 1.f / d : 1.f;
 #pragma unroll
     for (int q = 0; q < RPT; q++) {
@@ -436,12 +450,26 @@ __global__ void __launch_bounds__(CT, 1) panel_cluster_reg_kernel(ClusterPanelAr
       } else {
         if (pos[q] == j) pos[q] = piv;  // the displaced row takes the pivot's place
         if (pos[q] > j) {
-          const float x = pick(v[q], c);
-          const float l = d != 0.f ? x * sc : x;
+          if constexpr (ROT) {
+            const float l = d != 0.f ? v[q][0] * sc : v[q][0];
+            v[q][0] = l;
 #pragma unroll
-          for (int k = 0; k < CW; k++)
-            v[q][k] = k == c ? l : (k > c ? fmaf(-l, uu[k], v[q][k]) : v[q][k]);
+            for (int k = 1; k < CW; k++) v[q][k] = fmaf(-l, uu[k], v[q][k]);
+          } else {
+            const float x = pick(v[q], c);
+            const float l = d != 0.f ? x * sc : x;
+#pragma unroll
+            for (int k = 0; k < CW; k++)
+              v[q][k] = k == c ? l : (k > c ? fmaf(-l, uu[k], v[q][k]) : v[q][k]);
+          }
         }
+      }
+      if constexpr (ROT) {
+        // rotate: the next column comes to slot 0, the finished value to the end
+        const float t = v[q][0];
+#pragma unroll
+        for (int k = 0; k < CW - 1; k++) v[q][k] = v[q][k + 1];
+        v[q][CW - 1] = t;
       }
     }
     if (g == 0 && tid == 0) {
@@ -451,6 +479,16 @@ __global__ void __launch_bounds__(CT, 1) panel_cluster_reg_kernel(ClusterPanelAr
   }
   cluster_sync();  // no CTA leaves while pushes into its shared memory may be in flight
   if (!ok) return;
+  // jb rotations so far; 32 in all bring every value back to its column
+  if (ROT)
+    for (int r = jb; r < CW; r++)
+#pragma unroll
+    for (int q = 0; q < RPT; q++) {
+      const float t = v[q][0];
+#pragma unroll
+      for (int k = 0; k < CW - 1; k++) v[q][k] = v[q][k + 1];
+      v[q][CW - 1] = t;
+    }
 
   // each row to its final position
 #pragma unroll
