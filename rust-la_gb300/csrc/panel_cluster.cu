@@ -46,6 +46,8 @@ namespace {
 constexpr int CW = 32;      // panel width
 constexpr int CP = CW + 1;  // padded row pitch in shared memory
 constexpr int CT = 256;     // threads per CTA
+constexpr int PNW = CT / 32;  // warps per CTA
+constexpr int PSLOT = 36;     // words per pushed candidate: key (2), padding (2), row (32)
 
 __device__ __forceinline__ uint32_t cta_rank() {
   uint32_t r;
@@ -300,63 +302,18 @@ __device__ __forceinline__ float pick(const float (&v)[CW], int c) {
   return x;
 }
 
-template <int RPT>
-__global__ void __launch_bounds__(CT, 1) panel_cluster_reg_kernel(ClusterPanelArgs p) {
-  constexpr int NW = CT / 32;
-  constexpr int SLOT = 36;  // words per pushed candidate: key (2), padding (2), row (32)
-  constexpr uint32_t SLOT_BYTES = SLOT * 4;
-  __shared__ __align__(16) float wrow[2][NW][CW];
-  __shared__ unsigned long long wkey[2][NW];
-  __shared__ __align__(16) uint32_t recv[2][16][SLOT];
-  __shared__ __align__(8) uint64_t rbar[2];
-  __shared__ int s_pivs[CW];
-
-  const int g = (int)cta_rank();
-  const int C = (int)gridDim.x;  // one cluster per launch, C <= 16
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int rpc = p.rpc, jb = p.jb;
-  const int row0 = p.j0 + g * rpc;
-  const int nrows = max(0, min(rpc, p.m - row0));
-  const bool vec = (p.ld % 4 == 0) && (p.j0 % 4 == 0) &&
-                   (reinterpret_cast<uintptr_t>(p.A) % 16 == 0);
-
-  if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(
-                     static_cast<uint32_t>(__cvta_generic_to_shared(&rbar[0]))));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(
-                     static_cast<uint32_t>(__cvta_generic_to_shared(&rbar[1]))));
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-
-  float v[RPT][CW];
-  int pos[RPT];
-#pragma unroll
-  for (int q = 0; q < RPT; q++) {
-    const int lr = q * CT + tid;
-    pos[q] = lr < nrows ? row0 + lr : -1;
-    const float* src = p.A + (size_t)(lr < nrows ? row0 + lr : 0) * p.ld + p.j0;
-    if (pos[q] >= 0 && vec && jb == CW) {
-#pragma unroll
-      for (int c4 = 0; c4 < CW / 4; c4++) {
-        const float4 t = reinterpret_cast<const float4*>(src)[c4];
-        v[q][4 * c4] = t.x;
-        v[q][4 * c4 + 1] = t.y;
-        v[q][4 * c4 + 2] = t.z;
-        v[q][4 * c4 + 3] = t.w;
-      }
-    } else {
-#pragma unroll
-      for (int c = 0; c < CW; c++) v[q][c] = (pos[q] >= 0 && c < jb) ? src[c] : 0.f;
-    }
-  }
-  cluster_sync();  // every CTA's receive barriers are initialised before any push
-
-  // Register windows rotate for up to 2 rows per thread; with 4 the rotation
-  // would exceed the register budget, so the current column is picked by
-  // selects and the update is predicated per slot.
-  constexpr bool ROT = RPT <= 2;
-  bool ok = true;
-  for (int c = 0; c < jb; c++) {
+// One column of panel_cluster_reg_kernel (see there); false when a wait gave
+// up. ROT: the rows' register windows rotate (current column in slot 0);
+// otherwise the column is picked by selects, which the caller unrolls.
+template <int RPT, bool ROT>
+__device__ __forceinline__ bool panel_column(int c, const ClusterPanelArgs& p, int g, int C,
+                                             int tid, int lane, int warp, float (&v)[RPT][CW],
+                                             int (&pos)[RPT], float (*wrow)[PNW][CW],
+                                             unsigned long long (*wkey)[PNW],
+                                             uint32_t (*recv)[16][PSLOT], uint64_t* rbar,
+                                             int* s_pivs) {
+  constexpr int NW = PNW;
+  constexpr uint32_t SLOT_BYTES = PSLOT * 4;
     const int j = p.j0 + c, par = c & 1;
     const int cur = ROT ? 0 : c;  // slot of the current column
     // 1. this thread's and this warp's best candidate
@@ -421,10 +378,7 @@ __global__ void __launch_bounds__(CT, 1) panel_cluster_reg_kernel(ClusterPanelAr
     }
     // 3. every CTA's candidate has landed here (or the wait gave up)
     const bool got = cluster_mbar_wait(&rbar[par], (uint32_t)((c >> 1) & 1), p.err);
-    if (!__syncthreads_and(got ? 1 : 0)) {
-      ok = false;
-      break;
-    }
+    if (!__syncthreads_and(got ? 1 : 0)) return false;
     // 4. the winner and its row, from local shared memory
     const unsigned long long gk =
         lane < C ? *reinterpret_cast<const unsigned long long*>(&recv[par][lane][0]) : 0ull;
@@ -475,6 +429,80 @@ __global__ void __launch_bounds__(CT, 1) panel_cluster_reg_kernel(ClusterPanelAr
     if (g == 0 && tid == 0) {
       p.ipiv[j] = piv;
       s_pivs[c] = piv;
+    }
+  return true;
+}
+
+template <int RPT>
+__global__ void __launch_bounds__(CT, 1) panel_cluster_reg_kernel(ClusterPanelArgs p) {
+  __shared__ __align__(16) float wrow[2][PNW][CW];
+  __shared__ unsigned long long wkey[2][PNW];
+  __shared__ __align__(16) uint32_t recv[2][16][PSLOT];
+  __shared__ __align__(8) uint64_t rbar[2];
+  __shared__ int s_pivs[CW];
+
+  const int g = (int)cta_rank();
+  const int C = (int)gridDim.x;  // one cluster per launch, C <= 16
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int rpc = p.rpc, jb = p.jb;
+  const int row0 = p.j0 + g * rpc;
+  const int nrows = max(0, min(rpc, p.m - row0));
+  const bool vec = (p.ld % 4 == 0) && (p.j0 % 4 == 0) &&
+                   (reinterpret_cast<uintptr_t>(p.A) % 16 == 0);
+
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(
+                     static_cast<uint32_t>(__cvta_generic_to_shared(&rbar[0]))));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(
+                     static_cast<uint32_t>(__cvta_generic_to_shared(&rbar[1]))));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+
+  float v[RPT][CW];
+  int pos[RPT];
+#pragma unroll
+  for (int q = 0; q < RPT; q++) {
+    const int lr = q * CT + tid;
+    pos[q] = lr < nrows ? row0 + lr : -1;
+    const float* src = p.A + (size_t)(lr < nrows ? row0 + lr : 0) * p.ld + p.j0;
+    if (pos[q] >= 0 && vec && jb == CW) {
+#pragma unroll
+      for (int c4 = 0; c4 < CW / 4; c4++) {
+        const float4 t = reinterpret_cast<const float4*>(src)[c4];
+        v[q][4 * c4] = t.x;
+        v[q][4 * c4 + 1] = t.y;
+        v[q][4 * c4 + 2] = t.z;
+        v[q][4 * c4 + 3] = t.w;
+      }
+    } else {
+#pragma unroll
+      for (int c = 0; c < CW; c++) v[q][c] = (pos[q] >= 0 && c < jb) ? src[c] : 0.f;
+    }
+  }
+  cluster_sync();  // every CTA's receive barriers are initialised before any push
+
+  // Register windows rotate for up to 2 rows per thread; with 4 the rotation
+  // would exceed the register budget, so the current column is picked by
+  // selects and the update is predicated per slot.
+  constexpr bool ROT = RPT <= 2;
+  bool ok = true;
+  if constexpr (ROT) {
+    for (int c = 0; c < jb; c++)
+      if (!panel_column<RPT, true>(c, p, g, C, tid, lane, warp, v, pos, wrow, wkey, recv, rbar,
+                                   s_pivs)) {
+        ok = false;
+        break;
+      }
+  } else {
+    // unrolled over the 32 columns: every register index is static
+#pragma unroll
+    for (int c = 0; c < CW; c++) {
+      if (c >= jb) break;
+      if (!panel_column<RPT, false>(c, p, g, C, tid, lane, warp, v, pos, wrow, wkey, recv, rbar,
+                                    s_pivs)) {
+        ok = false;
+        break;
+      }
     }
   }
   cluster_sync();  // no CTA leaves while pushes into its shared memory may be in flight
