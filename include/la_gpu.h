@@ -87,7 +87,12 @@ typedef enum la_option {
    * LU-IR contracts but slowly (BF16 / FP8 storage of well-conditioned
    * systems); with FP32 factors the stalled systems have kappa u_32 near 1 and
    * need more Krylov steps than the FP64 redo costs. */
-  LA_OPT_BATCH_GMRES = 7
+  LA_OPT_BATCH_GMRES = 7,
+  /* Triangular solves of la_lu_solve (lu.rs:256-275): 1-8 (default 2) runs
+   * them as one persistent wavefront kernel per triangle with that many CTAs
+   * per SM; 0 launches one kernel per 16-row block step. Both apply every
+   * term in the same order, so their results are bit-identical. */
+  LA_OPT_SOLVE_WAVE = 8
 } la_option;
 
 #define LA_ARITH_FAST 0

@@ -141,6 +141,7 @@ la_status la_ctx_create(int device, la_ctx* out) {
   const size_t o_ds = off; off = align_up(off + 2 * MAX_PANEL_W * sizeof(double), 256);
   const size_t o_sw = off; off = align_up(off + (1 + 4 * MAX_PANEL_W) * sizeof(int), 256);
   const size_t o_sm = off; off = align_up(off + 8 * sizeof(double), 256);
+  const size_t o_sv = off; off = align_up(off + (2 + 2 * SOLVE_WAVE_MAX_GROUPS) * sizeof(int), 256);
   e = cudaMalloc(&ctx->d_scratch, off);
   if (e != cudaSuccess) {
     la_status s = la_cuda_fail(ctx, e, "scratch");
@@ -161,6 +162,7 @@ la_status la_ctx_create(int device, la_ctx* out) {
   ctx->d_diag_s = reinterpret_cast<double*>(base + o_ds);
   ctx->d_swaps = reinterpret_cast<int*>(base + o_sw);
   ctx->d_small = reinterpret_cast<double*>(base + o_sm);
+  ctx->d_solve_sync = reinterpret_cast<int*>(base + o_sv);
   e = cudaMallocHost(&ctx->h_pinned, 4096);
   if (e != cudaSuccess) {
     la_status s = la_cuda_fail(ctx, e, "pinned");
@@ -235,6 +237,10 @@ la_status la_ctx_set_option(la_ctx ctx, int option, int64_t value) {
       if (value < 0 || value > 20) return LA_INVALID;
       ctx->batch_gmres = (int)value;
       return LA_OK;
+    case LA_OPT_SOLVE_WAVE:
+      if (value < 0 || value > 8) return LA_INVALID;
+      ctx->solve_wave = (int)value;
+      return LA_OK;
   }
   return LA_INVALID;
 }
@@ -249,6 +255,7 @@ la_status la_ctx_get_option(la_ctx ctx, int option, int64_t* value) {
     case LA_OPT_LOOKAHEAD: *value = ctx->lookahead; return LA_OK;
     case LA_OPT_CLUSTER_PANEL: *value = ctx->cluster_panels; return LA_OK;
     case LA_OPT_BATCH_GMRES: *value = ctx->batch_gmres; return LA_OK;
+    case LA_OPT_SOLVE_WAVE: *value = ctx->solve_wave; return LA_OK;
   }
   return LA_INVALID;
 }

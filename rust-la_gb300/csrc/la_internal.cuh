@@ -31,6 +31,9 @@ enum GemmMode : int {
 
 constexpr int MAX_PANEL_CTAS = 1024;
 constexpr int MAX_PANEL_W = 64;
+// Column groups (4 right-hand sides each) of the wavefront triangular solve;
+// more right-hand sides take the block-step solve.
+constexpr int SOLVE_WAVE_MAX_GROUPS = 1024;
 
 // Device-side error codes written to la_context::d_err.
 enum DeviceErr : int {
@@ -54,6 +57,7 @@ struct la_context {
   int lookahead = 1;
   int cluster_panels = 1;                // FP32 panels on one thread-block cluster
   int batch_gmres = 0;                   // Krylov steps per GMRES correction in batch plans (0: off)
+  int solve_wave = 2;                    // CTAs per SM of the wavefront solve (0: block steps)
   int sm_count = 0;
   size_t smem_optin = 0;
   int arith = LA_ARITH_FAST;
@@ -79,6 +83,7 @@ struct la_context {
   double* d_diag_s = nullptr;    // [2][64]
   int* d_swaps = nullptr;        // [1 + 2*128] composed row moves of one panel
   double* d_small = nullptr;     // [8] small device results (det, flags)
+  int* d_solve_sync = nullptr;   // [2 + 2*SOLVE_WAVE_MAX_GROUPS] wavefront solve tickets, progress
   void* h_pinned = nullptr;      // pinned host staging for small readbacks
 };
 

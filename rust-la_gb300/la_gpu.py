@@ -27,6 +27,7 @@ LIB_PATH = os.path.join(_HERE, "liblagpu.so")
 OK, SINGULAR, BADSHAPE, INVALID, NOMEM, CUDA_ERROR, TIMEOUT, NOT_CONVERGED, UNSUPPORTED = range(9)
 OPT_ARITH, OPT_PANEL_WIDTH, OPT_PANEL_CTAS, OPT_PROFILE, OPT_LOOKAHEAD, OPT_CLUSTER_PANEL = 1, 2, 3, 4, 5, 6
 OPT_BATCH_GMRES = 7
+OPT_SOLVE_WAVE = 8
 ARITH_FAST, ARITH_EXACT = 0, 1
 
 
