@@ -73,25 +73,49 @@ __global__ void invert_diag_kernel(const TF* __restrict__ LU, size_t ld, int n, 
 }
 
 // Factors in TF (FP32 for the mixed LU), vectors and the inverted diagonal
-// blocks in T (FP64): the solves run at working precision, which GMRES-IR
-// needs from its preconditioner.
+// blocks in T (FP64 for GMRES-IR, whose preconditioner must run at working
+// precision; FP32 for plain refinement).
+constexpr int LPRE = BS * BS / TT;    // elements of an off-diagonal tile per thread
+constexpr int YPRE = BS * MAXR / TT;  // elements of a block of x per thread
+
 template <typename TF, typename T>
 constexpr size_t wave_smem() {
-  return sizeof(TF) * BS * (BS + 1) + sizeof(T) * (BS * (BS + 1) + 2 * BS * MAXR);
+  return sizeof(T) * (BS * (BS + 1) + 3 * BS * MAXR) + sizeof(TF) * 2 * BS * (BS + 1);
 }
 
+// Largest u' >= u whose block is already solved, looking at most 8 blocks
+// further (a solved block implies every earlier one is solved).
+__device__ __forceinline__ int peek_solved(const int* flags, int nb, bool upper, int u, int t) {
+  const int lim = min(t - 1, u + 8);
+  while (u < lim) {
+    const int kb = upper ? nb - 2 - u : u + 1;
+    if (ld_acquire(flags + kb) == 0) break;
+    u++;
+  }
+  return u;
+}
+
+// CTA with ticket t owns block b and takes the t earlier blocks in order
+// (u = 0 .. t-1). The history loop is pipelined: the next off-diagonal tile is
+// loaded into registers while the current one is applied, and the next block
+// of x too once its flag is known to be set, so a CTA that is far from the
+// frontier applies a block per tile product instead of per two memory round
+// trips. The terms of each element are applied in the same order as a plain
+// loop over u and k.
 template <typename TF, typename T, bool UPPER>
 __global__ void __launch_bounds__(TT)
 trsv_wave_kernel(const TF* __restrict__ LU, size_t ld, const T* __restrict__ dinv, T* X, size_t ldx,
                  int n, int nrhs, int nb, int* flags, int* ticket, int* err) {
   extern __shared__ __align__(16) double wave_raw[];
   T(*db)[BS + 1] = reinterpret_cast<T(*)[BS + 1]>(wave_raw);
-  T(*ys)[MAXR] = reinterpret_cast<T(*)[MAXR]>(reinterpret_cast<T*>(wave_raw) + BS * (BS + 1));
+  T(*ys)[BS][MAXR] = reinterpret_cast<T(*)[BS][MAXR]>(reinterpret_cast<T*>(wave_raw) +
+                                                      BS * (BS + 1));
   T(*acc)[MAXR] = reinterpret_cast<T(*)[MAXR]>(reinterpret_cast<T*>(wave_raw) + BS * (BS + 1) +
-                                               BS * MAXR);
-  TF(*lb)[BS + 1] = reinterpret_cast<TF(*)[BS + 1]>(reinterpret_cast<T*>(wave_raw) +
-                                                    BS * (BS + 1) + 2 * BS * MAXR);
+                                               2 * BS * MAXR);
+  TF(*lb)[BS][BS + 1] = reinterpret_cast<TF(*)[BS][BS + 1]>(reinterpret_cast<T*>(wave_raw) +
+                                                            BS * (BS + 1) + 3 * BS * MAXR);
   __shared__ int s_t;
+  __shared__ int s_known;
   __shared__ int s_ok;
   const int tid = threadIdx.x;
   if (tid == 0) s_t = atomicAdd(ticket, 1);
@@ -105,50 +129,99 @@ trsv_wave_kernel(const TF* __restrict__ LU, size_t ld, const T* __restrict__ din
     int r = idx / MAXR, c = idx % MAXR;
     acc[r][c] = (r < bs && c < nrhs) ? X[(size_t)(r0 + r) * ldx + c] : T(0);
   }
-  for (int u = 0; u < t; u++) {
+  {
+    const T* d = dinv + ((size_t)b * 2 + (UPPER ? 1 : 0)) * BS * BS;
+    for (int idx = tid; idx < BS * BS; idx += TT) db[idx / BS][idx % BS] = __ldg(d + idx);
+  }
+
+  TF pre[LPRE];
+  T yv[YPRE];
+  auto fetch_tile = [&](int u) {
     const int kb = UPPER ? nb - 1 - u : u;
     const int k0 = kb * BS, kbs = min(BS, n - k0);
-    // The off-diagonal block does not depend on the flag: load it first.
-    for (int idx = tid; idx < BS * BS; idx += TT) {
-      int r = idx / BS, k = idx % BS;
-      lb[r][k] = (r < bs && k < kbs) ? LU[(size_t)(r0 + r) * ld + k0 + k] : TF(0);
+#pragma unroll
+    for (int e = 0; e < LPRE; e++) {
+      const int idx = tid + TT * e;
+      const int r = idx / BS, k = idx % BS;
+      pre[e] = (r < bs && k < kbs) ? __ldg(LU + (size_t)(r0 + r) * ld + k0 + k) : TF(0);
     }
-    if (tid == 0) {
-      int ok = 1;
-      unsigned long long t0 = 0;
-      unsigned spins = 0;
-      while (ld_acquire(flags + kb) == 0) {
-        if ((++spins & 63u) == 0) {
-          if (*reinterpret_cast<volatile int*>(err) != 0) { ok = 0; break; }
-          unsigned long long now = gtime();
-          if (t0 == 0) t0 = now;
-          else if (now - t0 > WAIT_NS) { atomicCAS(err, 0, (int)DERR_TRSV_TIMEOUT); ok = 0; break; }
-        }
+  };
+  auto fetch_x = [&](int u, T (&dst)[YPRE]) {
+    const int kb = UPPER ? nb - 1 - u : u;
+    const int k0 = kb * BS, kbs = min(BS, n - k0);
+#pragma unroll
+    for (int e = 0; e < YPRE; e++) {
+      const int idx = tid + TT * e;
+      const int r = idx / MAXR, c = idx % MAXR;
+      dst[e] = (r < kbs && c < nrhs) ? __ldcg(X + (size_t)(k0 + r) * ldx + c) : T(0);
+    }
+  };
+
+  int known = -1;       // last block u known to be solved (uniform)
+  bool have_y = false;  // yv holds block u's x (uniform)
+  if (t > 0) fetch_tile(0);
+  for (int u = 0; u < t; u++) {
+    const int buf = u & 1;
+#pragma unroll
+    for (int e = 0; e < LPRE; e++) {
+      const int idx = tid + TT * e;
+      lb[buf][idx / BS][idx % BS] = pre[e];
+    }
+    if (have_y) {
+#pragma unroll
+      for (int e = 0; e < YPRE; e++) {
+        const int idx = tid + TT * e;
+        ys[buf][idx / MAXR][idx % MAXR] = yv[e];
       }
-      s_ok = ok;
     }
-    __syncthreads();
-    if (!s_ok) return;
-    for (int idx = tid; idx < BS * MAXR; idx += TT) {
-      int r = idx / MAXR, c = idx % MAXR;
-      ys[r][c] = (r < kbs && c < nrhs) ? __ldcg(X + (size_t)(k0 + r) * ldx + c) : T(0);
+    if (u + 1 < t) fetch_tile(u + 1);
+    if (!have_y) {
+      if (tid == 0) {
+        int ok = 1;
+        int kn = known;
+        if (kn < u) {
+          const int kb = UPPER ? nb - 1 - u : u;
+          unsigned long long t0 = 0;
+          unsigned spins = 0;
+          while (ld_acquire(flags + kb) == 0) {
+            if ((++spins & 63u) == 0) {
+              if (*reinterpret_cast<volatile int*>(err) != 0) { ok = 0; break; }
+              unsigned long long now = gtime();
+              if (t0 == 0) t0 = now;
+              else if (now - t0 > WAIT_NS) { atomicCAS(err, 0, (int)DERR_TRSV_TIMEOUT); ok = 0; break; }
+            }
+          }
+          if (ok) kn = peek_solved(flags, nb, UPPER, u, t);
+        }
+        s_known = kn;
+        s_ok = ok;
+      }
+      __syncthreads();
+      if (!s_ok) return;
+      known = s_known;
+      T yt[YPRE];
+      fetch_x(u, yt);
+#pragma unroll
+      for (int e = 0; e < YPRE; e++) {
+        const int idx = tid + TT * e;
+        ys[buf][idx / MAXR][idx % MAXR] = yt[e];
+      }
     }
+    have_y = (u + 1 < t) && known >= u + 1;
+    if (have_y) fetch_x(u + 1, yv);
     __syncthreads();
 #pragma unroll
     for (int q = 0; q < MAXR / 4; q++) {
       const int j = jq + 4 * q;
       if (j < nrhs) {
         T s = acc[i][j];
-        for (int k = 0; k < BS; k++) s = fma(-(T)lb[i][k], ys[k][j], s);
+        for (int k = 0; k < BS; k++) s = fma(-(T)lb[buf][i][k], ys[buf][k][j], s);
         acc[i][j] = s;
       }
     }
-    __syncthreads();
   }
-  // y_b = D_b^-1 acc
-  const T* d = dinv + ((size_t)b * 2 + (UPPER ? 1 : 0)) * BS * BS;
-  for (int idx = tid; idx < BS * BS; idx += TT) db[idx / BS][idx % BS] = d[idx];
   __syncthreads();
+  // y_b = D_b^-1 acc
 #pragma unroll
   for (int q = 0; q < MAXR / 4; q++) {
     const int j = jq + 4 * q;
