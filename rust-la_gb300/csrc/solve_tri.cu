@@ -323,10 +323,13 @@ solve_wave_kernel(const T* __restrict__ LU, size_t ld, T* X, size_t ldx, int n, 
           if (lane > k) x = apply<EXACT, T>(x, xk, tile[lane][k]);
         }
       } else {
+        // Every lane takes row k's undivided value and divides it by u_kk in
+        // lockstep (the same operands give the same quotient in every lane), so
+        // the division is not a divergent branch on the chain.
         for (int k = sb - 1; k >= 0; k--) {
-          if (lane == k) x = x / tile[k][k];
-          const T xk = __shfl_sync(full, x, k);
-          if (lane < k) x = apply<EXACT, T>(x, xk, tile[lane][k]);
+          const T xk = __shfl_sync(full, x, k) / tile[k][k];
+          if (lane == k) x = xk;
+          else if (lane < k) x = apply<EXACT, T>(x, xk, tile[lane][k]);
         }
       }
     }
