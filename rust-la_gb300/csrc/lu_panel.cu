@@ -26,6 +26,7 @@
 // Every wait is bounded: a CTA that waits past the limit (or sees another CTA
 // give up) records DERR_PANEL_TIMEOUT and returns; the host reports LA_TIMEOUT.
 #include "la_internal.cuh"
+#include "swap_compose.cuh"
 
 namespace {
 
@@ -140,6 +141,7 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
   __shared__ int s_win_pos;
   __shared__ T s_scale;
   __shared__ int s_pivs[W];
+  __shared__ int s_atp[SWAP_SLOTS], s_atr[SWAP_SLOTS];
 
   const int g = blockIdx.x;
   const int tid = threadIdx.x;
@@ -320,29 +322,8 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
   }
   // Compose this panel's swaps into a list of row moves (dest <- src) for the
   // columns outside the panel (applied by the row-swap kernel).
-  if (g == 0 && tid == 0) {
-    int cnt = 0;
-    int* dst = p.swaps + 1;
-    int* src = p.swaps + 1 + 2 * W;
-    auto find_or_add = [&](int pos) {
-      for (int q = 0; q < cnt; q++)
-        if (dst[q] == pos) return q;
-      dst[cnt] = pos;
-      src[cnt] = pos;
-      return cnt++;
-    };
-    for (int c = 0; c < jb; c++) {
-      int a = find_or_add(p.j0 + c);
-      int b = find_or_add(s_pivs[c]);
-      int t = src[a];
-      src[a] = src[b];
-      src[b] = t;
-    }
-    int k = 0;
-    for (int q = 0; q < cnt; q++)
-      if (src[q] != dst[q]) { dst[k] = dst[q]; src[k] = src[q]; k++; }
-    p.swaps[0] = k;
-  }
+  if (g == 0 && warp == 0)
+    compose_swaps_warp(s_pivs, jb, p.j0, false, nullptr, p.swaps, s_atp, s_atr, lane);
 }
 
 }  // namespace

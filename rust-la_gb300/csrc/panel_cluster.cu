@@ -40,6 +40,7 @@
 // only at the start (barriers initialised) and the end (no CTA leaves while
 // pushes into it may be in flight).
 #include "la_internal.cuh"
+#include "swap_compose.cuh"
 
 namespace {
 
@@ -96,33 +97,6 @@ struct ClusterPanelArgs {
   int* err;  // the context's error word (bounded waits)
 };
 
-// The panel's row moves as one list for the row-swap kernel: swaps[0] = k,
-// swaps[1 + i] = destination row, swaps[1 + 2 MAX_PANEL_W + i] = source row
-// (the composition of the swaps (j0 + c, pivs[c]), c < jb).
-__device__ void build_swap_list(const ClusterPanelArgs& p, const int* pivs) {
-  int cnt = 0;
-  int* dst = p.swaps + 1;
-  int* src = p.swaps + 1 + 2 * MAX_PANEL_W;
-  auto find_or_add = [&](int pos) {
-    for (int q = 0; q < cnt; q++)
-      if (dst[q] == pos) return q;
-    dst[cnt] = pos;
-    src[cnt] = pos;
-    return cnt++;
-  };
-  for (int c = 0; c < p.jb; c++) {
-    int a = find_or_add(p.j0 + c);
-    int b = find_or_add(pivs[c]);
-    int t = src[a];
-    src[a] = src[b];
-    src[b] = t;
-  }
-  int k = 0;
-  for (int q = 0; q < cnt; q++)
-    if (src[q] != dst[q]) { dst[k] = dst[q]; src[k] = src[q]; k++; }
-  p.swaps[0] = k;
-}
-
 __global__ void __launch_bounds__(CT, 1) panel_cluster_kernel(ClusterPanelArgs p) {
   extern __shared__ __align__(16) float csm[];
   __shared__ unsigned s_key[2];
@@ -134,6 +108,7 @@ __global__ void __launch_bounds__(CT, 1) panel_cluster_kernel(ClusterPanelArgs p
   __shared__ unsigned red_k[CT / 32];
   __shared__ int red_p[CT / 32];
   __shared__ int s_win;
+  __shared__ int s_atp[SWAP_SLOTS], s_atr[SWAP_SLOTS];
   __shared__ int s_pivs[CW];
   __shared__ float s_scale;
 
@@ -250,7 +225,8 @@ __global__ void __launch_bounds__(CT, 1) panel_cluster_kernel(ClusterPanelArgs p
     int r = idx / CW, c = idx % CW;
     if (c < jb) p.A[(size_t)(row0 + r) * p.ld + p.j0 + c] = va[r * CP + c];
   }
-  if (g == 0 && tid == 0) build_swap_list(p, s_pivs);
+  if (g == 0 && warp == 0)
+    compose_swaps_warp(s_pivs, jb, p.j0, false, nullptr, p.swaps, s_atp, s_atr, lane);
 }
 
 __device__ __forceinline__ unsigned long long gtimer_ns() {
@@ -440,6 +416,7 @@ __global__ void __launch_bounds__(CT, 1) panel_cluster_reg_kernel(ClusterPanelAr
   __shared__ __align__(16) uint32_t recv[2][16][PSLOT];
   __shared__ __align__(8) uint64_t rbar[2];
   __shared__ int s_pivs[CW];
+  __shared__ int s_atp[SWAP_SLOTS], s_atr[SWAP_SLOTS];
 
   const int g = (int)cta_rank();
   const int C = (int)gridDim.x;  // one cluster per launch, C <= 16
@@ -534,8 +511,10 @@ __global__ void __launch_bounds__(CT, 1) panel_cluster_reg_kernel(ClusterPanelAr
           if (c < jb) dst[c] = v[q][c];
       }
     }
-  if (g == 0 && tid == 0) build_swap_list(p, s_pivs);
+  if (g == 0 && warp == 0)
+    compose_swaps_warp(s_pivs, jb, p.j0, false, nullptr, p.swaps, s_atp, s_atr, lane);
 }
+
 
 }  // namespace
 
@@ -595,6 +574,7 @@ la_status launch_reg(la_ctx ctx, float* A, size_t ld, int m, int j0, int jb, int
   ctx->launches++;
   return LA_OK;
 }
+
 
 // Returns LA_UNSUPPORTED (without launching) when the panel does not fit one
 // cluster; the caller then uses the cooperative kernel.
