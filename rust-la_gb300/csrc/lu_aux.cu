@@ -110,6 +110,40 @@ trsm_rowpanel_kernel(T* A, const T* S, size_t ld, int j0, int jb, int c_begin, i
     for (int i = ty; i < jb; i += 8) A[(size_t)(j0 + i) * ld + c] = xa[i][tx];
 }
 
+// FP32 form for the mixed LU's 32-row blocks (jb <= 32, FMA): one thread per
+// column holds the column's jb values in registers and applies the terms in
+// ascending k (the same FMAs in the same order as the kernel above, so the
+// same bits), with the unit-lower block broadcast from shared memory. No
+// barrier inside the sweep: at FP32 rates the barriers, not the FMAs, were the
+// cost of the 32-step sweep.
+constexpr int TRR_W = 32;
+constexpr int TRR_T = 128;
+__global__ void __launch_bounds__(TRR_T)
+trsm_rowpanel_reg_kernel(float* A, size_t ld, int j0, int jb, int c_begin, int c_end) {
+  __shared__ float L[TRR_W][TRR_W + 1];
+  for (int idx = threadIdx.x; idx < jb * jb; idx += TRR_T) {
+    const int i = idx / jb, k = idx % jb;
+    L[i][k] = A[(size_t)(j0 + i) * ld + j0 + k];
+  }
+  __syncthreads();
+  const int c = c_begin + blockIdx.x * TRR_T + threadIdx.x;
+  if (c >= c_end) return;
+  float x[TRR_W];
+#pragma unroll
+  for (int i = 0; i < TRR_W; i++) x[i] = i < jb ? A[(size_t)(j0 + i) * ld + c] : 0.f;
+#pragma unroll
+  for (int k = 0; k < TRR_W; k++) {
+    if (k >= jb) break;
+    const float xk = x[k];
+#pragma unroll
+    for (int i = k + 1; i < TRR_W; i++)
+      if (i < jb) x[i] = fmaf(-L[i][k], xk, x[i]);
+  }
+#pragma unroll
+  for (int i = 0; i < TRR_W; i++)
+    if (i < jb) A[(size_t)(j0 + i) * ld + c] = x[i];
+}
+
 // ---- after the factorization: permutation vector, sign, zero diagonal ------
 // The swap list (LAPACK ipiv form) is replayed in order on a permutation
 // vector (lu.rs:147-149), the sign flips once per real swap (lu.rs:151), and
@@ -293,7 +327,12 @@ la_status launch_trsm_rowpanel(la_ctx ctx, bool exact, double* A, double* S, siz
 }
 la_status launch_trsm_rowpanel_f32(la_ctx ctx, float* A, size_t ld, int j0, int jb, int c_begin,
                                    int c_end) {
-  return launch_trsm_t<float>(ctx, false, A, nullptr, ld, j0, jb, c_begin, c_end);
+  if (jb > TRR_W) return launch_trsm_t<float>(ctx, false, A, nullptr, ld, j0, jb, c_begin, c_end);
+  if (c_end <= c_begin) return LA_OK;
+  const int grid = (c_end - c_begin + TRR_T - 1) / TRR_T;
+  trsm_rowpanel_reg_kernel<<<grid, TRR_T, 0, ctx->stream>>>(A, ld, j0, jb, c_begin, c_end);
+  ctx->launches++;
+  return la_check_launch(ctx, "trsm_rowpanel_reg_kernel");
 }
 
 la_status launch_lu_finish(la_ctx ctx, la_lu h, int* d_flags) {
