@@ -522,7 +522,7 @@ la_status la_lu_solve_auto_device(la_ctx ctx, const double* d_a, size_t lda, siz
     }
     if (s != LA_NOT_CONVERGED && s != LA_SINGULAR) return s;
   }
-  // 3. The plain FP64 LU (the reference's algorithm) answers, and judges: a
+  // 3. The plain FP64 LU (the reference's algorithm) answers, and decides: a
   //    zero pivot there is the reference's None.
   la_lu lu = nullptr;
   la_status s = la_lu_new_device(ctx, d_a, lda, n, n, &lu);

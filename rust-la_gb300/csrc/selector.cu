@@ -4,7 +4,7 @@
 // dominance, row/column scaling spread, a few-step Lanczos estimate of the
 // condition number); a small MLP (16 -> 64 -> 64 -> 3, ReLU, softmax, FP32)
 // proposes the storage precision of the system's LU factors (FP8, BF16, FP32);
-// the FP64 pass of the batched solver stays the fallback and the judge.
+// the FP64 pass of the batched solver stays the fallback and the arbiter of every answer.
 //
 // The network is trained on the GPU by the kernels below: forward (one thread
 // per sample), per-sample deltas, parameter gradients (one thread per

@@ -2,7 +2,7 @@
 
 Each system of a batch is factored in FP32 arithmetic with its LU factors
 stored in FP8 (e4m3), BF16 or FP32, then refined in FP64; systems whose
-refinement stalls are redone by the plan's FP64 pass, which is also the judge
+refinement stalls are redone by the plan's FP64 pass, which is also the arbiter
 of every answer (backward error <= tol or FP64). Narrow storage lets larger
 systems factor in shared memory, but converges only for well-conditioned
 systems: the best class depends on n and on the conditioning.
