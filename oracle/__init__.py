@@ -1,11 +1,12 @@
 """ORACLE — test infrastructure only.
 
 A CPU restatement of the `la` crate's LU path (xasmx/rust-la 0.2.0,
-src/decomp/lu.rs:104-278, src/matrix/mod.rs:957-980 and :1025-1047) used by
+src/decomp/lu.rs:104-278, src/matrix/mod.rs:957-980 and :1025-1047) and of
+its Cholesky decomposition (src/decomp/cholesky.rs:56-145) used by
 the tests, the smoke check and the benchmark's CPU-baseline leg as the checker.
 Nothing on the product path may import this package.
 
-`liboracle.so` is built from lu_oracle.c / lu_oracle_mt.c by `make` in this
+`liboracle.so` is built from lu_oracle.c / lu_oracle_mt.c / chol_oracle.c by `make` in this
 directory (the repository's build step runs it). `pyref` holds an independent
 pure-Python restatement used to cross-check the C one on small cases.
 """
@@ -62,6 +63,10 @@ def lib():
         L.oracle_mt_lu_factor_partial.argtypes = [P, S, S, S, P, P, P, I]
         L.oracle_mt_lu_solve_nocheck.argtypes = [P, S, P, P, S, P, I]
         L.oracle_mt_matmul_rows.argtypes = [P, S, S, P, S, P, S, S, I]
+        L.oracle_chol_new_partial.argtypes = [P, S, S, S, P]
+        L.oracle_chol_new_partial.restype = I
+        L.oracle_chol_solve.argtypes = [P, S, P, S, S, P]
+        L.oracle_chol_solve.restype = I
         _LIB = L
     return _LIB
 
@@ -222,3 +227,31 @@ def backward_error(a, x, b):
 
 def max_threads():
     return lib().oracle_mt_max_threads()
+
+
+def chol_new(a, j_end=None):
+    """cholesky.rs:56-111: the n x n factor L (zeros above the diagonal), or
+    None for a non-square, non-symmetric or not positive definite matrix.
+    `j_end` stops after that many rows (a bounded sample; rows past it are
+    left unset)."""
+    a = _c(a)
+    if a.ndim != 2:
+        raise ValueError("a must be 2-D")
+    m, n = a.shape
+    lo = np.zeros((n, n), dtype=np.float64)
+    je = n if j_end is None else min(int(j_end), n)
+    r = lib().oracle_chol_new_partial(_p(a), m, n, je, _p(lo))
+    return None if r == NONE else lo
+
+
+def chol_solve(l, b):
+    """cholesky.rs:116-145; ReferencePanic when b's row count differs from L's."""
+    l = _c(l)
+    b = _c(b)
+    if b.ndim == 1:
+        b = b.reshape(-1, 1)
+    n = l.shape[0]
+    x = np.empty((n, b.shape[1]), dtype=np.float64)
+    if lib().oracle_chol_solve(_p(l), n, _p(b), b.shape[0], b.shape[1], _p(x)) == PANIC:
+        raise ReferencePanic("assertion failed: l.rows() == b.rows()")
+    return x

@@ -1,7 +1,8 @@
 """ORACLE — test infrastructure only.
 
 An independent pure-Python restatement of src/decomp/lu.rs:104-168 (factor),
-:224-232 (det) and :237-278 (solve), and src/matrix/mod.rs:957-980 (Mul), written
+:224-232 (det) and :237-278 (solve), src/matrix/mod.rs:957-980 (Mul) and
+src/decomp/cholesky.rs:56-145 (Cholesky factor and solve), written
 with plain Python floats (IEEE binary64, no fused multiply-add) and lists. It is
 slow and meant only for small matrices: it cross-checks the C restatement.
 """
@@ -71,3 +72,47 @@ def matmul(a, b):
             row.append(res)
         out.append(row)
     return out
+
+
+def chol_new(a):
+    """src/decomp/cholesky.rs:56-111 with Python floats: the n*n factor as a flat
+    list, or None (non-square, non-symmetric, not positive definite)."""
+    import math
+    if len(a) != len(a[0]):
+        return None
+    n = len(a)
+    l = [0.0] * (n * n)
+    for j in range(n):
+        d = 0.0
+        for k in range(j):
+            s = 0.0
+            for i in range(k):
+                s = s + l[k * n + i] * l[j * n + i]
+            s = (float(a[j][k]) - s) / l[k * n + k]
+            l[j * n + k] = s
+            d = d + s * s
+            if float(a[k][j]) != float(a[j][k]):
+                return None
+        d = float(a[j][j]) - d
+        if d <= 0.0:
+            return None
+        l[j * n + j] = math.sqrt(d)
+        for k in range(j + 1, n):
+            l[j * n + k] = 0.0
+    return l
+
+
+def chol_solve(l, n, b, nx):
+    """src/decomp/cholesky.rs:116-145 (b flat, row-major n x nx)."""
+    x = [float(v) for v in b]
+    for k in range(n):
+        for j in range(nx):
+            for i in range(k):
+                x[k * nx + j] = x[k * nx + j] - x[i * nx + j] * l[k * n + i]
+            x[k * nx + j] = x[k * nx + j] / l[k * n + k]
+    for k in range(n - 1, -1, -1):
+        for j in range(nx):
+            for i in range(k + 1, n):
+                x[k * nx + j] = x[k * nx + j] - x[i * nx + j] * l[i * n + k]
+            x[k * nx + j] = x[k * nx + j] / l[k * n + k]
+    return x
