@@ -167,6 +167,66 @@ def pick_prefix(oracle, a, n, target_s, threads):
     return lo
 
 
+def run_cholesky(la_gpu, torch, ctx, stream, n, nrhs, fp64_peak, cpu_s=5.0):
+    """CholeskyDecomposition::new + solve (src/decomp/cholesky.rs:56-145) at
+    n = 8192 with 16 RHS, FAST arithmetic, on a seeded symmetric diagonally
+    dominant matrix ((G + G')/2 + n I, G iid U(-1, 1)); nominal flops
+    n^3/3 + 2 n^2 nrhs. The CPU line is the oracle (the reference's row order,
+    one thread) on the first rows of the same factorization."""
+    g = torch.Generator(device="cuda").manual_seed(4)
+    x0 = torch.rand((n, n), generator=g, device="cuda", dtype=torch.float64) * 2 - 1
+    a = (x0 + x0.T) / 2 + n * torch.eye(n, device="cuda", dtype=torch.float64)
+    del x0
+    b = torch.randn((n, nrhs), generator=g, device="cuda", dtype=torch.float64)
+    x = torch.empty_like(b)
+    torch.cuda.synchronize()
+
+    def step():
+        c = la_gpu.CholeskyDecomposition.new_device(a.data_ptr(), n, n, ctx)
+        c.solve_device(b.data_ptr(), nrhs, n, nrhs, x.data_ptr(), nrhs)
+        return c
+
+    step().free()
+    ctx.synchronize()
+    reps = 3
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        c = step()
+        c.free()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    flops = n ** 3 / 3.0 + 2.0 * n * n * nrhs
+    eta = la_gpu.backward_error_device(ctx, a.data_ptr(), n, x.data_ptr(), nrhs, b.data_ptr(),
+                                       nrhs, n, nrhs)
+    out = {"workload": "Cholesky factor + solve, n=8192, 16 RHS, A = (G + G')/2 + n I",
+           "ms": ms, "gflops": flops / (ms * 1e-3) / 1e9,
+           "frac_of_fp64_peak": flops / (ms * 1e-3) / 1e12 / fp64_peak,
+           "flops_basis": "nominal n^3/3 + 2 n^2 nrhs", "eta": eta, "cpu_oracle": None}
+    if cpu_s > 0:
+        import oracle
+        a_np = a.cpu().numpy()
+        rows, took = 256, 0.0
+        while True:
+            t0 = time.perf_counter()
+            oracle.chol_new(a_np, j_end=rows)
+            took = time.perf_counter() - t0
+            if took >= cpu_s or rows >= n:
+                break
+            rows = min(n, int(rows * max(1.3, (cpu_s / max(took, 1e-3)) ** (1.0 / 3.0))))
+        cf = rows ** 3 / 3.0
+        out["cpu_oracle"] = {"value": cf / took / 1e9, "unit": "GFLOP/s", "cores": 1,
+                             "kind": "port",
+                             "sample": "rows [0,%d) of the n=8192 factorization in the reference's "
+                                       "row order (cholesky.rs:64-107), %.3g flops in %.1f s"
+                                       % (rows, cf, took)}
+    del a, b, x
+    return out
+
+
 def cpu_baseline(a, n, nrhs, target_s=15.0, threads=1):
     """Times the oracle on a bounded prefix of the same factorization."""
     import oracle
@@ -604,6 +664,11 @@ def run_ours(args):
                 "frac_of_fp64_peak": 2.0 * n ** 3 / (gms * 1e-3) / 1e12 / fp64_peak}
         del db2, dc
 
+    chol = None
+    if not args.no_cholesky and rank == 0:
+        chol = run_cholesky(la_gpu, torch, ctx, stream, n, nrhs, fp64_peak,
+                            cpu_s=0.0 if args.no_cpu else 4.0)
+
     mixed = None
     if not args.no_mixed:
         mixed = run_mixed(la_gpu, torch, ctx, args.mixed_n)
@@ -635,6 +700,7 @@ def run_ours(args):
             "clocks": clk,
             "cpu_baseline": cpu,
             "gemm_8192": gemm,
+            "cholesky_8192": chol,
             "mixed_ir": mixed,
             "batched_uneven": batched,
             "learned_selector": selected,
@@ -657,6 +723,7 @@ def main():
     ap.add_argument("--no-gemm", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-cholesky", action="store_true")
     ap.add_argument("--mixed-n", type=int, default=16384)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-count", type=int, default=20000)

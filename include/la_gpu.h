@@ -43,6 +43,7 @@ typedef enum la_status {
 
 typedef struct la_context* la_ctx;
 typedef struct la_lu_handle* la_lu;
+typedef struct la_chol_handle* la_chol;
 
 /* ---- context ------------------------------------------------------------ */
 
@@ -364,6 +365,30 @@ la_status la_backward_error_device(la_ctx ctx, const double* d_a, size_t lda, co
                                    size_t nrhs, double* eta);
 la_status la_backward_error(la_ctx ctx, const double* a, const double* x, const double* b,
                             size_t n, size_t nrhs, double* eta);
+
+/* ---- Cholesky decomposition (src/decomp/cholesky.rs) ------------------------ */
+
+/* CholeskyDecomposition::new (cholesky.rs:56-111): A (m x n, row-major host
+ * memory) = L L'. LA_OK with *out set, or LA_SINGULAR with *out = NULL where
+ * the reference returns None: A not square (:57-59), A[k][j] != A[j][k] for
+ * some k < j (:89-91, so a NaN off the diagonal too), or A[j][j] - d <= 0 at
+ * some row (:97-100). LA_BADSHAPE for m == 0 or n == 0 (Matrix::new asserts).
+ * LA_OPT_ARITH = LA_ARITH_EXACT gives L bit-identical to the reference;
+ * LA_ARITH_FAST (default) uses FMA and a blocked order. */
+la_status la_chol_new(la_ctx ctx, const double* a, size_t m, size_t n, la_chol* out);
+/* The same from an n x n device matrix with pitch lda (elements). */
+la_status la_chol_new_device(la_ctx ctx, const double* d_a, size_t lda, size_t n, la_chol* out);
+void la_chol_free(la_chol c);
+la_status la_chol_n(la_chol c, size_t* n);
+/* CholeskyDecomposition::get_l (cholesky.rs:113): L, n x n row-major host
+ * memory, zeros above the diagonal. */
+la_status la_chol_get_l(la_chol c, double* out);
+/* CholeskyDecomposition::solve (cholesky.rs:116-145): x (n x nrhs host) with
+ * A x = b. LA_BADSHAPE where the reference's assert! panics (brows != n). */
+la_status la_chol_solve(la_chol c, const double* b, size_t brows, size_t nrhs, double* x);
+/* The same on device memory (pitches ldb, ldx in elements). */
+la_status la_chol_solve_device(la_chol c, const double* d_b, size_t ldb, size_t brows,
+                               size_t nrhs, double* d_x, size_t ldx);
 
 /* ---- diagnostics ---------------------------------------------------------- */
 

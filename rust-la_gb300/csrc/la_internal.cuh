@@ -162,6 +162,8 @@ la_status launch_lu_finish(la_ctx ctx, la_lu h, int* d_flags);
 // Enqueues the whole factorization of h (no readback, no synchronization);
 // lu_finish writes {pospivsign, zero-on-diagonal} to d_flags.
 la_status lu_factor_enqueue(la_ctx ctx, la_lu h, int* d_flags);
+la_status launch_tri_wave(la_ctx ctx, bool exact, bool upper, bool divide, const double* T,
+                          size_t ld, double* X, size_t ldx, int n, int nrhs);
 la_status launch_lu_solve(la_ctx ctx, bool exact, const double* LU, size_t ld, double* X,
                           size_t ldx, int n, int nrhs);
 la_status launch_permute_rows(la_ctx ctx, const uint64_t* d_piv, const double* B, size_t ldb,

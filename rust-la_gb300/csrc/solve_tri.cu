@@ -238,7 +238,9 @@ __device__ __forceinline__ void wave_fetch_tile(const T* __restrict__ LU, size_t
   }
 }
 
-template <typename T, bool EXACT, bool UPPER>
+// DIVL: the lower triangle has a non-unit diagonal (a Cholesky factor): each
+// row's value is divided by it once its terms are applied.
+template <typename T, bool EXACT, bool UPPER, bool DIVL = false>
 __global__ void __launch_bounds__(WT)
 solve_wave_kernel(const T* __restrict__ LU, size_t ld, T* X, size_t ldx, int n, int nrhs,
                   int nb, int groups, int* ticket, int* prog, int* err) {
@@ -317,10 +319,17 @@ solve_wave_kernel(const T* __restrict__ LU, size_t ld, T* X, size_t ldx, int n, 
               x = apply<EXACT, T>(x, __shfl_sync(full, xc, k), tile[lane][k]);
           }
         }
-      } else if (!UPPER) {
+      } else if (!UPPER && !DIVL) {
         for (int k = 0; k < sb; k++) {
           const T xk = __shfl_sync(full, x, k);
           if (lane > k) x = apply<EXACT, T>(x, xk, tile[lane][k]);
+        }
+      } else if (!UPPER) {
+        // as in the backward case: every lane divides row k's value in lockstep
+        for (int k = 0; k < sb; k++) {
+          const T xk = __shfl_sync(full, x, k) / tile[k][k];
+          if (lane == k) x = xk;
+          else if (lane > k) x = apply<EXACT, T>(x, xk, tile[lane][k]);
         }
       } else {
         // Every lane takes row k's undivided value and divides it by u_kk in
@@ -360,6 +369,30 @@ la_status solve_wave(la_ctx ctx, const T* LU, size_t ld, T* X, size_t ldx, int n
   return la_check_launch(ctx, "solve_wave_kernel");
 }
 
+// One triangle with the wavefront kernel, right-hand sides in chunks of at
+// most 4 * SOLVE_WAVE_MAX_GROUPS columns.
+template <bool EXACT, bool UPPER, bool DIVL>
+la_status tri_wave(la_ctx ctx, const double* T, size_t ld, double* X, size_t ldx, int n,
+                   int nrhs) {
+  const int nb = (n + WB - 1) / WB;
+  const int per = WC * SOLVE_WAVE_MAX_GROUPS;
+  for (int c0 = 0; c0 < nrhs; c0 += per) {
+    const int nr = std::min(per, nrhs - c0);
+    const int groups = (nr + WC - 1) / WC;
+    int* tickets = ctx->d_solve_sync;
+    int* prog = tickets + 2;
+    LA_CUDA(ctx, cudaMemsetAsync(tickets, 0, (2 + (size_t)groups) * sizeof(int), ctx->stream));
+    const long long items = (long long)nb * groups;
+    const int cps = ctx->solve_wave > 0 ? ctx->solve_wave : 2;
+    const int grid = (int)std::min<long long>(items, (long long)cps * ctx->sm_count);
+    solve_wave_kernel<double, EXACT, UPPER, DIVL><<<grid, WT, 0, ctx->stream>>>(
+        T, ld, X + c0, ldx, n, nr, nb, groups, tickets, prog, ctx->d_err);
+    ctx->launches++;
+    LA_TRY(la_check_launch(ctx, "solve_wave_kernel"));
+  }
+  return LA_OK;
+}
+
 template <typename T, bool EXACT>
 la_status solve_any(la_ctx ctx, const T* LU, size_t ld, T* X, size_t ldx, int n, int nrhs) {
   if (ctx->solve_wave > 0 && ctx->d_solve_sync && ctx->sm_count > 0 &&
@@ -384,4 +417,21 @@ la_status launch_lu_solve_f32(la_ctx ctx, const float* LU, size_t ld, float* X, 
                               int nrhs) {
   if (n <= 0 || nrhs <= 0) return LA_OK;
   return solve_any<float, false>(ctx, LU, ld, X, ldx, n, nrhs);
+}
+
+// One triangle of a solve by the wavefront kernel: lower (unit diagonal, or
+// divide = true for a non-unit one) or upper (always divides). The Cholesky
+// solves use it (cholesky.rs:123-141).
+la_status launch_tri_wave(la_ctx ctx, bool exact, bool upper, bool divide, const double* T,
+                          size_t ld, double* X, size_t ldx, int n, int nrhs) {
+  if (n <= 0 || nrhs <= 0) return LA_OK;
+  if (!ctx->d_solve_sync || ctx->sm_count <= 0) return LA_UNSUPPORTED;
+  if (upper)
+    return exact ? tri_wave<true, true, false>(ctx, T, ld, X, ldx, n, nrhs)
+                 : tri_wave<false, true, false>(ctx, T, ld, X, ldx, n, nrhs);
+  if (divide)
+    return exact ? tri_wave<true, false, true>(ctx, T, ld, X, ldx, n, nrhs)
+                 : tri_wave<false, false, true>(ctx, T, ld, X, ldx, n, nrhs);
+  return exact ? tri_wave<true, false, false>(ctx, T, ld, X, ldx, n, nrhs)
+               : tri_wave<false, false, false>(ctx, T, ld, X, ldx, n, nrhs);
 }

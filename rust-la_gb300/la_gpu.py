@@ -83,6 +83,13 @@ SIGNATURES = {
     "la_backward_error_device": ([_P, _P, _S, _P, _S, _P, _S, _S, _S, _P], _I),
     "la_backward_error": ([_P, _P, _P, _P, _S, _S, _P], _I),
     "la_lu_factor_noalloc": ([_P, _P, _S, _S, _S, _P, _P, _P], _I),
+    "la_chol_new": ([_P, _P, _S, _S, _P], _I),
+    "la_chol_new_device": ([_P, _P, _S, _S, _P], _I),
+    "la_chol_free": ([_P], None),
+    "la_chol_n": ([_P, _P], _I),
+    "la_chol_get_l": ([_P, _P], _I),
+    "la_chol_solve": ([_P, _P, _S, _S, _P], _I),
+    "la_chol_solve_device": ([_P, _P, _S, _S, _S, _P, _S], _I),
     "la_lu_mixed_new_device": ([_P, _P, _S, _S, _I, _P], _I),
     "la_lu_solve_refined_device": ([_P, _P, _S, _S, _P, _S, _I, _D, _P], _I),
     "la_lu_solve_auto_device": ([_P, _P, _S, _S, _P, _S, _S, _P, _S, _D, _P], _I),
@@ -255,6 +262,10 @@ class Matrix:
     def get_data(self):
         return self.data.ravel()
 
+    def t(self):
+        """mod.rs:653-662: the transpose (a host copy)."""
+        return Matrix(np.ascontiguousarray(self.data.T), self.ctx)
+
     def get(self, r, c):
         if r >= self.rows() or c >= self.cols():
             raise Panic("Matrix::get out of range")
@@ -422,6 +433,66 @@ class LUDecomposition:
         st = lib().la_lu_solve_device(self.h, ctypes.c_void_p(b_ptr), ldb, brows, nrhs,
                                       ctypes.c_void_p(x_ptr), ldx)
         return _check(self.ctx, st, (OK, SINGULAR))
+
+
+class CholeskyDecomposition:
+    """Mirror of CholeskyDecomposition<f64> (src/decomp/cholesky.rs:52-145)."""
+
+    def __init__(self, h, ctx, n):
+        self.h = h
+        self.ctx = ctx
+        self.n = n
+
+    @staticmethod
+    def new(a, ctx=None):
+        """cholesky.rs:56-111: None for a non-square, non-symmetric or not
+        positive definite matrix."""
+        if not isinstance(a, Matrix):
+            a = Matrix(a, ctx)
+        ctx = ctx or a._c()
+        h = ctypes.c_void_p()
+        st = lib().la_chol_new(ctx.h, _ptr(a.data), a.rows(), a.cols(), ctypes.byref(h))
+        if _check(ctx, st, (OK, SINGULAR)) == SINGULAR:
+            return None
+        return CholeskyDecomposition(h, ctx, a.rows())
+
+    @staticmethod
+    def new_device(ptr, lda, n, ctx):
+        h = ctypes.c_void_p()
+        st = lib().la_chol_new_device(ctx.h, ctypes.c_void_p(ptr), lda, n, ctypes.byref(h))
+        if _check(ctx, st, (OK, SINGULAR)) == SINGULAR:
+            return None
+        return CholeskyDecomposition(h, ctx, n)
+
+    def free(self):
+        if self.h:
+            lib().la_chol_free(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def get_l(self):
+        """cholesky.rs:113."""
+        out = np.empty((self.n, self.n))
+        _check(self.ctx, lib().la_chol_get_l(self.h, _ptr(out)))
+        return Matrix(out, self.ctx)
+
+    def solve(self, b):
+        """cholesky.rs:116-145: Panic when b's row count differs from L's."""
+        if not isinstance(b, Matrix):
+            b = Matrix(np.asarray(b, dtype=np.float64).reshape(-1, 1)
+                       if np.ndim(b) == 1 else b, self.ctx)
+        x = np.empty((b.rows(), b.cols()))
+        _check(self.ctx, lib().la_chol_solve(self.h, _ptr(b.data), b.rows(), b.cols(), _ptr(x)))
+        return Matrix(x, self.ctx)
+
+    def solve_device(self, b_ptr, ldb, brows, nrhs, x_ptr, ldx):
+        _check(self.ctx, lib().la_chol_solve_device(self.h, ctypes.c_void_p(b_ptr), ldb, brows,
+                                                     nrhs, ctypes.c_void_p(x_ptr), ldx))
 
 
 def backward_error(ctx, a, x, b):
