@@ -227,6 +227,48 @@ def run_cholesky(la_gpu, torch, ctx, stream, n, nrhs, fp64_peak, cpu_s=5.0):
     return out
 
 
+def run_read_csv(la_gpu, n=2048):
+    """util::read_csv (src/util.rs:9-35) with the f64 parser: the native reader
+    (all host threads) on an n x n file of %.17g values, against the oracle
+    (the reference's rules restated in Python, one thread) on its first 256
+    lines. Host-only work; no GPU."""
+    import tempfile
+    from oracle import csv_ref
+    rng = np.random.default_rng(5)
+    a = rng.standard_normal((n, n))
+    path = os.path.join(tempfile.gettempdir(), "la_bench_%d.csv" % os.getpid())
+    head = path + ".head"
+    try:
+        with open(path, "w") as f:
+            for r in range(n):
+                f.write(",".join("%.17g" % v for v in a[r]) + "\n")
+        size = os.path.getsize(path)
+        la_gpu.read_csv(path)
+        reps, t0 = 3, time.perf_counter()
+        for _ in range(reps):
+            m = la_gpu.read_csv(path)
+        t = (time.perf_counter() - t0) / reps
+        same = bool(np.array_equal(m.data, a))
+        with open(path) as f, open(head, "w") as g:
+            for i, line in enumerate(f):
+                if i >= 256:
+                    break
+                g.write(line)
+        t1 = time.perf_counter()
+        csv_ref.read_csv(head)
+        to = time.perf_counter() - t1
+        return {"workload": "read_csv of a %d x %d file of %%.17g values (%.1f MB)" % (n, n, size / 1e6),
+                "ms": t * 1e3, "mb_per_s": size / t / 1e6, "threads": os.cpu_count(),
+                "round_trip_exact": same,
+                "cpu_oracle": {"value": os.path.getsize(head) / to / 1e6, "unit": "MB/s",
+                               "cores": 1, "kind": "port",
+                               "sample": "first 256 lines of the same file"}}
+    finally:
+        for p in (path, head):
+            if os.path.exists(p):
+                os.remove(p)
+
+
 def cpu_baseline(a, n, nrhs, target_s=15.0, threads=1):
     """Times the oracle on a bounded prefix of the same factorization."""
     import oracle
@@ -669,6 +711,10 @@ def run_ours(args):
         chol = run_cholesky(la_gpu, torch, ctx, stream, n, nrhs, fp64_peak,
                             cpu_s=0.0 if args.no_cpu else 4.0)
 
+    csv = None
+    if not args.no_csv and rank == 0:
+        csv = run_read_csv(la_gpu)
+
     mixed = None
     if not args.no_mixed:
         mixed = run_mixed(la_gpu, torch, ctx, args.mixed_n)
@@ -701,6 +747,7 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "gemm_8192": gemm,
             "cholesky_8192": chol,
+            "read_csv": csv,
             "mixed_ir": mixed,
             "batched_uneven": batched,
             "learned_selector": selected,
@@ -724,6 +771,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-cholesky", action="store_true")
+    ap.add_argument("--no-csv", action="store_true")
     ap.add_argument("--mixed-n", type=int, default=16384)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-count", type=int, default=20000)

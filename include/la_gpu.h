@@ -390,6 +390,20 @@ la_status la_chol_solve(la_chol c, const double* b, size_t brows, size_t nrhs, d
 la_status la_chol_solve_device(la_chol c, const double* d_b, size_t ldb, size_t brows,
                                size_t nrhs, double* d_x, size_t ldx);
 
+/* ---- reading matrices (src/util.rs) ----------------------------------------- */
+
+/* util::read_csv (util.rs:9-35) with the f64 parser s.parse::<f64>().unwrap():
+ * the comma-separated file at `path` as a new row-major rows x cols matrix in
+ * host memory (release it with la_host_free). Lines end at '\n' (a '\r' before
+ * it is dropped), items are split at ',' and trimmed of Unicode white space,
+ * and each must be a Rust f64 literal (sign, digits with an optional '.',
+ * optional exponent; or inf, infinity, nan in any case), rounded to nearest.
+ * LA_BADSHAPE where the reference panics: the file cannot be opened or is not
+ * UTF-8, an item does not parse, a line has another item count than the first
+ * (:25-27), or the file has no line (:32). No context or GPU is involved. */
+la_status la_read_csv_f64(const char* path, double** data, size_t* rows, size_t* cols);
+void la_host_free(void* p);
+
 /* ---- diagnostics ---------------------------------------------------------- */
 
 /* Measures this GPU's FP64 FMA issue rate (TFLOP/s) with a short all-SM

@@ -1,7 +1,8 @@
 """Builds liblagpu.so (the C-ABI library of include/la_gpu.h) in-tree for sm_103a.
 
-Each .cu translation unit is compiled by nvcc in parallel, then linked into
-rust-la_gb300/liblagpu.so. Usage: python rust-la_gb300/build.py [--force]
+Each .cu translation unit is compiled by nvcc and each host-only .cpp unit by
+the C++ compiler, in parallel, then linked into rust-la_gb300/liblagpu.so.
+Usage: python rust-la_gb300/build.py [--force]
 """
 import concurrent.futures as cf
 import os
@@ -13,6 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liblagpu.so")
 NVCC = os.environ.get("NVCC", "nvcc")
+CXX = os.environ.get("CXX", "g++")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
@@ -20,8 +22,12 @@ FLAGS = ARCH + [
 ]
 
 
+CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-pthread",
+            "-I" + os.path.join(HERE, "..", "include")]
+
+
 def sources():
-    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
 
 
 def headers():
@@ -36,7 +42,10 @@ def _compile(src, force):
     newest_dep = max([os.path.getmtime(src)] + [os.path.getmtime(h) for h in headers()])
     if not force and os.path.exists(obj) and os.path.getmtime(obj) >= newest_dep:
         return obj
-    cmd = [NVCC] + FLAGS + ["-c", src, "-o", obj]
+    if src.endswith(".cpp"):
+        cmd = [CXX] + CXXFLAGS + ["-c", src, "-o", obj]
+    else:
+        cmd = [NVCC] + FLAGS + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, r.stdout, r.stderr))
@@ -49,7 +58,7 @@ def build(force=False, verbose=False):
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: _compile(s, force), srcs))
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
-        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-lcuda"]
+        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-lcuda", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))

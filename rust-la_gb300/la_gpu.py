@@ -83,6 +83,8 @@ SIGNATURES = {
     "la_backward_error_device": ([_P, _P, _S, _P, _S, _P, _S, _S, _S, _P], _I),
     "la_backward_error": ([_P, _P, _P, _P, _S, _S, _P], _I),
     "la_lu_factor_noalloc": ([_P, _P, _S, _S, _S, _P, _P, _P], _I),
+    "la_read_csv_f64": ([ctypes.c_char_p, _P, _P, _P], _I),
+    "la_host_free": ([_P], None),
     "la_chol_new": ([_P, _P, _S, _S, _P], _I),
     "la_chol_new_device": ([_P, _P, _S, _S, _P], _I),
     "la_chol_free": ([_P], None),
@@ -493,6 +495,25 @@ class CholeskyDecomposition:
     def solve_device(self, b_ptr, ldb, brows, nrhs, x_ptr, ldx):
         _check(self.ctx, lib().la_chol_solve_device(self.h, ctypes.c_void_p(b_ptr), ldb, brows,
                                                      nrhs, ctypes.c_void_p(x_ptr), ldx))
+
+
+def read_csv(path):
+    """util::read_csv (src/util.rs:9-35) with the f64 parser: a Matrix, or Panic
+    where the reference panics (no file, not UTF-8, an item that is not an f64
+    literal, ragged lines, an empty file)."""
+    data = ctypes.c_void_p()
+    rows = ctypes.c_size_t()
+    cols = ctypes.c_size_t()
+    st = lib().la_read_csv_f64(os.fsencode(path), ctypes.byref(data), ctypes.byref(rows),
+                               ctypes.byref(cols))
+    _check(None, st)
+    try:
+        n = rows.value * cols.value
+        buf = (ctypes.c_double * n).from_address(data.value)
+        out = np.frombuffer(buf, dtype=np.float64, count=n).reshape(rows.value, cols.value).copy()
+    finally:
+        lib().la_host_free(data)
+    return Matrix(out)
 
 
 def backward_error(ctx, a, x, b):
