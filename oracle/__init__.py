@@ -2,11 +2,12 @@
 
 A CPU restatement of the `la` crate's LU path (xasmx/rust-la 0.2.0,
 src/decomp/lu.rs:104-278, src/matrix/mod.rs:957-980 and :1025-1047) and of
-its Cholesky decomposition (src/decomp/cholesky.rs:56-145) used by
+its Cholesky decomposition (src/decomp/cholesky.rs:56-145) and QR
+decomposition (src/decomp/qr.rs:26-238, src/matrix/mod.rs:1049-1057) used by
 the tests, the smoke check and the benchmark's CPU-baseline leg as the checker.
 Nothing on the product path may import this package.
 
-`liboracle.so` is built from lu_oracle.c / lu_oracle_mt.c / chol_oracle.c by `make` in this
+`liboracle.so` is built from lu_oracle.c / lu_oracle_mt.c / chol_oracle.c / qr_oracle.c by `make` in this
 directory (the repository's build step runs it). `pyref` holds an independent
 pure-Python restatement used to cross-check the C one on small cases.
 """
@@ -67,6 +68,14 @@ def lib():
         L.oracle_chol_new_partial.restype = I
         L.oracle_chol_solve.argtypes = [P, S, P, S, S, P]
         L.oracle_chol_solve.restype = I
+        L.oracle_qr_new.argtypes = [P, S, S, P, P]
+        L.oracle_qr_is_full_rank.argtypes = [P, S, S]
+        L.oracle_qr_is_full_rank.restype = I
+        L.oracle_qr_get_h.argtypes = [P, S, S, P]
+        L.oracle_qr_get_r.argtypes = [P, P, S, S, P]
+        L.oracle_qr_get_q.argtypes = [P, P, S, S, P]
+        L.oracle_qr_solve.argtypes = [P, P, S, S, P, S, S, P]
+        L.oracle_qr_solve.restype = I
         _LIB = L
     return _LIB
 
@@ -255,3 +264,83 @@ def chol_solve(l, b):
     if lib().oracle_chol_solve(_p(l), n, _p(b), b.shape[0], b.shape[1], _p(x)) == PANIC:
         raise ReferencePanic("assertion failed: l.rows() == b.rows()")
     return x
+
+
+class QR:
+    """QRDecomposition as the reference holds it (qr.rs:20-23): qr and rdiag."""
+
+    def __init__(self, qr, rdiag):
+        self.qr = qr
+        self.rdiag = rdiag
+
+    @property
+    def m(self):
+        return self.qr.shape[0]
+
+    @property
+    def n(self):
+        return self.qr.shape[1]
+
+
+def qr_new(a):
+    """qr.rs:26-105."""
+    a = _c(a)
+    m, n = a.shape
+    qr = np.empty_like(a)
+    rd = np.empty(min(m, n))
+    lib().oracle_qr_new(_p(a), m, n, _p(qr), _p(rd))
+    return QR(qr, rd)
+
+
+def qr_is_full_rank(f):
+    """qr.rs:108-115; ReferencePanic where it indexes past rdiag (n > m)."""
+    r = lib().oracle_qr_is_full_rank(_p(f.rdiag), f.m, f.n)
+    if r < 0:
+        raise ReferencePanic("index out of bounds in is_full_rank (n > m)")
+    return bool(r)
+
+
+def qr_get_h(f):
+    out = np.empty((f.m, f.n))
+    lib().oracle_qr_get_h(_p(f.qr), f.m, f.n, _p(out))
+    return out
+
+
+def qr_get_r(f):
+    out = np.empty((f.m, f.n))
+    lib().oracle_qr_get_r(_p(f.qr), _p(f.rdiag), f.m, f.n, _p(out))
+    return out
+
+
+def qr_get_q(f):
+    out = np.empty((f.m, f.m))
+    lib().oracle_qr_get_q(_p(f.qr), _p(f.rdiag), f.m, f.n, _p(out))
+    return out
+
+
+def qr_solve(f, b):
+    """qr.rs:199-238: the solution, None (not full rank) or ReferencePanic."""
+    b = _c(b)
+    if b.ndim == 1:
+        b = b.reshape(-1, 1)
+    x = np.empty((f.n, b.shape[1]))
+    r = lib().oracle_qr_solve(_p(f.qr), _p(f.rdiag), f.m, f.n, _p(b), b.shape[0], b.shape[1], _p(x))
+    if r == PANIC:
+        raise ReferencePanic("QRDecomposition::solve panics (shape)")
+    if r == NONE:
+        return None
+    return x
+
+
+def pinverse(a):
+    """Matrix::pinverse (mod.rs:1049-1057): (R' R)^-1 A' with the crate's Mul
+    (mod.rs:957-980) and inverse (LU, mod.rs:1034-1037); ReferencePanic where
+    the inverse is None (unwrap)."""
+    a = _c(a)
+    r = qr_get_r(qr_new(a))
+    rtr = matmul(np.ascontiguousarray(r.T), r)
+    f = lu_factor(rtr)
+    inv = solve(f, np.eye(rtr.shape[0]))
+    if inv is None:
+        raise ReferencePanic("called `Option::unwrap()` on a `None` value")
+    return matmul(inv, np.ascontiguousarray(a.T))

@@ -1,8 +1,9 @@
 """ORACLE — test infrastructure only.
 
 An independent pure-Python restatement of src/decomp/lu.rs:104-168 (factor),
-:224-232 (det) and :237-278 (solve), src/matrix/mod.rs:957-980 (Mul) and
-src/decomp/cholesky.rs:56-145 (Cholesky factor and solve), written
+:224-232 (det) and :237-278 (solve), src/matrix/mod.rs:957-980 (Mul),
+src/decomp/cholesky.rs:56-145 (Cholesky factor and solve) and
+src/decomp/qr.rs:26-235 (QR factor, Q and solve), written
 with plain Python floats (IEEE binary64, no fused multiply-add) and lists. It is
 slow and meant only for small matrices: it cross-checks the C restatement.
 """
@@ -115,4 +116,66 @@ def chol_solve(l, n, b, nx):
             for i in range(k + 1, n):
                 x[k * nx + j] = x[k * nx + j] - x[i * nx + j] * l[i * n + k]
             x[k * nx + j] = x[k * nx + j] / l[k * n + k]
+    return x
+
+
+def qr_new(a):
+    """src/decomp/qr.rs:26-105 with Python floats: (qr flat m*n, rdiag)."""
+    import math
+    m, n = len(a), len(a[0])
+    q = [float(v) for row in a for v in row]
+    rd = []
+    for minor in range(min(m, n)):
+        x = 0.0
+        for i in range(minor, m):
+            c = q[i * n + minor]
+            x = x + c * c
+        a0 = -math.sqrt(x) if q[minor * n + minor] > 0.0 else math.sqrt(x)
+        rd.append(a0)
+        if a0 != 0.0:
+            q[minor * n + minor] = q[minor * n + minor] - a0
+            for col in range(minor + 1, n):
+                d = 0.0
+                for row in range(minor, m):
+                    d = d + q[row * n + minor] * q[row * n + col]
+                f = d / (a0 * q[minor * n + minor])
+                for row in range(minor, m):
+                    q[row * n + col] = q[row * n + col] + f * q[row * n + minor]
+    return q, rd
+
+
+def qr_get_q(q, rd, m, n):
+    """src/decomp/qr.rs:151-194 (m x m, flat)."""
+    out = [0.0] * (m * m)
+    for k in range(min(m, n)):
+        out[k * m + k] = 1.0
+    for k in range(min(m, n) - 1, -1, -1):
+        if q[k * n + k] != 0.0:
+            for col in range(k, m):
+                d = 0.0
+                for row in range(k, m):
+                    d = d + q[row * n + k] * out[row * m + col]
+                f = d / (rd[k] * q[k * n + k])
+                for row in range(k, m):
+                    out[row * m + col] = out[row * m + col] + f * q[row * n + k]
+    return out
+
+
+def qr_solve(q, rd, m, n, b, nx):
+    """src/decomp/qr.rs:211-235 for a square, full-rank factor (b flat m x nx)."""
+    x = [float(v) for v in b]
+    for k in range(n):
+        for j in range(nx):
+            s = 0.0
+            for i in range(k, m):
+                s = s + q[i * n + k] * x[i * nx + j]
+            s = -s / q[k * n + k]
+            for i in range(k, m):
+                x[i * nx + j] = x[i * nx + j] + s * q[i * n + k]
+    for k in range(n - 1, -1, -1):
+        for j in range(nx):
+            x[k * nx + j] = x[k * nx + j] / rd[k]
+        for i in range(k):
+            for j in range(nx):
+                x[i * nx + j] = x[i * nx + j] - x[k * nx + j] * q[i * n + k]
     return x
