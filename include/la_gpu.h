@@ -44,6 +44,7 @@ typedef enum la_status {
 typedef struct la_context* la_ctx;
 typedef struct la_lu_handle* la_lu;
 typedef struct la_chol_handle* la_chol;
+typedef struct la_qr_handle* la_qr;
 
 /* ---- context ------------------------------------------------------------ */
 
@@ -389,6 +390,32 @@ la_status la_chol_solve(la_chol c, const double* b, size_t brows, size_t nrhs, d
 /* The same on device memory (pitches ldb, ldx in elements). */
 la_status la_chol_solve_device(la_chol c, const double* d_b, size_t ldb, size_t brows,
                                size_t nrhs, double* d_x, size_t ldx);
+
+/* ---- QR decomposition (src/decomp/qr.rs) ------------------------------------ */
+
+/* QRDecomposition::new (qr.rs:26-105): Householder reflections, one column at
+ * a time, on A (m x n host memory); LA_BADSHAPE for m == 0 or n == 0. EXACT
+ * arithmetic gives the reference's bits (factors, Q, solution). */
+la_status la_qr_new(la_ctx ctx, const double* a, size_t m, size_t n, la_qr* out);
+la_status la_qr_new_device(la_ctx ctx, const double* d_a, size_t lda, size_t m, size_t n,
+                           la_qr* out);
+void la_qr_free(la_qr qr);
+/* is_full_rank (qr.rs:108-115); LA_BADSHAPE where the reference indexes past
+ * its min(m, n) diagonal (n > m and no zero among the first m). */
+la_status la_qr_is_full_rank(la_qr qr, int* out);
+/* get_h (qr.rs:119-132) and get_r (:135-148): m x n; get_q (:151-194): m x m. */
+la_status la_qr_get_h(la_qr qr, double* out);
+la_status la_qr_get_r(la_qr qr, double* out);
+la_status la_qr_get_q(la_qr qr, double* out);
+/* solve (qr.rs:199-238): x (n x nrhs). LA_SINGULAR where it returns None (not
+ * full rank); LA_BADSHAPE where it panics: brows != m (:200), the rank test's
+ * out-of-bounds index, or m != n (Matrix::new's length assert, :237). The
+ * reference's arithmetic is kept, which for a general A is not A^-1 b: its
+ * Q'B step divides by -u_k where its reflection uses a * u_k. */
+la_status la_qr_solve(la_qr qr, const double* b, size_t brows, size_t nrhs, double* x);
+/* Matrix::pinverse (mod.rs:1049-1057): (R'R)^-1 A' (n x m); LA_BADSHAPE where
+ * inverse() is None and unwrap panics. */
+la_status la_matrix_pinverse(la_ctx ctx, const double* a, size_t m, size_t n, double* out);
 
 /* ---- reading matrices (src/util.rs) ----------------------------------------- */
 

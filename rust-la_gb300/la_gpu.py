@@ -83,6 +83,15 @@ SIGNATURES = {
     "la_backward_error_device": ([_P, _P, _S, _P, _S, _P, _S, _S, _S, _P], _I),
     "la_backward_error": ([_P, _P, _P, _P, _S, _S, _P], _I),
     "la_lu_factor_noalloc": ([_P, _P, _S, _S, _S, _P, _P, _P], _I),
+    "la_qr_new": ([_P, _P, _S, _S, _P], _I),
+    "la_qr_new_device": ([_P, _P, _S, _S, _S, _P], _I),
+    "la_qr_free": ([_P], None),
+    "la_qr_is_full_rank": ([_P, _P], _I),
+    "la_qr_get_h": ([_P, _P], _I),
+    "la_qr_get_r": ([_P, _P], _I),
+    "la_qr_get_q": ([_P, _P], _I),
+    "la_qr_solve": ([_P, _P, _S, _S, _P], _I),
+    "la_matrix_pinverse": ([_P, _P, _S, _S, _P], _I),
     "la_read_csv_f64": ([ctypes.c_char_p, _P, _P, _P], _I),
     "la_host_free": ([_P], None),
     "la_chol_new": ([_P, _P, _S, _S, _P], _I),
@@ -264,6 +273,14 @@ class Matrix:
     def get_data(self):
         return self.data.ravel()
 
+    def pinverse(self):
+        """mod.rs:1049-1057: (R' R)^-1 A' (Panic where inverse() is None)."""
+        ctx = self._c()
+        out = np.empty((self.cols(), self.rows()))
+        _check(ctx, lib().la_matrix_pinverse(ctx.h, _ptr(self.data), self.rows(), self.cols(),
+                                             _ptr(out)))
+        return Matrix(out, self.ctx)
+
     def t(self):
         """mod.rs:653-662: the transpose (a host copy)."""
         return Matrix(np.ascontiguousarray(self.data.T), self.ctx)
@@ -435,6 +452,75 @@ class LUDecomposition:
         st = lib().la_lu_solve_device(self.h, ctypes.c_void_p(b_ptr), ldb, brows, nrhs,
                                       ctypes.c_void_p(x_ptr), ldx)
         return _check(self.ctx, st, (OK, SINGULAR))
+
+
+class QRDecomposition:
+    """Mirror of QRDecomposition<f64> (src/decomp/qr.rs:20-238)."""
+
+    def __init__(self, h, ctx, m, n):
+        self.h = h
+        self.ctx = ctx
+        self.m = m
+        self.n = n
+
+    @staticmethod
+    def new(a, ctx=None):
+        """qr.rs:26-105."""
+        if not isinstance(a, Matrix):
+            a = Matrix(a, ctx)
+        ctx = ctx or a._c()
+        h = ctypes.c_void_p()
+        _check(ctx, lib().la_qr_new(ctx.h, _ptr(a.data), a.rows(), a.cols(), ctypes.byref(h)))
+        return QRDecomposition(h, ctx, a.rows(), a.cols())
+
+    @staticmethod
+    def new_device(ptr, lda, m_, n_, ctx):
+        h = ctypes.c_void_p()
+        _check(ctx, lib().la_qr_new_device(ctx.h, ctypes.c_void_p(ptr), lda, m_, n_,
+                                           ctypes.byref(h)))
+        return QRDecomposition(h, ctx, m_, n_)
+
+    def free(self):
+        if self.h:
+            lib().la_qr_free(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def is_full_rank(self):
+        """qr.rs:108-115 (Panic where it indexes past rdiag)."""
+        out = ctypes.c_int()
+        _check(self.ctx, lib().la_qr_is_full_rank(self.h, ctypes.byref(out)))
+        return bool(out.value)
+
+    def _get(self, fn, shape):
+        out = np.empty(shape)
+        _check(self.ctx, fn(self.h, _ptr(out)))
+        return Matrix(out, self.ctx)
+
+    def get_h(self):
+        return self._get(lib().la_qr_get_h, (self.m, self.n))
+
+    def get_r(self):
+        return self._get(lib().la_qr_get_r, (self.m, self.n))
+
+    def get_q(self):
+        return self._get(lib().la_qr_get_q, (self.m, self.m))
+
+    def solve(self, b):
+        """qr.rs:199-238: None if not full rank, Panic where the reference panics."""
+        if not isinstance(b, Matrix):
+            b = Matrix(np.asarray(b, dtype=np.float64).reshape(-1, 1)
+                       if np.ndim(b) == 1 else b, self.ctx)
+        x = np.empty((self.n, b.cols()))
+        st = lib().la_qr_solve(self.h, _ptr(b.data), b.rows(), b.cols(), _ptr(x))
+        if _check(self.ctx, st, (OK, SINGULAR)) == SINGULAR:
+            return None
+        return Matrix(x, self.ctx)
 
 
 class CholeskyDecomposition:
