@@ -227,6 +227,51 @@ def run_cholesky(la_gpu, torch, ctx, stream, n, nrhs, fp64_peak, cpu_s=5.0):
     return out
 
 
+def run_qr(la_gpu, torch, ctx, n=2048, nrhs=4, cpu=True):
+    """QRDecomposition::new + solve (src/decomp/qr.rs:26-238), FAST arithmetic,
+    on an n x n N(0,1) matrix (seed 6): nominal flops 4/3 n^3 + 4 n^2 nrhs
+    (the reference's unblocked Householder form). The CPU line is the oracle
+    (the reference's order, one thread) on n = 1024."""
+    try:
+        rng = np.random.default_rng(6)
+        a_np = rng.standard_normal((n, n))
+        b_np = rng.standard_normal((n, nrhs))
+        a = torch.from_numpy(a_np).cuda()
+        torch.cuda.synchronize()
+        qr = la_gpu.QRDecomposition.new_device(a.data_ptr(), n, n, n, ctx)
+        qr.free()
+        reps, t0 = 2, time.perf_counter()
+        for _ in range(reps):
+            qr = la_gpu.QRDecomposition.new_device(a.data_ptr(), n, n, n, ctx)
+            ctx.synchronize()
+            qr.free()
+        tf = (time.perf_counter() - t0) / reps
+        qr = la_gpu.QRDecomposition.new_device(a.data_ptr(), n, n, n, ctx)
+        t1 = time.perf_counter()
+        qr.solve(la_gpu.Matrix(b_np, ctx))
+        ts = time.perf_counter() - t1
+        qr.free()
+        flops = 4.0 / 3.0 * n ** 3
+        out = {"workload": "QR factor (Householder, reference order) n=%d, then solve %d RHS" % (n, nrhs),
+               "factor_ms": tf * 1e3, "solve_ms": ts * 1e3,
+               "factor_gflops": flops / tf / 1e9, "flops_basis": "nominal 4/3 n^3",
+               "cpu_oracle": None}
+        if cpu:
+            import oracle
+            m = 1024
+            c = rng.standard_normal((m, m))
+            t2 = time.perf_counter()
+            oracle.qr_new(c)
+            tc = time.perf_counter() - t2
+            out["cpu_oracle"] = {"value": 4.0 / 3.0 * m ** 3 / tc / 1e9, "unit": "GFLOP/s",
+                                 "cores": 1, "kind": "port",
+                                 "sample": "qr_new at n=1024 in the reference's order, %.1f s" % tc}
+        del a
+        return out
+    except Exception as e:  # this section must not take the benchmark line down with it
+        return {"error": "%s: %s" % (type(e).__name__, e)}
+
+
 def run_read_csv(la_gpu, n=2048):
     """util::read_csv (src/util.rs:9-35) with the f64 parser: the native reader
     (all host threads) on an n x n file of %.17g values, against the oracle
@@ -711,6 +756,10 @@ def run_ours(args):
         chol = run_cholesky(la_gpu, torch, ctx, stream, n, nrhs, fp64_peak,
                             cpu_s=0.0 if args.no_cpu else 4.0)
 
+    qrs = None
+    if not args.no_qr and rank == 0:
+        qrs = run_qr(la_gpu, torch, ctx, cpu=not args.no_cpu)
+
     csv = None
     if not args.no_csv and rank == 0:
         csv = run_read_csv(la_gpu)
@@ -747,6 +796,7 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "gemm_8192": gemm,
             "cholesky_8192": chol,
+            "qr_2048": qrs,
             "read_csv": csv,
             "mixed_ir": mixed,
             "batched_uneven": batched,
@@ -772,6 +822,7 @@ def main():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-cholesky", action="store_true")
     ap.add_argument("--no-csv", action="store_true")
+    ap.add_argument("--no-qr", action="store_true")
     ap.add_argument("--mixed-n", type=int, default=16384)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-count", type=int, default=20000)
