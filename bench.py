@@ -555,16 +555,35 @@ def run_selector(la_gpu, torch, ctx, count=50000, seed=7):
     return out
 
 
-def dist_setup(args):
+def dist_setup(args, backend="nccl"):
+    """One process per GPU (replicas): (world, rank, local rank, the process
+    group module or None when the job has one rank)."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     dist = None
     if world > 1:
         import torch.distributed as dist_mod
-        dist_mod.init_process_group(backend="nccl")
+        dist_mod.init_process_group(backend=backend)
         dist = dist_mod
     return world, rank, local, dist
+
+
+def max_over_ranks(dist, value, device="cuda"):
+    """The largest of one float per rank, returned on every rank (the job's
+    step time is its slowest replica's); the value itself with no group."""
+    if dist is None:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank, world, seconds):
+    """Whole-job throughput of independent replicas (weak scaling): every rank
+    processed units_per_rank in the job's (slowest) time."""
+    return units_per_rank * world / seconds
 
 
 def run_reference(args):
@@ -671,12 +690,9 @@ def run_ours(args):
         lu.free()
     ctx.set_option(la_gpu.OPT_PROFILE, 0)
     torch.cuda.synchronize()
-    if dist:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(dist, ms)
     flops = lu_solve_flops(n, nrhs)
-    value = flops * world / (ms * 1e-3) / 1e9
+    value = replica_throughput(flops, world, ms * 1e-3) / 1e9
 
     eta = la_gpu.backward_error_device(ctx, da.data_ptr(), n, dx.data_ptr(), nrhs, db.data_ptr(),
                                        nrhs, n, nrhs)
@@ -722,11 +738,8 @@ def run_ours(args):
         e2e_step()
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / K
-    if dist:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": flops * world / e2e_s / 1e9, "unit": "GFLOP/s",
+    e2e_s = max_over_ranks(dist, e2e_s)
+    e2e = {"value": replica_throughput(flops, world, e2e_s) / 1e9, "unit": "GFLOP/s",
            "h2d_bytes_per_step": 8 * n * n + 8 * n * nrhs, "d2h_bytes_per_step": 8 * n * nrhs,
            "ms_per_step": e2e_s * 1e3}
 
