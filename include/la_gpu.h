@@ -94,7 +94,14 @@ typedef enum la_option {
    * them as one persistent wavefront kernel per triangle with that many CTAs
    * per SM; 0 launches one kernel per 16-row block step. Both apply every
    * term in the same order, so their results are bit-identical. */
-  LA_OPT_SOLVE_WAVE = 8
+  LA_OPT_SOLVE_WAVE = 8,
+  /* Failure injection on the host, for tests (0 = off; reads back what is
+   * left). INJECT_ALLOC_FAIL = k: the k-th device allocation of this context
+   * from now returns LA_NOMEM, as an exhausted pool would. INJECT_IR_STALL = k:
+   * the next k refinement calls (la_lu_solve_refined_device and each stage of
+   * la_lu_solve_auto_device) report a stall before their first correction. */
+  LA_OPT_INJECT_ALLOC_FAIL = 10,
+  LA_OPT_INJECT_IR_STALL = 11
 } la_option;
 
 #define LA_ARITH_FAST 0

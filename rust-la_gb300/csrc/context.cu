@@ -23,6 +23,12 @@ la_status la_check_launch(la_ctx ctx, const char* what) {
 
 la_status la_device_alloc(la_ctx ctx, void** p, size_t bytes) {
   *p = nullptr;
+  // A failure injected for tests (LA_OPT_INJECT_ALLOC_FAIL): the caller sees
+  // exactly what an exhausted device pool gives it.
+  if (ctx->inject_alloc_at > 0 && --ctx->inject_alloc_at == 0) {
+    ctx->last_error = "la_device_alloc: injected allocation failure";
+    return LA_NOMEM;
+  }
   if (bytes == 0) bytes = 256;
   cudaError_t e = cudaMallocAsync(p, bytes, ctx->stream);
   if (e != cudaSuccess) {
@@ -241,6 +247,14 @@ la_status la_ctx_set_option(la_ctx ctx, int option, int64_t value) {
       if (value < 0 || value > 8) return LA_INVALID;
       ctx->solve_wave = (int)value;
       return LA_OK;
+    case LA_OPT_INJECT_ALLOC_FAIL:
+      if (value < 0 || value > (1 << 20)) return LA_INVALID;
+      ctx->inject_alloc_at = (int)value;
+      return LA_OK;
+    case LA_OPT_INJECT_IR_STALL:
+      if (value < 0 || value > (1 << 20)) return LA_INVALID;
+      ctx->inject_ir_stall = (int)value;
+      return LA_OK;
   }
   return LA_INVALID;
 }
@@ -256,6 +270,8 @@ la_status la_ctx_get_option(la_ctx ctx, int option, int64_t* value) {
     case LA_OPT_CLUSTER_PANEL: *value = ctx->cluster_panels; return LA_OK;
     case LA_OPT_BATCH_GMRES: *value = ctx->batch_gmres; return LA_OK;
     case LA_OPT_SOLVE_WAVE: *value = ctx->solve_wave; return LA_OK;
+    case LA_OPT_INJECT_ALLOC_FAIL: *value = ctx->inject_alloc_at; return LA_OK;
+    case LA_OPT_INJECT_IR_STALL: *value = ctx->inject_ir_stall; return LA_OK;
   }
   return LA_INVALID;
 }

@@ -58,6 +58,8 @@ struct la_context {
   int cluster_panels = 1;                // FP32 panels on one thread-block cluster
   int batch_gmres = 0;                   // Krylov steps per GMRES correction in batch plans (0: off)
   int solve_wave = 2;                    // CTAs per SM of the wavefront solve (0: block steps)
+  int inject_alloc_at = 0;               // the n-th device allocation from now fails (0: none)
+  int inject_ir_stall = 0;               // this many refinement calls report a stall at once
   int sm_count = 0;
   size_t smem_optin = 0;
   int arith = LA_ARITH_FAST;

@@ -607,8 +607,14 @@ la_status refine_impl(la_lu h, const double* d_b, size_t ldb, size_t nrhs, doubl
   double prev = INFINITY;
   int it = 0, gsteps = 0;
   bool converged = eta <= tol;
+  // A stall injected for tests (LA_OPT_INJECT_IR_STALL): no correction runs.
+  bool stall = false;
+  if (ctx->inject_ir_stall > 0) {
+    ctx->inject_ir_stall--;
+    stall = true;
+  }
   // Plain refinement: d = LU32 \ (r(piv) / rmax), x += d * rmax.
-  while (!converged && it < max_iters && eta < 0.9 * prev) {
+  while (!stall && !converged && it < max_iters && eta < 0.9 * prev) {
     prev = eta;
     it++;
     scale_permute_kernel<<<grid_for(ctx, (size_t)n * nrhs), 256, 0, st>>>(
@@ -626,7 +632,7 @@ la_status refine_impl(la_lu h, const double* d_b, size_t ldb, size_t nrhs, doubl
   // GMRES-IR once plain refinement stalls.
   int outer = 0;
   prev = INFINITY;
-  while (allow_gmres && !converged && it + outer < max_iters && eta < 0.5 * prev) {
+  while (!stall && allow_gmres && !converged && it + outer < max_iters && eta < 0.5 * prev) {
     prev = eta;
     outer++;
     for (int j = 0; j < R; j++) {

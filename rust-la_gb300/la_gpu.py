@@ -28,6 +28,7 @@ OK, SINGULAR, BADSHAPE, INVALID, NOMEM, CUDA_ERROR, TIMEOUT, NOT_CONVERGED, UNSU
 OPT_ARITH, OPT_PANEL_WIDTH, OPT_PANEL_CTAS, OPT_PROFILE, OPT_LOOKAHEAD, OPT_CLUSTER_PANEL = 1, 2, 3, 4, 5, 6
 OPT_BATCH_GMRES = 7
 OPT_SOLVE_WAVE = 8
+OPT_INJECT_ALLOC_FAIL, OPT_INJECT_IR_STALL = 10, 11
 ARITH_FAST, ARITH_EXACT = 0, 1
 
 
