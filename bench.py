@@ -227,6 +227,15 @@ def run_cholesky(la_gpu, torch, ctx, stream, n, nrhs, fp64_peak, cpu_s=5.0):
     return out
 
 
+def guarded(section, *args, **kwargs):
+    """Runs one side section of the benchmark; a failure there is reported in
+    its own entry and does not take the benchmark line down with it."""
+    try:
+        return section(*args, **kwargs)
+    except Exception as e:
+        return {"error": "%s: %s" % (type(e).__name__, e)}
+
+
 def run_qr(la_gpu, torch, ctx, n=2048, nrhs=4, cpu=True):
     """QRDecomposition::new + solve (src/decomp/qr.rs:26-238), FAST arithmetic,
     on an n x n N(0,1) matrix (seed 6): nominal flops 4/3 n^3 + 4 n^2 nrhs
@@ -766,8 +775,8 @@ def run_ours(args):
 
     chol = None
     if not args.no_cholesky and rank == 0:
-        chol = run_cholesky(la_gpu, torch, ctx, stream, n, nrhs, fp64_peak,
-                            cpu_s=0.0 if args.no_cpu else 4.0)
+        chol = guarded(run_cholesky, la_gpu, torch, ctx, stream, n, nrhs, fp64_peak,
+                       cpu_s=0.0 if args.no_cpu else 4.0)
 
     qrs = None
     if not args.no_qr and rank == 0:
@@ -775,7 +784,7 @@ def run_ours(args):
 
     csv = None
     if not args.no_csv and rank == 0:
-        csv = run_read_csv(la_gpu)
+        csv = guarded(run_read_csv, la_gpu)
 
     mixed = None
     if not args.no_mixed:
