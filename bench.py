@@ -62,17 +62,61 @@ def lu_solve_flops(n, nrhs):
     return 2.0 / 3.0 * n ** 3 + 2.0 * n ** 2 * nrhs
 
 
-def trailing_gemm_flops(n, w):
-    """Algorithmic flops of all trailing-update GEMM launches of one LU (square n, panel w)."""
-    total = 0.0
-    launches = 0
+def trailing_gemm_launches(n, w, lookahead=True):
+    """(M, N, K) of every trailing-update GEMM launch of one LU of a square n
+    with panel width w, as the library issues them: with lookahead each panel
+    updates the next panel's columns first and the rest in a second launch."""
+    out = []
     for j0 in range(0, n, w):
-        j1 = min(n, j0 + w)
-        r = n - j1
-        if r > 0:
-            total += 2.0 * r * r * (j1 - j0)
-            launches += 1
-    return total, launches
+        jb = min(w, n - j0)
+        j1 = j0 + jb
+        if j1 >= n:
+            break
+        jbn = min(w, n - j1)
+        m = n - j1
+        if lookahead:
+            out.append((m, jbn, jb))
+            if n - (j1 + jbn) > 0:
+                out.append((m, n - (j1 + jbn), jb))
+        else:
+            out.append((m, n - j1, jb))
+    return out
+
+
+def gemm_algorithmic(launches):
+    """Total flops, and mean flops and mean DRAM bytes per launch (read A and B
+    once, read and write C once: 8 (MK + KN + 2 MN) bytes) of the launches."""
+    flops = sum(2.0 * m * n * k for m, n, k in launches)
+    nbytes = sum(8.0 * (m * k + k * n + 2.0 * m * n) for m, n, k in launches)
+    return flops, flops / len(launches), nbytes / len(launches)
+
+
+# DRAM traffic of the trailing-update GEMM (gemm_f64_tma_kernel) measured by
+# ncu (dram__bytes_read.sum + dram__bytes_write.sum) over all 253 launches of
+# one n = 8192 factorization of this benchmark's matrix: bytes per launch
+# (mean). Summary and command: profiles/gemm_f64_tma_traffic_n8192.md.
+GEMM_TRAFFIC_BYTES_PER_LAUNCH = None
+
+
+def event_ms(torch, fn, reps=5, warmup=1):
+    """Median and all device times (ms) of reps calls of fn, each bracketed by
+    CUDA events on the current stream (the library's stream) after warmup
+    untimed calls, with a synchronize on both sides."""
+    s = torch.cuda.current_stream()
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(s)
+        fn()
+        e1.record(s)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    return statistics.median(times), times
 
 
 def prefix_flops(n, jend):
@@ -136,18 +180,6 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(smax) if smax else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
-
-
-def read_traffic_summary():
-    """Per-launch DRAM traffic of the trailing GEMM from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "gemm_f64_trailing_update_n4096.md")
-    try:
-        for line in open(path):
-            if line.startswith("traffic_bytes_per_algorithmic_flop:"):
-                return float(line.split(":", 1)[1].split()[0])
-    except OSError:
-        pass
-    return None
 
 
 def pick_prefix(oracle, a, n, target_s, threads):
@@ -358,9 +390,11 @@ def householder_conditioned(torch, n, kappa, seed):
     return a.contiguous()
 
 
-def run_mixed(la_gpu, torch, ctx, n, nrhs=4, kappas=(1e2, 1e6, 1e10), precs=(1, 2, 3)):
-    """Mixed-precision LU + FP64 refinement against the plain FP64 LU at size n."""
-    names = {1: "bf16", 2: "fp16", 3: "fp32"}
+def run_mixed(la_gpu, torch, ctx, n, nrhs=4, kappas=(1e2, 1e6, 1e10), precs=(1, 2, 3), reps=5):
+    """Mixed-precision LU + FP64 refinement against the plain FP64 LU at size n.
+    Every time is the median of `reps` runs (CUDA events on the library's
+    stream, after one untimed run) of factor + refined solve."""
+    names = {1: "bf16", 2: "fp16", 3: "fp32", 4: "fp8"}
     flops = lu_solve_flops(n, nrhs)
     rng = np.random.default_rng(3)
     b = torch.from_numpy(rng.standard_normal((n, nrhs))).cuda()
@@ -372,99 +406,96 @@ def run_mixed(la_gpu, torch, ctx, n, nrhs=4, kappas=(1e2, 1e6, 1e10), precs=(1, 
         a = householder_conditioned(torch, n, kappa, 30 + int(round(np.log10(kappa))))
         torch.cuda.synchronize()
         for prec in precs:
-            for rep in range(2):  # first run warms up
-                t0 = time.perf_counter()
+            last = {}
+
+            def fixed():
                 lu = la_gpu.lu_mixed_new_device(ctx, a.data_ptr(), n, n, prec)
-                code, st = la_gpu.lu_solve_refined_device(lu, b.data_ptr(), nrhs, nrhs,
-                                                          x.data_ptr(), nrhs, max_iters=100,
-                                                          tol=5e-15)
-                t1 = time.perf_counter()
+                last["r"] = la_gpu.lu_solve_refined_device(lu, b.data_ptr(), nrhs, nrhs,
+                                                           x.data_ptr(), nrhs, max_iters=100,
+                                                           tol=5e-15)
                 lu.free()
+
+            ms, times = event_ms(torch, fixed, reps=reps)
+            code, st = last["r"]
             eta = la_gpu.backward_error_device(ctx, a.data_ptr(), n, x.data_ptr(), nrhs,
                                                b.data_ptr(), nrhs, n, nrhs)
             ok = bool(st.converged) and eta <= 1e-14
-            r = {"kappa": kappa, "precision": names[prec], "ms": (t1 - t0) * 1e3,
-                 "gflops": flops / (t1 - t0) / 1e9, "iterations": st.iterations,
+            r = {"kappa": kappa, "precision": names[prec], "ms": ms,
+                 "ms_min_max": [min(times), max(times)],
+                 "gflops": flops / (ms * 1e-3) / 1e9, "iterations": st.iterations,
                  "converged": ok, "eta": eta}
             results.append(r)
             if ok and (kappa not in best_by_kappa or r["ms"] < best_by_kappa[kappa]["ms"]):
                 best_by_kappa[kappa] = r
-        # automatic precision: FP16 factors, then FP32, then the plain FP64 LU
-        for rep in range(2):  # first run warms up
-            t0 = time.perf_counter()
-            code, st = la_gpu.lu_solve_auto_device(ctx, a.data_ptr(), n, n, b.data_ptr(), nrhs,
-                                                   nrhs, x.data_ptr(), nrhs, tol=5e-15)
-            t1 = time.perf_counter()
+        # automatic precision: the library's choice, then the cascade
+        last = {}
+
+        def auto():
+            last["r"] = la_gpu.lu_solve_auto_device(ctx, a.data_ptr(), n, n, b.data_ptr(), nrhs,
+                                                    nrhs, x.data_ptr(), nrhs, tol=5e-15)
+
+        ms, times = event_ms(torch, auto, reps=reps)
+        code, st = last["r"]
         eta = la_gpu.backward_error_device(ctx, a.data_ptr(), n, x.data_ptr(), nrhs,
                                            b.data_ptr(), nrhs, n, nrhs)
-        auto_by_kappa[kappa] = {"kappa": kappa, "precision_used": {0: "fp64", 2: "fp16",
-                                                                    3: "fp32"}[st.precision],
-                                "ms": (t1 - t0) * 1e3, "gflops": flops / (t1 - t0) / 1e9,
+        auto_by_kappa[kappa] = {"kappa": kappa,
+                                "precision_used": {0: "fp64", 1: "bf16", 2: "fp16", 3: "fp32",
+                                                   4: "fp8"}[st.precision],
+                                "ms": ms, "ms_min_max": [min(times), max(times)],
+                                "gflops": flops / (ms * 1e-3) / 1e9,
                                 "iterations": st.iterations, "fell_back": st.fell_back,
                                 "converged": eta <= 1e-14, "eta": eta}
         del a
-    # plain FP64 LU + solve on the kappa = 1e2 matrix
+    # plain FP64 LU + solve on the kappa = 1e2 matrix (one warm-up, 3 timed)
     a = householder_conditioned(torch, n, 1e2, 32)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    lu = la_gpu.LUDecomposition.new_device(a.data_ptr(), n, n, n, ctx)
-    lu.solve_device(b.data_ptr(), nrhs, n, nrhs, x.data_ptr(), nrhs)
-    ctx.synchronize()
-    t1 = time.perf_counter()
-    lu.free()
+
+    def plain_step():
+        lu = la_gpu.LUDecomposition.new_device(a.data_ptr(), n, n, n, ctx)
+        lu.solve_device(b.data_ptr(), nrhs, n, nrhs, x.data_ptr(), nrhs)
+        lu.free()
+
+    pms, ptimes = event_ms(torch, plain_step, reps=3)
     plain_eta = la_gpu.backward_error_device(ctx, a.data_ptr(), n, x.data_ptr(), nrhs,
                                              b.data_ptr(), nrhs, n, nrhs)
-    plain = {"ms": (t1 - t0) * 1e3, "gflops": flops / (t1 - t0) / 1e9, "eta": plain_eta}
+    plain = {"ms": pms, "ms_min_max": [min(ptimes), max(ptimes)],
+             "gflops": flops / (pms * 1e-3) / 1e9, "eta": plain_eta}
     del a
     speed = {("%.0e" % k): (auto_by_kappa[k]["gflops"] / plain["gflops"]
                             if auto_by_kappa[k]["converged"] else None) for k in kappas}
     return {"workload": "mixed-precision LU + FP64 iterative refinement, n=%d, %d RHS, "
                         "A = H1 diag(s) H2 (4 Householder reflectors each), s geometric 1 -> "
                         "1/kappa; nominal flops 2/3 n^3 + 2 n^2 nrhs" % (n, nrhs),
+            "timing": "median of %d runs, CUDA events on the library stream, after one "
+                      "untimed run (plain FP64: median of 3)" % reps,
             "auto_by_kappa": {("%.0e" % k): v for k, v in auto_by_kappa.items()},
             "speedup_vs_plain_fp64": speed,
-            "speedup_basis": "la_lu_solve_auto_device (FP16 factors, then FP32, then the plain "
-                             "FP64 LU; precision chosen at run time, not after the fact) against "
-                             "the plain FP64 LU + solve, wall clock of factor + solve",
+            "speedup_basis": "la_lu_solve_auto_device (precision chosen at run time, not after "
+                             "the fact) against the plain FP64 LU + solve, device time of "
+                             "factor + solve",
+            "max_eta": max([r["eta"] for r in results if r["converged"]] +
+                           [v["eta"] for v in auto_by_kappa.values()] + [plain_eta]),
             "plain_fp64": plain, "runs": results,
             "fastest_fixed_precision_by_kappa": {("%.0e" % k): v
                                                  for k, v in best_by_kappa.items()}}
 
 
-def _wall_ms(ctx, torch, fn, reps=3):
-    """Best of reps wall-clock runs of fn, synchronised on both sides (the
-    batches below run for tens to hundreds of milliseconds, so launch and
-    synchronisation overheads are negligible)."""
-    best = float("inf")
-    for _ in range(reps):
-        torch.cuda.synchronize()
-        ctx.synchronize()
-        t0 = time.perf_counter()
-        fn()
-        ctx.synchronize()
-        best = min(best, time.perf_counter() - t0)
-    return best * 1e3
-
-
-def _sample_eta(la_gpu, ctx, systems, da, db, dx, count=64, seed=0):
-    """Largest normwise backward error over a seeded sample of the systems,
-    by the library's compensated FP64 residual."""
-    rng = np.random.default_rng(seed)
-    worst = 0.0
-    for i in rng.choice(len(systems), min(count, len(systems)), replace=False):
-        s = systems[int(i)]
-        e = la_gpu.backward_error_device(ctx, da.data_ptr() + 8 * s.a_offset, s.n,
-                                         dx.data_ptr() + 8 * s.b_offset, s.nrhs,
-                                         db.data_ptr() + 8 * s.b_offset, s.nrhs, s.n, s.nrhs)
-        worst = max(worst, e)
+def all_eta(la_gpu, ctx, torch, systems, da, db, dx):
+    """Largest normwise backward error over every system of the batch, each
+    by the library's compensated FP64 residual (one device kernel)."""
+    eta = torch.empty(len(systems), dtype=torch.float64, device="cuda")
+    worst = la_gpu.batch_backward_error_device(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(),
+                                               systems, eta.data_ptr())
+    del eta
     return worst
 
 
-def run_batched(la_gpu, torch, ctx, count=20000, seed=4):
+def run_batched(la_gpu, torch, ctx, count=20000, seed=4, reps=5):
     """Uneven batch: count systems, n uniform in [8, 256], 1-4 RHS, A iid N(0,1)
     plus 0.5 n I on even-indexed systems, B iid N(0,1) (generated on the device,
     seeded). Each arm runs its autotuned plan shape (CTAs per SM x warps per
-    system) from a captured CUDA graph; solves/s = count / batch time."""
+    system) from a captured CUDA graph; solves/s = count / batch time (median of
+    `reps` graph launches, CUDA events)."""
     rng = np.random.default_rng(seed)
     ns = rng.integers(8, 257, size=count)
     rs = rng.integers(1, 5, size=count)
@@ -480,17 +511,19 @@ def run_batched(la_gpu, torch, ctx, count=20000, seed=4):
     da[torch.from_numpy(idx).cuda()] += torch.from_numpy(shift).cuda()
     torch.cuda.synchronize()
     out = {"workload": "uneven batch: %d systems, n uniform in [8, 256], 1-4 RHS, A iid N(0,1) "
-                       "+ 0.5 n I on even systems" % count, "count": count}
+                       "+ 0.5 n I on even systems" % count, "count": count,
+           "timing": "median of %d graph launches, CUDA events" % reps}
     for mode, name in ((la_gpu.BATCH_FP64, "plain_fp64"), (la_gpu.BATCH_MIXED, "mixed_ir")):
         c, w, _ = la_gpu.batch_autotune(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems,
                                         mode)
         plan = la_gpu.BatchPlan(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems, mode,
                                 ctas_per_sm=c, warps_per_system=w)
-        ms = _wall_ms(ctx, torch, plan.run, reps=5)
+        ms, times = event_ms(torch, plan.run, reps=reps)
         its, eta, fb = plan.stats()
-        out[name] = {"ms": ms, "solves_per_s": count / (ms * 1e-3), "ctas_per_sm": c,
+        out[name] = {"ms": ms, "ms_min_max": [min(times), max(times)],
+                     "solves_per_s": count / (ms * 1e-3), "ctas_per_sm": c,
                      "warps_per_system": w, "fell_back": int(fb.sum()),
-                     "max_eta_sample": _sample_eta(la_gpu, ctx, systems, da, db, dx)}
+                     "max_eta_all": all_eta(la_gpu, ctx, torch, systems, da, db, dx)}
         plan.free()
     out["speedup_solves_per_s"] = (out["mixed_ir"]["solves_per_s"] /
                                    out["plain_fp64"]["solves_per_s"])
@@ -499,29 +532,29 @@ def run_batched(la_gpu, torch, ctx, count=20000, seed=4):
     return out
 
 
-def run_selector(la_gpu, torch, ctx, count=50000, seed=7):
+def run_selector(la_gpu, torch, ctx, count=50000, seed=7, reps=5):
     """Learned precision selector on a held-out Householder-conditioned batch:
     count systems, n uniform in [16, 512], 1-4 RHS, log10 kappa_2 uniform in
     [1, 12] (seed 7; the committed weights were trained on 200,000 systems with
-    seeds 1000+). Times, per batch: the plain FP64 plan; the mixed plan with
-    FP32 factors for every system (the method without the selector); and the
-    selector path (features + MLP inference + per-system class choice + the
-    same mixed plan), everything on the device."""
+    seeds 1000+). Times, per batch (median of `reps`, CUDA events): the plain
+    FP64 plan; the mixed plan with FP32 factors for every system (the method
+    without the selector); and the selector path (features + MLP inference +
+    per-system class choice + the same mixed plan), everything on the device."""
     import selector as S
     weights = os.path.join(ROOT, "rust-la_gb300", "selector_weights.npy")
     systems, da, db, dx, kappa = S.conditioned_batch(ctx, count, seed)
     sel = S.PrecisionSelector.from_file(ctx, weights)
     out = {"workload": "learned selector: %d systems, n uniform in [16, 512], 1-4 RHS, "
                        "A = H1 diag(s) H2, log10 kappa uniform in [1, 12]" % count,
-           "count": count}
+           "count": count, "timing": "median of %d runs, CUDA events" % reps}
     c64, w64, _ = la_gpu.batch_autotune(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems,
                                         la_gpu.BATCH_FP64)
     p64 = la_gpu.BatchPlan(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems,
                            la_gpu.BATCH_FP64, ctas_per_sm=c64, warps_per_system=w64)
-    t64 = _wall_ms(ctx, torch, p64.run)
+    t64, _ = event_ms(torch, p64.run, reps=reps)
     out["plain_fp64"] = {"ms": t64, "solves_per_s": count / (t64 * 1e-3), "ctas_per_sm": c64,
                          "warps_per_system": w64,
-                         "max_eta_sample": _sample_eta(la_gpu, ctx, systems, da, db, dx)}
+                         "max_eta_all": all_eta(la_gpu, ctx, torch, systems, da, db, dx)}
     p64.free()
     plan = la_gpu.BatchPlan(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems,
                             la_gpu.BATCH_MIXED, ctas_per_sm=2, warps_per_system=8)
@@ -543,25 +576,77 @@ def run_selector(la_gpu, torch, ctx, count=50000, seed=7):
         plan.select_device(cls.data_ptr())
         plan.run()
 
-    t32 = _wall_ms(ctx, torch, fixed)
+    t32, _ = event_ms(torch, fixed, reps=reps)
     its, eta, fb = plan.stats()
     out["mixed_fp32_factors"] = {"ms": t32, "solves_per_s": count / (t32 * 1e-3),
                                  "fell_back": int(fb.sum()),
-                                 "max_eta_sample": _sample_eta(la_gpu, ctx, systems, da, db, dx)}
-    tf = _wall_ms(ctx, torch, choose)
-    ts = _wall_ms(ctx, torch, selected)
+                                 "max_eta_all": all_eta(la_gpu, ctx, torch, systems, da, db, dx)}
+    tf, _ = event_ms(torch, choose, reps=reps)
+    ts, _ = event_ms(torch, selected, reps=reps)
     its, eta, fb = plan.stats()
-    counts = np.bincount(cls.cpu().numpy(), minlength=3).tolist()
+    counts = np.bincount(cls.cpu().numpy(), minlength=4).tolist()
     out["mixed_selector"] = {"ms": ts, "solves_per_s": count / (ts * 1e-3),
                              "features_inference_ms": tf, "fell_back": int(fb.sum()),
-                             "class_counts_fp8_bf16_fp32": counts,
-                             "max_eta_sample": _sample_eta(la_gpu, ctx, systems, da, db, dx)}
+                             "class_counts_fp8_bf16_fp32_fp64": counts,
+                             "max_eta_all": all_eta(la_gpu, ctx, torch, systems, da, db, dx)}
     plan.free()
     out["speedup_selector_vs_plain_fp64"] = t64 / ts
     out["speedup_selector_vs_fp32_factors"] = t32 / ts
     del da, db, dx
     torch.cuda.empty_cache()
     return out
+
+
+def summarize(line):
+    """The headline figures of every section in one small object."""
+    def get(d, *keys):
+        for k in keys:
+            if not isinstance(d, dict) or k not in d:
+                return None
+            d = d[k]
+        return d
+
+    def r3(v):
+        return round(v, 3) if isinstance(v, float) else v
+
+    out = {"plain_fp64_gflops": r3(line.get("value")), "e2e_gflops": r3(get(line, "e2e", "value")),
+           "gemm_roofline_frac": r3(get(line, "roofline", "frac")),
+           "backward_error": line.get("backward_error")}
+    mixed = line.get("mixed_ir")
+    if isinstance(mixed, dict) and "auto_by_kappa" in mixed:
+        out["mixed_auto"] = {k: {"ms": r3(v["ms"]), "precision": v["precision_used"],
+                                 "speedup_vs_plain_fp64": r3(get(mixed, "speedup_vs_plain_fp64", k)),
+                                 "eta": v["eta"]}
+                             for k, v in mixed["auto_by_kappa"].items()}
+        out["mixed_plain_fp64_ms"] = r3(get(mixed, "plain_fp64", "ms"))
+    bat = line.get("batched_uneven")
+    if isinstance(bat, dict) and "speedup_solves_per_s" in bat:
+        out["batched"] = {"speedup_solves_per_s": r3(bat["speedup_solves_per_s"]),
+                          "mixed_solves_per_s": r3(get(bat, "mixed_ir", "solves_per_s")),
+                          "max_eta_all": max(get(bat, "mixed_ir", "max_eta_all"),
+                                             get(bat, "plain_fp64", "max_eta_all"))}
+    sel = line.get("learned_selector")
+    if isinstance(sel, dict) and "speedup_selector_vs_fp32_factors" in sel:
+        out["selector"] = {"vs_fp32_factors": r3(sel["speedup_selector_vs_fp32_factors"]),
+                           "vs_plain_fp64": r3(sel["speedup_selector_vs_plain_fp64"]),
+                           "max_eta_all": max(get(sel, "mixed_selector", "max_eta_all"),
+                                              get(sel, "plain_fp64", "max_eta_all"))}
+    for key in ("gemm_8192", "cholesky_8192", "qr_2048"):
+        sec = line.get(key)
+        if isinstance(sec, dict):
+            out[key + "_gflops"] = r3(sec.get("gflops", sec.get("factor_gflops")))
+    return out
+
+
+DEFAULT_PANEL_WIDTH = 64  # the library's default LA_OPT_PANEL_WIDTH
+
+
+def bench_config(args, panel_w, world):
+    """The workload's description, identical for this library's line and the
+    reference arm's line."""
+    return {"workload": WORKLOAD, "n": args.n, "nrhs": args.nrhs, "arith": args.arith,
+            "panel_width": panel_w, "parallelism": "replicas" if world > 1 else "1 GPU",
+            "l2": "inputs larger than L2 (512 MiB matrix), no flush"}
 
 
 def dist_setup(args, backend="nccl"):
@@ -622,8 +707,7 @@ def run_reference(args):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic: A iid N(0,1), seed 2",
-        "config": {"workload": WORKLOAD, "n": n, "nrhs": nrhs,
-                   "l2": "CPU run; not applicable"},
+        "config": bench_config(args, DEFAULT_PANEL_WIDTH, world),
         "cpu_baseline": {"value": gf, "unit": "GFLOP/s", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": gf, "unit": "GFLOP/s", "h2d_bytes_per_step": 0,
@@ -706,21 +790,25 @@ def run_ours(args):
     eta = la_gpu.backward_error_device(ctx, da.data_ptr(), n, dx.data_ptr(), nrhs, db.data_ptr(),
                                        nrhs, n, nrhs)
 
-    # roofline of the trailing-update GEMM
-    gflops_gemm, gemm_launches = trailing_gemm_flops(n, panel_w)
+    # roofline of the trailing-update GEMM: all its launches of one factorization
+    gl = trailing_gemm_launches(n, panel_w, lookahead=bool(ctx.get_option(la_gpu.OPT_LOOKAHEAD)))
+    flops_gemm, flops_per_launch, bytes_per_launch = gemm_algorithmic(gl)
     gemm_ms = phases[3] / PK
-    achieved = gflops_gemm / (gemm_ms * 1e-3) / 1e12 if gemm_ms > 0 else None
-    tpf = read_traffic_summary()
+    achieved = flops_gemm / (gemm_ms * 1e-3) / 1e12 if gemm_ms > 0 else None
     roof = {
-        "bound": "tensor", "compute_pipe": "FP64 FMA (DFMA); GB300 has no faster FP64 path",
-        "kernel": "gemm_f64_kernel (trailing update A22 -= L21*U12)",
+        "bound": "fp64", "compute_pipe": "FP64 FMA (DFMA): GB300 has no faster FP64 path "
+                                         "(no FP64 tensor-core rate above it)",
+        "kernel": "gemm_f64_tma_kernel (trailing update A22 -= L21*U12)",
         "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
         "frac": (achieved / fp64_peak) if achieved else None,
-        "peak_source": "FP64 FMA microbenchmark run live in this process (la_probe_fp64_peak); "
-                       "the driver's measured-peaks file has no FP64 figure",
-        "traffic": (tpf * gflops_gemm / gemm_launches) if tpf else None,
-        "traffic_unit": "bytes per launch (mean), scaled from the ncu capture at n=4096",
-        "algorithmic_flops_per_launch": gflops_gemm / gemm_launches,
+        "peak_source": "FP64 FMA issue rate measured live in this process "
+                       "(la_probe_fp64_peak); the measured-peaks file has no FP64 figure",
+        "traffic": GEMM_TRAFFIC_BYTES_PER_LAUNCH,
+        "traffic_unit": "DRAM bytes per launch (mean over the factorization's launches), one "
+                        "ncu capture of the same n=8192 factorization",
+        "launches_per_factorization": len(gl),
+        "algorithmic_flops_per_launch": flops_per_launch,
+        "algorithmic_bytes_per_launch": bytes_per_launch,
         "gemm_ms_per_factorization": gemm_ms,
         "phase_ms_per_factorization": {"panel": phases[0] / PK, "row_swaps": phases[1] / PK,
                                        "row_panel_trsm": phases[2] / PK,
@@ -806,9 +894,7 @@ def run_ours(args):
             "warmup": W, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: A iid N(0,1) f64 n=8192 (seed 2), 16 RHS iid N(0,1)",
-            "config": {"workload": WORKLOAD, "n": n, "nrhs": nrhs, "arith": args.arith,
-                       "panel_width": panel_w, "parallelism": "replicas" if world > 1 else "1 GPU",
-                       "l2": "inputs larger than L2 (512 MiB matrix), no flush"},
+            "config": bench_config(args, panel_w, world),
             "solves_per_s": world / (ms * 1e-3),
             "backward_error": eta,
             "gpu_launches": int(launches),
@@ -825,6 +911,7 @@ def run_ours(args):
             "learned_selector": selected,
             "fp64_peak_tflops": fp64_peak,
         }
+        line["summary"] = summarize(line)  # last, so that a tail of the line shows it
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

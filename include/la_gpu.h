@@ -181,6 +181,7 @@ la_status la_matrix_mul_device(la_ctx ctx, const double* d_a, size_t lda, const 
 #define LA_PREC_FP16 2  /* tcgen05 FP16 x FP16 -> FP32, per-panel power-of-two scaling */
 #define LA_PREC_FP32 3  /* FP32 FMA (no tensor cores) */
 #define LA_PREC_FP8 4   /* batched solves: factors stored as FP8 e4m3 (power-of-two scaled) */
+#define LA_PREC_FP64 5  /* batched solves: no mixed attempt, the plan's FP64 pass answers */
 
 typedef struct la_refine_stats {
   int iterations;    /* refinement steps (plain and GMRES) */
@@ -234,7 +235,8 @@ la_status la_lowp_update_device(la_ctx ctx, int fmt, size_t m, size_t n, size_t 
  * 1 <= nrhs <= 4. `precision` (mixed batches) is the storage of its LU
  * factors: LA_PREC_FP8, LA_PREC_BF16 or LA_PREC_FP32 (0 = FP32); arithmetic is
  * FP32 either way, and narrower storage lets larger systems stay in shared
- * memory at the cost of less accurate factors. */
+ * memory at the cost of less accurate factors. LA_PREC_FP64 sends the system
+ * straight to the plan's FP64 pass (no mixed attempt). */
 typedef struct la_batch_system {
   size_t a_offset;
   size_t b_offset;
@@ -281,9 +283,16 @@ la_status la_batch_autotune(la_ctx ctx, const double* d_a, const double* d_b, do
 
 /* Sets each system's factor storage from d_class (device, caller's order, one
  * int per system: 0 = FP8, 1 = BF16, 2 = FP32, the classes of the precision
- * selector) for the following runs of a LA_BATCH_MIXED plan, without
- * rebuilding it; asynchronous on the context's stream. */
+ * selector, or 3 = no mixed attempt, straight to the FP64 pass) for the
+ * following runs of a LA_BATCH_MIXED plan, without rebuilding it;
+ * asynchronous on the context's stream. */
 la_status la_batch_plan_select_device(la_batch_plan plan, const int* d_class);
+/* Row order of the factorization that produced each system's X in the last
+ * run (lu.rs:147-149 piv: piv[i] = the original row at position i): the FP64
+ * pass's for systems it answered, the mixed pass's otherwise. piv (host) holds
+ * sum of n_i entries, the systems one after the other in the caller's order.
+ * Synchronizes. */
+la_status la_batch_plan_pivots(la_batch_plan plan, uint64_t* piv);
 /* Phase profile of the last run: SM cycles summed over all CTAs, phase[0..3]
  * = load (and FP8 scaling), factorization, triangular solves, residuals and
  * convergence tests of the first pass; phase[4..7] the same for the FP64 redo
@@ -352,14 +361,22 @@ la_status la_mlp_predict(la_mlp mlp, const float* d_x, int count, float* d_probs
  * 16-byte aligned, lda even) in place on `stream` (a cudaStream_t, NULL for
  * the default stream) and writes the swap list d_ipiv (min(m,n) int32), the
  * permutation vector d_piv (m uint64, the form of lu.rs piv) and d_flags[0] =
- * pospivsign, d_flags[1] = 1 if U has an exact zero on its diagonal. Returns
- * after the stream has finished the factorization.
+ * pospivsign, d_flags[1] = 1 if U has an exact zero on its diagonal.
+ * The call blocks until the stream has finished the factorization (it waits on
+ * the stream and reads the device error word with a synchronous copy), so it
+ * cannot be called while any stream is being captured into a CUDA graph.
  * Limit: m <= 16384 (LA_UNSUPPORTED beyond). Its working memory is one static
  * device array of about 70 KB per device, kept until the process exits and
  * shared by every call: calls that overlap on the GPU (other host threads,
  * other streams) race and must be serialized by the caller. The first call on
- * a device looks up that array's device address; make it before any stream
- * capture. */
+ * a device looks up that array's device address; after cudaDeviceReset that
+ * address is stale and the library must not be called again in the process.
+ * Status: LA_INVALID for null pointers, lda < n, or d_a not 16-byte aligned or
+ * lda odd; LA_BADSHAPE for m or n = 0; LA_UNSUPPORTED beyond the limit (or a
+ * panel that does not fit the kernel's shared memory); LA_TIMEOUT when any
+ * bounded device wait of the factorization (panel barrier, TMA stage of the
+ * trailing update) gave up; LA_CUDA_ERROR when a CUDA call failed. There is no
+ * context, so no message is kept beyond the status. */
 la_status la_lu_factor_noalloc(void* stream, double* d_a, size_t lda, size_t m, size_t n,
                                int* d_ipiv, uint64_t* d_piv, int* d_flags);
 
@@ -373,6 +390,14 @@ la_status la_backward_error_device(la_ctx ctx, const double* d_a, size_t lda, co
                                    size_t nrhs, double* eta);
 la_status la_backward_error(la_ctx ctx, const double* a, const double* x, const double* b,
                             size_t n, size_t nrhs, double* eta);
+/* The same for every system of a batch (systems as in la_batch_plan_create,
+ * any n >= 1 and nrhs >= 1): d_eta[i] (device, count doubles, caller's order)
+ * is system i's eta, computed with the same compensated FP64 residual; when
+ * max_eta (host) is not NULL it receives the largest of them (NaN if any is
+ * NaN). Synchronizes. */
+la_status la_batch_backward_error_device(la_ctx ctx, const double* d_a, const double* d_b,
+                                         const double* d_x, const la_batch_system* systems,
+                                         int count, double* d_eta, double* max_eta);
 
 /* ---- Cholesky decomposition (src/decomp/cholesky.rs) ------------------------ */
 

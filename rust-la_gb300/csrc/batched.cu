@@ -51,7 +51,8 @@ constexpr size_t GM_V_OFFSET = (size_t)NMAX * NMAX * sizeof(float);
 struct SysDesc {
   long long a;  // offset of A_i (n x n, row-major) in the A buffer, elements
   long long b;  // offset of B_i / X_i (n x nrhs, row-major), elements
-  int n, nrhs, cls, pad;
+  int n, nrhs, cls;
+  int poff;     // offset of the system's row order in BatchArgs::piv
 };
 
 // Storage policies: element type in memory, arithmetic type, conversions.
@@ -456,6 +457,7 @@ struct BatchArgs {
   double tol;
   int only_flagged;  // FP64 pass: process only systems with status < 0
   int gmres_m;       // largest Krylov basis of the GMRES-IR stage (0: no GMRES-IR)
+  int* piv;          // per system at desc.poff: the row order (lu.rs piv) of the factors used
   long long* cycles; // per system: SM cycles spent on it, summed over the passes
   unsigned long long* phase;  // [8]: load, factor, solves, residuals of the first pass,
                               // then the same for the FP64 redo pass (summed over CTAs)
@@ -825,6 +827,7 @@ __device__ void process_system(const BatchArgs& a, int sidx, const SysDesc& d, S
   if (tid == 0) pc.mark(0);
   block_lu<P>(M, n, n, rmap, st, us, sh);
   if (tid == 0) pc.mark(1);
+  for (int i = tid; i < n; i += BT) a.piv[d.poff + i] = rmap[i];
 
   if (!MIXED) {
     for (int idx = tid; idx < n * nrhs; idx += BT) {
@@ -916,7 +919,8 @@ __device__ void process_system(const BatchArgs& a, int sidx, const SysDesc& d, S
   }
 }
 
-// Storage classes of the mixed pass.
+// Storage classes of the mixed pass; CLS_F64 systems skip it and go straight
+// to the FP64 pass.
 enum { CLS_F64 = 0, CLS_F32 = 1, CLS_BF16 = 2, CLS_FP8 = 3 };
 
 template <bool MIXED>
@@ -942,6 +946,12 @@ __global__ void __launch_bounds__(BT_MAX, MIXED ? 2 : 1) batched_kernel(BatchArg
     const long long t0 = clock64();
     if (!MIXED) {
       process_system<StF64, false>(a, sidx, d, sh, smem);
+    } else if (d.cls == CLS_F64) {
+      if (tid == 0) {
+        a.status[sidx] = -1;
+        a.eta[sidx] = INFINITY;
+        a.redo[1 + atomicAdd(&a.redo[0], 1)] = sidx;
+      }
     } else if (d.cls == CLS_FP8) {
       process_system<StFP8, true>(a, sidx, d, sh, smem);
     } else if (d.cls == CLS_BF16) {
@@ -954,14 +964,14 @@ __global__ void __launch_bounds__(BT_MAX, MIXED ? 2 : 1) batched_kernel(BatchArg
   }
 }
 
-// desc[i].cls from the selector's class (0 FP8, 1 BF16, 2 FP32) of the caller's
-// system perm[i].
+// desc[i].cls from the selector's class (0 FP8, 1 BF16, 2 FP32, 3 straight to
+// the FP64 pass) of the caller's system perm[i].
 __global__ void select_kernel(SysDesc* desc, const int* __restrict__ perm,
                               const int* __restrict__ sel, int count) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
   const int c = sel[perm[i]];
-  desc[i].cls = c == 0 ? CLS_FP8 : (c == 1 ? CLS_BF16 : CLS_F32);
+  desc[i].cls = c == 0 ? CLS_FP8 : (c == 1 ? CLS_BF16 : (c == 3 ? CLS_F64 : CLS_F32));
 }
 
 constexpr size_t BATCH_STATIC_SMEM = 1024;  // bound of the kernel's static shared memory
@@ -983,6 +993,10 @@ struct la_batch_plan_s {
   long long* d_cycles = nullptr;
   unsigned long long* d_phase = nullptr;
   int* d_perm = nullptr;
+  int* d_piv = nullptr;     // row orders, system after system in queue order
+  std::vector<int> poff;    // caller's system -> offset in d_piv
+  std::vector<int> n_of;    // caller's system -> n
+  long long piv_total = 0;
   void* d_scratch = nullptr;
   std::vector<int> perm;  // sorted position -> caller's system index
   size_t smem = 0, smem_fp64 = 0, scratch_bytes = 0;
@@ -1041,6 +1055,7 @@ la_status launch_pass(la_batch_plan_s* pl, int* queue, int only_flagged, size_t 
   a.only_flagged = only_flagged;
   a.gmres_m = pl->gmres_m;
   a.cycles = pl->d_cycles;
+  a.piv = pl->d_piv;
   a.phase = pl->d_phase;
   batched_kernel<MIXED><<<grid, threads, smem, ctx->stream>>>(a);
   ctx->launches++;
@@ -1069,6 +1084,7 @@ int class_of(int prec) {
   switch (prec) {
     case LA_PREC_FP8: return CLS_FP8;
     case LA_PREC_BF16: return CLS_BF16;
+    case LA_PREC_FP64: return CLS_F64;
     default: return CLS_F32;
   }
 }
@@ -1134,6 +1150,10 @@ la_status la_batch_plan_create(la_ctx ctx, const double* d_a, const double* d_b,
   std::stable_sort(pl->perm.begin(), pl->perm.end(),
                    [&](int x, int y) { return systems[x].n > systems[y].n; });
   std::vector<SysDesc> h(count);
+  pl->poff.assign(count, 0);
+  pl->n_of.resize(count);
+  for (int i = 0; i < count; i++) pl->n_of[i] = systems[i].n;
+  long long off = 0;
   for (int i = 0; i < count; i++) {
     const la_batch_system& s = systems[pl->perm[i]];
     h[i].a = (long long)s.a_offset;
@@ -1141,8 +1161,11 @@ la_status la_batch_plan_create(la_ctx ctx, const double* d_a, const double* d_b,
     h[i].n = s.n;
     h[i].nrhs = s.nrhs;
     h[i].cls = class_of(s.precision);
-    h[i].pad = 0;
+    h[i].poff = (int)off;
+    pl->poff[pl->perm[i]] = (int)off;
+    off += s.n;
   }
+  pl->piv_total = off;  // at most count * 512, checked below
   const int slices = std::max(pl->grid, pl->grid_fp64);
   la_status s = la_device_alloc(ctx, reinterpret_cast<void**>(&pl->d_desc), count * sizeof(SysDesc));
   if (s == LA_OK) s = la_device_alloc(ctx, reinterpret_cast<void**>(&pl->d_queue), 64);
@@ -1152,6 +1175,9 @@ la_status la_batch_plan_create(la_ctx ctx, const double* d_a, const double* d_b,
   if (s == LA_OK) s = la_device_alloc(ctx, reinterpret_cast<void**>(&pl->d_eta), count * sizeof(double));
   if (s == LA_OK) s = la_device_alloc(ctx, reinterpret_cast<void**>(&pl->d_cycles), count * sizeof(long long));
   if (s == LA_OK) s = la_device_alloc(ctx, reinterpret_cast<void**>(&pl->d_perm), count * sizeof(int));
+  if (s == LA_OK && pl->piv_total > INT32_MAX) s = LA_UNSUPPORTED;
+  if (s == LA_OK)
+    s = la_device_alloc(ctx, reinterpret_cast<void**>(&pl->d_piv), (size_t)pl->piv_total * sizeof(int));
   if (s == LA_OK) s = la_device_alloc(ctx, reinterpret_cast<void**>(&pl->d_phase), 8 * sizeof(unsigned long long));
   if (s == LA_OK) s = la_device_alloc(ctx, &pl->d_scratch, (size_t)slices * pl->scratch_bytes);
   if (s == LA_OK) {
@@ -1223,6 +1249,25 @@ la_status la_batch_plan_stats(la_batch_plan pl, int* iterations, double* eta, in
   return LA_OK;
 }
 
+la_status la_batch_plan_pivots(la_batch_plan pl, uint64_t* piv) {
+  if (!pl || !piv) return LA_INVALID;
+  la_ctx ctx = pl->ctx;
+  LA_CUDA(ctx, cudaSetDevice(ctx->device));
+  std::vector<int> p((size_t)pl->piv_total);
+  LA_CUDA(ctx, cudaMemcpyAsync(p.data(), pl->d_piv, p.size() * sizeof(int),
+                               cudaMemcpyDeviceToHost, ctx->stream));
+  LA_TRY(la_sync_and_check(ctx, "batch pivots"));
+  // Device order is the work queue's; the caller's order packs the systems
+  // one after the other as given.
+  size_t out = 0;
+  for (int i = 0; i < pl->count; i++) {
+    const int n = pl->n_of[i];
+    for (int r = 0; r < n; r++) piv[out + r] = (uint64_t)p[(size_t)pl->poff[i] + r];
+    out += n;
+  }
+  return LA_OK;
+}
+
 la_status la_batch_plan_select_device(la_batch_plan pl, const int* d_class) {
   if (!pl || !d_class) return LA_INVALID;
   if (pl->mode != LA_BATCH_MIXED) return LA_INVALID;
@@ -1268,6 +1313,7 @@ void la_batch_plan_destroy(la_batch_plan pl) {
   la_device_free(ctx, pl->d_eta);
   la_device_free(ctx, pl->d_cycles);
   la_device_free(ctx, pl->d_perm);
+  la_device_free(ctx, pl->d_piv);
   la_device_free(ctx, pl->d_phase);
   la_device_free(ctx, pl->d_scratch);
   cudaStreamSynchronize(ctx->stream);

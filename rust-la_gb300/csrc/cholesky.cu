@@ -193,14 +193,18 @@ __global__ void chol_back_exact_kernel(const double* __restrict__ L, size_t ld, 
   }
 }
 
-void configure_chol() {
-  static bool done = false;
-  if (done) return;
-  cudaFuncSetAttribute(chol_diag_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)(2 * CHW * CHP * sizeof(double)));
-  cudaFuncSetAttribute(chol_diag_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)(CHW * CHP * sizeof(double)));
-  done = true;
+cudaError_t configure_chol() {
+  static la_device_once once;
+  return once.run([](int) {
+    cudaError_t e = cudaFuncSetAttribute(chol_diag_kernel<true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(2 * CHW * CHP * sizeof(double)));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(chol_diag_kernel<false>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(CHW * CHP * sizeof(double)));
+    return e;
+  });
 }
 
 la_status chol_check_ctx(la_ctx ctx) {
@@ -217,7 +221,7 @@ la_status chol_factor(la_ctx ctx, la_chol h, int* none) {
   const bool exact = h->arith == LA_ARITH_EXACT;
   double* L = h->d_l;
   cudaStream_t st = ctx->stream;
-  configure_chol();
+  LA_CUDA(ctx, configure_chol());
   int* d_flags = reinterpret_cast<int*>(ctx->d_small);
   LA_CUDA(ctx, cudaMemsetAsync(d_flags, 0, 2 * sizeof(int), st));
   const int nt = (n + 31) / 32;

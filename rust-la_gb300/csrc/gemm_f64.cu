@@ -298,14 +298,12 @@ la_status launch_tma(la_ctx ctx, int M, int N, int K, const double* A, size_t ld
       !la_tma::encode_2d(ctx, &tb, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, B, (size_t)K, (size_t)N,
                          ldb, 32u, (uint32_t)BK, CU_TENSOR_MAP_SWIZZLE_NONE))
     return LA_UNSUPPORTED;
-  static bool configured = false;  // one attribute call per instantiation
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(gemm_f64_tma_kernel<MODE>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)GEMM_SMEM_CAP);
-    if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaFuncSetAttribute(gemm_tma)");
-    configured = true;
-  }
+  static la_device_once configured;  // one attribute call per instantiation and device
+  cudaError_t e = configured.run([](int) {
+    return cudaFuncSetAttribute(gemm_f64_tma_kernel<MODE>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GEMM_SMEM_CAP);
+  });
+  if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaFuncSetAttribute(gemm_tma)");
   const size_t smem = std::min(GEMM_SMEM_CAP, std::max(TMA_SMEM, min_smem));
   dim3 grid((N + TMA_BN - 1) / TMA_BN, (M + BM - 1) / BM);
   gemm_f64_tma_kernel<MODE><<<grid, THREADS, smem, ctx->stream>>>(ta, tb, M, N, K, C, ldc,
@@ -319,14 +317,12 @@ la_status launch_mode(la_ctx ctx, int M, int N, int K, const T* A, size_t lda, c
                       size_t ldb, T* C, size_t ldc, size_t min_smem) {
   const size_t smem =
       std::min(GEMM_SMEM_CAP, std::max((size_t)2 * (BM * BK + BK * BN) * sizeof(T), min_smem));
-  static bool configured = false;  // one attribute call per instantiation
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(gemm_f64_kernel<T, MODE, BN>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)GEMM_SMEM_CAP);
-    if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaFuncSetAttribute(gemm)");
-    configured = true;
-  }
+  static la_device_once configured;  // one attribute call per instantiation and device
+  cudaError_t e = configured.run([](int) {
+    return cudaFuncSetAttribute(gemm_f64_kernel<T, MODE, BN>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GEMM_SMEM_CAP);
+  });
+  if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaFuncSetAttribute(gemm)");
   dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
   gemm_f64_kernel<T, MODE, BN><<<grid, THREADS, smem, ctx->stream>>>(M, N, K, A, lda, B, ldb, C,
                                                                      ldc);

@@ -247,13 +247,12 @@ la_status launch_tc_update(la_ctx ctx, cudaStream_t stream, int fmt, int M, int 
   if (!la_tma::encode_2d(ctx, &tc, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, C, (size_t)M, (size_t)N,
                          ldc, 32u, (uint32_t)TM, CU_TENSOR_MAP_SWIZZLE_128B))
     return LA_CUDA_ERROR;
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(tc_update_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
-    if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaFuncSetAttribute(tc_update)");
-    configured = true;
-  }
+  static la_device_once configured;
+  cudaError_t e = configured.run([](int) {
+    return cudaFuncSetAttribute(tc_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)TC_SMEM);
+  });
+  if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaFuncSetAttribute(tc_update)");
   dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM);
   const uint32_t idesc = idesc_f16(fmt == LA_LOWP_BF16 ? 1u : 0u);
   tc_update_kernel<<<grid, TC_THREADS, TC_SMEM, stream>>>(ta, tb, tc, N, K, d_alpha, idesc,

@@ -6,13 +6,52 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstddef>
 #include <cstdint>
+#include <mutex>
 #include <string>
 #include <vector>
 
 #include "../../include/la_gpu.h"
+
+// Largest device ordinal whose one-time set-up results are cached.
+constexpr int LA_MAX_DEVICES = 64;
+
+// The current CUDA device, or -1 when it cannot be read.
+inline int la_current_device() {
+  int dev = -1;
+  return cudaGetDevice(&dev) == cudaSuccess ? dev : -1;
+}
+
+// One-time set-up per device. Kernel attributes (cudaFuncSetAttribute) and
+// occupancy answers belong to the device that is current at the call, and
+// several host threads (one context each) may arrive at once: each device runs
+// the set-up once under the lock, later calls only read an atomic bit mask. A
+// set-up that fails runs again on the next call.
+struct la_device_once {
+  std::mutex mu;
+  std::atomic<uint64_t> done{0};
+  // f(dev) returns cudaError_t; cudaSuccess when this device ran it before.
+  template <typename F>
+  cudaError_t run(F&& f) {
+    const int dev = la_current_device();
+    if (dev < 0) return cudaErrorInvalidDevice;
+    std::unique_lock<std::mutex> lock(mu, std::defer_lock);
+    if (dev >= LA_MAX_DEVICES) {  // not cached: set up on every call
+      lock.lock();
+      return f(dev);
+    }
+    const uint64_t bit = 1ull << dev;
+    if (done.load(std::memory_order_acquire) & bit) return cudaSuccess;
+    lock.lock();
+    if (done.load(std::memory_order_relaxed) & bit) return cudaSuccess;
+    cudaError_t e = f(dev);
+    if (e == cudaSuccess) done.fetch_or(bit, std::memory_order_release);
+    return e;
+  }
+};
 
 // Accumulation forms of the FP64 kernels.
 //  FAST : c = fma(-a, b, c)                      (blocked LU, in place)

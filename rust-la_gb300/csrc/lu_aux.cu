@@ -255,16 +255,22 @@ __global__ void copy2d_kernel(const double* __restrict__ src, size_t lds, double
 }
 
 // Dynamic shared memory above 48 KB needs an opt-in per kernel.
-void configure_smem_attrs() {
-  static bool done = false;
-  if (done) return;
-  cudaFuncSetAttribute(trsm_rowpanel_kernel<double, true>,
-                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)trsm_smem<double>(true));
-  cudaFuncSetAttribute(trsm_rowpanel_kernel<double, false>,
-                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)trsm_smem<double>(false));
-  cudaFuncSetAttribute(trsm_rowpanel_kernel<float, false>,
-                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)trsm_smem<float>(false));
-  done = true;
+cudaError_t configure_smem_attrs() {
+  static la_device_once once;
+  return once.run([](int) {
+    cudaError_t e = cudaFuncSetAttribute(trsm_rowpanel_kernel<double, true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)trsm_smem<double>(true));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(trsm_rowpanel_kernel<double, false>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)trsm_smem<double>(false));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(trsm_rowpanel_kernel<float, false>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)trsm_smem<float>(false));
+    return e;
+  });
 }
 
 int grid_for(la_ctx ctx, size_t total) {
@@ -309,7 +315,7 @@ template <typename T>
 la_status launch_trsm_t(la_ctx ctx, bool exact, T* A, T* S, size_t ld, int j0, int jb,
                         int c_begin, int c_end) {
   if (c_end <= c_begin) return LA_OK;
-  configure_smem_attrs();
+  LA_CUDA(ctx, configure_smem_attrs());
   dim3 grid((c_end - c_begin + TR_COLS - 1) / TR_COLS);
   if (exact)
     trsm_rowpanel_kernel<T, true><<<grid, 256, trsm_smem<T>(true), ctx->stream>>>(A, S, ld, j0, jb,
@@ -338,14 +344,18 @@ la_status launch_trsm_rowpanel_f32(la_ctx ctx, float* A, size_t ld, int j0, int 
 la_status launch_lu_finish(la_ctx ctx, la_lu h, int* d_flags) {
   const int kmin = (int)std::min(h->m, h->n);
   const int smem_rows = 50000;  // 200 KB of int32 (opt-in); larger m replays in global memory
-  static bool configured = false;
-  if (!configured) {
-    cudaFuncSetAttribute(lu_finish_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         smem_rows * (int)sizeof(int));
-    cudaFuncSetAttribute(lu_finish_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         smem_rows * (int)sizeof(int));
-    configured = true;
-  }
+  static la_device_once configured;
+  cudaError_t ce = configured.run([&](int) {
+    cudaError_t e = cudaFuncSetAttribute(lu_finish_kernel<double>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         smem_rows * (int)sizeof(int));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(lu_finish_kernel<float>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               smem_rows * (int)sizeof(int));
+    return e;
+  });
+  if (ce != cudaSuccess) return la_cuda_fail(ctx, ce, "cudaFuncSetAttribute(lu_finish)");
   const size_t smem = (size_t)std::min((int)h->m, smem_rows) * sizeof(int);
   if (h->d_lu32)
     lu_finish_kernel<float><<<1, 1024, smem, ctx->stream>>>(h->d_ipiv, h->d_piv, (int)h->m, kmin,

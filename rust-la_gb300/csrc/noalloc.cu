@@ -3,12 +3,17 @@
 // Some hosts of this library cannot call cudaMalloc at all: code running under
 // a memory manager that owns every device allocation (a pool sized at start-up,
 // a framework that hands out only pre-registered buffers), or code that must
-// not allocate while it is being captured into a CUDA graph or run in a hot
-// loop with a fixed memory budget. la_lu_factor_noalloc serves them: the caller
-// passes the matrix and the output buffers, and the only working memory the
-// factorization needs beyond them, the panel kernel's pivot-exchange scratch,
-// lives in the file-scope device array below. That array exists once per
-// device that loads the library and stays allocated until the process exits.
+// keep a fixed device-memory footprint in a hot loop. la_lu_factor_noalloc
+// serves them: the caller passes the matrix and the output buffers, and the
+// only working memory the factorization needs beyond them, the panel kernel's
+// pivot-exchange scratch, lives in the file-scope device array below. That
+// array exists once per device that loads the library and stays allocated
+// until the process exits.
+//
+// The call blocks: it waits for the stream to finish the factorization and
+// reads the device error word back with a synchronous copy. So it cannot be
+// called while any stream is being captured into a CUDA graph (the wait and the
+// copy would fail and invalidate the capture).
 #include "la_internal.cuh"
 
 namespace {
@@ -31,21 +36,24 @@ constexpr size_t NA_BYTES = NA_OFF_SWAPS + 4096;  // about 70 KB in total
 
 static __device__ __align__(256) unsigned char g_lu_scratch[NA_BYTES];
 
-constexpr int NA_MAX_DEVICES = 64;
-unsigned char* g_scratch_addr[NA_MAX_DEVICES] = {nullptr};
+// Device address of the scratch array per device, looked up once per device
+// (the host-side symbol is only a stand-in and must never be handed to a
+// kernel). Atomic, so host threads making their first calls at the same time
+// do not race; after cudaDeviceReset the cached address is no longer valid.
+std::atomic<unsigned char*> g_scratch_addr[LA_MAX_DEVICES];
 
-// Once per device, with that device current: the device address of the
-// scratch array (the host-side symbol is only a stand-in and must never be
-// handed to a kernel).
+// With that device current: the scratch array's device address.
 la_status scratch_for_device(int dev, unsigned char** out) {
-  if (dev < 0 || dev >= NA_MAX_DEVICES) return LA_UNSUPPORTED;
-  if (!g_scratch_addr[dev]) {
+  if (dev < 0 || dev >= LA_MAX_DEVICES) return LA_UNSUPPORTED;
+  unsigned char* a = g_scratch_addr[dev].load(std::memory_order_acquire);
+  if (!a) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_lu_scratch);
     if (e != cudaSuccess) return LA_CUDA_ERROR;
-    g_scratch_addr[dev] = static_cast<unsigned char*>(p);
+    a = static_cast<unsigned char*>(p);
+    g_scratch_addr[dev].store(a, std::memory_order_release);  // every thread stores the same value
   }
-  *out = g_scratch_addr[dev];
+  *out = a;
   return LA_OK;
 }
 
@@ -106,6 +114,9 @@ extern "C" la_status la_lu_factor_noalloc(void* stream, double* d_a, size_t lda,
   int err = 0;
   if (cudaMemcpy(&err, c.d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
     return LA_CUDA_ERROR;
+  // Device error words: a panel that does not fit is LA_UNSUPPORTED; every
+  // other code is a bounded device wait that gave up (panel barrier, TMA
+  // GEMM), LA_TIMEOUT.
   if (err != DERR_NONE) return err == DERR_PANEL_CAPACITY ? LA_UNSUPPORTED : LA_TIMEOUT;
   return LA_OK;
 }

@@ -523,9 +523,13 @@ __global__ void __launch_bounds__(CT, 1) panel_cluster_reg_kernel(ClusterPanelAr
 template <int RPT>
 la_status launch_reg(la_ctx ctx, float* A, size_t ld, int m, int j0, int jb, int* d_ipiv,
                      int cluster, int rpc) {
-  static int ok_for = -1;  // cluster size checked once per instantiation (0: none)
-  if (ok_for < 0) {
-    ok_for = 0;
+  // Cluster size checked once per instantiation and device (0: none).
+  static int ok_for[LA_MAX_DEVICES];
+  static la_device_once once;
+  const int dev = la_current_device();
+  if (dev < 0 || dev >= LA_MAX_DEVICES) return LA_UNSUPPORTED;
+  once.run([cluster](int d) {
+    ok_for[d] = 0;
     if (cudaFuncSetAttribute(panel_cluster_reg_kernel<RPT>,
                              cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
       cudaLaunchConfig_t cfg = {};
@@ -542,11 +546,12 @@ la_status launch_reg(la_ctx ctx, float* A, size_t ld, int m, int j0, int jb, int
       if (cudaOccupancyMaxActiveClusters(&nclusters, panel_cluster_reg_kernel<RPT>, &cfg) ==
               cudaSuccess &&
           nclusters >= 1)
-        ok_for = cluster;
+        ok_for[d] = cluster;
     }
     cudaGetLastError();
-  }
-  if (ok_for != cluster) return LA_UNSUPPORTED;
+    return cudaSuccess;
+  });
+  if (ok_for[dev] != cluster) return LA_UNSUPPORTED;
   ClusterPanelArgs a;
   a.A = A;
   a.ld = ld;
@@ -583,24 +588,30 @@ la_status launch_panel_cluster_f32(la_ctx ctx, float* A, size_t ld, int m, int j
   const int R = m - j0;
   if (R <= 0 || jb <= 0) return LA_OK;
   if (jb > CW) return LA_UNSUPPORTED;
-  static int cluster = -1;  // 16, 8 or 0 (no cluster launch possible)
-  static size_t max_smem = 0;
-  if (cluster < 0) {
-    cluster = 0;
-    max_smem = ctx->smem_optin - 2048;  // room for the static buffers
+  // Per device: the cluster size (16, 8 or 0 = no cluster launch possible)
+  // and the dynamic shared memory the cluster kernel may use.
+  static int cluster_of[LA_MAX_DEVICES];
+  static size_t max_smem_of[LA_MAX_DEVICES];
+  static la_device_once once;
+  const int dev = la_current_device();
+  if (dev < 0 || dev >= LA_MAX_DEVICES) return LA_UNSUPPORTED;
+  const size_t optin = ctx->smem_optin;
+  once.run([optin](int d) {
+    int cl = 0;
+    size_t ms = optin - 2048;  // room for the static buffers
     if (cudaFuncSetAttribute(panel_cluster_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed,
                              1) != cudaSuccess ||
         cudaFuncSetAttribute(panel_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)max_smem) != cudaSuccess) {
+                             (int)ms) != cudaSuccess) {
       cudaGetLastError();
-      max_smem = 0;
+      ms = 0;
     }
     for (int c : {16, 8}) {
-      if (max_smem == 0) break;
+      if (ms == 0) break;
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(c);
       cfg.blockDim = dim3(CT);
-      cfg.dynamicSmemBytes = max_smem;
+      cfg.dynamicSmemBytes = ms;
       cudaLaunchAttribute at[1];
       at[0].id = cudaLaunchAttributeClusterDimension;
       at[0].val.clusterDim.x = c;
@@ -611,12 +622,17 @@ la_status launch_panel_cluster_f32(la_ctx ctx, float* A, size_t ld, int m, int j
       int nclusters = 0;
       if (cudaOccupancyMaxActiveClusters(&nclusters, panel_cluster_kernel, &cfg) == cudaSuccess &&
           nclusters >= 1) {
-        cluster = c;
+        cl = c;
         break;
       }
       cudaGetLastError();
     }
-  }
+    cluster_of[d] = cl;
+    max_smem_of[d] = ms;
+    return cudaSuccess;
+  });
+  const int cluster = cluster_of[dev];
+  const size_t max_smem = max_smem_of[dev];
   if (cluster == 0) return LA_UNSUPPORTED;
   const int rpc = (R + cluster - 1) / cluster;
   {

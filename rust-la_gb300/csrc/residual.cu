@@ -11,6 +11,8 @@
 // non-negative doubles (their order matches the integers').
 #include "la_internal.cuh"
 
+#include <vector>
+
 namespace {
 
 constexpr int RES_MAX_RHS = 16;
@@ -129,9 +131,145 @@ la_status eta_device(la_ctx ctx, const double* A, size_t lda, const double* X, s
   return st;
 }
 
+// Backward error of every system of a batch: one CTA per system (grid-stride
+// over the systems), warps over its rows, the same compensated residual as
+// residual_kernel, right-hand sides in groups of BE_R, the maxima merged in
+// shared memory; thread 0 writes the system's eta.
+constexpr int BE_R = 4;
+
+__global__ void __launch_bounds__(256)
+batch_eta_kernel(const double* __restrict__ A, const double* __restrict__ B,
+                 const double* __restrict__ X, const la_batch_system* __restrict__ sys, int count,
+                 double* __restrict__ eta_out) {
+  __shared__ double s_max[1 + 3 * BE_R];
+  __shared__ double s_worst;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int q = blockIdx.x; q < count; q += gridDim.x) {
+    const la_batch_system d = sys[q];
+    const int n = d.n, nrhs = d.nrhs;
+    const double* Ai = A + d.a_offset;
+    const double* Bi = B + d.b_offset;
+    const double* Xi = X + d.b_offset;
+    if (threadIdx.x == 0) s_worst = 0.0;
+    for (int j0 = 0; j0 < nrhs; j0 += BE_R) {
+      const int cnt = min(BE_R, nrhs - j0);
+      if (threadIdx.x < 1 + 3 * BE_R) s_max[threadIdx.x] = 0.0;
+      __syncthreads();
+      for (int i = warp; i < n; i += nw) {
+        double s[BE_R], c[BE_R];
+#pragma unroll
+        for (int j = 0; j < BE_R; j++) { s[j] = 0.0; c[j] = 0.0; }
+        double asum = 0.0;
+        const double* arow = Ai + (size_t)i * n;
+        for (int k = lane; k < n; k += 32) {
+          const double a = arow[k];
+          asum += fabs(a);
+          const double* xr = Xi + (size_t)k * nrhs + j0;
+#pragma unroll
+          for (int j = 0; j < BE_R; j++) {
+            if (j < cnt) {
+              const double x = xr[j];
+              const double p = -a * x;
+              const double pe = fma(-a, x, -p);
+              double t, te;
+              two_sum(s[j], p, t, te);
+              s[j] = t;
+              c[j] += pe + te;
+            }
+          }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+          asum += __shfl_down_sync(0xffffffffu, asum, off);
+#pragma unroll
+          for (int j = 0; j < BE_R; j++) {
+            const double os = __shfl_down_sync(0xffffffffu, s[j], off);
+            const double oc = __shfl_down_sync(0xffffffffu, c[j], off);
+            double t, te;
+            two_sum(s[j], os, t, te);
+            s[j] = t;
+            c[j] += oc + te;
+          }
+        }
+        if (lane == 0) {
+          atomic_max_nonneg(s_max, asum);
+#pragma unroll
+          for (int j = 0; j < BE_R; j++) {
+            if (j < cnt) {
+              const double bij = Bi[(size_t)i * nrhs + j0 + j];
+              double t, te;
+              two_sum(s[j], bij, t, te);
+              atomic_max_nonneg(s_max + 1 + j, fabs(t + (c[j] + te)));
+              atomic_max_nonneg(s_max + 1 + BE_R + j, fabs(Xi[(size_t)i * nrhs + j0 + j]));
+              atomic_max_nonneg(s_max + 1 + 2 * BE_R + j, fabs(bij));
+            }
+          }
+        }
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double worst = s_worst;
+        for (int j = 0; j < cnt; j++) {
+          const double r = s_max[1 + j];
+          const double den = s_max[0] * s_max[1 + BE_R + j] + s_max[1 + 2 * BE_R + j];
+          const double v = den > 0 ? r / den : (r > 0 ? INFINITY : 0.0);
+          if (!(v <= worst)) worst = v;  // keeps NaN
+        }
+        s_worst = worst;
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) eta_out[q] = s_worst;
+    __syncthreads();
+  }
+}
+
 }  // namespace
 
 extern "C" {
+
+la_status la_batch_backward_error_device(la_ctx ctx, const double* d_a, const double* d_b,
+                                         const double* d_x, const la_batch_system* systems,
+                                         int count, double* d_eta, double* max_eta) {
+  if (!ctx || !d_a || !d_b || !d_x || !systems || !d_eta || count < 0) return LA_INVALID;
+  for (int i = 0; i < count; i++)
+    if (systems[i].n < 1 || systems[i].nrhs < 1) return LA_BADSHAPE;
+  if (count == 0) {
+    if (max_eta) *max_eta = 0.0;
+    return LA_OK;
+  }
+  LA_CUDA(ctx, cudaSetDevice(ctx->device));
+  la_batch_system* d_sys = nullptr;
+  LA_TRY(la_device_alloc(ctx, reinterpret_cast<void**>(&d_sys),
+                         (size_t)count * sizeof(la_batch_system)));
+  la_status st = LA_OK;
+  cudaError_t e = cudaMemcpyAsync(d_sys, systems, (size_t)count * sizeof(la_batch_system),
+                                  cudaMemcpyHostToDevice, ctx->stream);
+  if (e != cudaSuccess) st = la_cuda_fail(ctx, e, "copy batch descriptors");
+  if (st == LA_OK) {
+    const int grid = std::min(count, ctx->sm_count * 8);
+    batch_eta_kernel<<<grid, 256, 0, ctx->stream>>>(d_a, d_b, d_x, d_sys, count, d_eta);
+    ctx->launches++;
+    st = la_check_launch(ctx, "batch_eta_kernel");
+  }
+  if (st == LA_OK && max_eta) {
+    std::vector<double> h(count);
+    e = cudaMemcpyAsync(h.data(), d_eta, (size_t)count * sizeof(double), cudaMemcpyDeviceToHost,
+                        ctx->stream);
+    if (e != cudaSuccess) st = la_cuda_fail(ctx, e, "copy batch eta");
+    if (st == LA_OK) st = la_sync_and_check(ctx, "batch backward error");
+    if (st == LA_OK) {
+      double worst = 0.0;
+      for (double v : h)
+        if (!(v <= worst)) worst = v;  // keeps NaN
+      *max_eta = worst;
+    }
+  } else if (st == LA_OK) {
+    st = la_sync_and_check(ctx, "batch backward error");
+  }
+  la_device_free(ctx, d_sys);
+  return st;
+}
 
 la_status la_backward_error_device(la_ctx ctx, const double* d_a, size_t lda, const double* d_x,
                                    size_t ldx, const double* d_b, size_t ldb, size_t n,

@@ -238,29 +238,34 @@ trsv_wave_kernel(const TF* __restrict__ LU, size_t ld, const T* __restrict__ din
 
 }  // namespace
 
-void configure_wave() {
-  static bool done = false;
-  if (done) return;
-  cudaFuncSetAttribute(invert_diag_kernel<float, double>,
-                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)(2 * BS * (BS + 1) * sizeof(double)));
-  cudaFuncSetAttribute(invert_diag_kernel<float, float>,
-                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)(2 * BS * (BS + 1) * sizeof(float)));
-  cudaFuncSetAttribute(trsv_wave_kernel<float, double, false>,
-                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wave_smem<float, double>());
-  cudaFuncSetAttribute(trsv_wave_kernel<float, double, true>,
-                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wave_smem<float, double>());
-  cudaFuncSetAttribute(trsv_wave_kernel<float, float, false>,
-                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wave_smem<float, float>());
-  cudaFuncSetAttribute(trsv_wave_kernel<float, float, true>,
-                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wave_smem<float, float>());
-  done = true;
+cudaError_t configure_wave() {
+  static la_device_once once;
+  return once.run([](int) {
+    const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    cudaError_t e = cudaFuncSetAttribute(invert_diag_kernel<float, double>, at,
+                                         (int)(2 * BS * (BS + 1) * sizeof(double)));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(invert_diag_kernel<float, float>, at,
+                               (int)(2 * BS * (BS + 1) * sizeof(float)));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(trsv_wave_kernel<float, double, false>, at,
+                               (int)wave_smem<float, double>());
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(trsv_wave_kernel<float, double, true>, at,
+                               (int)wave_smem<float, double>());
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(trsv_wave_kernel<float, float, false>, at,
+                               (int)wave_smem<float, float>());
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(trsv_wave_kernel<float, float, true>, at,
+                               (int)wave_smem<float, float>());
+    return e;
+  });
 }
 
 la_status launch_invert_diag_f32(la_ctx ctx, const float* LU, size_t ld, int n, double* dinv) {
   const int nb = (n + BS - 1) / BS;
-  configure_wave();
+  LA_CUDA(ctx, configure_wave());
   invert_diag_kernel<float, double><<<dim3(nb, 2), BS, 2 * BS * (BS + 1) * sizeof(double),
                                       ctx->stream>>>(LU, ld, n, dinv);
   ctx->launches++;
@@ -278,7 +283,7 @@ la_status launch_trsv_wave_f32(la_ctx ctx, const float* LU, size_t ld, const dou
   int* fu = sync + nb;
   int* tickets = sync + 2 * nb;
   LA_CUDA(ctx, cudaMemsetAsync(sync, 0, (2 * nb + 2) * sizeof(int), ctx->stream));
-  configure_wave();
+  LA_CUDA(ctx, configure_wave());
   const size_t sm = wave_smem<float, double>();
   trsv_wave_kernel<float, double, false><<<nb, TT, sm, ctx->stream>>>(LU, ld, dinv, X, ldx, n, nrhs,
                                                                      nb, fl, tickets, ctx->d_err);
@@ -294,7 +299,7 @@ la_status launch_trsv_wave_f32(la_ctx ctx, const float* LU, size_t ld, const dou
 // the factorization's own accuracy): inverted blocks in FP32 too.
 la_status launch_invert_diag_f32f(la_ctx ctx, const float* LU, size_t ld, int n, float* dinv) {
   const int nb = (n + BS - 1) / BS;
-  configure_wave();
+  LA_CUDA(ctx, configure_wave());
   invert_diag_kernel<float, float><<<dim3(nb, 2), BS, 2 * BS * (BS + 1) * sizeof(float),
                                      ctx->stream>>>(LU, ld, n, dinv);
   ctx->launches++;
@@ -309,7 +314,7 @@ la_status launch_trsv_wave_f32f(la_ctx ctx, const float* LU, size_t ld, const fl
   int* fu = sync + nb;
   int* tickets = sync + 2 * nb;
   LA_CUDA(ctx, cudaMemsetAsync(sync, 0, (2 * nb + 2) * sizeof(int), ctx->stream));
-  configure_wave();
+  LA_CUDA(ctx, configure_wave());
   const size_t sm = wave_smem<float, float>();
   trsv_wave_kernel<float, float, false><<<nb, TT, sm, ctx->stream>>>(LU, ld, dinv, X, ldx, n, nrhs,
                                                                     nb, fl, tickets, ctx->d_err);

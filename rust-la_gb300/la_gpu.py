@@ -113,6 +113,8 @@ SIGNATURES = {
     "la_batch_autotune": ([_P, _P, _P, _P, _P, _I, _I, _D, _I, ctypes.c_char_p, _P, _P, _P], _I),
     "la_batch_plan_cycles": ([_P, _P], _I),
     "la_batch_plan_select_device": ([_P, _P], _I),
+    "la_batch_plan_pivots": ([_P, _P], _I),
+    "la_batch_backward_error_device": ([_P, _P, _P, _P, _P, _I, _P, _P], _I),
     "la_batch_plan_phase_cycles": ([_P, _P], _I),
     "la_batch_features_device": ([_P, _P, _P, _I, _P], _I),
     "la_generate_conditioned_batch": ([_P, _P, _I, _D, _D, ctypes.c_ulonglong, _P, _P, _P], _I),
@@ -134,7 +136,7 @@ class BatchSystem(ctypes.Structure):
                 ("n", ctypes.c_int), ("nrhs", ctypes.c_int), ("precision", ctypes.c_int),
                 ("reserved", ctypes.c_int)]
 
-PREC_BF16, PREC_FP16, PREC_FP32, PREC_FP8 = 1, 2, 3, 4
+PREC_BF16, PREC_FP16, PREC_FP32, PREC_FP8, PREC_FP64 = 1, 2, 3, 4, 5
 
 
 class RefineStats(ctypes.Structure):
@@ -622,6 +624,18 @@ def backward_error_device(ctx, a_ptr, lda, x_ptr, ldx, b_ptr, ldb, n, nrhs):
     return out.value
 
 
+def batch_backward_error_device(ctx, a_ptr, b_ptr, x_ptr, systems, eta_ptr):
+    """Every system's backward error into the device buffer eta_ptr (count
+    doubles, caller's order); returns the largest."""
+    worst = ctypes.c_double()
+    _check(ctx, lib().la_batch_backward_error_device(ctx.h, ctypes.c_void_p(a_ptr),
+                                                     ctypes.c_void_p(b_ptr),
+                                                     ctypes.c_void_p(x_ptr), systems,
+                                                     len(systems), ctypes.c_void_p(eta_ptr),
+                                                     ctypes.byref(worst)))
+    return worst.value
+
+
 def lu_mixed_new_device(ctx, a_ptr, lda, n, prec):
     h = ctypes.c_void_p()
     _check(ctx, lib().la_lu_mixed_new_device(ctx.h, ctypes.c_void_p(a_ptr), lda, n, prec,
@@ -698,8 +712,21 @@ class BatchPlan:
         return its, eta, fb
 
     def select_device(self, class_ptr):
-        """Per-system factor storage from selector classes (device int32, 0/1/2)."""
+        """Per-system factor storage from selector classes (device int32: 0 FP8,
+        1 BF16, 2 FP32, 3 straight to the FP64 pass)."""
         _check(self.ctx, lib().la_batch_plan_select_device(self.h, ctypes.c_void_p(class_ptr)))
+
+    def pivots(self, ns):
+        """Row order (lu.rs piv) of each system's factors in the last run, as a
+        list of arrays in the caller's order; ns are the systems' sizes."""
+        total = int(np.sum(ns))
+        p = np.empty(total, dtype=np.uint64)
+        _check(self.ctx, lib().la_batch_plan_pivots(self.h, _ptr(p)))
+        out, o = [], 0
+        for n in ns:
+            out.append(p[o:o + int(n)])
+            o += int(n)
+        return out
 
     def phase_cycles(self):
         """[load, factor, solves, residuals] cycles of the first pass, then of the FP64 redo."""

@@ -1,0 +1,167 @@
+"""Parity at the benchmark's own configurations, through the C ABI, against
+the oracle (the CPU restatement of src/decomp/lu.rs:104-278).
+
+* n = 8192, A and B iid N(0,1) (seed 2, 16 right-hand sides), the workload of
+  the benchmark line: FAST arithmetic reproduces the reference's pivot vector
+  bit for bit (lu.rs:132-149) with a normwise backward error <= 1e-14; EXACT
+  arithmetic reproduces the packed LU, the pivots, the sign and the solution
+  bit for bit.
+* n = 16384, A = H1 diag(s) H2 with kappa in {1e2, 1e6, 1e10}, 4 right-hand
+  sides (the mixed-precision workload): the automatic path's answer and every
+  fixed low precision's refined answer reach eta <= 1e-14 by the oracle's
+  compensated residual.
+* Batches: every system's eta by the device kernel, checked against the
+  oracle on a sample, and the FP64 pass's row order against the oracle's
+  pivots system by system.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+ETA_MAX = 1e-14
+
+
+@pytest.fixture(scope="module")
+def torch():
+    return pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def config2():
+    n, nrhs = 8192, 16
+    rng = np.random.default_rng(2)  # the benchmark's inputs
+    a = rng.standard_normal((n, n))
+    b = rng.standard_normal((n, nrhs))
+    ref = oracle.lu_factor(a, threads=os.cpu_count() or 4)
+    return a, b, ref
+
+
+def test_config2_fast_pivots_and_eta(lagpu, ctx_fast, config2):
+    a, b, ref = config2
+    lu = lagpu.LUDecomposition.new(a, ctx_fast)
+    assert np.array_equal(lu.get_piv(), ref.piv)
+    assert lu.pospivsign() == bool(ref.pospivsign)
+    x = lu.solve(lagpu.Matrix(b, ctx_fast)).data
+    lu.free()
+    assert oracle.backward_error(a, x, b) <= ETA_MAX
+
+
+def test_config2_exact_bit_identical(lagpu, ctx_exact, config2):
+    a, b, ref = config2
+    lu = lagpu.LUDecomposition.new(a, ctx_exact)
+    assert np.array_equal(lu.get_piv(), ref.piv)
+    assert lu.pospivsign() == bool(ref.pospivsign)
+    assert np.array_equal(lu.get_packed().data, ref.lu)
+    x = lu.solve(lagpu.Matrix(b, ctx_exact)).data
+    lu.free()
+    assert np.array_equal(x, oracle.solve_mt(ref, b, os.cpu_count() or 4))
+
+
+@pytest.fixture(scope="module")
+def config3(torch):
+    import bench
+    n, nrhs = 16384, 4
+    rng = np.random.default_rng(3)
+    b = torch.from_numpy(rng.standard_normal((n, nrhs))).cuda()
+    return bench, n, nrhs, b
+
+
+@pytest.mark.parametrize("kappa", [1e2, 1e6, 1e10])
+def test_config3_auto_path_eta_by_oracle(lagpu, ctx_fast, torch, config3, kappa):
+    bench, n, nrhs, b = config3
+    a = bench.householder_conditioned(torch, n, kappa, 30 + int(round(np.log10(kappa))))
+    x = torch.zeros((n, nrhs), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    st, stats = lagpu.lu_solve_auto_device(ctx_fast, a.data_ptr(), n, n, b.data_ptr(), nrhs,
+                                           nrhs, x.data_ptr(), nrhs, tol=5e-15)
+    assert st == lagpu.OK
+    eta = oracle.backward_error(a.cpu().numpy(), x.cpu().numpy(), b.cpu().numpy())
+    assert eta <= ETA_MAX
+    del a
+
+
+@pytest.mark.parametrize("prec", [1, 2, 3], ids=["bf16", "fp16", "fp32"])
+def test_config3_fixed_precision_eta_by_oracle(lagpu, ctx_fast, torch, config3, prec):
+    bench, n, nrhs, b = config3
+    a = bench.householder_conditioned(torch, n, 1e2, 32)
+    x = torch.zeros((n, nrhs), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    lu = lagpu.lu_mixed_new_device(ctx_fast, a.data_ptr(), n, n, prec)
+    st, stats = lagpu.lu_solve_refined_device(lu, b.data_ptr(), nrhs, nrhs, x.data_ptr(), nrhs,
+                                              max_iters=100, tol=5e-15)
+    lu.free()
+    assert st == lagpu.OK and stats.converged
+    assert oracle.backward_error(a.cpu().numpy(), x.cpu().numpy(), b.cpu().numpy()) <= ETA_MAX
+    del a
+
+
+def _uneven_batch(count, seed):
+    rng = np.random.default_rng(seed)
+    ns = rng.integers(8, 257, size=count)
+    rs = rng.integers(1, 5, size=count)
+    mats = [rng.standard_normal((n, n)) + (0.5 * n * np.eye(n) if i % 2 == 0 else 0)
+            for i, n in enumerate(ns)]
+    rhss = [rng.standard_normal((n, r)) for n, r in zip(ns, rs)]
+    return ns, rs, mats, rhss
+
+
+@pytest.mark.parametrize("mode", [0, 1], ids=["fp64", "mixed"])
+def test_batched_every_system_eta_and_fp64_row_order(lagpu, ctx_fast, torch, mode):
+    ns, rs, mats, rhss = _uneven_batch(300, 404 + mode)
+    systems, na, nb = lagpu.batch_systems(ns, rs)
+    a = torch.from_numpy(np.concatenate([m.ravel() for m in mats])).cuda()
+    b = torch.from_numpy(np.concatenate([r.ravel() for r in rhss])).cuda()
+    x = torch.zeros(nb, dtype=torch.float64, device="cuda")
+    eta = torch.zeros(len(ns), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    plan = lagpu.BatchPlan(ctx_fast, a.data_ptr(), b.data_ptr(), x.data_ptr(), systems, mode,
+                           ctas_per_sm=2, warps_per_system=4 if mode == 0 else 8, tol=5e-15)
+    plan.run()
+    _, _, fb = plan.stats()
+    pivs = plan.pivots(ns)
+    plan.free()
+    worst = lagpu.batch_backward_error_device(ctx_fast, a.data_ptr(), b.data_ptr(), x.data_ptr(),
+                                              systems, eta.data_ptr())
+    assert worst <= ETA_MAX
+    etas = eta.cpu().numpy()
+    xs = x.cpu().numpy()
+    for i in range(0, len(ns), 7):  # the device eta against the oracle's on a sample
+        s = systems[i]
+        xi = xs[s.b_offset:s.b_offset + s.n * s.nrhs].reshape(s.n, s.nrhs)
+        want = oracle.backward_error(mats[i], xi, rhss[i])
+        assert abs(etas[i] - want) <= 1e-3 * want + 1e-30
+    for i, m in enumerate(mats):
+        if mode == 0 or fb[i]:  # answered by the FP64 pass: the reference's row order
+            assert np.array_equal(pivs[i], oracle.lu_factor(m).piv), "system %d" % i
+        else:  # a low-precision factorization: a permutation of the rows
+            assert np.array_equal(np.sort(pivs[i]), np.arange(len(m), dtype=np.uint64))
+
+
+def test_batched_fp64_class_goes_straight_to_fp64_pass(lagpu, ctx_fast, torch):
+    ns, rs, mats, rhss = _uneven_batch(64, 77)
+    systems, na, nb = lagpu.batch_systems(ns, rs)
+    a = torch.from_numpy(np.concatenate([m.ravel() for m in mats])).cuda()
+    b = torch.from_numpy(np.concatenate([r.ravel() for r in rhss])).cuda()
+    x = torch.zeros(nb, dtype=torch.float64, device="cuda")
+    cls = torch.tensor([3 if i % 3 == 0 else 2 for i in range(len(ns))], dtype=torch.int32,
+                       device="cuda")
+    torch.cuda.synchronize()
+    plan = lagpu.BatchPlan(ctx_fast, a.data_ptr(), b.data_ptr(), x.data_ptr(), systems, 1,
+                           ctas_per_sm=2, warps_per_system=8, tol=5e-15)
+    plan.select_device(cls.data_ptr())
+    plan.run()
+    its, eta, fb = plan.stats()
+    pivs = plan.pivots(ns)
+    plan.free()
+    xs = x.cpu().numpy()
+    for i, m in enumerate(mats):
+        s = systems[i]
+        xi = xs[s.b_offset:s.b_offset + s.n * s.nrhs].reshape(s.n, s.nrhs)
+        assert oracle.backward_error(m, xi, rhss[i]) <= ETA_MAX
+        if i % 3 == 0:
+            assert fb[i] == 1 and its[i] == 0
+            assert np.array_equal(pivs[i], oracle.lu_factor(m).piv)

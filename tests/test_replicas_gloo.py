@@ -96,7 +96,7 @@ def test_reference_arm_rank0_prints_one_line(monkeypatch, capsys):
     import bench
 
     class Args:
-        n, nrhs, steps, warmup, ref_step_seconds = 96, 1, 1, 3, 0.01
+        n, nrhs, steps, warmup, ref_step_seconds, arith = 96, 1, 1, 3, 0.01, "fast"
 
     bench.run_reference(Args())
     lines = [l for l in capsys.readouterr().out.splitlines() if l.strip()]
@@ -104,3 +104,5 @@ def test_reference_arm_rank0_prints_one_line(monkeypatch, capsys):
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0
+    # the same workload description as the library's own line
+    assert d["config"] == bench.bench_config(Args(), bench.DEFAULT_PANEL_WIDTH, 2)

@@ -35,9 +35,24 @@ def _noalloc(lagpu, torch, a, stream):
 
 def _regular(lagpu, ctx, a):
     lu = lagpu.LUDecomposition.new(a, ctx)
-    out = lu.get_packed().data, lu.get_piv(), lu.pospivsign(), lu.is_singular()
+    try:
+        singular = lu.is_singular()
+    except lagpu.Panic:  # m < n and no zero pivot: the reference indexes past U (lu.rs:174-182)
+        singular = False
+    out = lu.get_packed().data, lu.get_piv(), lu.pospivsign(), singular
     lu.free()
     return out
+
+
+def _check_same(lagpu, torch, ctx, a, stream):
+    lu_na, piv_na, flags = _noalloc(lagpu, torch, a, stream)
+    lu_ref, piv_ref, pos_ref, sing_ref = _regular(lagpu, ctx, a)
+    # Both run the same FAST kernels, in which every element takes the same
+    # fused multiply-adds in the same order, so the results are identical.
+    assert np.array_equal(piv_na, piv_ref)
+    assert np.array_equal(lu_na, lu_ref)
+    assert bool(flags[0]) == pos_ref
+    assert bool(flags[1]) == sing_ref
 
 
 def test_noalloc_matches_regular_entry_point_twice(lagpu):
@@ -46,13 +61,19 @@ def test_noalloc_matches_regular_entry_point_twice(lagpu):
     stream = torch.cuda.Stream()
     rng = np.random.default_rng(2024)
     for n in (700, 513):  # two calls in a row share the static scratch
-        a = rng.standard_normal((n, n))
-        lu_na, piv_na, flags = _noalloc(lagpu, torch, a, stream.cuda_stream)
-        lu_ref, piv_ref, pos_ref, sing_ref = _regular(lagpu, ctx, a)
-        assert np.array_equal(piv_na, piv_ref)
-        assert np.allclose(lu_na, lu_ref, rtol=1e-12, atol=1e-12)
-        assert bool(flags[0]) == pos_ref
-        assert bool(flags[1]) == sing_ref
+        _check_same(lagpu, torch, ctx, rng.standard_normal((n, n)), stream.cuda_stream)
+    ctx.close()
+
+
+@pytest.mark.parametrize("m,n", [(16384, 64), (300, 517), (517, 300), (1, 40), (40, 1)])
+def test_noalloc_shapes_and_row_limit(lagpu, m, n):
+    # The documented row limit (the 64-CTA panel's shared memory is sized for
+    # it), wide matrices (columns right of the last panel) and tall ones.
+    torch = pytest.importorskip("torch")
+    ctx = lagpu.Context(0, lagpu.ARITH_FAST)
+    stream = torch.cuda.Stream()
+    rng = np.random.default_rng(m * 7 + n)
+    _check_same(lagpu, torch, ctx, rng.standard_normal((m, n)), stream.cuda_stream)
     ctx.close()
 
 
