@@ -449,6 +449,23 @@ la_status la_qr_solve(la_qr qr, const double* b, size_t brows, size_t nrhs, doub
  * inverse() is None and unwrap panics. */
 la_status la_matrix_pinverse(la_ctx ctx, const double* a, size_t m, size_t n, double* out);
 
+/* ---- SVD::direct (src/decomp/svd.rs) ---------------------------------------- */
+
+/* SVD::direct (svd.rs:454-497) of A (m x n, row-major host memory):
+ * u (m x m), s (m x n, the singular values on its diagonal, descending) and
+ * v (n x n) with A = U S V' (to rounding). A'A and A V S^-1 run on the GPU
+ * (la_matrix_mul), S^-1 by the GPU LU inverse; the eigendecomposition of A'A
+ * (EigenDecomposition::new, eigen.rs:755-790: tred2 + tql2) runs on the host,
+ * as in the reference. For m > n the last m - n columns of U are zero, as the
+ * reference computes them; for m < n the SVD of A' is taken and U and V swap
+ * (:458-466). LA_OPT_ARITH = LA_ARITH_EXACT gives the reference's bits.
+ * LA_BADSHAPE where the reference panics: m or n = 0, or a zero singular value
+ * (s.inverse().unwrap() on None, :483). LA_UNSUPPORTED where A'A holds a NaN
+ * (the reference's nonsymmetric eigen branch, not built) or the QL iteration
+ * does not converge (non-finite data; the reference's loop would not end). */
+la_status la_svd_direct(la_ctx ctx, const double* a, size_t m, size_t n, double* u, double* s,
+                        double* v);
+
 /* ---- reading matrices (src/util.rs) ----------------------------------------- */
 
 /* util::read_csv (util.rs:9-35) with the f64 parser s.parse::<f64>().unwrap():

@@ -2,12 +2,13 @@
 
 A CPU restatement of the `la` crate's LU path (xasmx/rust-la 0.2.0,
 src/decomp/lu.rs:104-278, src/matrix/mod.rs:957-980 and :1025-1047) and of
-its Cholesky decomposition (src/decomp/cholesky.rs:56-145) and QR
-decomposition (src/decomp/qr.rs:26-238, src/matrix/mod.rs:1049-1057) used by
+its Cholesky decomposition (src/decomp/cholesky.rs:56-145), QR
+decomposition (src/decomp/qr.rs:26-238, src/matrix/mod.rs:1049-1057) and
+SVD::direct (src/decomp/svd.rs:454-497 with eigen.rs:33-247, 755-790) used by
 the tests, the smoke check and the benchmark's CPU-baseline leg as the checker.
 Nothing on the product path may import this package.
 
-`liboracle.so` is built from lu_oracle.c / lu_oracle_mt.c / chol_oracle.c / qr_oracle.c by `make` in this
+`liboracle.so` is built from lu_oracle.c / lu_oracle_mt.c / chol_oracle.c / qr_oracle.c / svd_oracle.c by `make` in this
 directory (the repository's build step runs it). `pyref` holds an independent
 pure-Python restatement used to cross-check the C one on small cases.
 """
@@ -76,6 +77,10 @@ def lib():
         L.oracle_qr_get_q.argtypes = [P, P, S, S, P]
         L.oracle_qr_solve.argtypes = [P, P, S, S, P, S, S, P]
         L.oracle_qr_solve.restype = I
+        L.oracle_eig_sym.argtypes = [P, S, P, P, P]
+        L.oracle_eig_sym.restype = I
+        L.oracle_svd_direct.argtypes = [P, S, S, P, P, P]
+        L.oracle_svd_direct.restype = I
         _LIB = L
     return _LIB
 
@@ -344,3 +349,36 @@ def pinverse(a):
     if inv is None:
         raise ReferencePanic("called `Option::unwrap()` on a `None` value")
     return matmul(inv, np.ascontiguousarray(a.T))
+
+
+UNSUPPORTED, NOT_FINITE = 3, 4
+
+
+def eig_sym(a):
+    """eigen.rs:755-790 symmetric branch (tred2 + tql2): (d, e, v), eigenvalues
+    descending, eigenvectors as the columns of v."""
+    a = _c(a)
+    n = a.shape[0]
+    d = np.empty(n)
+    e = np.empty(n)
+    v = np.empty((n, n))
+    r = lib().oracle_eig_sym(_p(a), n, _p(d), _p(e), _p(v))
+    if r != OK:
+        raise ValueError("oracle_eig_sym status %d" % r)
+    return d, e, v
+
+
+def svd_direct(a):
+    """svd.rs:454-497: (u m x m, s m x n, v n x n). ReferencePanic where the
+    reference's s.inverse().unwrap() panics (a zero singular value)."""
+    a = _c(a)
+    m, n = a.shape
+    u = np.empty((m, m))
+    s = np.empty((m, n))
+    v = np.empty((n, n))
+    r = lib().oracle_svd_direct(_p(a), m, n, _p(u), _p(s), _p(v))
+    if r == PANIC:
+        raise ReferencePanic("SVD::direct: a zero singular value (inverse().unwrap() on None)")
+    if r != OK:
+        raise ValueError("oracle_svd_direct status %d" % r)
+    return u, s, v

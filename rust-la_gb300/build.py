@@ -22,7 +22,9 @@ FLAGS = ARCH + [
 ]
 
 
-CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-pthread",
+# -ffp-contract=off: host arithmetic that restates the reference (SVD::direct's
+# eigendecomposition) must not be fused into FMAs (aarch64 GCC fuses by default).
+CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-pthread", "-ffp-contract=off",
             "-I" + os.path.join(HERE, "..", "include")]
 
 

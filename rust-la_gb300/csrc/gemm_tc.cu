@@ -1,13 +1,23 @@
 // Tensor-core trailing update of the mixed-precision LU:
-//   C (M x N, f32, row-major) -= alpha * A (M x K, 16-bit) * B^T (B: N x K, 16-bit)
-// with A and B both K-major (K contiguous), in BF16 or FP16, accumulated in
-// FP32 by tcgen05.mma into tensor memory.
+//   C (M x N, f32, row-major) -= alpha * A (M x K) * B^T (B: N x K)
+// with A and B both K-major (K contiguous), accumulated in FP32 by
+// tcgen05.mma into tensor memory. Operand formats:
+//   BF16 or FP16 (kind::f16, K = 16 per instruction);
+//   FP8 e4m3 split in two parts (kind::f8f6f4, K = 32 per instruction): each
+//   operand row holds its high parts in columns [0, K) and its low parts in
+//   columns [lo, lo + K) (v * scale ~ hi + lo, both e4m3), and the kernel
+//   accumulates hi*hi + hi*lo + lo*hi. Three 8-bit products give factors about
+//   as accurate as BF16 ones (one e4m3 product alone leaves errors of a few
+//   per cent, too much for refinement at kappa >= 1e2), and each chunk of the
+//   ring is still a 128-byte-wide box of A and one of B: the producer walks
+//   three "virtual" chunks per 128 columns of K, (hi, hi), (hi, lo), (lo, hi).
 //
 // One CTA per 128 x 128 output tile, 128 threads:
-//   warp 0 lane 0 : TMA producer. 64-deep K chunks of A and B (16 KB each,
-//                   128B swizzle) into a 3-stage ring, one mbarrier per stage
-//   warp 1 lane 0 : MMA issuer. 4 x tcgen05.mma (M=128, N=128, K=16) per chunk;
-//                   tcgen05.commit releases the stage
+//   warp 0 lane 0 : TMA producer. 128-byte-deep K chunks of A and B (64 16-bit
+//                   or 128 8-bit elements, 16 KB each, 128B swizzle) into a
+//                   3-stage ring, one mbarrier per stage
+//   warp 1 lane 0 : MMA issuer. 4 x tcgen05.mma (M=128, N=128, 32 bytes of K)
+//                   per chunk; tcgen05.commit releases the stage
 //   all 4 warps   : epilogue. tcgen05.ld of the warp's 32 TMEM lanes (rows),
 //                   -alpha * acc into swizzled shared-memory boxes, added to C
 //                   by TMA tensor reductions (the SMs never load C)
@@ -22,11 +32,12 @@
 
 namespace {
 
-constexpr int TM = 128, TN = 128, TK = 64;
+constexpr int TM = 128, TN = 128;
+constexpr int TKB = 128;  // bytes of K per chunk (one 128-byte swizzle row)
 constexpr int STAGES = 3;
 constexpr int TC_THREADS = 128;
-constexpr uint32_t A_BYTES = TM * TK * 2;  // 16 KB
-constexpr uint32_t B_BYTES = TN * TK * 2;  // 16 KB
+constexpr uint32_t A_BYTES = TM * TKB;  // 16 KB
+constexpr uint32_t B_BYTES = TN * TKB;  // 16 KB
 constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr size_t TC_SMEM = (size_t)STAGES * STAGE_BYTES + 1024;  // + alignment slack
 constexpr uint32_t C_BOX_BYTES = TM * 32 * 4;  // one 128 x 32 FP32 box of the epilogue
@@ -56,17 +67,21 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
   return d;
 }
 
-// Instruction descriptor of kind::f16: D f32, A/B bf16 (1) or f16 (0), both
-// K-major, N = 128, M = 128.
-__host__ __device__ constexpr uint32_t idesc_f16(uint32_t ab_fmt) {
+// Instruction descriptor of kind::f16 and kind::f8f6f4: D f32 (bits 4-5 = 1),
+// A and B formats in bits 7-9 and 10-12 (kind::f16: 0 f16, 1 bf16;
+// kind::f8f6f4: 0 e4m3), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t idesc_mma(uint32_t ab_fmt) {
   return (1u << 4) | (ab_fmt << 7) | (ab_fmt << 10) | ((uint32_t)(TN >> 3) << 17) |
          ((uint32_t)(TM >> 4) << 24);
 }
 
+// F8: e4m3 hi/lo operands (kind::f8f6f4); else 16-bit (kind::f16). K counts
+// elements; lo is the column of the low parts (F8 only).
+template <bool F8>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 tc_update_kernel(const __grid_constant__ CUtensorMap tmap_a,
                  const __grid_constant__ CUtensorMap tmap_b,
-                 const __grid_constant__ CUtensorMap tmap_c, int N, int K,
+                 const __grid_constant__ CUtensorMap tmap_c, int N, int K, int lo,
                  const float* __restrict__ alpha_ptr, uint32_t idesc, int* err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], done;
@@ -77,7 +92,8 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tmap_a,
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
-  const int nk = (K + TK - 1) / TK;
+  constexpr int TKE = F8 ? TKB : TKB / 2;  // elements of K per chunk
+  const int nk = (F8 ? 3 : 1) * ((K + TKE - 1) / TKE);
 
   if (tid == 0) {
     for (int s = 0; s < STAGES; s++) {
@@ -110,8 +126,14 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tmap_a,
       unsigned char* sa = smem + s * STAGE_BYTES;
       unsigned char* sb = sa + A_BYTES;
       mbar_expect_tx(&full[s], STAGE_BYTES);
-      tma_load_2d(sa, &tmap_a, kc * TK, m0, &full[s]);
-      tma_load_2d(sb, &tmap_b, kc * TK, n0, &full[s]);
+      int ax = kc * TKE, bx = ax;
+      if (F8) {  // virtual chunk kc: K columns [c, c + 128) as (hi, hi), (hi, lo), (lo, hi)
+        const int c = (kc / 3) * TKE, t = kc % 3;
+        ax = c + (t == 2 ? lo : 0);
+        bx = c + (t == 1 ? lo : 0);
+      }
+      tma_load_2d(sa, &tmap_a, ax, m0, &full[s]);
+      tma_load_2d(sb, &tmap_b, bx, n0, &full[s]);
       issued = kc + 1;
     }
   } else if (warp == 1 && lane == 0) {
@@ -127,14 +149,20 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tmap_a,
       const uint32_t sa = smem_u32(smem + s * STAGE_BYTES);
       const uint32_t sb = sa + A_BYTES;
 #pragma unroll
-      for (int k = 0; k < TK / 16; k++) {
+      for (int k = 0; k < TKB / 32; k++) {  // 32 bytes of K per instruction
         const uint64_t ad = sdesc(sa + k * 32);
         const uint64_t bd = sdesc(sb + k * 32);
         const uint32_t acc = (kc > 0 || k > 0) ? 1u : 0u;
-        asm volatile(
-            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-            "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+        if (F8)
+          asm volatile(
+              "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+              " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+              "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+        else
+          asm volatile(
+              "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+              " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+              "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
       }
       asm volatile(
           "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -216,32 +244,46 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tmap_a,
                  "r"(TMEM_COLS));
 }
 
-// 2-D K-major operand map: `rows` rows of `k` 16-bit elements, pitch `ld`
-// elements (ld * 2 bytes must be a multiple of 16), box 64 (K) x 128 (rows).
+// 2-D K-major operand map: `rows` rows of `cols` elements, pitch `ld`
+// elements (ld * element size must be a multiple of 16), box of 128 bytes of
+// K x 128 rows. 8-bit operands are mapped as bytes.
 bool encode_operand(la_ctx ctx, CUtensorMap* map, const void* base, int fmt, size_t rows,
-                    size_t k, size_t ld) {
+                    size_t cols, size_t ld) {
+  if (fmt == LA_LOWP_E4M3X3)
+    return la_tma::encode_2d(ctx, map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, base, rows, cols, ld,
+                             (uint32_t)TKB, (uint32_t)TM, CU_TENSOR_MAP_SWIZZLE_128B);
   return la_tma::encode_2d(ctx, map,
                            fmt == LA_LOWP_BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
                                                : CU_TENSOR_MAP_DATA_TYPE_FLOAT16,
-                           2, base, rows, k, ld, (uint32_t)TK, (uint32_t)TM,
+                           2, base, rows, cols, ld, (uint32_t)(TKB / 2), (uint32_t)TM,
                            CU_TENSOR_MAP_SWIZZLE_128B);
 }
 
 }  // namespace
 
 // C (M x N f32, pitch ldc, 16-byte aligned rows) -= alpha * A * B^T where A is
-// M x K and B is N x K, both 16-bit K-major with pitches lda, ldb (multiples of
-// 8 elements, 16-byte aligned bases). alpha is read on the device.
+// M x K and B is N x K, K-major with pitches lda, ldb in elements and
+// 16-byte aligned bases. 16-bit formats: pitches multiples of 8 elements.
+// LA_LOWP_E4M3X3: bytes, the low parts at column lo = lda / 2 = ldb / 2, at or
+// beyond K rounded up to a whole 128-byte chunk (the high parts' last chunk
+// must not reach them); pitches multiples of 32. alpha is read on the device.
 la_status launch_tc_update(la_ctx ctx, cudaStream_t stream, int fmt, int M, int N, int K,
                            const void* A, size_t lda, const void* B, size_t ldb, float* C,
                            size_t ldc, const float* d_alpha) {
   if (M <= 0 || N <= 0 || K <= 0) return LA_OK;
-  if ((lda % 8) || (ldb % 8) || (ldc % 4) || (reinterpret_cast<uintptr_t>(A) % 16) ||
+  const bool f8 = fmt == LA_LOWP_E4M3X3;
+  const size_t pq = f8 ? 32 : 8;  // pitch quantum in elements
+  if ((lda % pq) || (ldb % pq) || (ldc % 4) || (reinterpret_cast<uintptr_t>(A) % 16) ||
       (reinterpret_cast<uintptr_t>(B) % 16) || (reinterpret_cast<uintptr_t>(C) % 16))
     return LA_INVALID;
+  if (f8 && (lda != ldb || (size_t)(K + TKB - 1) / TKB * TKB > lda / 2)) return LA_INVALID;
+  const int lo = f8 ? (int)(lda / 2) : 0;
+  // The maps span the columns the kernel reads: [0, K), or for split FP8
+  // [0, lo + K) (the high parts, padding, the low parts).
+  const size_t cols = f8 ? (size_t)lo + (size_t)K : (size_t)K;
   CUtensorMap ta, tb, tc;
-  if (!encode_operand(ctx, &ta, A, fmt, (size_t)M, (size_t)K, lda)) return LA_CUDA_ERROR;
-  if (!encode_operand(ctx, &tb, B, fmt, (size_t)N, (size_t)K, ldb)) return LA_CUDA_ERROR;
+  if (!encode_operand(ctx, &ta, A, fmt, (size_t)M, cols, lda)) return LA_CUDA_ERROR;
+  if (!encode_operand(ctx, &tb, B, fmt, (size_t)N, cols, ldb)) return LA_CUDA_ERROR;
   // C (M x N FP32, pitch ldc) in 128 x 32 boxes, 128-byte swizzle: the epilogue's
   // reduction target.
   if (!la_tma::encode_2d(ctx, &tc, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, C, (size_t)M, (size_t)N,
@@ -249,14 +291,21 @@ la_status launch_tc_update(la_ctx ctx, cudaStream_t stream, int fmt, int M, int 
     return LA_CUDA_ERROR;
   static la_device_once configured;
   cudaError_t e = configured.run([](int) {
-    return cudaFuncSetAttribute(tc_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)TC_SMEM);
+    cudaError_t r = cudaFuncSetAttribute(tc_update_kernel<false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
+    if (r == cudaSuccess)
+      r = cudaFuncSetAttribute(tc_update_kernel<true>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
+    return r;
   });
   if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaFuncSetAttribute(tc_update)");
   dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM);
-  const uint32_t idesc = idesc_f16(fmt == LA_LOWP_BF16 ? 1u : 0u);
-  tc_update_kernel<<<grid, TC_THREADS, TC_SMEM, stream>>>(ta, tb, tc, N, K, d_alpha, idesc,
-                                                           ctx->d_err);
+  if (f8)
+    tc_update_kernel<true><<<grid, TC_THREADS, TC_SMEM, stream>>>(ta, tb, tc, N, K, lo, d_alpha,
+                                                                  idesc_mma(0u), ctx->d_err);
+  else
+    tc_update_kernel<false><<<grid, TC_THREADS, TC_SMEM, stream>>>(
+        ta, tb, tc, N, K, 0, d_alpha, idesc_mma(fmt == LA_LOWP_BF16 ? 1u : 0u), ctx->d_err);
   ctx->launches++;
   return la_check_launch(ctx, "tc_update_kernel");
 }
@@ -265,7 +314,7 @@ extern "C" la_status la_lowp_update_device(la_ctx ctx, int fmt, size_t m, size_t
                                            const void* d_a16, size_t lda, const void* d_b16,
                                            size_t ldb, float* d_c, size_t ldc, float alpha) {
   if (!ctx || !d_a16 || !d_b16 || !d_c) return LA_INVALID;
-  if (fmt != LA_LOWP_BF16 && fmt != LA_LOWP_FP16) return LA_INVALID;
+  if (fmt != LA_LOWP_BF16 && fmt != LA_LOWP_FP16 && fmt != LA_LOWP_E4M3X3) return LA_INVALID;
   if (m > INT32_MAX || n > INT32_MAX || k > INT32_MAX) return LA_UNSUPPORTED;
   LA_CUDA(ctx, cudaSetDevice(ctx->device));
   float* d_alpha = reinterpret_cast<float*>(ctx->d_small + 4);

@@ -85,7 +85,9 @@ enum DeviceErr : int {
 };
 
 // 16-bit operand formats of the tensor-core update.
-enum LowpFormat : int { LA_LOWP_BF16 = 1, LA_LOWP_FP16 = 2 };
+// LA_LOWP_E4M3X3: FP8 e4m3 operands split in a high and a low part each
+// (v ~ hi + lo), three products hi*hi + hi*lo + lo*hi.
+enum LowpFormat : int { LA_LOWP_BF16 = 1, LA_LOWP_FP16 = 2, LA_LOWP_E4M3X3 = 3 };
 
 struct la_context {
   int device = 0;

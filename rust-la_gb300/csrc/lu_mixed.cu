@@ -9,13 +9,17 @@
 //   triangular update, FP32 SIMT updates);
 //   outer row-panel triangular update U12 = L11^-1 A12 in FP32;
 //   trailing update A22 -= L21 * U12 on the tensor cores (gemm_tc.cu) with
-//   BF16 or FP16 operands and FP32 accumulation, or in FP32 SIMT (LA_PREC_FP32).
-//   FP16 operands use a per-panel power-of-two scale of U12 (L's entries are
-//   bounded by 1 under partial pivoting); the scale is undone in the epilogue.
+//   BF16, FP16 or split FP8 e4m3 operands and FP32 accumulation, or in FP32
+//   SIMT (LA_PREC_FP32). FP16 operands use a per-panel power-of-two scale of
+//   U12 (L's entries are bounded by 1 under partial pivoting); FP8 operands
+//   scale L21 by 2^8 and U12 by a per-panel power of two, and store each value
+//   as a high and a low e4m3 part; the scales are undone in the epilogue.
 // Solve: x0 = 0, r = b; repeat d = LU32 \ (r scaled to unit max per column),
 // x += d (FP64), r = b - A x in FP64 (A kept in FP64), until the normwise
 // backward error max_j ||r_j|| / (||A|| ||x_j|| + ||b_j||) <= tol or the
 // refinement stalls.
+#include <cuda_fp8.h>
+
 #include "la_internal.cuh"
 
 namespace {
@@ -109,6 +113,68 @@ __global__ void pack_ut_kernel(const float* __restrict__ src, size_t lds, uint16
 }
 
 __global__ void set_alpha_one(float* stat) { stat[0] = 0.f; stat[1] = 1.f; }
+
+// Split FP8: v (already scaled) ~ hi + lo with hi = e4m3(v), lo = e4m3(v - hi)
+// (round to nearest, saturating at the largest finite e4m3 value).
+__device__ __forceinline__ void split_e4m3(float v, uint8_t& hi, uint8_t& lo) {
+  const __nv_fp8_e4m3 h(v);
+  const __nv_fp8_e4m3 l(v - static_cast<float>(h));
+  hi = h.__x;
+  lo = l.__x;
+}
+
+constexpr float F8_L_SCALE = 256.f;  // |l| <= 1 -> |l| * 2^8 <= 256 < 448 (e4m3 max)
+
+// L21 (rows x k FP32, pitch lds) * 2^8 -> split e4m3 rows of ldd bytes: high
+// parts in columns [0, k), low parts in [ldd / 2, ldd / 2 + k), zeros elsewhere.
+__global__ void pack_l_f8_kernel(const float* __restrict__ src, size_t lds,
+                                 uint8_t* __restrict__ dst, size_t ldd, int rows, int k) {
+  const size_t half = ldd / 2;
+  size_t total = (size_t)rows * half;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(i / half), c = (int)(i % half);
+    uint8_t hi = 0, lo = 0;
+    if (c < k) split_e4m3(src[(size_t)r * lds + c] * F8_L_SCALE, hi, lo);
+    dst[(size_t)r * ldd + c] = hi;
+    dst[(size_t)r * ldd + half + c] = lo;
+  }
+}
+
+// U12 (k x cols, pitch lds) -> U^T split e4m3 (cols rows of ldd bytes, as
+// pack_l_f8_kernel) times a power of two that takes max |U12| (stat[0]) just
+// below 2^8; stat[1] receives alpha = 1 / (2^8 * scale). 32x32 tiles through
+// shared memory.
+__global__ void pack_ut_f8_kernel(const float* __restrict__ src, size_t lds,
+                                  uint8_t* __restrict__ dst, size_t ldd, int k, int cols,
+                                  float* stat) {
+  __shared__ float t[32][33];
+  float scale = 1.f;
+  const float mx = stat[0];
+  int e = 0;
+  if (mx > 0.f && mx < INFINITY) {
+    frexpf(mx, &e);  // mx = f 2^e, 0.5 <= f < 1
+    scale = ldexpf(1.f, 8 - e);
+  }
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0)
+    stat[1] = 1.f / (F8_L_SCALE * scale);
+  const size_t half = ldd / 2;
+  const int c0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    int kk = k0 + i, cc = c0 + threadIdx.x;
+    t[i][threadIdx.x] = (kk < k && cc < cols) ? src[(size_t)kk * lds + cc] * scale : 0.f;
+  }
+  __syncthreads();
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    int cc = c0 + i, kk = k0 + threadIdx.x;
+    if (cc < cols && kk < (int)half) {
+      uint8_t hi, lo;
+      split_e4m3(t[threadIdx.x][i], hi, lo);
+      dst[(size_t)cc * ldd + kk] = hi;
+      dst[(size_t)cc * ldd + half + kk] = lo;
+    }
+  }
+}
 
 // r = b - A x in FP64 for nrhs <= R: the CTA stages 256-row chunks of X in
 // shared memory and each of its 8 warps handles RPW rows (lanes stride along
@@ -306,7 +372,11 @@ la_status mixed_factor(la_ctx ctx, la_lu h, int prec) {
   unsigned bar_base = 0;
   Buf lh(ctx), uh(ctx), stat(ctx);
   const size_t ldk = pad8(WO);
-  if (prec != LA_PREC_FP32) {
+  const size_t ldk8 = 2 * WO;  // split FP8 rows: high parts, then low parts at WO
+  if (prec == LA_PREC_FP8) {
+    LA_TRY(lh.alloc((size_t)m * ldk8 + 256));
+    LA_TRY(uh.alloc((size_t)n * ldk8 + 256));
+  } else if (prec != LA_PREC_FP32) {
     LA_TRY(lh.alloc((size_t)m * ldk * 2 + 256));
     LA_TRY(uh.alloc((size_t)n * ldk * 2 + 256));
   } else {
@@ -368,9 +438,28 @@ la_status mixed_factor(la_ctx ctx, la_lu h, int prec) {
       return launch_gemm_f32(ctx, GM_FMA_SUB, M, N, jbo, lh.as<float>(), ldk,
                              A + (size_t)j0 * ld + c0, ld, C, ld);
     }
-    const int fmt = prec == LA_PREC_BF16 ? LA_LOWP_BF16 : LA_LOWP_FP16;
     const float* L21 = A + (size_t)j1o * ld + j0;
     const float* U12 = A + (size_t)j0 * ld + c0;
+    if (prec == LA_PREC_FP8) {
+      uint8_t* ub8 = uh.as<uint8_t>() + (size_t)(c0 - j1o) * ldk8;
+      LA_CUDA(ctx, cudaMemsetAsync(d_stat, 0, 2 * sizeof(float), ms));
+      absmax_kernel<<<grid_for(ctx, (size_t)jbo * N), 256, 0, ms>>>(U12, ld, jbo, N, d_stat);
+      ctx->launches++;
+      LA_TRY(la_check_launch(ctx, "absmax_kernel"));
+      if (pack_l) {
+        pack_l_f8_kernel<<<grid_for(ctx, (size_t)M * WO), 256, 0, ms>>>(L21, ld, lh.as<uint8_t>(),
+                                                                        ldk8, M, jbo);
+        ctx->launches++;
+        LA_TRY(la_check_launch(ctx, "pack_l_f8_kernel"));
+      }
+      dim3 pg8((N + 31) / 32, (WO + 31) / 32);
+      pack_ut_f8_kernel<<<pg8, dim3(32, 8), 0, ms>>>(U12, ld, ub8, ldk8, jbo, N, d_stat);
+      ctx->launches++;
+      LA_TRY(la_check_launch(ctx, "pack_ut_f8_kernel"));
+      return launch_tc_update(ctx, ms, LA_LOWP_E4M3X3, M, N, jbo, lh.p, ldk8, ub8, ldk8, C, ld,
+                              d_stat + 1);
+    }
+    const int fmt = prec == LA_PREC_BF16 ? LA_LOWP_BF16 : LA_LOWP_FP16;
     uint16_t* ub = uh.as<uint16_t>() + (size_t)(c0 - j1o) * ldk;
     if (fmt == LA_LOWP_FP16) {
       LA_CUDA(ctx, cudaMemsetAsync(d_stat, 0, 2 * sizeof(float), ms));
@@ -448,7 +537,9 @@ la_status la_lu_mixed_new_device(la_ctx ctx, const double* d_a, size_t lda, size
   if (!ctx || !d_a || !out || lda < n) return LA_INVALID;
   if (n == 0) return LA_BADSHAPE;
   if (n > (size_t)INT32_MAX / 4) return LA_UNSUPPORTED;
-  if (prec != LA_PREC_BF16 && prec != LA_PREC_FP16 && prec != LA_PREC_FP32) return LA_INVALID;
+  if (prec != LA_PREC_BF16 && prec != LA_PREC_FP16 && prec != LA_PREC_FP32 &&
+      prec != LA_PREC_FP8)
+    return LA_INVALID;
   LA_CUDA(ctx, cudaSetDevice(ctx->device));
   *out = nullptr;
   la_lu h = new (std::nothrow) la_lu_handle();

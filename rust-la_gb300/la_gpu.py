@@ -9,6 +9,7 @@ The names, argument meaning and failure behaviour follow the reference crate
   a.det(), a.solve(b), a.inverse()    mod.rs:1025-1037
   a.is_singular(), a.is_non_singular() mod.rs:1039-1047
   LUDecomposition.new(a)              src/decomp/lu.rs:104-168
+  SVD.direct(a)                       src/decomp/svd.rs:454-497
   lu.solve(b) / det / is_singular / is_non_singular / get_l / get_u / get_p / get_piv
                                       lu.rs:170-278
 
@@ -93,6 +94,7 @@ SIGNATURES = {
     "la_qr_get_q": ([_P, _P], _I),
     "la_qr_solve": ([_P, _P, _S, _S, _P], _I),
     "la_matrix_pinverse": ([_P, _P, _S, _S, _P], _I),
+    "la_svd_direct": ([_P, _P, _S, _S, _P, _P, _P], _I),
     "la_read_csv_f64": ([ctypes.c_char_p, _P, _P, _P], _I),
     "la_host_free": ([_P], None),
     "la_chol_new": ([_P, _P, _S, _S, _P], _I),
@@ -584,6 +586,36 @@ class CholeskyDecomposition:
     def solve_device(self, b_ptr, ldb, brows, nrhs, x_ptr, ldx):
         _check(self.ctx, lib().la_chol_solve_device(self.h, ctypes.c_void_p(b_ptr), ldb, brows,
                                                      nrhs, ctypes.c_void_p(x_ptr), ldx))
+
+
+class SVD:
+    """Mirror of SVD<f64>'s direct method (src/decomp/svd.rs:454-497, get_u / get_s /
+    get_v at :427-437): U (m x m), S (m x n), V (n x n) with A = U S V'."""
+
+    def __init__(self, u, s, v):
+        self.u, self.s, self.v = u, s, v
+
+    @staticmethod
+    def direct(a, ctx=None):
+        """svd.rs:454-497. Panic where the reference panics (a zero singular value)."""
+        if not isinstance(a, Matrix):
+            a = Matrix(a, ctx)
+        ctx = ctx or a._c()
+        m, n = a.rows(), a.cols()
+        u = np.empty((m, m))
+        s = np.empty((m, n))
+        v = np.empty((n, n))
+        _check(ctx, lib().la_svd_direct(ctx.h, _ptr(a.data), m, n, _ptr(u), _ptr(s), _ptr(v)))
+        return SVD(Matrix(u, ctx), Matrix(s, ctx), Matrix(v, ctx))
+
+    def get_u(self):
+        return self.u
+
+    def get_s(self):
+        return self.s
+
+    def get_v(self):
+        return self.v
 
 
 def read_csv(path):
