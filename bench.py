@@ -22,7 +22,8 @@ count 2/3 n^3 + 2 n^2 nrhs (factor + solve).
 
 Further sections of the same JSON line (skipped with --no-mixed,
 --no-batched, --no-selector):
-  mixed_ir : mixed-precision LU (tcgen05 BF16/FP16 or FP32 trailing updates)
+  mixed_ir : mixed-precision LU (tcgen05 BF16, FP16 or split-FP8 trailing
+          updates, or FP32 SIMT ones)
           + FP64 refinement at n=16384, kappa in {1e2, 1e6, 1e10}, 4 RHS,
           against the plain FP64 LU at the same size; the headline speed-up is
           the automatic path (la_lu_solve_auto_device), each fixed precision
@@ -390,7 +391,7 @@ def householder_conditioned(torch, n, kappa, seed):
     return a.contiguous()
 
 
-def run_mixed(la_gpu, torch, ctx, n, nrhs=4, kappas=(1e2, 1e6, 1e10), precs=(1, 2, 3), reps=5):
+def run_mixed(la_gpu, torch, ctx, n, nrhs=4, kappas=(1e2, 1e6, 1e10), precs=(1, 2, 3, 4), reps=5):
     """Mixed-precision LU + FP64 refinement against the plain FP64 LU at size n.
     Every time is the median of `reps` runs (CUDA events on the library's
     stream, after one untimed run) of factor + refined solve."""

@@ -101,7 +101,19 @@ typedef enum la_option {
    * the next k refinement calls (la_lu_solve_refined_device and each stage of
    * la_lu_solve_auto_device) report a stall before their first correction. */
   LA_OPT_INJECT_ALLOC_FAIL = 10,
-  LA_OPT_INJECT_IR_STALL = 11
+  LA_OPT_INJECT_IR_STALL = 11,
+  /* Limit, in microseconds, of the grid-barrier wait of the cooperative panel
+   * kernel (1 to 10,000,000; 0 = the default of 2 s). A CTA whose wait runs
+   * out records the failure and returns, every other CTA sees it and returns,
+   * the kernels queued behind the panel that would use its row interchanges
+   * return at entry, and the call reports LA_TIMEOUT; the context stays
+   * usable. */
+  LA_OPT_WAIT_LIMIT_US = 12,
+  /* Failure injection for tests (0 = off; reads back what is left): the k-th
+   * launch of the cooperative panel kernel from now makes its CTAs wait for
+   * one arrival more than there are CTAs, so that the wait runs out (after
+   * LA_OPT_WAIT_LIMIT_US) exactly as when a CTA cannot reach the barrier. */
+  LA_OPT_INJECT_PANEL_STALL = 13
 } la_option;
 
 #define LA_ARITH_FAST 0

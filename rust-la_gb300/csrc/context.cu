@@ -255,6 +255,14 @@ la_status la_ctx_set_option(la_ctx ctx, int option, int64_t value) {
       if (value < 0 || value > (1 << 20)) return LA_INVALID;
       ctx->inject_ir_stall = (int)value;
       return LA_OK;
+    case LA_OPT_WAIT_LIMIT_US:
+      if (value < 0 || value > 10000000) return LA_INVALID;
+      ctx->wait_limit_us = value;
+      return LA_OK;
+    case LA_OPT_INJECT_PANEL_STALL:
+      if (value < 0 || value > (1 << 20)) return LA_INVALID;
+      ctx->inject_panel_stall = (int)value;
+      return LA_OK;
   }
   return LA_INVALID;
 }
@@ -272,6 +280,8 @@ la_status la_ctx_get_option(la_ctx ctx, int option, int64_t* value) {
     case LA_OPT_SOLVE_WAVE: *value = ctx->solve_wave; return LA_OK;
     case LA_OPT_INJECT_ALLOC_FAIL: *value = ctx->inject_alloc_at; return LA_OK;
     case LA_OPT_INJECT_IR_STALL: *value = ctx->inject_ir_stall; return LA_OK;
+    case LA_OPT_WAIT_LIMIT_US: *value = ctx->wait_limit_us; return LA_OK;
+    case LA_OPT_INJECT_PANEL_STALL: *value = ctx->inject_panel_stall; return LA_OK;
   }
   return LA_INVALID;
 }

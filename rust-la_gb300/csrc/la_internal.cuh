@@ -101,6 +101,8 @@ struct la_context {
   int solve_wave = 2;                    // CTAs per SM of the wavefront solve (0: block steps)
   int inject_alloc_at = 0;               // the n-th device allocation from now fails (0: none)
   int inject_ir_stall = 0;               // this many refinement calls report a stall at once
+  int inject_panel_stall = 0;            // the n-th FP64 panel launch from now waits for a CTA too many
+  long long wait_limit_us = 0;           // limit of the panel's grid-barrier wait (0: 2 s)
   int sm_count = 0;
   size_t smem_optin = 0;
   int arith = LA_ARITH_FAST;

@@ -8,11 +8,23 @@ namespace {
 // [c_begin, c_end) of one matrix. All sources are read into shared memory
 // before any destination is written, so the moves act as one permutation.
 constexpr int SW_COLS = 32;
+
+// The context's error word (nonzero after a device wait gave up). The kernels
+// that apply a panel's row interchanges return at entry when it is set: a
+// panel that gave up left no valid interchanges behind.
+__device__ __forceinline__ bool aborted(const int* err) {
+  return err != nullptr && *reinterpret_cast<const volatile int*>(err) != 0;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256)
 laswp_kernel(T* M0, T* M1, T* M2, size_t ld, int b0, int e0, int b1, int e1,
-             int b2, int e2, const int* __restrict__ swaps) {
+             int b2, int e2, const int* __restrict__ swaps, const int* err) {
   __shared__ T tmp[2 * MAX_PANEL_W][SW_COLS];
+  __shared__ int s_abort;
+  if (threadIdx.x == 0) s_abort = aborted(err);
+  __syncthreads();
+  if (s_abort) return;
   const int cnt = swaps[0];
   if (cnt == 0) return;
   const int* dst = swaps + 1;
@@ -41,9 +53,9 @@ laswp_kernel(T* M0, T* M1, T* M2, size_t ld, int b0, int e0, int b1, int e1,
 // panel; this form serves columns whose swaps were deferred).
 template <typename T>
 __global__ void laswp_seq_kernel(T* A, size_t ld, const int* __restrict__ ipiv, int k0, int k1,
-                                 int c0, int c1) {
+                                 int c0, int c1, const int* err) {
   const int c = c0 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= c1) return;
+  if (c >= c1 || aborted(err)) return;  // no barrier in this kernel
   for (int k = k0; k < k1; k++) {
     const int p = ipiv[k];
     if (p != k) {
@@ -150,9 +162,13 @@ trsm_rowpanel_reg_kernel(float* A, size_t ld, int j0, int jb, int c_begin, int c
 // U's diagonal is scanned for an exact zero (lu.rs:177).
 template <typename T>
 __global__ void lu_finish_kernel(const int* __restrict__ ipiv, uint64_t* piv, int m, int kmin,
-                                 const T* LU, size_t ld, int* flags, int smem_rows) {
+                                 const T* LU, size_t ld, int* flags, int smem_rows,
+                                 const int* err) {
   extern __shared__ int sperm[];  // permutation in shared memory when m fits
-  __shared__ int zero;
+  __shared__ int zero, s_abort;
+  if (threadIdx.x == 0) s_abort = aborted(err);
+  __syncthreads();
+  if (s_abort) return;  // the host reports the error; flags and piv are not used
   if (threadIdx.x == 0) zero = 0;
   const bool in_smem = m <= smem_rows;
   if (in_smem) {
@@ -290,7 +306,7 @@ la_status launch_laswp_t(la_ctx ctx, cudaStream_t stream, bool exact, T* A, T* S
   if (gx == 0) return LA_OK;
   dim3 grid(gx, exact ? 3 : 2);
   laswp_kernel<T><<<grid, 256, 0, stream>>>(A, A, exact ? S : nullptr, ld, 0, j0, j1, n, j1, n,
-                                            ctx->d_swaps);
+                                            ctx->d_swaps, ctx->d_err);
   ctx->launches++;
   return la_check_launch(ctx, "laswp_kernel");
 }
@@ -306,7 +322,7 @@ la_status launch_laswp_seq_f32(la_ctx ctx, float* A, size_t ld, const int* ipiv,
                                int c0, int c1) {
   if (k1 <= k0 || c1 <= c0) return LA_OK;
   laswp_seq_kernel<float><<<(c1 - c0 + 255) / 256, 256, 0, ctx->stream>>>(A, ld, ipiv, k0, k1, c0,
-                                                                          c1);
+                                                                          c1, ctx->d_err);
   ctx->launches++;
   return la_check_launch(ctx, "laswp_seq_kernel");
 }
@@ -359,10 +375,12 @@ la_status launch_lu_finish(la_ctx ctx, la_lu h, int* d_flags) {
   const size_t smem = (size_t)std::min((int)h->m, smem_rows) * sizeof(int);
   if (h->d_lu32)
     lu_finish_kernel<float><<<1, 1024, smem, ctx->stream>>>(h->d_ipiv, h->d_piv, (int)h->m, kmin,
-                                                            h->d_lu32, h->ld32, d_flags, smem_rows);
+                                                            h->d_lu32, h->ld32, d_flags, smem_rows,
+                                                            ctx->d_err);
   else
     lu_finish_kernel<double><<<1, 1024, smem, ctx->stream>>>(h->d_ipiv, h->d_piv, (int)h->m, kmin,
-                                                             h->d_lu, h->ld, d_flags, smem_rows);
+                                                             h->d_lu, h->ld, d_flags, smem_rows,
+                                                             ctx->d_err);
   ctx->launches++;
   return la_check_launch(ctx, "lu_finish_kernel");
 }

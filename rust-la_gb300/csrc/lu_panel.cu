@@ -23,15 +23,18 @@
 // v = a - s only when the column is reached (lu.rs:128); finished entries
 // carry s = 0 so v = a - 0 = a for them. FAST updates v in place with FMA.
 //
-// Every wait is bounded: a CTA that waits past the limit (or sees another CTA
-// give up) records DERR_PANEL_TIMEOUT and returns; the host reports LA_TIMEOUT.
+// Every wait is bounded: a CTA that waits past the limit (2 s, or the
+// context's LA_OPT_WAIT_LIMIT_US) or sees another CTA give up records
+// DERR_PANEL_TIMEOUT and returns; the host reports LA_TIMEOUT. A panel launched
+// after an error has been recorded returns at once, and so do the kernels that
+// would apply its row interchanges (lu_aux.cu).
 #include "la_internal.cuh"
 #include "swap_compose.cuh"
 
 namespace {
 
 constexpr int PT = 256;  // threads per panel CTA
-constexpr unsigned long long WAIT_LIMIT_NS = 2000000000ull;  // 2 s
+constexpr unsigned long long WAIT_LIMIT_NS = 2000000000ull;  // 2 s (default)
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
   unsigned v;
@@ -53,7 +56,8 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
 // cooperative-groups grid sync: CTA barrier, one thread fences, arrives with a
 // release add and polls with acquire loads). Returns false when the wait gave up
 // (this CTA timed out or another CTA reported an error).
-__device__ bool grid_barrier(unsigned* counter, unsigned target, int* err) {
+__device__ bool grid_barrier(unsigned* counter, unsigned target, int* err,
+                             unsigned long long wait_ns) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -67,7 +71,7 @@ __device__ bool grid_barrier(unsigned* counter, unsigned target, int* err) {
         if (ld_volatile_i32(err) != 0) { good = 0; break; }
         unsigned long long now = globaltimer_ns();
         if (t0 == 0) t0 = now;
-        else if (now - t0 > WAIT_LIMIT_NS) {
+        else if (now - t0 > wait_ns) {
           atomicCAS(err, 0, (int)DERR_PANEL_TIMEOUT);
           good = 0;
           break;
@@ -111,6 +115,8 @@ struct PanelParams {
   int* ipiv;
   unsigned* bar;
   unsigned bar_base;  // counter value at kernel start (the counter only grows)
+  unsigned stall;     // arrivals added to every barrier target (failure injection; 0)
+  unsigned long long wait_ns;  // limit of each barrier wait
   int* err;
   unsigned long long* cand_key;
   int* cand_pos;
@@ -142,9 +148,15 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
   __shared__ T s_scale;
   __shared__ int s_pivs[W];
   __shared__ int s_atp[SWAP_SLOTS], s_atr[SWAP_SLOTS];
+  __shared__ int s_abort;
 
   const int g = blockIdx.x;
   const int tid = threadIdx.x;
+  // An error recorded earlier in this factorization (a wait that gave up):
+  // the panel's inputs are not valid, return before touching anything.
+  if (tid == 0) s_abort = ld_volatile_i32(p.err);
+  __syncthreads();
+  if (s_abort) return;
   const int lane = tid & 31, warp = tid >> 5;
   const int jb = p.jb;
   const int row0 = p.j0 + g * rpc;                  // position of local row 0
@@ -215,7 +227,8 @@ __global__ void __launch_bounds__(PT) panel_kernel(PanelParams p) {
         if (EXACT) p.diag_s[par * W + t] = (double)vs[r * W + t];
       }
     }
-    if (!grid_barrier(p.bar, p.bar_base + (unsigned)(p.G * (c + 1)), p.err)) return;
+    if (!grid_barrier(p.bar, p.bar_base + (unsigned)(p.G * (c + 1)) + p.stall, p.err, p.wait_ns))
+      return;
 
     // 3. global winner (identical in every CTA): one candidate per thread; the
     //    last W threads fetch row j at the same time (needed if it moves here).
@@ -359,6 +372,10 @@ la_status launch_panel_t(la_ctx ctx, cudaStream_t stream, bool exact, T* A, T* S
   p.ipiv = d_ipiv;
   p.bar = ctx->d_bar;
   p.bar_base = *bar_base;
+  p.stall = 0;
+  if (ctx->inject_panel_stall > 0 && --ctx->inject_panel_stall == 0) p.stall = 1;
+  p.wait_ns = ctx->wait_limit_us > 0 ? (unsigned long long)ctx->wait_limit_us * 1000ull
+                                     : WAIT_LIMIT_NS;
   p.err = ctx->d_err;
   p.cand_key = reinterpret_cast<unsigned long long*>(ctx->d_cand_abs);
   p.cand_pos = ctx->d_cand_pos;

@@ -30,6 +30,7 @@ OPT_ARITH, OPT_PANEL_WIDTH, OPT_PANEL_CTAS, OPT_PROFILE, OPT_LOOKAHEAD, OPT_CLUS
 OPT_BATCH_GMRES = 7
 OPT_SOLVE_WAVE = 8
 OPT_INJECT_ALLOC_FAIL, OPT_INJECT_IR_STALL = 10, 11
+OPT_WAIT_LIMIT_US, OPT_INJECT_PANEL_STALL = 12, 13
 ARITH_FAST, ARITH_EXACT = 0, 1
 
 

@@ -1,7 +1,10 @@
 """Failure detection without a GPU fault: failures injected on the host
-(LA_OPT_INJECT_ALLOC_FAIL, LA_OPT_INJECT_IR_STALL) and the statuses the C ABI
-returns for them. Every call that fails must leave the context usable: the
-next call on it gives the same answer as before the failure.
+(LA_OPT_INJECT_ALLOC_FAIL, LA_OPT_INJECT_IR_STALL), a bounded device wait made
+to run out (LA_OPT_INJECT_PANEL_STALL with a short LA_OPT_WAIT_LIMIT_US: the
+panel's grid barrier waits for one arrival more than it has CTAs), and the
+statuses the C ABI returns for them. Every call that fails must leave the
+context usable: the next call on it gives the same answer as before the
+failure.
 
 The injected calls run in a child process, so that an unexpected crash in an
 error path fails this test alone and not the rest of the GPU suite."""
@@ -91,6 +94,29 @@ out["auto_status"] = st
 out["auto_fell_back"] = stats.fell_back
 out["auto_eta"] = la_gpu.backward_error_device(ctx, ta.data_ptr(), m, tx.data_ptr(), 2,
                                                tb.data_ptr(), 2, m, 2)
+
+# A bounded device wait that runs out: the k-th cooperative panel launch of
+# the FP64 LU waits for a CTA too many; after 50 ms every CTA gives up and
+# returns, the kernels that would apply its interchanges return at entry, and
+# the call reports LA_TIMEOUT. The next factorization on the context is normal.
+big = np.random.default_rng(77).standard_normal((1024, 1024))
+bb = np.random.default_rng(78).standard_normal((1024, 2))
+lu0 = la_gpu.LUDecomposition.new(big, ctx)
+out["panel_piv0"] = [int(v) for v in lu0.get_piv()]
+xb0 = lu0.solve(la_gpu.Matrix(bb, ctx)).data
+lu0.free()
+ctx.set_option(la_gpu.OPT_WAIT_LIMIT_US, 50000)
+out["wait_limit"] = ctx.get_option(la_gpu.OPT_WAIT_LIMIT_US)
+for k in (1, 3):
+    ctx.set_option(la_gpu.OPT_INJECT_PANEL_STALL, k)
+    out["panel_stall_%d" % k] = status(lambda: la_gpu.LUDecomposition.new(big, ctx))
+    out["panel_stall_%d_msg" % k] = "gave up" in ctx.last_error()
+    out["panel_stall_%d_left" % k] = ctx.get_option(la_gpu.OPT_INJECT_PANEL_STALL)
+    lu1 = la_gpu.LUDecomposition.new(big, ctx)
+    out["panel_after_%d_piv" % k] = [int(v) for v in lu1.get_piv()]
+    out["panel_after_%d_x" % k] = bool(np.array_equal(lu1.solve(la_gpu.Matrix(bb, ctx)).data, xb0))
+    lu1.free()
+ctx.set_option(la_gpu.OPT_WAIT_LIMIT_US, 0)
 ctx.close()
 print(json.dumps(out))
 """
@@ -120,12 +146,26 @@ def test_injected_failures_return_statuses_and_leave_the_context_usable(lagpu):
     assert out["auto_status"] == la_gpu.OK
     assert out["auto_fell_back"] == 1
     assert out["auto_eta"] <= 1e-14
+    # the wait that ran out, and the same answer afterwards
+    import numpy as np
+    import oracle
+    big = np.random.default_rng(77).standard_normal((1024, 1024))
+    ref = [int(v) for v in oracle.lu_factor(big, threads=4).piv]
+    assert out["panel_piv0"] == ref
+    assert out["wait_limit"] == 50000
+    for k in (1, 3):
+        assert out["panel_stall_%d" % k] == la_gpu.TIMEOUT
+        assert out["panel_stall_%d_msg" % k]
+        assert out["panel_stall_%d_left" % k] == 0
+        assert out["panel_after_%d_piv" % k] == ref
+        assert out["panel_after_%d_x" % k]
 
 
 def test_injection_options_range(lagpu):
     ctx = lagpu.Context()
     try:
-        for opt in (lagpu.OPT_INJECT_ALLOC_FAIL, lagpu.OPT_INJECT_IR_STALL):
+        for opt in (lagpu.OPT_INJECT_ALLOC_FAIL, lagpu.OPT_INJECT_IR_STALL,
+                    lagpu.OPT_INJECT_PANEL_STALL, lagpu.OPT_WAIT_LIMIT_US):
             assert ctx.get_option(opt) == 0
             with pytest.raises(lagpu.LaError):
                 ctx.set_option(opt, -1)
