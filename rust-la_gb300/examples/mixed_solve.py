@@ -2,7 +2,8 @@
 
     python rust-la_gb300/examples/mixed_solve.py [n] [precision]
 
-precision: 1 = BF16, 2 = FP16 (default), 3 = FP32 trailing updates. A is
+precision: 1 = BF16, 2 = FP16 (default), 3 = FP32, 4 = split FP8 (e4m3 high and
+low parts) trailing updates. A is
 N(0,1) + 2 sqrt(n) I (seed 3), four right-hand sides; prints the factor and
 refinement times and the final backward error.
 """
