@@ -498,12 +498,32 @@ def all_eta(la_gpu, ctx, torch, systems, da, db, dx):
     return worst
 
 
-def run_batched(la_gpu, torch, ctx, count=20000, seed=4, reps=5):
+def shard(la_gpu, systems, world, rank, da, db, dx):
+    """This rank's cost-balanced slice of a batch (la_batch_partition): its
+    systems rebased to the slice and views of the device buffers."""
+    bounds = la_gpu.batch_partition(systems, world)
+    sl, a0, alen, b0, blen = la_gpu.batch_slice(systems, bounds[rank], bounds[rank + 1])
+    return sl, da[a0:a0 + alen], db[b0:b0 + blen], dx[b0:b0 + blen], bounds
+
+
+def sum_over_ranks(dist, value, device="cuda"):
+    """The sum of one number per rank, on every rank (the value itself alone)."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return t.item()
+
+
+def run_batched(la_gpu, torch, ctx, count=20000, seed=4, reps=5, dist=None, world=1, rank=0):
     """Uneven batch: count systems, n uniform in [8, 256], 1-4 RHS, A iid N(0,1)
     plus 0.5 n I on even-indexed systems, B iid N(0,1) (generated on the device,
     seeded). Each arm runs its autotuned plan shape (CTAs per SM x warps per
     system) from a captured CUDA graph; solves/s = count / batch time (median of
-    `reps` graph launches, CUDA events)."""
+    `reps` graph launches, CUDA events). With several GPUs every rank takes a
+    cost-balanced contiguous slice of the same batch (no collective in the
+    plans) and the batch time is the slowest rank's."""
     rng = np.random.default_rng(seed)
     ns = rng.integers(8, 257, size=count)
     rs = rng.integers(1, 5, size=count)
@@ -518,57 +538,87 @@ def run_batched(la_gpu, torch, ctx, count=20000, seed=4, reps=5):
     shift = np.concatenate([np.full(s.n, 0.5 * s.n) for i, s in enumerate(systems) if i % 2 == 0])
     da[torch.from_numpy(idx).cuda()] += torch.from_numpy(shift).cuda()
     torch.cuda.synchronize()
+    mine, va, vb, vx, bounds = shard(la_gpu, systems, world, rank, da, db, dx)
     out = {"workload": "uneven batch: %d systems, n uniform in [8, 256], 1-4 RHS, A iid N(0,1) "
                        "+ 0.5 n I on even systems" % count, "count": count,
-           "timing": "median of %d graph launches, CUDA events" % reps}
+           "timing": "median of %d graph launches, CUDA events" % reps,
+           "ranks": world, "scaling": "strong" if world > 1 else None,
+           "systems_per_rank": [bounds[r + 1] - bounds[r] for r in range(world)]}
     for mode, name in ((la_gpu.BATCH_FP64, "plain_fp64"), (la_gpu.BATCH_MIXED, "mixed_ir")):
-        c, w, _ = la_gpu.batch_autotune(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems,
-                                        mode, tol=BATCH_TOL)
-        plan = la_gpu.BatchPlan(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems, mode,
-                                ctas_per_sm=c, warps_per_system=w, tol=BATCH_TOL)
-        ms, times = event_ms(torch, plan.run, reps=reps)
-        its, eta, fb = plan.stats()
-        out[name] = {"ms": ms, "ms_min_max": [min(times), max(times)],
-                     "solves_per_s": count / (ms * 1e-3), "ctas_per_sm": c,
-                     "warps_per_system": w, "fell_back": int(fb.sum()),
-                     "max_eta_all": all_eta(la_gpu, ctx, torch, systems, da, db, dx)}
-        plan.free()
+        ms, c, w, fell, worst = 0.0, 0, 0, 0, 0.0
+        if len(mine) > 0:
+            c, w, _ = la_gpu.batch_autotune(ctx, va.data_ptr(), vb.data_ptr(), vx.data_ptr(), mine,
+                                            mode, tol=BATCH_TOL)
+            plan = la_gpu.BatchPlan(ctx, va.data_ptr(), vb.data_ptr(), vx.data_ptr(), mine, mode,
+                                    ctas_per_sm=c, warps_per_system=w, tol=BATCH_TOL)
+            if dist:
+                dist.barrier()
+            ms, times = event_ms(torch, plan.run, reps=reps)
+            its, eta, fb = plan.stats()
+            fell = int(fb.sum())
+            worst = all_eta(la_gpu, ctx, torch, mine, va, vb, vx)
+            plan.free()
+        elif dist:
+            dist.barrier()
+        ms = max_over_ranks(dist, ms)
+        out[name] = {"ms": ms, "solves_per_s": count / (ms * 1e-3), "ctas_per_sm": c,
+                     "warps_per_system": w, "fell_back": int(sum_over_ranks(dist, fell)),
+                     "max_eta_all": max_over_ranks(dist, worst)}
     out["speedup_solves_per_s"] = (out["mixed_ir"]["solves_per_s"] /
                                    out["plain_fp64"]["solves_per_s"])
-    del da, db, dx
+    del da, db, dx, va, vb, vx
     torch.cuda.empty_cache()
     return out
 
 
-def run_selector(la_gpu, torch, ctx, count=50000, seed=7, reps=5):
+def run_selector(la_gpu, torch, ctx, count=50000, seed=7, reps=5, dist=None, world=1, rank=0):
     """Learned precision selector on a held-out Householder-conditioned batch:
     count systems, n uniform in [16, 512], 1-4 RHS, log10 kappa_2 uniform in
     [1, 12] (seed 7; the committed weights were trained on 200,000 systems with
     seeds 1000+). Times, per batch (median of `reps`, CUDA events): the plain
     FP64 plan; the mixed plan with FP32 factors for every system (the method
     without the selector); and the selector path (features + MLP inference +
-    per-system class choice + the same mixed plan), everything on the device."""
+    per-system class choice + the same mixed plan), everything on the device.
+    With several GPUs every rank takes a cost-balanced slice, as for the
+    uneven batch."""
     import selector as S
     weights = os.path.join(ROOT, "rust-la_gb300", "selector_weights.npy")
     systems, da, db, dx, kappa = S.conditioned_batch(ctx, count, seed)
+    mine, va, vb, vx, bounds = shard(la_gpu, systems, world, rank, da, db, dx)
+    cnt = len(mine)
     sel = S.PrecisionSelector.from_file(ctx, weights)
     out = {"workload": "learned selector: %d systems, n uniform in [16, 512], 1-4 RHS, "
                        "A = H1 diag(s) H2, log10 kappa uniform in [1, 12]" % count,
-           "count": count, "timing": "median of %d runs, CUDA events" % reps}
-    c64, w64, _ = la_gpu.batch_autotune(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems,
-                                        la_gpu.BATCH_FP64, tol=BATCH_TOL)
-    p64 = la_gpu.BatchPlan(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems,
-                           la_gpu.BATCH_FP64, ctas_per_sm=c64, warps_per_system=w64, tol=BATCH_TOL)
-    t64, _ = event_ms(torch, p64.run, reps=reps)
+           "count": count, "timing": "median of %d runs, CUDA events" % reps,
+           "ranks": world, "scaling": "strong" if world > 1 else None}
+
+    def timed(fn):
+        if dist:
+            dist.barrier()
+        ms = event_ms(torch, fn, reps=reps)[0] if cnt > 0 else 0.0
+        return max_over_ranks(dist, ms)
+
+    def worst():
+        return max_over_ranks(dist, all_eta(la_gpu, ctx, torch, mine, va, vb, vx) if cnt else 0.0)
+
+    c64 = w64 = 0
+    if cnt:
+        c64, w64, _ = la_gpu.batch_autotune(ctx, va.data_ptr(), vb.data_ptr(), vx.data_ptr(), mine,
+                                            la_gpu.BATCH_FP64, tol=BATCH_TOL)
+        p64 = la_gpu.BatchPlan(ctx, va.data_ptr(), vb.data_ptr(), vx.data_ptr(), mine,
+                               la_gpu.BATCH_FP64, ctas_per_sm=c64, warps_per_system=w64,
+                               tol=BATCH_TOL)
+    t64 = timed(p64.run if cnt else None)
     out["plain_fp64"] = {"ms": t64, "solves_per_s": count / (t64 * 1e-3), "ctas_per_sm": c64,
-                         "warps_per_system": w64,
-                         "max_eta_all": all_eta(la_gpu, ctx, torch, systems, da, db, dx)}
-    p64.free()
-    plan = la_gpu.BatchPlan(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems,
-                            la_gpu.BATCH_MIXED, ctas_per_sm=2, warps_per_system=8, tol=BATCH_TOL)
-    fp32 = torch.full((count,), 2, dtype=torch.int32, device="cuda")
-    cls = torch.empty(count, dtype=torch.int32, device="cuda")
-    fbuf = torch.empty((count, 16), dtype=torch.float32, device="cuda")
+                         "warps_per_system": w64, "max_eta_all": worst()}
+    if cnt:
+        p64.free()
+        plan = la_gpu.BatchPlan(ctx, va.data_ptr(), vb.data_ptr(), vx.data_ptr(), mine,
+                                la_gpu.BATCH_MIXED, ctas_per_sm=2, warps_per_system=8,
+                                tol=BATCH_TOL)
+    fp32 = torch.full((max(cnt, 1),), 2, dtype=torch.int32, device="cuda")
+    cls = torch.empty(max(cnt, 1), dtype=torch.int32, device="cuda")
+    fbuf = torch.empty((max(cnt, 1), 16), dtype=torch.float32, device="cuda")
     torch.cuda.synchronize()
 
     def fixed():
@@ -576,7 +626,7 @@ def run_selector(la_gpu, torch, ctx, count=50000, seed=7, reps=5):
         plan.run()
 
     def choose():
-        la_gpu.batch_features_device(ctx, da.data_ptr(), systems, fbuf.data_ptr())
+        la_gpu.batch_features_device(ctx, va.data_ptr(), mine, fbuf.data_ptr())
         sel.predict(fbuf, out=cls, sync=False)
 
     def selected():
@@ -584,23 +634,25 @@ def run_selector(la_gpu, torch, ctx, count=50000, seed=7, reps=5):
         plan.select_device(cls.data_ptr())
         plan.run()
 
-    t32, _ = event_ms(torch, fixed, reps=reps)
-    its, eta, fb = plan.stats()
+    def fell():
+        return int(sum_over_ranks(dist, int(plan.stats()[2].sum()) if cnt else 0))
+
+    t32 = timed(fixed)
     out["mixed_fp32_factors"] = {"ms": t32, "solves_per_s": count / (t32 * 1e-3),
-                                 "fell_back": int(fb.sum()),
-                                 "max_eta_all": all_eta(la_gpu, ctx, torch, systems, da, db, dx)}
-    tf, _ = event_ms(torch, choose, reps=reps)
-    ts, _ = event_ms(torch, selected, reps=reps)
-    its, eta, fb = plan.stats()
-    counts = np.bincount(cls.cpu().numpy(), minlength=4).tolist()
+                                 "fell_back": fell(), "max_eta_all": worst()}
+    tf = timed(choose)
+    ts = timed(selected)
+    counts = np.bincount(cls[:cnt].cpu().numpy(), minlength=4).astype(np.float64)
+    counts = [int(sum_over_ranks(dist, float(c))) for c in counts]
     out["mixed_selector"] = {"ms": ts, "solves_per_s": count / (ts * 1e-3),
-                             "features_inference_ms": tf, "fell_back": int(fb.sum()),
+                             "features_inference_ms": tf, "fell_back": fell(),
                              "class_counts_fp8_bf16_fp32_fp64": counts,
-                             "max_eta_all": all_eta(la_gpu, ctx, torch, systems, da, db, dx)}
-    plan.free()
+                             "max_eta_all": worst()}
+    if cnt:
+        plan.free()
     out["speedup_selector_vs_plain_fp64"] = t64 / ts
     out["speedup_selector_vs_fp32_factors"] = t32 / ts
-    del da, db, dx
+    del da, db, dx, va, vb, vx
     torch.cuda.empty_cache()
     return out
 
@@ -887,10 +939,12 @@ def run_ours(args):
         mixed = run_mixed(la_gpu, torch, ctx, args.mixed_n)
     batched = None
     if not args.no_batched:
-        batched = run_batched(la_gpu, torch, ctx, args.batched_count)
+        batched = run_batched(la_gpu, torch, ctx, args.batched_count, dist=dist, world=world,
+                              rank=rank)
     selected = None
     if not args.no_selector:
-        selected = run_selector(la_gpu, torch, ctx, args.selector_count)
+        selected = run_selector(la_gpu, torch, ctx, args.selector_count, dist=dist, world=world,
+                                rank=rank)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

@@ -284,6 +284,14 @@ la_status la_batch_plan_run(la_batch_plan plan);
  * Any pointer may be NULL. Synchronizes. */
 la_status la_batch_plan_stats(la_batch_plan plan, int* iterations, double* eta, int* fell_back);
 void la_batch_plan_destroy(la_batch_plan plan);
+/* Splits a batch (caller's order) into `parts` contiguous slices of about
+ * equal cost for `parts` GPUs, one plan per GPU over its slice and no
+ * collective in the plans: the cost of system i is its LU and solve flops,
+ * 2/3 n^3 + 2 n^2 nrhs, and bounds[p] (parts + 1 ints, bounds[0] = 0,
+ * bounds[parts] = count, non-decreasing) is the system where the cumulative
+ * cost comes nearest to p / parts of the total; slice p is systems
+ * [bounds[p], bounds[p + 1]). Host only, no context. */
+la_status la_batch_partition(const la_batch_system* systems, int count, int parts, int* bounds);
 /* Autotuner: times every supported (ctas_per_sm, warps_per_system) pair in
  * {1, 2, 4, 8} x {8, 4, 2} on this batch and returns the fastest; appends
  * "mode count mean_n ctas_per_sm warps_per_system ms" lines for all candidates
@@ -361,8 +369,14 @@ la_status la_mlp_gradients(la_mlp mlp, const float* d_x, const int* d_y, int cou
 la_status la_mlp_train_step(la_mlp mlp, const float* d_x, const int* d_y, int count, float lr,
                             float* loss);
 /* Class probabilities (d_probs [count][3], may be NULL) and argmax classes
- * (d_class, may be NULL); asynchronous on the context's stream. */
+ * (d_class, may be NULL; 3 where the gate below sends the system straight to
+ * the FP64 pass); asynchronous on the context's stream. */
 la_status la_mlp_predict(la_mlp mlp, const float* d_x, int count, float* d_probs, int* d_class);
+/* Gate of la_mlp_predict's classes: a system whose FP32-class probability is
+ * at least p_min and whose raw (unnormalised) feature `feature` is at least
+ * feature_min gets class 3, no mixed attempt (la_batch_plan_select_device sends
+ * it straight to the FP64 pass). feature < 0 turns the gate off (the default). */
+la_status la_mlp_set_gate(la_mlp mlp, float p_min, int feature, float feature_min);
 
 /* ---- allocation-free factorization (no reference counterpart) ------------ */
 

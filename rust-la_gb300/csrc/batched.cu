@@ -1249,6 +1249,31 @@ la_status la_batch_plan_stats(la_batch_plan pl, int* iterations, double* eta, in
   return LA_OK;
 }
 
+la_status la_batch_partition(const la_batch_system* systems, int count, int parts, int* bounds) {
+  if (!systems || !bounds || count < 0 || parts < 1) return LA_INVALID;
+  // cost of system i: its LU and solve flops, 2/3 n^3 + 2 n^2 nrhs
+  std::vector<double> cum((size_t)count + 1, 0.0);
+  for (int i = 0; i < count; i++) {
+    const double n = systems[i].n, r = systems[i].nrhs;
+    if (systems[i].n < 1 || systems[i].nrhs < 1) return LA_BADSHAPE;
+    cum[i + 1] = cum[i] + 2.0 / 3.0 * n * n * n + 2.0 * n * n * r;
+  }
+  const double total = cum[count];
+  bounds[0] = 0;
+  int lo = 0;
+  for (int p = 1; p < parts; p++) {
+    // the boundary whose cumulative cost is nearest to p / parts of the total
+    const double target = total * p / parts;
+    int b = (int)(std::lower_bound(cum.begin() + lo, cum.end(), target) - cum.begin());
+    if (b > lo && b <= count && target - cum[b - 1] < cum[b] - target) b--;
+    b = std::min(std::max(b, lo), count);
+    bounds[p] = b;
+    lo = b;
+  }
+  bounds[parts] = count;
+  return LA_OK;
+}
+
 la_status la_batch_plan_pivots(la_batch_plan pl, uint64_t* piv) {
   if (!pl || !piv) return LA_INVALID;
   la_ctx ctx = pl->ctx;

@@ -1,7 +1,8 @@
 """Trains the precision selector and writes its weights.
 
     python rust-la_gb300/examples/train_selector.py [--train 200000] [--test 50000]
-        [--out rust-la_gb300/selector_weights.npy] [--summary path.json]
+        [--out rust-la_gb300/selector_weights.npy] [--summary path.json] [--gate-only]
+        [--dump path.npz]
 
 Training data: --train Householder-conditioned systems (n uniform in [16, 512],
 1-4 right-hand sides, log10 kappa_2 uniform in [1, 12]) generated on the GPU
@@ -10,7 +11,12 @@ three times, with every system's factors stored in FP8, BF16 and FP32 in turn
 (the FP64 pass redoing whatever refinement cannot finish); the label of a
 system is the class with the fewest SM cycles spent on it, redo included. The
 MLP (16 -> 64 -> 64 -> 3) is then trained on the GPU by the library's own
-forward, backward and Adam kernels.
+forward, backward and Adam kernels. Each chunk also runs the plain FP64 plan,
+whose per-system cycles are the cost of sending a system straight to the FP64
+pass; the gate (FP32-class probability and one feature above thresholds ->
+FP64 directly) is fitted on them and written beside the weights
+(<out>.gate.json). --gate-only keeps the weights in --out and fits the gate
+alone; --dump writes the labelled training arrays.
 
 Evaluation: a separately seeded batch of --test systems. Reports the label
 accuracy, the summed per-system cycles of the selector's choices against
@@ -40,7 +46,8 @@ def labelled_chunk(ctx, count, seed, ctas, warps):
     feats = S.features(ctx, systems, da)
     cyc, conv = S.measure_costs(ctx, systems, da, db, dx, ctas_per_sm=ctas,
                                 warps_per_system=warps)
-    out = (systems, da, db, dx, kappa, feats, cyc, conv)
+    cyc64 = S.fp64_costs(ctx, systems, da, db, dx, ctas_per_sm=ctas, warps_per_system=warps)
+    out = (systems, da, db, dx, kappa, feats, cyc, conv, cyc64)
     return out
 
 
@@ -66,6 +73,8 @@ def main():
     ap.add_argument("--out", default=os.path.join(os.path.dirname(os.path.abspath(__file__)), "..",
                                                   "selector_weights.npy"))
     ap.add_argument("--summary", default=None)
+    ap.add_argument("--gate-only", action="store_true")
+    ap.add_argument("--dump", default=None)
     args = ap.parse_args()
     ctx = la_gpu.Context(0)
     t_start = time.perf_counter()
@@ -77,14 +86,18 @@ def main():
     del probe
     print("plan shape: %d CTAs/SM x %d warps" % (ctas, warps), flush=True)
 
-    feats, labels = [], []
+    feats, labels, cycs, cyc64s, convs, ns = [], [], [], [], [], []
     done, k = 0, 0
     while done < args.train:
         m = min(args.chunk, args.train - done)
-        systems, da, db, dx, kappa, f, cyc, conv = labelled_chunk(ctx, m, TRAIN_SEED0 + k, ctas,
-                                                                  warps)
+        systems, da, db, dx, kappa, f, cyc, conv, cyc64 = labelled_chunk(ctx, m, TRAIN_SEED0 + k,
+                                                                         ctas, warps)
         feats.append(f.cpu())
         labels.append(S.labels_from_costs(cyc))
+        cycs.append(cyc)
+        cyc64s.append(cyc64)
+        convs.append(conv)
+        ns.append(np.array([s.n for s in systems]))
         del systems, da, db, dx
         torch.cuda.empty_cache()
         done += m
@@ -94,29 +107,46 @@ def main():
               flush=True)
     X = torch.cat(feats).cuda()
     y = np.concatenate(labels)
-    sel = S.PrecisionSelector(ctx, seed=1)
-    t0 = time.perf_counter()
-    log = sel.fit(X, y, steps=args.steps, lr=args.lr, batch=4096, log_every=500)
-    t_fit = time.perf_counter() - t0
+    cyc_all, cyc64_all = np.concatenate(cycs), np.concatenate(cyc64s)
+    if args.gate_only:
+        sel = S.PrecisionSelector.from_file(ctx, args.out, gate=False)
+        log, t_fit = [], 0.0
+    else:
+        sel = S.PrecisionSelector(ctx, seed=1)
+        t0 = time.perf_counter()
+        log = sel.fit(X, y, steps=args.steps, lr=args.lr, batch=4096, log_every=500)
+        t_fit = time.perf_counter() - t0
+        sel.save(args.out)
     train_acc = float((sel.predict(X).cpu().numpy() == y).mean())
     print("fit %.1f s, loss %s, train accuracy %.3f" % (t_fit, log, train_acc), flush=True)
-    sel.save(args.out)
+    probs = sel.probs(X).cpu().numpy()
+    fx = X.cpu().numpy()
+    gate = S.fit_gate(probs, fx, cyc_all, cyc64_all)
+    print("gate p_min %.2f feature %d threshold %.4g: cycles x%.3f of the ungated choice"
+          % gate, flush=True)
+    sel.set_gate(gate[0], gate[1], gate[2])
+    sel.save_gate(os.path.splitext(args.out)[0] + ".gate.json")
+    if args.dump:
+        np.savez_compressed(args.dump, feats=fx, labels=y, cycles=cyc_all, cycles64=cyc64_all,
+                            converged=np.concatenate(convs), n=np.concatenate(ns), probs=probs)
     del X
 
     # held-out evaluation
-    systems, da, db, dx, kappa, f, cyc, conv = labelled_chunk(ctx, args.test, TEST_SEED, ctas,
-                                                              warps)
+    systems, da, db, dx, kappa, f, cyc, conv, cyc64 = labelled_chunk(ctx, args.test, TEST_SEED,
+                                                                     ctas, warps)
     lab = S.labels_from_costs(cyc)
-    pred = sel.predict(f).cpu().numpy()
+    pred = sel.predict(f).cpu().numpy()  # with the gate: 3 = straight to the FP64 pass
+    test_acc = float((np.minimum(pred, 2) == lab).mean())
     idx = np.arange(len(lab))
-    c_sel = float(cyc[idx, pred].sum())
-    c_best = float(cyc[idx, lab].sum())
+    cyc4 = np.concatenate([cyc, cyc64[:, None]], axis=1)
+    c_sel = float(cyc4[idx, pred].sum())
+    c_best = float(cyc4.min(axis=1).sum())
     c_f32 = float(cyc[:, 2].sum())
     plan = la_gpu.BatchPlan(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems,
                             la_gpu.BATCH_MIXED, ctas_per_sm=ctas, warps_per_system=warps)
     count = len(systems)
     fp32 = torch.full((count,), 2, dtype=torch.int32, device="cuda")
-    best_cls = torch.from_numpy(lab).cuda()
+    best_cls = torch.from_numpy(np.argmin(cyc4, axis=1).astype(np.int32)).cuda()
     cls = torch.empty(count, dtype=torch.int32, device="cuda")
     fbuf = torch.empty((count, 16), dtype=torch.float32, device="cuda")
     torch.cuda.synchronize()
@@ -153,9 +183,10 @@ def main():
     p64.free()
     summary = {
         "train_systems": args.train, "test_systems": count, "plan": [ctas, warps],
-        "train_accuracy": train_acc, "test_accuracy": float((pred == lab).mean()),
+        "train_accuracy": train_acc, "test_accuracy": test_acc,
         "test_label_counts": np.bincount(lab, minlength=3).tolist(),
-        "test_pred_counts": np.bincount(pred, minlength=3).tolist(),
+        "test_pred_counts": np.bincount(pred, minlength=4).tolist(),
+        "gate": list(gate), "test_all_classes_fail": int((~conv.any(axis=1)).sum()),
         "cycles_selector_over_fp32": c_sel / c_f32, "cycles_best_over_fp32": c_best / c_f32,
         "ms_fixed_fp32": t_fixed, "ms_best_labels": t_best, "ms_features_inference": t_feat,
         "ms_selector_total": t_sel, "ms_fp64_plan": t_64, "fp64_plan": [c64, w64],

@@ -117,6 +117,7 @@ SIGNATURES = {
     "la_batch_plan_cycles": ([_P, _P], _I),
     "la_batch_plan_select_device": ([_P, _P], _I),
     "la_batch_plan_pivots": ([_P, _P], _I),
+    "la_batch_partition": ([_P, _I, _I, _P], _I),
     "la_batch_backward_error_device": ([_P, _P, _P, _P, _P, _I, _P, _P], _I),
     "la_batch_plan_phase_cycles": ([_P, _P], _I),
     "la_batch_features_device": ([_P, _P, _P, _I, _P], _I),
@@ -129,6 +130,7 @@ SIGNATURES = {
     "la_mlp_gradients": ([_P, _P, _P, _I, _P, _P], _I),
     "la_mlp_train_step": ([_P, _P, _P, _I, ctypes.c_float, _P], _I),
     "la_mlp_predict": ([_P, _P, _I, _P, _P], _I),
+    "la_mlp_set_gate": ([_P, ctypes.c_float, _I, ctypes.c_float], _I),
 }
 
 BATCH_FP64, BATCH_MIXED = 0, 1
@@ -716,6 +718,36 @@ def batch_systems(ns, nrhss, precisions=None):
     return arr, ao, bo
 
 
+def batch_partition(systems, parts):
+    """Cost-balanced contiguous slices of a batch for `parts` GPUs
+    (la_batch_partition): bounds[0] = 0 <= ... <= bounds[parts] = count."""
+    bounds = np.empty(parts + 1, dtype=np.int32)
+    st = lib().la_batch_partition(systems, len(systems), parts, _ptr(bounds))
+    _check(None, st)
+    return [int(b) for b in bounds]
+
+
+def batch_slice(systems, lo, hi):
+    """Systems [lo, hi) of a densely packed batch (batch_systems) as their own
+    batch: (systems with offsets rebased to the slice, a_base, a_len, b_base,
+    b_len), so that a GPU holding only A[a_base : a_base + a_len] and
+    B, X[b_base : b_base + b_len] can build its plan over them."""
+    count = hi - lo
+    arr = (BatchSystem * max(count, 0))()
+    if count <= 0:
+        return arr, 0, 0, 0, 0
+    a_base, b_base = systems[lo].a_offset, systems[lo].b_offset
+    last = systems[hi - 1]
+    for i in range(count):
+        s = systems[lo + i]
+        arr[i].a_offset = s.a_offset - a_base
+        arr[i].b_offset = s.b_offset - b_base
+        arr[i].n, arr[i].nrhs, arr[i].precision = s.n, s.nrhs, s.precision
+    a_len = last.a_offset + last.n * last.n - a_base
+    b_len = last.b_offset + last.n * last.nrhs - b_base
+    return arr, a_base, a_len, b_base, b_len
+
+
 def set_precisions(systems, precisions):
     for i, p in enumerate(precisions):
         systems[i].precision = int(p)
@@ -851,6 +883,12 @@ class Mlp:
                                                  ctypes.c_void_p(y_ptr), count, ctypes.c_float(lr),
                                                  ctypes.byref(loss) if want_loss else None))
         return loss.value if want_loss else None
+
+    def set_gate(self, p_min, feature, feature_min):
+        """Class 3 (straight to the FP64 pass) where P(FP32) >= p_min and raw
+        feature `feature` >= feature_min; feature < 0 turns the gate off."""
+        _check(self.ctx, lib().la_mlp_set_gate(self.h, ctypes.c_float(p_min), int(feature),
+                                               ctypes.c_float(feature_min)))
 
     def predict(self, x_ptr, count, probs_ptr=None, class_ptr=None):
         _check(self.ctx, lib().la_mlp_predict(self.h, ctypes.c_void_p(x_ptr), count,

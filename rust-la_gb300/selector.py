@@ -11,9 +11,17 @@ systems: the best class depends on n and on the conditioning.
 (la_batch_features_device) with a 16 -> 64 -> 64 -> 3 MLP trained on the GPU
 (la_mlp_*). Labels come from running the batch once per class and taking, per
 system, the class with the fewest measured SM cycles including the FP64 redo
-(``measure_costs``). Everything runs through the C ABI of liblagpu.so; torch
+(``measure_costs``). A gate on top of the network (``fit_gate``, applied on the
+device by la_mlp_set_gate) sends the systems that the FP32-class probability
+and one feature mark as beyond what refinement of low-precision factors can
+reach straight to the plan's FP64 pass, so that they do not pay for a mixed
+attempt first; it is fitted on the same labelled data, against the cycles of
+the plain FP64 plan. Everything runs through the C ABI of liblagpu.so; torch
 only provides device memory.
 """
+import json
+import os
+
 import numpy as np
 import torch
 
@@ -81,6 +89,45 @@ def measure_costs(ctx, systems, da, db, dx, ctas_per_sm=2, warps_per_system=8, t
     return cyc, conv
 
 
+def fp64_costs(ctx, systems, da, db, dx, ctas_per_sm=2, warps_per_system=8):
+    """SM cycles per system of the plain FP64 plan (the cost of sending a
+    system straight to the FP64 pass)."""
+    plan = la_gpu.BatchPlan(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems,
+                            la_gpu.BATCH_FP64, ctas_per_sm=ctas_per_sm,
+                            warps_per_system=warps_per_system)
+    try:
+        plan.run()
+        return plan.cycles()
+    finally:
+        plan.free()
+
+
+def fit_gate(probs, feats, cycles, cycles64, features=None, p_grid=(0.0, 0.2, 0.35, 0.5, 0.65, 0.8,
+                                                                     0.9)):
+    """Grid search of the gate (P(FP32) >= p_min and feature f >= t -> FP64
+    directly) that minimises the summed cycles on labelled data: a gated system
+    costs its FP64-plan cycles, the others the cycles of the network's class.
+    probs [m,3], feats [m,16] raw, cycles [m,3], cycles64 [m]. Returns
+    (p_min, feature, threshold, cost ratio to the ungated choice); feature -1
+    when no gate helps."""
+    pred = np.argmax(probs, axis=1)
+    base = cycles[np.arange(len(pred)), pred].astype(np.float64)
+    total0 = base.sum()
+    gain = base - cycles64  # cycles saved by gating each system
+    best = (1.0, -1, 0.0, 1.0)
+    for f in (range(feats.shape[1]) if features is None else features):
+        col = feats[:, f]
+        qs = np.unique(np.quantile(col, np.linspace(0.0, 1.0, 201)))
+        for p_min in p_grid:
+            ok = probs[:, 2] >= p_min
+            for t in qs:
+                g = ok & (col >= t)
+                ratio = (total0 - gain[g].sum()) / total0
+                if ratio < best[3]:
+                    best = (float(p_min), int(f), float(t), float(ratio))
+    return best
+
+
 def labels_from_costs(cycles):
     """Cheapest class per system."""
     return np.argmin(cycles, axis=1).astype(np.int32)
@@ -92,6 +139,7 @@ class PrecisionSelector:
     def __init__(self, ctx, seed=0):
         self.ctx = ctx
         self.mlp = la_gpu.Mlp(ctx, seed)
+        self.gate = (1.0, -1, 0.0)
 
     def fit(self, feats, labels, steps=1500, lr=3e-3, batch=4096, seed=0, log_every=0):
         """Adam on minibatches of (feats [m,16] FP32 device, labels [m] int32).
@@ -127,6 +175,19 @@ class PrecisionSelector:
         self.ctx.synchronize()
         return log
 
+    def set_gate(self, p_min, feature, threshold):
+        """Class 3 (straight to the FP64 pass) where P(FP32) >= p_min and raw
+        feature `feature` >= threshold; feature < 0 turns the gate off."""
+        self.gate = (float(p_min), int(feature), float(threshold))
+        self.mlp.set_gate(p_min, feature, threshold)
+
+    def probs(self, feats):
+        """[m, 3] class probabilities (device FP32 tensor)."""
+        pr = torch.empty((feats.shape[0], 3), dtype=torch.float32, device="cuda")
+        self.mlp.predict(feats.data_ptr(), feats.shape[0], pr.data_ptr(), None)
+        self.ctx.synchronize()
+        return pr
+
     def predict(self, feats, out=None, sync=True):
         """Class per system (device int32 tensor). With sync=False the result
         is ordered on the context's stream only (e.g. for a plan's
@@ -152,8 +213,19 @@ class PrecisionSelector:
     def save(self, path):
         np.save(path, self.params())
 
+    def save_gate(self, path):
+        with open(path, "w") as f:
+            json.dump({"p_min": self.gate[0], "feature": self.gate[1],
+                       "threshold": self.gate[2]}, f, indent=1)
+
     @classmethod
-    def from_file(cls, ctx, path):
+    def from_file(cls, ctx, path, gate=True):
+        """Weights from `path`; the gate from the .gate.json file beside it
+        when it exists and `gate` is true."""
         s = cls(ctx)
         s.load(np.load(path))
+        gpath = os.path.splitext(path)[0] + ".gate.json"
+        if gate and os.path.exists(gpath):
+            g = json.load(open(gpath))
+            s.set_gate(g["p_min"], g["feature"], g["threshold"])
         return s
