@@ -10,11 +10,15 @@
 // min(m, n) diagonal entries; solve applies them to b with the factor
 // -(dot / u_k) and back-substitutes with R.
 //
-// Here every reflection is one launch of qr_reflect_kernel, one thread per
-// target column, each walking the rows in the reference's order (EXACT:
-// unfused products and sums, so the factors, Q and the solution are
-// bit-identical to the reference; FAST: the same walk with FMA). The column
-// norm is one warp's work. The back-substitution of solve is the wavefront
+// EXACT: every reflection is one launch of qr_reflect_kernel, one thread per
+// target column, each walking the rows in the reference's order with unfused
+// products and sums, so the factors, Q and the solution are bit-identical to
+// the reference; the column norm is one thread's ascending sum.
+// FAST: qr_reflect_fast_kernel, 16 target columns per CTA and 16 row slots
+// (coalesced 128-byte row segments), the dot products reduced across the row
+// slots in shared memory, then the update with FMA; in the factorization the
+// CTA that holds the next column also takes that column's norm and diagonal
+// once its update is done, so each column costs one launch. The back-substitution of solve is the wavefront
 // upper solve on R (the reference's descending term order, then the division
 // by rdiag). The reflections are sequential by nature (each depends on the
 // last); the work per step is spread over the columns.
@@ -113,6 +117,78 @@ __global__ void qr_reflect_kernel(const double* U, size_t ldu, int ucol, int r0,
   }
 }
 
+// FAST form of qr_reflect_kernel (same modes and denominators): CTA b takes
+// columns [c0 + 16 b, c0 + 16 b + 16) of T; thread (s, c) = (tid / 16, tid % 16)
+// walks rows r0 + s, r0 + s + 16, ... of its column. When next >= 0
+// (factorization) the CTA that holds column `next` then takes its norm over
+// rows [next, m), a = -/+ sqrt, rdiag[next] = a and the diagonal entry minus a
+// (qr.rs:49-76 for the next step), so every column costs one launch.
+constexpr int RF_C = 16, RF_R = 16;  // 256 threads
+__global__ void __launch_bounds__(RF_C * RF_R)
+qr_reflect_fast_kernel(const double* U, size_t ldu, int ucol, int r0, int m, double* rdiag,
+                       double* T, size_t ldt, int c0, int c1, int mode, int next) {
+  __shared__ double red[RF_R][RF_C + 1];
+  __shared__ double fac[RF_C];
+  __shared__ double nred[RF_C * RF_R / 32];
+  const int tid = threadIdx.x, cl = tid % RF_C, rs = tid / RF_C;
+  const int cb = c0 + blockIdx.x * RF_C;
+  const int c = cb + cl;
+  const double u0 = U[(size_t)r0 * ldu + ucol];
+  double den = 1.0;
+  bool skip = false;
+  if (mode == 0) {
+    const double a = rdiag[ucol];
+    skip = a == 0.0;
+    den = a * u0;
+  } else if (mode == 1) {
+    skip = u0 == 0.0;
+    den = rdiag[ucol] * u0;
+  } else {
+    den = -u0;
+  }
+  if (!skip) {
+    double dot = 0.0;
+    if (c < c1)
+      for (int row = r0 + rs; row < m; row += RF_R)
+        dot = fma(U[(size_t)row * ldu + ucol], T[(size_t)row * ldt + c], dot);
+    red[rs][cl] = dot;
+    __syncthreads();
+    if (rs == 0) {
+      double s = 0.0;
+#pragma unroll
+      for (int r = 0; r < RF_R; r++) s += red[r][cl];
+      fac[cl] = s / den;
+    }
+    __syncthreads();
+    const double f = fac[cl];
+    if (c < c1)
+      for (int row = r0 + rs; row < m; row += RF_R) {
+        double* t = T + (size_t)row * ldt + c;
+        *t = fma(f, U[(size_t)row * ldu + ucol], *t);
+      }
+  }
+  if (next >= 0 && next >= cb && next < cb + RF_C) {
+    __syncthreads();  // this CTA's updates of column `next` are visible to the block
+    double x = 0.0;
+    for (int row = next + tid; row < m; row += RF_C * RF_R) {
+      const double v = T[(size_t)row * ldt + next];
+      x = fma(v, v, x);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+    if ((tid & 31) == 0) nred[tid >> 5] = x;
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int w = 0; w < RF_C * RF_R / 32; w++) t += nred[w];
+      const double q = T[(size_t)next * ldt + next];
+      const double a = q > 0.0 ? -sqrt(t) : sqrt(t);
+      rdiag[next] = a;
+      if (a != 0.0) T[(size_t)next * ldt + next] = q - a;
+    }
+  }
+}
+
 // get_r (qr.rs:135-148, which = 0), get_h (:119-132, which = 1), m x n, and
 // the n x n upper block of R for the back-substitution (which = 0, rows < n).
 __global__ void qr_extract_kernel(const double* Q, size_t ld, const double* rdiag, int rows,
@@ -151,7 +227,7 @@ la_status qr_check_ctx(la_ctx ctx) {
 
 template <bool EXACT>
 la_status launch_reflect(la_ctx ctx, const double* U, size_t ldu, int ucol, int r0, int m,
-                         const double* rdiag, double* T, size_t ldt, int c0, int c1, int mode) {
+                         double* rdiag, double* T, size_t ldt, int c0, int c1, int mode) {
   if (c1 <= c0) return LA_OK;
   qr_reflect_kernel<EXACT><<<blocks_for((size_t)(c1 - c0), QT), QT, 0, ctx->stream>>>(
       U, ldu, ucol, r0, m, rdiag, T, ldt, c0, c1, mode);
@@ -159,25 +235,47 @@ la_status launch_reflect(la_ctx ctx, const double* U, size_t ldu, int ucol, int 
   return la_check_launch(ctx, "qr_reflect_kernel");
 }
 
-la_status reflect(la_ctx ctx, bool exact, const double* U, size_t ldu, int ucol, int r0, int m,
-                  const double* rdiag, double* T, size_t ldt, int c0, int c1, int mode) {
-  return exact ? launch_reflect<true>(ctx, U, ldu, ucol, r0, m, rdiag, T, ldt, c0, c1, mode)
-               : launch_reflect<false>(ctx, U, ldu, ucol, r0, m, rdiag, T, ldt, c0, c1, mode);
+// FAST reflection; next >= 0 also prepares column `next` (factorization). At
+// least one CTA runs even for an empty column range when `next` needs it.
+la_status launch_reflect_fast(la_ctx ctx, const double* U, size_t ldu, int ucol, int r0, int m,
+                              double* rdiag, double* T, size_t ldt, int c0, int c1, int mode,
+                              int next) {
+  if (c1 <= c0 && next < 0) return LA_OK;
+  const int blocks = std::max(1, (c1 - c0 + RF_C - 1) / RF_C);
+  qr_reflect_fast_kernel<<<blocks, RF_C * RF_R, 0, ctx->stream>>>(U, ldu, ucol, r0, m, rdiag, T,
+                                                                  ldt, c0, c1, mode, next);
+  ctx->launches++;
+  return la_check_launch(ctx, "qr_reflect_fast_kernel");
 }
 
-// qr.rs:26-42: one norm launch and one reflection launch per column.
+la_status reflect(la_ctx ctx, bool exact, const double* U, size_t ldu, int ucol, int r0, int m,
+                  double* rdiag, double* T, size_t ldt, int c0, int c1, int mode) {
+  return exact ? launch_reflect<true>(ctx, U, ldu, ucol, r0, m, rdiag, T, ldt, c0, c1, mode)
+               : launch_reflect_fast(ctx, U, ldu, ucol, r0, m, rdiag, T, ldt, c0, c1, mode, -1);
+}
+
+// qr.rs:26-42. EXACT: one norm launch and one reflection launch per column;
+// FAST: the first column's norm, then one launch per column (the reflection
+// and the next column's norm).
 la_status qr_factor(la_ctx ctx, la_qr h) {
   const int m = (int)h->m, n = (int)h->n, dc = std::min(m, n);
   const bool exact = h->arith == LA_ARITH_EXACT;
-  for (int minor = 0; minor < dc; minor++) {
-    if (exact)
-      qr_norm_kernel<true><<<1, 32, 0, ctx->stream>>>(h->d_qr, h->ld, m, minor, h->d_rdiag);
-    else
-      qr_norm_kernel<false><<<1, 32, 0, ctx->stream>>>(h->d_qr, h->ld, m, minor, h->d_rdiag);
+  if (!exact) {
+    qr_norm_kernel<false><<<1, 32, 0, ctx->stream>>>(h->d_qr, h->ld, m, 0, h->d_rdiag);
     ctx->launches++;
     LA_TRY(la_check_launch(ctx, "qr_norm_kernel"));
-    LA_TRY(reflect(ctx, exact, h->d_qr, h->ld, minor, minor, m, h->d_rdiag, h->d_qr, h->ld,
-                   minor + 1, n, 0));
+  }
+  for (int minor = 0; minor < dc; minor++) {
+    if (exact) {
+      qr_norm_kernel<true><<<1, 32, 0, ctx->stream>>>(h->d_qr, h->ld, m, minor, h->d_rdiag);
+      ctx->launches++;
+      LA_TRY(la_check_launch(ctx, "qr_norm_kernel"));
+      LA_TRY(reflect(ctx, true, h->d_qr, h->ld, minor, minor, m, h->d_rdiag, h->d_qr, h->ld,
+                     minor + 1, n, 0));
+    } else {
+      LA_TRY(launch_reflect_fast(ctx, h->d_qr, h->ld, minor, minor, m, h->d_rdiag, h->d_qr,
+                                 h->ld, minor + 1, n, 0, minor + 1 < dc ? minor + 1 : -1));
+    }
   }
   h->rdiag.assign((size_t)dc, 0.0);
   LA_CUDA(ctx, cudaMemcpyAsync(h->rdiag.data(), h->d_rdiag, (size_t)dc * sizeof(double),
