@@ -391,11 +391,12 @@ def householder_conditioned(torch, n, kappa, seed):
     return a.contiguous()
 
 
-def run_mixed(la_gpu, torch, ctx, n, nrhs=4, kappas=(1e2, 1e6, 1e10), precs=(1, 2, 3, 4), reps=5):
+def run_mixed(la_gpu, torch, ctx, n, nrhs=4, kappas=(1e2, 1e6, 1e10), precs=(1, 2, 3, 4, 6),
+              reps=5):
     """Mixed-precision LU + FP64 refinement against the plain FP64 LU at size n.
     Every time is the median of `reps` runs (CUDA events on the library's
     stream, after one untimed run) of factor + refined solve."""
-    names = {1: "bf16", 2: "fp16", 3: "fp32", 4: "fp8"}
+    names = {1: "bf16", 2: "fp16", 3: "fp32", 4: "fp8", 6: "fp16x3"}
     flops = lu_solve_flops(n, nrhs)
     rng = np.random.default_rng(3)
     b = torch.from_numpy(rng.standard_normal((n, nrhs))).cuda()
@@ -441,7 +442,7 @@ def run_mixed(la_gpu, torch, ctx, n, nrhs=4, kappas=(1e2, 1e6, 1e10), precs=(1, 
                                            b.data_ptr(), nrhs, n, nrhs)
         auto_by_kappa[kappa] = {"kappa": kappa,
                                 "precision_used": {0: "fp64", 1: "bf16", 2: "fp16", 3: "fp32",
-                                                   4: "fp8"}[st.precision],
+                                                   4: "fp8", 6: "fp16x3"}[st.precision],
                                 "ms": ms, "ms_min_max": [min(times), max(times)],
                                 "gflops": flops / (ms * 1e-3) / 1e9,
                                 "iterations": st.iterations, "fell_back": st.fell_back,

@@ -192,8 +192,15 @@ la_status la_matrix_mul_device(la_ctx ctx, const double* d_a, size_t lda, const 
 #define LA_PREC_BF16 1  /* tcgen05 BF16 x BF16 -> FP32 */
 #define LA_PREC_FP16 2  /* tcgen05 FP16 x FP16 -> FP32, per-panel power-of-two scaling */
 #define LA_PREC_FP32 3  /* FP32 FMA (no tensor cores) */
-#define LA_PREC_FP8 4   /* batched solves: factors stored as FP8 e4m3 (power-of-two scaled) */
+/* mixed LU: tcgen05 FP8 e4m3 with each operand split in a high and a low part
+ * (three products, about BF16 accuracy); batched solves: factors stored as FP8
+ * e4m3 (power-of-two scaled) */
+#define LA_PREC_FP8 4
 #define LA_PREC_FP64 5  /* batched solves: no mixed attempt, the plan's FP64 pass answers */
+/* mixed LU: tcgen05 FP16 x FP16 -> FP32 with each operand split in a high and
+ * a low FP16 part (three products, about 2^-22 relative error each: factors
+ * close to FP32 ones at the cost of the FP16 update) */
+#define LA_PREC_FP16X3 6
 
 typedef struct la_refine_stats {
   int iterations;    /* refinement steps (plain and GMRES) */
@@ -234,8 +241,12 @@ la_status la_lu_solve_auto_device(la_ctx ctx, const double* d_a, size_t lda, siz
                                   const double* d_b, size_t ldb, size_t nrhs, double* d_x,
                                   size_t ldx, double tol, la_refine_stats* stats);
 /* Tensor-core building block of the mixed LU, exposed for testing:
- * C (m x n f32, pitch ldc) -= alpha * A (m x k) * B^T (B: n x k), A and B 16-bit
- * (fmt 1 = BF16, 2 = FP16) K-major with pitches multiple of 8 elements. */
+ * C (m x n f32, pitch ldc) -= alpha * A (m x k) * B^T (B: n x k), K-major.
+ * fmt 1 = BF16, 2 = FP16: pitches multiples of 8 elements. Split formats,
+ * fmt 3 = FP8 e4m3 (bytes) and 4 = FP16: each row holds the high parts in
+ * columns [0, k) and the low parts from column lda / 2 (lda == ldb, lda / 2 at
+ * or beyond k rounded up to 128 bytes, pitches multiples of 32 bytes); the
+ * kernel accumulates Ah Bh^T + Ah Bl^T + Al Bh^T. */
 la_status la_lowp_update_device(la_ctx ctx, int fmt, size_t m, size_t n, size_t k,
                                 const void* d_a16, size_t lda, const void* d_b16, size_t ldb,
                                 float* d_c, size_t ldc, float alpha);

@@ -3,14 +3,15 @@
 // with A and B both K-major (K contiguous), accumulated in FP32 by
 // tcgen05.mma into tensor memory. Operand formats:
 //   BF16 or FP16 (kind::f16, K = 16 per instruction);
-//   FP8 e4m3 split in two parts (kind::f8f6f4, K = 32 per instruction): each
-//   operand row holds its high parts in columns [0, K) and its low parts in
-//   columns [lo, lo + K) (v * scale ~ hi + lo, both e4m3), and the kernel
+//   split formats, FP8 e4m3 (kind::f8f6f4, K = 32 per instruction) or FP16
+//   (kind::f16): each operand row holds its high parts in columns [0, K) and
+//   its low parts in columns [lo, lo + K) (v * scale ~ hi + lo), and the kernel
 //   accumulates hi*hi + hi*lo + lo*hi. Three 8-bit products give factors about
 //   as accurate as BF16 ones (one e4m3 product alone leaves errors of a few
-//   per cent, too much for refinement at kappa >= 1e2), and each chunk of the
-//   ring is still a 128-byte-wide box of A and one of B: the producer walks
-//   three "virtual" chunks per 128 columns of K, (hi, hi), (hi, lo), (lo, hi).
+//   per cent, too much for refinement at kappa >= 1e2); three FP16 products
+//   give about 2^-22 per product, close to FP32. Each chunk of the ring is
+//   still a 128-byte-wide box of A and one of B: the producer walks three
+//   "virtual" chunks per 128 bytes of K, (hi, hi), (hi, lo), (lo, hi).
 //
 // One CTA per 128 x 128 output tile, 128 threads:
 //   warp 0 lane 0 : TMA producer. 128-byte-deep K chunks of A and B (64 16-bit
@@ -75,9 +76,9 @@ __host__ __device__ constexpr uint32_t idesc_mma(uint32_t ab_fmt) {
          ((uint32_t)(TM >> 4) << 24);
 }
 
-// F8: e4m3 hi/lo operands (kind::f8f6f4); else 16-bit (kind::f16). K counts
-// elements; lo is the column of the low parts (F8 only).
-template <bool F8>
+// F8: 8-bit operands (kind::f8f6f4), else 16-bit (kind::f16). SPLIT: hi/lo
+// operands, lo the column of the low parts. K counts elements.
+template <bool F8, bool SPLIT>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 tc_update_kernel(const __grid_constant__ CUtensorMap tmap_a,
                  const __grid_constant__ CUtensorMap tmap_b,
@@ -93,7 +94,7 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tmap_a,
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
   constexpr int TKE = F8 ? TKB : TKB / 2;  // elements of K per chunk
-  const int nk = (F8 ? 3 : 1) * ((K + TKE - 1) / TKE);
+  const int nk = (SPLIT ? 3 : 1) * ((K + TKE - 1) / TKE);
 
   if (tid == 0) {
     for (int s = 0; s < STAGES; s++) {
@@ -127,7 +128,7 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tmap_a,
       unsigned char* sb = sa + A_BYTES;
       mbar_expect_tx(&full[s], STAGE_BYTES);
       int ax = kc * TKE, bx = ax;
-      if (F8) {  // virtual chunk kc: K columns [c, c + 128) as (hi, hi), (hi, lo), (lo, hi)
+      if (SPLIT) {  // virtual chunk kc: K columns [c, c + TKE) as (hi, hi), (hi, lo), (lo, hi)
         const int c = (kc / 3) * TKE, t = kc % 3;
         ax = c + (t == 2 ? lo : 0);
         bx = c + (t == 1 ? lo : 0);
@@ -249,6 +250,9 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tmap_a,
 // K x 128 rows. 8-bit operands are mapped as bytes.
 bool encode_operand(la_ctx ctx, CUtensorMap* map, const void* base, int fmt, size_t rows,
                     size_t cols, size_t ld) {
+  if (fmt == LA_LOWP_F16X3)
+    return la_tma::encode_2d(ctx, map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, base, rows, cols, ld,
+                             (uint32_t)(TKB / 2), (uint32_t)TM, CU_TENSOR_MAP_SWIZZLE_128B);
   if (fmt == LA_LOWP_E4M3X3)
     return la_tma::encode_2d(ctx, map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, base, rows, cols, ld,
                              (uint32_t)TKB, (uint32_t)TM, CU_TENSOR_MAP_SWIZZLE_128B);
@@ -264,23 +268,26 @@ bool encode_operand(la_ctx ctx, CUtensorMap* map, const void* base, int fmt, siz
 // C (M x N f32, pitch ldc, 16-byte aligned rows) -= alpha * A * B^T where A is
 // M x K and B is N x K, K-major with pitches lda, ldb in elements and
 // 16-byte aligned bases. 16-bit formats: pitches multiples of 8 elements.
-// LA_LOWP_E4M3X3: bytes, the low parts at column lo = lda / 2 = ldb / 2, at or
-// beyond K rounded up to a whole 128-byte chunk (the high parts' last chunk
-// must not reach them); pitches multiples of 32. alpha is read on the device.
+// Split formats (LA_LOWP_E4M3X3 bytes, LA_LOWP_F16X3 16-bit): the low parts
+// at column lo = lda / 2 = ldb / 2, at or beyond K rounded up to a whole
+// 128-byte chunk (the high parts' last chunk must not reach them); pitches
+// multiples of 32 bytes. alpha is read on the device.
 la_status launch_tc_update(la_ctx ctx, cudaStream_t stream, int fmt, int M, int N, int K,
                            const void* A, size_t lda, const void* B, size_t ldb, float* C,
                            size_t ldc, const float* d_alpha) {
   if (M <= 0 || N <= 0 || K <= 0) return LA_OK;
   const bool f8 = fmt == LA_LOWP_E4M3X3;
-  const size_t pq = f8 ? 32 : 8;  // pitch quantum in elements
+  const bool split = f8 || fmt == LA_LOWP_F16X3;
+  const size_t pq = f8 ? 32 : (split ? 16 : 8);  // pitch quantum in elements
+  const int tke = f8 ? TKB : TKB / 2;           // elements per 128-byte chunk
   if ((lda % pq) || (ldb % pq) || (ldc % 4) || (reinterpret_cast<uintptr_t>(A) % 16) ||
       (reinterpret_cast<uintptr_t>(B) % 16) || (reinterpret_cast<uintptr_t>(C) % 16))
     return LA_INVALID;
-  if (f8 && (lda != ldb || (size_t)(K + TKB - 1) / TKB * TKB > lda / 2)) return LA_INVALID;
-  const int lo = f8 ? (int)(lda / 2) : 0;
-  // The maps span the columns the kernel reads: [0, K), or for split FP8
+  if (split && (lda != ldb || (size_t)(K + tke - 1) / tke * tke > lda / 2)) return LA_INVALID;
+  const int lo = split ? (int)(lda / 2) : 0;
+  // The maps span the columns the kernel reads: [0, K), or for split formats
   // [0, lo + K) (the high parts, padding, the low parts).
-  const size_t cols = f8 ? (size_t)lo + (size_t)K : (size_t)K;
+  const size_t cols = split ? (size_t)lo + (size_t)K : (size_t)K;
   CUtensorMap ta, tb, tc;
   if (!encode_operand(ctx, &ta, A, fmt, (size_t)M, cols, lda)) return LA_CUDA_ERROR;
   if (!encode_operand(ctx, &tb, B, fmt, (size_t)N, cols, ldb)) return LA_CUDA_ERROR;
@@ -291,20 +298,22 @@ la_status launch_tc_update(la_ctx ctx, cudaStream_t stream, int fmt, int M, int 
     return LA_CUDA_ERROR;
   static la_device_once configured;
   cudaError_t e = configured.run([](int) {
-    cudaError_t r = cudaFuncSetAttribute(tc_update_kernel<false>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
-    if (r == cudaSuccess)
-      r = cudaFuncSetAttribute(tc_update_kernel<true>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
+    const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    cudaError_t r = cudaFuncSetAttribute(tc_update_kernel<false, false>, at, (int)TC_SMEM);
+    if (r == cudaSuccess) r = cudaFuncSetAttribute(tc_update_kernel<false, true>, at, (int)TC_SMEM);
+    if (r == cudaSuccess) r = cudaFuncSetAttribute(tc_update_kernel<true, true>, at, (int)TC_SMEM);
     return r;
   });
   if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaFuncSetAttribute(tc_update)");
   dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM);
   if (f8)
-    tc_update_kernel<true><<<grid, TC_THREADS, TC_SMEM, stream>>>(ta, tb, tc, N, K, lo, d_alpha,
-                                                                  idesc_mma(0u), ctx->d_err);
+    tc_update_kernel<true, true><<<grid, TC_THREADS, TC_SMEM, stream>>>(
+        ta, tb, tc, N, K, lo, d_alpha, idesc_mma(0u), ctx->d_err);
+  else if (split)
+    tc_update_kernel<false, true><<<grid, TC_THREADS, TC_SMEM, stream>>>(
+        ta, tb, tc, N, K, lo, d_alpha, idesc_mma(0u), ctx->d_err);
   else
-    tc_update_kernel<false><<<grid, TC_THREADS, TC_SMEM, stream>>>(
+    tc_update_kernel<false, false><<<grid, TC_THREADS, TC_SMEM, stream>>>(
         ta, tb, tc, N, K, 0, d_alpha, idesc_mma(fmt == LA_LOWP_BF16 ? 1u : 0u), ctx->d_err);
   ctx->launches++;
   return la_check_launch(ctx, "tc_update_kernel");
@@ -314,7 +323,7 @@ extern "C" la_status la_lowp_update_device(la_ctx ctx, int fmt, size_t m, size_t
                                            const void* d_a16, size_t lda, const void* d_b16,
                                            size_t ldb, float* d_c, size_t ldc, float alpha) {
   if (!ctx || !d_a16 || !d_b16 || !d_c) return LA_INVALID;
-  if (fmt != LA_LOWP_BF16 && fmt != LA_LOWP_FP16 && fmt != LA_LOWP_E4M3X3) return LA_INVALID;
+  if (fmt < LA_LOWP_BF16 || fmt > LA_LOWP_F16X3) return LA_INVALID;
   if (m > INT32_MAX || n > INT32_MAX || k > INT32_MAX) return LA_UNSUPPORTED;
   LA_CUDA(ctx, cudaSetDevice(ctx->device));
   float* d_alpha = reinterpret_cast<float*>(ctx->d_small + 4);

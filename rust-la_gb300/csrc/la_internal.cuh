@@ -84,10 +84,11 @@ enum DeviceErr : int {
   DERR_GEMM_TIMEOUT = 5
 };
 
-// 16-bit operand formats of the tensor-core update.
-// LA_LOWP_E4M3X3: FP8 e4m3 operands split in a high and a low part each
-// (v ~ hi + lo), three products hi*hi + hi*lo + lo*hi.
-enum LowpFormat : int { LA_LOWP_BF16 = 1, LA_LOWP_FP16 = 2, LA_LOWP_E4M3X3 = 3 };
+// Operand formats of the tensor-core update. The split formats store each
+// value as a high and a low part (v ~ hi + lo) and accumulate the three
+// products hi*hi + hi*lo + lo*hi: LA_LOWP_E4M3X3 in FP8 e4m3 (about BF16
+// accuracy), LA_LOWP_F16X3 in FP16 (about 2^-22 per product, near FP32).
+enum LowpFormat : int { LA_LOWP_BF16 = 1, LA_LOWP_FP16 = 2, LA_LOWP_E4M3X3 = 3, LA_LOWP_F16X3 = 4 };
 
 struct la_context {
   int device = 0;

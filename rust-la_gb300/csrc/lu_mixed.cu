@@ -9,11 +9,11 @@
 //   triangular update, FP32 SIMT updates);
 //   outer row-panel triangular update U12 = L11^-1 A12 in FP32;
 //   trailing update A22 -= L21 * U12 on the tensor cores (gemm_tc.cu) with
-//   BF16, FP16 or split FP8 e4m3 operands and FP32 accumulation, or in FP32
-//   SIMT (LA_PREC_FP32). FP16 operands use a per-panel power-of-two scale of
-//   U12 (L's entries are bounded by 1 under partial pivoting); FP8 operands
-//   scale L21 by 2^8 and U12 by a per-panel power of two, and store each value
-//   as a high and a low e4m3 part; the scales are undone in the epilogue.
+//   BF16, FP16, split FP8 e4m3 or split FP16 operands and FP32 accumulation,
+//   or in FP32 SIMT (LA_PREC_FP32). FP16 operands use a per-panel power-of-two
+//   scale of U12 (L's entries are bounded by 1 under partial pivoting); the
+//   split formats scale L21 and U12 by powers of two and store each value as a
+//   high and a low part; the scales are undone in the epilogue.
 // Solve: x0 = 0, r = b; repeat d = LU32 \ (r scaled to unit max per column),
 // x += d (FP64), r = b - A x in FP64 (A kept in FP64), until the normwise
 // backward error max_j ||r_j|| / (||A|| ||x_j|| + ||b_j||) <= tol or the
@@ -114,50 +114,69 @@ __global__ void pack_ut_kernel(const float* __restrict__ src, size_t lds, uint16
 
 __global__ void set_alpha_one(float* stat) { stat[0] = 0.f; stat[1] = 1.f; }
 
-// Split FP8: v (already scaled) ~ hi + lo with hi = e4m3(v), lo = e4m3(v - hi)
-// (round to nearest, saturating at the largest finite e4m3 value).
-__device__ __forceinline__ void split_e4m3(float v, uint8_t& hi, uint8_t& lo) {
-  const __nv_fp8_e4m3 h(v);
-  const __nv_fp8_e4m3 l(v - static_cast<float>(h));
-  hi = h.__x;
-  lo = l.__x;
-}
+// Split storage: v (already scaled) ~ hi + lo with hi = rn(v), lo = rn(v - hi)
+// in the storage format (FP8 e4m3 saturating at its largest finite value, or
+// FP16).
+struct SplitE4M3 {
+  using T = uint8_t;
+  static constexpr int L_EXP = 8;  // |l| <= 1 -> |l| * 2^8 <= 256 < 448 (e4m3 max)
+  static constexpr int U_EXP = 8;  // max |U12| scaled just below 2^8
+  static __device__ __forceinline__ void split(float v, T& hi, T& lo) {
+    const __nv_fp8_e4m3 h(v);
+    const __nv_fp8_e4m3 l(v - static_cast<float>(h));
+    hi = h.__x;
+    lo = l.__x;
+  }
+};
+struct SplitF16 {
+  using T = uint16_t;
+  static constexpr int L_EXP = 12;  // products of scaled parts stay far inside FP32
+  static constexpr int U_EXP = 14;  // max |U12| scaled just below 2^14 (FP16 max 65504)
+  static __device__ __forceinline__ void split(float v, T& hi, T& lo) {
+    const __half h = __float2half_rn(v);
+    const __half l = __float2half_rn(v - __half2float(h));
+    hi = __half_as_ushort(h);
+    lo = __half_as_ushort(l);
+  }
+};
 
-constexpr float F8_L_SCALE = 256.f;  // |l| <= 1 -> |l| * 2^8 <= 256 < 448 (e4m3 max)
-
-// L21 (rows x k FP32, pitch lds) * 2^8 -> split e4m3 rows of ldd bytes: high
-// parts in columns [0, k), low parts in [ldd / 2, ldd / 2 + k), zeros elsewhere.
-__global__ void pack_l_f8_kernel(const float* __restrict__ src, size_t lds,
-                                 uint8_t* __restrict__ dst, size_t ldd, int rows, int k) {
+// L21 (rows x k FP32, pitch lds) * 2^L_EXP -> split rows of ldd elements:
+// high parts in columns [0, k), low parts in [ldd / 2, ldd / 2 + k), zeros
+// elsewhere.
+template <typename SP>
+__global__ void pack_l_split_kernel(const float* __restrict__ src, size_t lds,
+                                    typename SP::T* __restrict__ dst, size_t ldd, int rows, int k) {
   const size_t half = ldd / 2;
+  const float sl = ldexpf(1.f, SP::L_EXP);
   size_t total = (size_t)rows * half;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
        i += (size_t)gridDim.x * blockDim.x) {
     const int r = (int)(i / half), c = (int)(i % half);
-    uint8_t hi = 0, lo = 0;
-    if (c < k) split_e4m3(src[(size_t)r * lds + c] * F8_L_SCALE, hi, lo);
+    typename SP::T hi = 0, lo = 0;
+    if (c < k) SP::split(src[(size_t)r * lds + c] * sl, hi, lo);
     dst[(size_t)r * ldd + c] = hi;
     dst[(size_t)r * ldd + half + c] = lo;
   }
 }
 
-// U12 (k x cols, pitch lds) -> U^T split e4m3 (cols rows of ldd bytes, as
-// pack_l_f8_kernel) times a power of two that takes max |U12| (stat[0]) just
-// below 2^8; stat[1] receives alpha = 1 / (2^8 * scale). 32x32 tiles through
-// shared memory.
-__global__ void pack_ut_f8_kernel(const float* __restrict__ src, size_t lds,
-                                  uint8_t* __restrict__ dst, size_t ldd, int k, int cols,
-                                  float* stat) {
+// U12 (k x cols, pitch lds) -> U^T split (cols rows of ldd elements, as
+// pack_l_split_kernel) times a power of two that takes max |U12| (stat[0])
+// just below 2^U_EXP; stat[1] receives alpha = 1 / (2^L_EXP * scale). 32x32
+// tiles through shared memory.
+template <typename SP>
+__global__ void pack_ut_split_kernel(const float* __restrict__ src, size_t lds,
+                                     typename SP::T* __restrict__ dst, size_t ldd, int k, int cols,
+                                     float* stat) {
   __shared__ float t[32][33];
   float scale = 1.f;
   const float mx = stat[0];
   int e = 0;
   if (mx > 0.f && mx < INFINITY) {
     frexpf(mx, &e);  // mx = f 2^e, 0.5 <= f < 1
-    scale = ldexpf(1.f, 8 - e);
+    scale = ldexpf(1.f, SP::U_EXP - e);
   }
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0)
-    stat[1] = 1.f / (F8_L_SCALE * scale);
+    stat[1] = 1.f / (ldexpf(1.f, SP::L_EXP) * scale);
   const size_t half = ldd / 2;
   const int c0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
   for (int i = threadIdx.y; i < 32; i += blockDim.y) {
@@ -168,8 +187,8 @@ __global__ void pack_ut_f8_kernel(const float* __restrict__ src, size_t lds,
   for (int i = threadIdx.y; i < 32; i += blockDim.y) {
     int cc = c0 + i, kk = k0 + threadIdx.x;
     if (cc < cols && kk < (int)half) {
-      uint8_t hi, lo;
-      split_e4m3(t[threadIdx.x][i], hi, lo);
+      typename SP::T hi, lo;
+      SP::split(t[threadIdx.x][i], hi, lo);
       dst[(size_t)cc * ldd + kk] = hi;
       dst[(size_t)cc * ldd + half + kk] = lo;
     }
@@ -372,10 +391,13 @@ la_status mixed_factor(la_ctx ctx, la_lu h, int prec) {
   unsigned bar_base = 0;
   Buf lh(ctx), uh(ctx), stat(ctx);
   const size_t ldk = pad8(WO);
-  const size_t ldk8 = 2 * WO;  // split FP8 rows: high parts, then low parts at WO
+  const size_t ldks = 2 * WO;  // split rows: high parts, then low parts from column WO
   if (prec == LA_PREC_FP8) {
-    LA_TRY(lh.alloc((size_t)m * ldk8 + 256));
-    LA_TRY(uh.alloc((size_t)n * ldk8 + 256));
+    LA_TRY(lh.alloc((size_t)m * ldks + 256));
+    LA_TRY(uh.alloc((size_t)n * ldks + 256));
+  } else if (prec == LA_PREC_FP16X3) {
+    LA_TRY(lh.alloc((size_t)m * ldks * 2 + 256));
+    LA_TRY(uh.alloc((size_t)n * ldks * 2 + 256));
   } else if (prec != LA_PREC_FP32) {
     LA_TRY(lh.alloc((size_t)m * ldk * 2 + 256));
     LA_TRY(uh.alloc((size_t)n * ldk * 2 + 256));
@@ -440,24 +462,35 @@ la_status mixed_factor(la_ctx ctx, la_lu h, int prec) {
     }
     const float* L21 = A + (size_t)j1o * ld + j0;
     const float* U12 = A + (size_t)j0 * ld + c0;
-    if (prec == LA_PREC_FP8) {
-      uint8_t* ub8 = uh.as<uint8_t>() + (size_t)(c0 - j1o) * ldk8;
+    if (prec == LA_PREC_FP8 || prec == LA_PREC_FP16X3) {
       LA_CUDA(ctx, cudaMemsetAsync(d_stat, 0, 2 * sizeof(float), ms));
       absmax_kernel<<<grid_for(ctx, (size_t)jbo * N), 256, 0, ms>>>(U12, ld, jbo, N, d_stat);
       ctx->launches++;
       LA_TRY(la_check_launch(ctx, "absmax_kernel"));
-      if (pack_l) {
-        pack_l_f8_kernel<<<grid_for(ctx, (size_t)M * WO), 256, 0, ms>>>(L21, ld, lh.as<uint8_t>(),
-                                                                        ldk8, M, jbo);
-        ctx->launches++;
-        LA_TRY(la_check_launch(ctx, "pack_l_f8_kernel"));
+      const dim3 pgs((N + 31) / 32, (WO + 31) / 32);
+      const size_t lg = grid_for(ctx, (size_t)M * WO);
+      void* ub;
+      if (prec == LA_PREC_FP8) {
+        uint8_t* u8 = uh.as<uint8_t>() + (size_t)(c0 - j1o) * ldks;
+        ub = u8;
+        if (pack_l)
+          pack_l_split_kernel<SplitE4M3><<<lg, 256, 0, ms>>>(L21, ld, lh.as<uint8_t>(), ldks, M,
+                                                             jbo);
+        pack_ut_split_kernel<SplitE4M3><<<pgs, dim3(32, 8), 0, ms>>>(U12, ld, u8, ldks, jbo, N,
+                                                                     d_stat);
+      } else {
+        uint16_t* u16 = uh.as<uint16_t>() + (size_t)(c0 - j1o) * ldks;
+        ub = u16;
+        if (pack_l)
+          pack_l_split_kernel<SplitF16><<<lg, 256, 0, ms>>>(L21, ld, lh.as<uint16_t>(), ldks, M,
+                                                            jbo);
+        pack_ut_split_kernel<SplitF16><<<pgs, dim3(32, 8), 0, ms>>>(U12, ld, u16, ldks, jbo, N,
+                                                                    d_stat);
       }
-      dim3 pg8((N + 31) / 32, (WO + 31) / 32);
-      pack_ut_f8_kernel<<<pg8, dim3(32, 8), 0, ms>>>(U12, ld, ub8, ldk8, jbo, N, d_stat);
-      ctx->launches++;
-      LA_TRY(la_check_launch(ctx, "pack_ut_f8_kernel"));
-      return launch_tc_update(ctx, ms, LA_LOWP_E4M3X3, M, N, jbo, lh.p, ldk8, ub8, ldk8, C, ld,
-                              d_stat + 1);
+      ctx->launches += pack_l ? 2 : 1;
+      LA_TRY(la_check_launch(ctx, "pack_split_kernel"));
+      return launch_tc_update(ctx, ms, prec == LA_PREC_FP8 ? LA_LOWP_E4M3X3 : LA_LOWP_F16X3, M, N,
+                              jbo, lh.p, ldks, ub, ldks, C, ld, d_stat + 1);
     }
     const int fmt = prec == LA_PREC_BF16 ? LA_LOWP_BF16 : LA_LOWP_FP16;
     uint16_t* ub = uh.as<uint16_t>() + (size_t)(c0 - j1o) * ldk;
@@ -538,7 +571,7 @@ la_status la_lu_mixed_new_device(la_ctx ctx, const double* d_a, size_t lda, size
   if (n == 0) return LA_BADSHAPE;
   if (n > (size_t)INT32_MAX / 4) return LA_UNSUPPORTED;
   if (prec != LA_PREC_BF16 && prec != LA_PREC_FP16 && prec != LA_PREC_FP32 &&
-      prec != LA_PREC_FP8)
+      prec != LA_PREC_FP8 && prec != LA_PREC_FP16X3)
     return LA_INVALID;
   LA_CUDA(ctx, cudaSetDevice(ctx->device));
   *out = nullptr;

@@ -141,7 +141,7 @@ class BatchSystem(ctypes.Structure):
                 ("n", ctypes.c_int), ("nrhs", ctypes.c_int), ("precision", ctypes.c_int),
                 ("reserved", ctypes.c_int)]
 
-PREC_BF16, PREC_FP16, PREC_FP32, PREC_FP8, PREC_FP64 = 1, 2, 3, 4, 5
+PREC_BF16, PREC_FP16, PREC_FP32, PREC_FP8, PREC_FP64, PREC_FP16X3 = 1, 2, 3, 4, 5, 6
 
 
 class RefineStats(ctypes.Structure):

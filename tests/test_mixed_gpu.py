@@ -44,36 +44,40 @@ def test_tc_update_matches_fp64_reference(lagpu, ctx_fast, torch, fmt, mnk):
         assert torch.isfinite(c[:, n:]).all()
 
 
+@pytest.mark.parametrize("fmt", [3, 4], ids=["e4m3x3", "fp16x3"])
 @pytest.mark.parametrize("mnk", [(128, 128, 128), (1, 1, 16), (200, 300, 100), (256, 384, 256),
                                  (1000, 130, 512), (129, 257, 8)])
-def test_tc_update_split_fp8_matches_fp64_reference(lagpu, ctx_fast, torch, mnk):
-    # Split e4m3 operands (high parts in columns [0, k), low parts from column
-    # lo = the padded k): C -= alpha (Ah Bh^T + Ah Bl^T + Al Bh^T), kind::f8f6f4.
+def test_tc_update_split_matches_fp64_reference(lagpu, ctx_fast, torch, fmt, mnk):
+    # Split operands (high parts in columns [0, k), low parts from column lo,
+    # k padded to a 128-byte chunk): C -= alpha (Ah Bh^T + Ah Bl^T + Al Bh^T);
+    # FP8 e4m3 by kind::f8f6f4, FP16 by kind::f16.
     m, n, k = mnk
-    f8 = torch.float8_e4m3fn
-    g = torch.Generator(device="cuda").manual_seed(m * 5 + n * 11 + k)
-    lo = (k + 127) // 128 * 128
+    dt = torch.float8_e4m3fn if fmt == 3 else torch.float16
+    st = torch.uint8 if fmt == 3 else torch.int16
+    per = 128 if fmt == 3 else 64  # elements per 128-byte chunk
+    g = torch.Generator(device="cuda").manual_seed(m * 5 + n * 11 + k + fmt)
+    lo = (k + per - 1) // per * per
     ldc = (n + 3) // 4 * 4
 
     def split(x):
-        hi = x.to(f8)
-        return hi, (x - hi.float()).to(f8)
+        hi = x.to(dt)
+        return hi, (x - hi.float()).to(dt)
 
     ah, al = split(torch.randn((m, k), generator=g, device="cuda") * 8)
     bh, bl = split(torch.randn((n, k), generator=g, device="cuda") * 8)
-    a = torch.zeros((m, 2 * lo), dtype=torch.uint8, device="cuda")
-    b = torch.zeros((n, 2 * lo), dtype=torch.uint8, device="cuda")
-    a[:, :k] = ah.view(torch.uint8)
-    a[:, lo:lo + k] = al.view(torch.uint8)
-    b[:, :k] = bh.view(torch.uint8)
-    b[:, lo:lo + k] = bl.view(torch.uint8)
+    a = torch.zeros((m, 2 * lo), dtype=st, device="cuda")
+    b = torch.zeros((n, 2 * lo), dtype=st, device="cuda")
+    a[:, :k] = ah.view(st)
+    a[:, lo:lo + k] = al.view(st)
+    b[:, :k] = bh.view(st)
+    b[:, lo:lo + k] = bl.view(st)
     c = torch.randn((m, ldc), generator=g, device="cuda", dtype=torch.float32)
     alpha = 1.0 / 64
     d = lambda t: t.double()
     prod = d(ah) @ d(bh).T + d(ah) @ d(bl).T + d(al) @ d(bh).T
     ref = c[:, :n].double() - alpha * prod
     torch.cuda.synchronize()
-    lagpu.lowp_update_device(ctx_fast, 3, m, n, k, a.data_ptr(), 2 * lo, b.data_ptr(), 2 * lo,
+    lagpu.lowp_update_device(ctx_fast, fmt, m, n, k, a.data_ptr(), 2 * lo, b.data_ptr(), 2 * lo,
                              c.data_ptr(), ldc, alpha)
     got = c[:, :n].double()
     scale = 1.0 + alpha * (d(ah).abs() @ d(bh).abs().T + d(ah).abs() @ d(bl).abs().T +
@@ -99,7 +103,7 @@ def _problem(n, nrhs, seed, shift=0.0):
     return a, b
 
 
-@pytest.mark.parametrize("prec", [1, 2, 3, 4], ids=["bf16", "fp16", "fp32", "fp8"])
+@pytest.mark.parametrize("prec", [1, 2, 3, 4, 6], ids=["bf16", "fp16", "fp32", "fp8", "fp16x3"])
 @pytest.mark.parametrize("n", [64, 300, 1000, 1536])
 def test_mixed_lu_ir_reaches_fp64_backward_error(lagpu, ctx_fast, torch, prec, n):
     a, b = _problem(n, 4, 100 + n, shift=0.0 if prec == 3 else 2.0 * np.sqrt(n))
@@ -143,8 +147,8 @@ def _hh(torch, n, kappa, seed):
     return a.contiguous()
 
 
-@pytest.mark.parametrize("prec,kappa", [(1, 1e6), (2, 1e8), (3, 1e10), (4, 1e3)],
-                         ids=["bf16-1e6", "fp16-1e8", "fp32-1e10", "fp8-1e3"])
+@pytest.mark.parametrize("prec,kappa", [(1, 1e6), (2, 1e8), (3, 1e10), (4, 1e3), (6, 1e10)],
+                         ids=["bf16-1e6", "fp16-1e8", "fp32-1e10", "fp8-1e3", "fp16x3-1e10"])
 def test_ill_conditioned_refinement_converges(lagpu, ctx_fast, torch, prec, kappa):
     n = 1024
     a = _hh(torch, n, kappa, 7)
