@@ -368,10 +368,56 @@ __device__ __forceinline__ bool panel_column(int c, const ClusterPanelArgs& p, i
     const int gsrc = __ffs(gmask) - 1;  // the row at position j is a candidate: gm != 0
     const int piv = (int)(~(unsigned)(gm & 0xffffffffull));
     const float* urow = reinterpret_cast<const float*>(&recv[par][gsrc][4]);
+    if constexpr (ROT) {
+      // The pivot row streams from shared memory in float4 chunks, each chunk
+      // applied to all of this thread's rows (4 registers for it, not 32).
+      const float d = urow[0];
+      const float sc = d != 0.f ? 1.f / d : 1.f;
+      float lq[RPT];
+      bool act[RPT];
+#pragma unroll
+      for (int q = 0; q < RPT; q++) {
+        act[q] = false;
+        if (pos[q] == piv) {
+          pos[q] = j;  // the pivot row; it keeps its values
+        } else {
+          if (pos[q] == j) pos[q] = piv;  // the displaced row takes the pivot's place
+          act[q] = pos[q] > j;
+        }
+        lq[q] = d != 0.f ? v[q][0] * sc : v[q][0];
+        if (act[q]) v[q][0] = lq[q];
+      }
+#pragma unroll
+      for (int k4 = 0; k4 < CW / 4; k4++) {
+        const float4 u4 = reinterpret_cast<const float4*>(urow)[k4];
+        const float uk[4] = {u4.x, u4.y, u4.z, u4.w};
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          const int k = 4 * k4 + i;
+          if (k == 0) continue;
+#pragma unroll
+          for (int q = 0; q < RPT; q++)
+            if (act[q]) v[q][k] = fmaf(-lq[q], uk[i], v[q][k]);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < RPT; q++) {
+        // rotate: the next column comes to slot 0, the finished value to the end
+        const float t = v[q][0];
+#pragma unroll
+        for (int k = 0; k < CW - 1; k++) v[q][k] = v[q][k + 1];
+        v[q][CW - 1] = t;
+      }
+      if (g == 0 && tid == 0) {
+        p.ipiv[j] = piv;
+        s_pivs[c] = piv;
+      }
+      return true;
+    }
     float uu[CW];
 #pragma unroll
     for (int k = 0; k < CW; k++) uu[k] = urow[k];
-    const float d = ROT ? uu[0] : pick(uu, cur);
+    const float d = pick(uu, cur);
     const float sc = d != 0.f ? 1.f / d : 1.f;
 #pragma unroll
     for (int q = 0; q < RPT; q++) {
