@@ -194,6 +194,9 @@ la_status launch_panel_cluster_f32(la_ctx ctx, float* A, size_t ld, int m, int j
                                    int* d_ipiv);
 la_status launch_trsm_rowpanel_f32(la_ctx ctx, float* A, size_t ld, int j0, int jb, int c_begin,
                                    int c_end);
+// X = L11^-1 X for rows [j0, j0 + jbo) (jbo <= 256) of columns [c_begin, c_end).
+la_status launch_trsm_block_f32(la_ctx ctx, float* A, size_t ld, int j0, int jbo, int c_begin,
+                                int c_end);
 la_status launch_gemm_f32(la_ctx ctx, int mode, int M, int N, int K, const float* A, size_t lda,
                           const float* B, size_t ldb, float* C, size_t ldc);
 la_status launch_lu_solve_f32(la_ctx ctx, const float* LU, size_t ld, float* X, size_t ldx, int n,

@@ -159,6 +159,77 @@ trsm_rowpanel_reg_kernel(float* A, size_t ld, int j0, int jb, int c_begin, int c
 // ---- after the factorization: permutation vector, sign, zero diagonal ------
 // The swap list (LAPACK ipiv form) is replayed in order on a permutation
 // vector (lu.rs:147-149), the sign flips once per real swap (lu.rs:151), and
+// ---- the mixed LU's outer-panel triangular update: X = L11^-1 X ----------------------
+// Rows [j0, j0 + jbo) (jbo <= 256) of columns [c_begin, c_end), L11 the unit
+// lower jbo x jbo block of A at (j0, j0). One CTA per 32 columns keeps its
+// jbo x 32 block of X in shared memory. Per 32-row block of L11: the block's
+// rows and everything below it in its 32 columns are staged in shared memory;
+// warp 0 solves the diagonal block (lane = column, the 32 values in registers,
+// no barrier inside); then the 256 threads subtract the block's contribution
+// from the rows below (8 threads per row, 4 columns each, 32-deep dot products
+// from shared memory). One launch instead of a row-panel solve and a GEMM per
+// 32 rows.
+constexpr int TB_R = 256, TB_C = 32;
+constexpr size_t TB_SMEM = (size_t)2 * TB_R * (TB_C + 1) * sizeof(float);
+__global__ void __launch_bounds__(256)
+trsm_block_kernel(float* A, size_t ld, int j0, int jbo, int c_begin, int c_end) {
+  extern __shared__ __align__(16) float tb_sm[];
+  float(*X)[TB_C + 1] = reinterpret_cast<float(*)[TB_C + 1]>(tb_sm);
+  float(*Lb)[TB_C + 1] = reinterpret_cast<float(*)[TB_C + 1]>(tb_sm + TB_R * (TB_C + 1));
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int cb = c_begin + blockIdx.x * TB_C;
+  for (int idx = tid; idx < jbo * TB_C; idx += 256) {
+    const int r = idx / TB_C, c = idx % TB_C;
+    X[r][c] = cb + c < c_end ? A[(size_t)(j0 + r) * ld + cb + c] : 0.f;
+  }
+  for (int kb = 0; kb < jbo; kb += TB_C) {
+    const int bw = min(TB_C, jbo - kb);
+    // L11 rows [kb, jbo) of columns [kb, kb + bw)
+    for (int idx = tid; idx < (jbo - kb) * TB_C; idx += 256) {
+      const int r = idx / TB_C, k = idx % TB_C;
+      Lb[r][k] = k < bw ? A[(size_t)(j0 + kb + r) * ld + j0 + kb + k] : 0.f;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      float x[TB_C];
+#pragma unroll
+      for (int i = 0; i < TB_C; i++) x[i] = i < bw ? X[kb + i][lane] : 0.f;
+#pragma unroll
+      for (int k = 0; k < TB_C; k++) {
+        if (k >= bw) break;
+        const float xk = x[k];
+#pragma unroll
+        for (int i = k + 1; i < TB_C; i++) x[i] = fmaf(-Lb[i][k], xk, x[i]);
+      }
+#pragma unroll
+      for (int i = 0; i < TB_C; i++)
+        if (i < bw) X[kb + i][lane] = x[i];
+    }
+    __syncthreads();
+    const int rows = jbo - kb - bw;
+    for (int e = tid; e < rows * 8; e += 256) {
+      const int r = e >> 3, c4 = (e & 7) * 4, i = kb + bw + r;
+      float a0 = X[i][c4], a1 = X[i][c4 + 1], a2 = X[i][c4 + 2], a3 = X[i][c4 + 3];
+      for (int k = 0; k < bw; k++) {
+        const float l = Lb[bw + r][k];
+        a0 = fmaf(-l, X[kb + k][c4], a0);
+        a1 = fmaf(-l, X[kb + k][c4 + 1], a1);
+        a2 = fmaf(-l, X[kb + k][c4 + 2], a2);
+        a3 = fmaf(-l, X[kb + k][c4 + 3], a3);
+      }
+      X[i][c4] = a0;
+      X[i][c4 + 1] = a1;
+      X[i][c4 + 2] = a2;
+      X[i][c4 + 3] = a3;
+    }
+    __syncthreads();
+  }
+  for (int idx = tid; idx < jbo * TB_C; idx += 256) {
+    const int r = idx / TB_C, c = idx % TB_C;
+    if (cb + c < c_end) A[(size_t)(j0 + r) * ld + cb + c] = X[r][c];
+  }
+}
+
 // U's diagonal is scanned for an exact zero (lu.rs:177).
 template <typename T>
 __global__ void lu_finish_kernel(const int* __restrict__ ipiv, uint64_t* piv, int m, int kmin,
@@ -318,6 +389,22 @@ la_status launch_laswp(la_ctx ctx, bool exact, double* A, double* S, size_t ld, 
 la_status launch_laswp_f32(la_ctx ctx, float* A, size_t ld, int n, int j0, int jb) {
   return launch_laswp_t<float>(ctx, ctx->stream, false, A, nullptr, ld, n, j0, jb);
 }
+la_status launch_trsm_block_f32(la_ctx ctx, float* A, size_t ld, int j0, int jbo, int c_begin,
+                                int c_end) {
+  if (c_end <= c_begin || jbo <= 0) return LA_OK;
+  if (jbo > TB_R) return LA_INVALID;
+  static la_device_once once;
+  LA_CUDA(ctx, once.run([](int) {
+            return cudaFuncSetAttribute(trsm_block_kernel,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)TB_SMEM);
+          }));
+  trsm_block_kernel<<<(c_end - c_begin + TB_C - 1) / TB_C, 256, TB_SMEM, ctx->stream>>>(
+      A, ld, j0, jbo, c_begin, c_end);
+  ctx->launches++;
+  return la_check_launch(ctx, "trsm_block_kernel");
+}
+
 la_status launch_laswp_seq_f32(la_ctx ctx, float* A, size_t ld, const int* ipiv, int k0, int k1,
                                int c0, int c1) {
   if (k1 <= k0 || c1 <= c0) return LA_OK;

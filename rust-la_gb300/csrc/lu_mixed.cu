@@ -432,8 +432,10 @@ la_status mixed_factor(la_ctx ctx, la_lu h, int prec) {
     ctx->stream = saved;
     return st;
   };
-  // U12 = L11^-1 A12 for rows [j0, j1o) on columns [c0, c1), blocked by WI.
+  // U12 = L11^-1 A12 for rows [j0, j1o) on columns [c0, c1): one blocked
+  // launch (the outer panel is at most 256 rows).
   auto outer_trsm = [&](int j0, int j1o, int c0, int c1) -> la_status {
+    if (j1o - j0 <= 256) return launch_trsm_block_f32(ctx, A, ld, j0, j1o - j0, c0, c1);
     for (int i0 = j0; i0 < j1o; i0 += WI) {
       const int ib = std::min(WI, j1o - i0);
       const int i1 = i0 + ib;
