@@ -472,9 +472,10 @@ def run_mixed(la_gpu, torch, ctx, n, nrhs=4, kappas=(1e2, 1e6, 1e10), precs=(1, 
                       "untimed run (plain FP64: median of 3)" % reps,
             "auto_by_kappa": {("%.0e" % k): v for k, v in auto_by_kappa.items()},
             "speedup_vs_plain_fp64": speed,
-            "speedup_basis": "la_lu_solve_auto_device (precision chosen at run time, not after "
-                             "the fact) against the plain FP64 LU + solve, device time of "
-                             "factor + solve",
+            "speedup_basis": "la_lu_solve_auto_device (split-FP16 factors with refinement and "
+                             "GMRES-IR, the plain FP64 LU where they do not reach tol; nothing "
+                             "chosen after the fact) against the plain FP64 LU + solve, device "
+                             "time of factor + solve",
             "max_eta": max([r["eta"] for r in results if r["converged"]] +
                            [v["eta"] for v in auto_by_kappa.values()] + [plain_eta]),
             "plain_fp64": plain, "runs": results,

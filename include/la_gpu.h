@@ -225,13 +225,12 @@ la_status la_lu_solve_refined_device(la_lu lu, const double* d_b, size_t ldb, si
                                      double* d_x, size_t ldx, int max_iters, double tol,
                                      la_refine_stats* stats);
 /* Solves A X = B (A n x n FP64 on the device, B and X n x nrhs, nrhs <= 16)
- * to a normwise backward error <= tol with the cheapest factorization that
- * gets there: (1) the mixed LU with FP16 trailing updates and plain iterative
- * refinement, at most 10 steps, given up as soon as refinement stalls;
- * (2) the mixed LU with FP32 trailing updates, refinement and GMRES-IR, at
- * most 40 steps; (3) the plain FP64 LU and solve (LUDecomposition::new +
- * solve, lu.rs:104-278), which answers whatever (1) and (2) could not.
- * stats->precision is LA_PREC_FP16, LA_PREC_FP32 or 0 (plain FP64, then
+ * to a normwise backward error <= tol: (1) the mixed LU with split-FP16
+ * trailing updates (LA_PREC_FP16X3: FP32-quality factors at the FP16
+ * update's cost), plain refinement and then GMRES-IR, at most 40 steps;
+ * (2) the plain FP64 LU and solve (LUDecomposition::new + solve,
+ * lu.rs:104-278), which answers whatever (1) could not.
+ * stats->precision is LA_PREC_FP16X3 or 0 (plain FP64, then
  * stats->fell_back = 1), stats->iterations the refinement steps of all stages
  * and stats->eta the final backward error. LA_SINGULAR only when the plain
  * FP64 LU has an exact zero pivot (the reference's None). No reference

@@ -25,8 +25,9 @@
 // current column is always slot 0 and the update is 31 FMAs with fixed
 // register indices; the finished values collect at the end of the window, and
 // the published pivot row carries zeros there so that the update leaves them
-// unchanged (with 4 rows the rotation would not fit the register budget, and
-// the current column is picked by selects). Per column: the warp's
+// unchanged. The column loop is not unrolled (an unrolled 32-column body with
+// 4 rows per thread outgrew the instruction cache), and the pivot row streams
+// from shared memory into the update. Per column: the warp's
 // best (key, position) is one 64-bit word (key high, bit-inverted position
 // low, so the integer maximum is the reference's first maximum), the winning
 // lane of each warp publishes its row, one CTA barrier, and warp 0 pushes the
@@ -270,18 +271,9 @@ __device__ __forceinline__ void st_async_v4(uint32_t dst, uint32_t bar, uint32_t
       : "memory");
 }
 
-// x = v[c] for a runtime c with compile-time register indices.
-__device__ __forceinline__ float pick(const float (&v)[CW], int c) {
-  float x = v[0];
-#pragma unroll
-  for (int k = 1; k < CW; k++) x = k == c ? v[k] : x;
-  return x;
-}
-
 // One column of panel_cluster_reg_kernel (see there); false when a wait gave
-// up. ROT: the rows' register windows rotate (current column in slot 0);
-// otherwise the column is picked by selects, which the caller unrolls.
-template <int RPT, bool ROT>
+// up. The rows' register windows rotate: the current column is slot 0.
+template <int RPT>
 __device__ __forceinline__ bool panel_column(int c, const ClusterPanelArgs& p, int g, int C,
                                              int tid, int lane, int warp, float (&v)[RPT][CW],
                                              int (&pos)[RPT], float (*wrow)[PNW][CW],
@@ -291,7 +283,6 @@ __device__ __forceinline__ bool panel_column(int c, const ClusterPanelArgs& p, i
   constexpr int NW = PNW;
   constexpr uint32_t SLOT_BYTES = PSLOT * 4;
     const int j = p.j0 + c, par = c & 1;
-    const int cur = ROT ? 0 : c;  // slot of the current column
     // 1. this thread's and this warp's best candidate
     unsigned long long best = 0ull;
     int bq = 0;
@@ -299,7 +290,7 @@ __device__ __forceinline__ bool panel_column(int c, const ClusterPanelArgs& p, i
     for (int q = 0; q < RPT; q++)
       if (pos[q] >= j) {
         const unsigned long long pk =
-            ((unsigned long long)ckey(ROT ? v[q][0] : pick(v[q], c), pos[q], j) << 32) |
+            ((unsigned long long)ckey(v[q][0], pos[q], j) << 32) |
             (unsigned)(~pos[q]);
         if (pk > best) { best = pk; bq = q; }
       }
@@ -318,7 +309,7 @@ __device__ __forceinline__ bool panel_column(int c, const ClusterPanelArgs& p, i
       for (int q = 0; q < RPT; q++)
         if (q == bq) {
 #pragma unroll
-          for (int k = 0; k < CW; k++) dst[k] = (!ROT || k < CW - c) ? v[q][k] : 0.f;
+          for (int k = 0; k < CW; k++) dst[k] = k < CW - c ? v[q][k] : 0.f;
         }
     }
     if (lane == 0) wkey[par][warp] = wb;
@@ -368,7 +359,7 @@ __device__ __forceinline__ bool panel_column(int c, const ClusterPanelArgs& p, i
     const int gsrc = __ffs(gmask) - 1;  // the row at position j is a candidate: gm != 0
     const int piv = (int)(~(unsigned)(gm & 0xffffffffull));
     const float* urow = reinterpret_cast<const float*>(&recv[par][gsrc][4]);
-    if constexpr (ROT) {
+    {
       // The pivot row streams from shared memory in float4 chunks, each chunk
       // applied to all of this thread's rows (4 registers for it, not 32).
       const float d = urow[0];
@@ -412,45 +403,6 @@ __device__ __forceinline__ bool panel_column(int c, const ClusterPanelArgs& p, i
         p.ipiv[j] = piv;
         s_pivs[c] = piv;
       }
-      return true;
-    }
-    float uu[CW];
-#pragma unroll
-    for (int k = 0; k < CW; k++) uu[k] = urow[k];
-    const float d = pick(uu, cur);
-    const float sc = d != 0.f ? 1.f / d : 1.f;
-#pragma unroll
-    for (int q = 0; q < RPT; q++) {
-      if (pos[q] == piv) {
-        pos[q] = j;  // the pivot row; it keeps its values
-      } else {
-        if (pos[q] == j) pos[q] = piv;  // the displaced row takes the pivot's place
-        if (pos[q] > j) {
-          if constexpr (ROT) {
-            const float l = d != 0.f ? v[q][0] * sc : v[q][0];
-            v[q][0] = l;
-#pragma unroll
-            for (int k = 1; k < CW; k++) v[q][k] = fmaf(-l, uu[k], v[q][k]);
-          } else {
-            const float x = pick(v[q], c);
-            const float l = d != 0.f ? x * sc : x;
-#pragma unroll
-            for (int k = 0; k < CW; k++)
-              v[q][k] = k == c ? l : (k > c ? fmaf(-l, uu[k], v[q][k]) : v[q][k]);
-          }
-        }
-      }
-      if constexpr (ROT) {
-        // rotate: the next column comes to slot 0, the finished value to the end
-        const float t = v[q][0];
-#pragma unroll
-        for (int k = 0; k < CW - 1; k++) v[q][k] = v[q][k + 1];
-        v[q][CW - 1] = t;
-      }
-    }
-    if (g == 0 && tid == 0) {
-      p.ipiv[j] = piv;
-      s_pivs[c] = piv;
     }
   return true;
 }
@@ -504,35 +456,21 @@ __global__ void __launch_bounds__(CT, 1) panel_cluster_reg_kernel(ClusterPanelAr
   }
   cluster_sync();  // every CTA's receive barriers are initialised before any push
 
-  // Register windows rotate for up to 2 rows per thread; with 4 the rotation
-  // would exceed the register budget, so the current column is picked by
-  // selects and the update is predicated per slot.
-  constexpr bool ROT = RPT <= 2;
+  // The register windows rotate for every row count: an unrolled 32-column
+  // body with static register indices (4 rows per thread) outgrew the
+  // instruction cache and stalled on instruction fetch; the rotating loop
+  // stays in cache even where it spills a little at 4 rows per thread.
   bool ok = true;
-  if constexpr (ROT) {
-    for (int c = 0; c < jb; c++)
-      if (!panel_column<RPT, true>(c, p, g, C, tid, lane, warp, v, pos, wrow, wkey, recv, rbar,
-                                   s_pivs)) {
-        ok = false;
-        break;
-      }
-  } else {
-    // unrolled over the 32 columns: every register index is static
-#pragma unroll
-    for (int c = 0; c < CW; c++) {
-      if (c >= jb) break;
-      if (!panel_column<RPT, false>(c, p, g, C, tid, lane, warp, v, pos, wrow, wkey, recv, rbar,
-                                    s_pivs)) {
-        ok = false;
-        break;
-      }
+  for (int c = 0; c < jb; c++)
+    if (!panel_column<RPT>(c, p, g, C, tid, lane, warp, v, pos, wrow, wkey, recv, rbar,
+                           s_pivs)) {
+      ok = false;
+      break;
     }
-  }
   cluster_sync();  // no CTA leaves while pushes into its shared memory may be in flight
   if (!ok) return;
   // jb rotations so far; 32 in all bring every value back to its column
-  if (ROT)
-    for (int r = jb; r < CW; r++)
+  for (int r = jb; r < CW; r++)
 #pragma unroll
     for (int q = 0; q < RPT; q++) {
       const float t = v[q][0];

@@ -14,11 +14,11 @@
 // target column, each walking the rows in the reference's order with unfused
 // products and sums, so the factors, Q and the solution are bit-identical to
 // the reference; the column norm is one thread's ascending sum.
-// FAST: qr_reflect_fast_kernel, 16 target columns per CTA and 16 row slots
-// (coalesced 128-byte row segments), the dot products reduced across the row
-// slots in shared memory, then the update with FMA; in the factorization the
-// CTA that holds the next column also takes that column's norm and diagonal
-// once its update is done, so each column costs one launch. The back-substitution of solve is the wavefront
+// FAST: qr_reflect_fast_kernel, 4 target columns per CTA and 64 row slots
+// (many CTAs per SM, short dependent chains), the dot products reduced by warp
+// shuffles and across warps, then the update with FMA; in the factorization
+// the CTA that holds the next column also takes that column's norm and
+// diagonal once its update is done, so each column costs one launch. The back-substitution of solve is the wavefront
 // upper solve on R (the reference's descending term order, then the division
 // by rdiag). The reflections are sequential by nature (each depends on the
 // last); the work per step is spread over the columns.
@@ -118,19 +118,24 @@ __global__ void qr_reflect_kernel(const double* U, size_t ldu, int ucol, int r0,
 }
 
 // FAST form of qr_reflect_kernel (same modes and denominators): CTA b takes
-// columns [c0 + 16 b, c0 + 16 b + 16) of T; thread (s, c) = (tid / 16, tid % 16)
-// walks rows r0 + s, r0 + s + 16, ... of its column. When next >= 0
+// columns [c0 + 4 b, c0 + 4 b + 4) of T; thread (s, c) = (tid / 4, tid % 4)
+// walks rows r0 + s, r0 + s + 64, ... of its column, four rows per step with
+// their loads issued together. Narrow column tiles give many CTAs per SM and
+// short dependent chains (the products are cheap, the L2 latency is not); the
+// 64 partial dot products of a column are combined by shuffles within each
+// warp (its 8 row slots) and then across the 8 warps. When next >= 0
 // (factorization) the CTA that holds column `next` then takes its norm over
 // rows [next, m), a = -/+ sqrt, rdiag[next] = a and the diagonal entry minus a
 // (qr.rs:49-76 for the next step), so every column costs one launch.
-constexpr int RF_C = 16, RF_R = 16;  // 256 threads
+constexpr int RF_C = 4, RF_R = 64;  // 256 threads
 __global__ void __launch_bounds__(RF_C * RF_R)
 qr_reflect_fast_kernel(const double* U, size_t ldu, int ucol, int r0, int m, double* rdiag,
                        double* T, size_t ldt, int c0, int c1, int mode, int next) {
-  __shared__ double red[RF_R][RF_C + 1];
+  __shared__ double red[8][RF_C];
   __shared__ double fac[RF_C];
-  __shared__ double nred[RF_C * RF_R / 32];
+  __shared__ double nred[8];
   const int tid = threadIdx.x, cl = tid % RF_C, rs = tid / RF_C;
+  const int lane = tid & 31, warp = tid >> 5;
   const int cb = c0 + blockIdx.x * RF_C;
   const int c = cb + cl;
   const double u0 = U[(size_t)r0 * ldu + ucol];
@@ -148,24 +153,57 @@ qr_reflect_fast_kernel(const double* U, size_t ldu, int ucol, int r0, int m, dou
   }
   if (!skip) {
     double dot = 0.0;
-    if (c < c1)
-      for (int row = r0 + rs; row < m; row += RF_R)
-        dot = fma(U[(size_t)row * ldu + ucol], T[(size_t)row * ldt + c], dot);
-    red[rs][cl] = dot;
+    if (c < c1) {
+      int row = r0 + rs;
+      for (; row + 3 * RF_R < m; row += 4 * RF_R) {
+        const double ua = U[(size_t)row * ldu + ucol], ub = U[(size_t)(row + RF_R) * ldu + ucol];
+        const double uc = U[(size_t)(row + 2 * RF_R) * ldu + ucol];
+        const double ud = U[(size_t)(row + 3 * RF_R) * ldu + ucol];
+        const double ta = T[(size_t)row * ldt + c], tb = T[(size_t)(row + RF_R) * ldt + c];
+        const double tc = T[(size_t)(row + 2 * RF_R) * ldt + c];
+        const double td = T[(size_t)(row + 3 * RF_R) * ldt + c];
+        dot = fma(ua, ta, dot);
+        dot = fma(ub, tb, dot);
+        dot = fma(uc, tc, dot);
+        dot = fma(ud, td, dot);
+      }
+      for (; row < m; row += RF_R) dot = fma(U[(size_t)row * ldu + ucol], T[(size_t)row * ldt + c], dot);
+    }
+    // the 8 row slots of a column within a warp (lanes cl, cl + 4, ..., cl + 28)
+    dot += __shfl_xor_sync(0xffffffffu, dot, 4);
+    dot += __shfl_xor_sync(0xffffffffu, dot, 8);
+    dot += __shfl_xor_sync(0xffffffffu, dot, 16);
+    if (lane < RF_C) red[warp][lane] = dot;
     __syncthreads();
-    if (rs == 0) {
-      double s = 0.0;
+    if (tid < RF_C) {
+      double sum = 0.0;
 #pragma unroll
-      for (int r = 0; r < RF_R; r++) s += red[r][cl];
-      fac[cl] = s / den;
+      for (int w = 0; w < 8; w++) sum += red[w][tid];
+      fac[tid] = sum / den;
     }
     __syncthreads();
     const double f = fac[cl];
-    if (c < c1)
-      for (int row = r0 + rs; row < m; row += RF_R) {
+    if (c < c1) {
+      int row = r0 + rs;
+      for (; row + 3 * RF_R < m; row += 4 * RF_R) {
+        double* ta = T + (size_t)row * ldt + c;
+        double* tb = T + (size_t)(row + RF_R) * ldt + c;
+        double* tc = T + (size_t)(row + 2 * RF_R) * ldt + c;
+        double* td = T + (size_t)(row + 3 * RF_R) * ldt + c;
+        const double ua = U[(size_t)row * ldu + ucol], ub = U[(size_t)(row + RF_R) * ldu + ucol];
+        const double uc = U[(size_t)(row + 2 * RF_R) * ldu + ucol];
+        const double ud = U[(size_t)(row + 3 * RF_R) * ldu + ucol];
+        const double va = *ta, vb = *tb, vc = *tc, vd = *td;
+        *ta = fma(f, ua, va);
+        *tb = fma(f, ub, vb);
+        *tc = fma(f, uc, vc);
+        *td = fma(f, ud, vd);
+      }
+      for (; row < m; row += RF_R) {
         double* t = T + (size_t)row * ldt + c;
         *t = fma(f, U[(size_t)row * ldu + ucol], *t);
       }
+    }
   }
   if (next >= 0 && next >= cb && next < cb + RF_C) {
     __syncthreads();  // this CTA's updates of column `next` are visible to the block
@@ -176,11 +214,11 @@ qr_reflect_fast_kernel(const double* U, size_t ldu, int ucol, int r0, int m, dou
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
-    if ((tid & 31) == 0) nred[tid >> 5] = x;
+    if (lane == 0) nred[warp] = x;
     __syncthreads();
     if (tid == 0) {
       double t = 0.0;
-      for (int w = 0; w < RF_C * RF_R / 32; w++) t += nred[w];
+      for (int w = 0; w < 8; w++) t += nred[w];
       const double q = T[(size_t)next * ldt + next];
       const double a = q > 0.0 ? -sqrt(t) : sqrt(t);
       rdiag[next] = a;

@@ -46,7 +46,7 @@ def labelled_chunk(ctx, count, seed, ctas, warps):
     feats = S.features(ctx, systems, da)
     cyc, conv = S.measure_costs(ctx, systems, da, db, dx, ctas_per_sm=ctas,
                                 warps_per_system=warps)
-    cyc64 = S.fp64_costs(ctx, systems, da, db, dx, ctas_per_sm=ctas, warps_per_system=warps)
+    cyc64 = S.fp64_costs(ctx, systems, da, db, dx)
     out = (systems, da, db, dx, kappa, feats, cyc, conv, cyc64)
     return out
 

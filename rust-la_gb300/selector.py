@@ -89,9 +89,10 @@ def measure_costs(ctx, systems, da, db, dx, ctas_per_sm=2, warps_per_system=8, t
     return cyc, conv
 
 
-def fp64_costs(ctx, systems, da, db, dx, ctas_per_sm=2, warps_per_system=8):
+def fp64_costs(ctx, systems, da, db, dx, ctas_per_sm=1, warps_per_system=8):
     """SM cycles per system of the plain FP64 plan (the cost of sending a
-    system straight to the FP64 pass)."""
+    system straight to the FP64 pass). One 8-warp CTA per SM: a system of
+    n = 512 in FP64 needs a whole SM's shared memory."""
     plan = la_gpu.BatchPlan(ctx, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems,
                             la_gpu.BATCH_FP64, ctas_per_sm=ctas_per_sm,
                             warps_per_system=warps_per_system)

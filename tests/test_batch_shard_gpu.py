@@ -29,8 +29,9 @@ def test_slices_reproduce_the_single_plan(lagpu, ctx_fast, torch, mode, parts):
             da[d] += 0.5 * s.n
     x1 = torch.zeros(nb, dtype=torch.float64, device="cuda")
     torch.cuda.synchronize()
+    warps = 4 if mode == 0 else 8  # two FP64 CTAs of 8 warps do not fit an SM at n = 256
     plan = lagpu.BatchPlan(ctx_fast, da.data_ptr(), db.data_ptr(), x1.data_ptr(), systems, mode,
-                           ctas_per_sm=2, warps_per_system=8, tol=5e-15)
+                           ctas_per_sm=2, warps_per_system=warps, tol=5e-15)
     plan.run()
     plan.free()
     xs = torch.zeros(nb, dtype=torch.float64, device="cuda")
@@ -39,7 +40,7 @@ def test_slices_reproduce_the_single_plan(lagpu, ctx_fast, torch, mode, parts):
         sl, a0, alen, b0, blen = lagpu.batch_slice(systems, bounds[p], bounds[p + 1])
         va, vb, vx = da[a0:a0 + alen], db[b0:b0 + blen], xs[b0:b0 + blen]
         pp = lagpu.BatchPlan(ctx_fast, va.data_ptr(), vb.data_ptr(), vx.data_ptr(), sl, mode,
-                             ctas_per_sm=2, warps_per_system=8, tol=5e-15)
+                             ctas_per_sm=2, warps_per_system=warps, tol=5e-15)
         pp.run()
         pp.free()
     torch.cuda.synchronize()

@@ -87,7 +87,7 @@ st, stats = la_gpu.lu_solve_refined_device(lm, tb.data_ptr(), 2, 2, tx.data_ptr(
 out["after_stall_status"] = st
 out["after_stall_eta"] = stats.eta
 lm.free()
-ctx.set_option(la_gpu.OPT_INJECT_IR_STALL, 2)  # the FP16 and the FP32 stage both stall
+ctx.set_option(la_gpu.OPT_INJECT_IR_STALL, 1)  # the split-FP16 stage stalls
 st, stats = la_gpu.lu_solve_auto_device(ctx, ta.data_ptr(), m, m, tb.data_ptr(), 2, 2,
                                         tx.data_ptr(), 2, tol=5e-15)
 out["auto_status"] = st

@@ -183,13 +183,13 @@ def test_cluster_and_cooperative_fp32_panels_agree(lagpu, torch, n):
     assert np.array_equal(outs[0], outs[1])
 
 
-@pytest.mark.parametrize("kappa,scale,want", [(1e2, 1.0, (2,)), (1e10, 1.0, (2, 3)),
+@pytest.mark.parametrize("kappa,scale,want", [(1e2, 1.0, (6,)), (1e10, 1.0, (6,)),
                                                (1e2, 1e40, (0,))],
                          ids=["kappa1e2", "kappa1e10", "fp32-overflow"])
 def test_auto_precision_cascade(lagpu, ctx_fast, torch, kappa, scale, want):
-    # FP16 factors where they refine to tol; FP16 or FP32 factors (GMRES-IR)
-    # at kappa 1e10; the plain FP64 LU where no FP32 copy of A exists (entries
-    # 1e40 overflow FP32); every answer at eta <= 1e-14.
+    # Split-FP16 factors (refinement, then GMRES-IR at kappa 1e10); the plain
+    # FP64 LU where no FP32 copy of A exists (entries 1e40 overflow FP32);
+    # every answer at eta <= 1e-14.
     n = 1024
     a = _hh(torch, n, kappa, 17) * scale
     rng = np.random.default_rng(18)
