@@ -194,6 +194,12 @@ la_status launch_panel_cluster_f32(la_ctx ctx, float* A, size_t ld, int m, int j
                                    int* d_ipiv);
 la_status launch_trsm_rowpanel_f32(la_ctx ctx, float* A, size_t ld, int j0, int jb, int c_begin,
                                    int c_end);
+// After an inner panel [i0, i0 + ib): U12 = L11^-1 A12 and A22 -= L21 U12 on the
+// columns [i0 + ib, j1o) (at most 224 of them; LA_UNSUPPORTED beyond). d_count:
+// a device word that is zero at the first launch (the kernel leaves it zero);
+// launches that share it must not overlap.
+la_status launch_panel_update_f32(la_ctx ctx, float* A, size_t ld, int m, int i0, int ib,
+                                  int j1o, unsigned* d_count);
 // X = L11^-1 X for rows [j0, j0 + jbo) (jbo <= 256) of columns [c_begin, c_end).
 la_status launch_trsm_block_f32(la_ctx ctx, float* A, size_t ld, int j0, int jbo, int c_begin,
                                 int c_end);

@@ -406,6 +406,9 @@ la_status mixed_factor(la_ctx ctx, la_lu h, int prec) {
   }
   LA_TRY(stat.alloc(256));
   float* d_stat = stat.as<float>();
+  // [0] max |U12|, [1] alpha of the current update, [32] the inner-panel
+  // update's arrival count (zero between launches)
+  LA_CUDA(ctx, cudaMemsetAsync(d_stat, 0, 256, ms));
 
   // Inner panels of the outer panel [j0, j1o) on stream s; row swaps on the
   // columns < climit only.
@@ -423,10 +426,14 @@ la_status mixed_factor(la_ctx ctx, la_lu h, int prec) {
       if (st == LA_UNSUPPORTED) st = launch_panel_f32(ctx, s, A, ld, m, i0, ib, h->d_ipiv, &bar_base);
       if (st == LA_OK) st = launch_laswp_f32(ctx, A, ld, climit, i0, ib);
       if (st == LA_OK && i1 < j1o) {
-        st = launch_trsm_rowpanel_f32(ctx, A, ld, i0, ib, i1, j1o);
-        if (st == LA_OK && i1 < m)
-          st = launch_gemm_f32(ctx, GM_FMA_SUB, m - i1, j1o - i1, ib, A + (size_t)i1 * ld + i0, ld,
-                               A + (size_t)i0 * ld + i1, ld, A + (size_t)i1 * ld + i1, ld);
+        st = launch_panel_update_f32(ctx, A, ld, m, i0, ib, j1o,
+                                     reinterpret_cast<unsigned*>(d_stat + 32));
+        if (st == LA_UNSUPPORTED) {
+          st = launch_trsm_rowpanel_f32(ctx, A, ld, i0, ib, i1, j1o);
+          if (st == LA_OK && i1 < m)
+            st = launch_gemm_f32(ctx, GM_FMA_SUB, m - i1, j1o - i1, ib, A + (size_t)i1 * ld + i0,
+                                 ld, A + (size_t)i0 * ld + i1, ld, A + (size_t)i1 * ld + i1, ld);
+        }
       }
     }
     ctx->stream = saved;
