@@ -382,11 +382,12 @@ la_status la_mlp_train_step(la_mlp mlp, const float* d_x, const int* d_y, int co
  * (d_class, may be NULL; 3 where the gate below sends the system straight to
  * the FP64 pass); asynchronous on the context's stream. */
 la_status la_mlp_predict(la_mlp mlp, const float* d_x, int count, float* d_probs, int* d_class);
-/* Gate of la_mlp_predict's classes: a system whose FP32-class probability is
- * at least p_min and whose raw (unnormalised) feature `feature` is at least
- * feature_min gets class 3, no mixed attempt (la_batch_plan_select_device sends
- * it straight to the FP64 pass). feature < 0 turns the gate off (the default). */
-la_status la_mlp_set_gate(la_mlp mlp, float p_min, int feature, float feature_min);
+/* Gate of la_mlp_predict's classes: with coef (19 floats) set, a system whose
+ * score coef[0..15] . x + coef[16..18] . p + bias >= 0 (x its raw, unnormalised
+ * features, p its three class probabilities) gets class 3, no mixed attempt
+ * (la_batch_plan_select_device sends it straight to the FP64 pass). coef NULL
+ * turns the gate off (the default). LA_INVALID for non-finite values. */
+la_status la_mlp_set_gate(la_mlp mlp, const float* coef, float bias);
 
 /* ---- allocation-free factorization (no reference counterpart) ------------ */
 

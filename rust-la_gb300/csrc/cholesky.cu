@@ -41,9 +41,6 @@ namespace {
 constexpr int CHW = 64;   // panel width
 constexpr int CHP = CHW + 1;
 constexpr int PANEL_T = 128;
-// Shared memory that keeps trailing-update GEMM CTAs at two per SM while a
-// panel runs beside them (room for the diagonal block's CTA).
-constexpr size_t CHOL_GEMM_SMEM_WITH_PANEL = 78 * 1024;
 
 size_t pad4c(size_t x) { return (x + 3) & ~size_t(3); }
 
@@ -232,88 +229,49 @@ la_status chol_factor(la_ctx ctx, la_chol h, int* none) {
   ctx->launches++;
   LA_TRY(la_check_launch(ctx, "chol_sym_check_kernel"));
 
-  Buf S(ctx), T0(ctx), T1(ctx);
+  // Panels and the trailing update run one after the other. A lookahead like
+  // the LU's (next panel on the side stream, the update's CTAs limited to two
+  // per SM to leave it room) measured slower at n = 8192 (253 ms against 227
+  // ms with 8 row strips; 274 against 233 ms with 16): the update loses more
+  // than the 64-column panels hide.
+  Buf S(ctx), T(ctx);
   if (exact) {
     LA_TRY(S.alloc((size_t)n * ld * sizeof(double)));
     LA_CUDA(ctx, cudaMemsetAsync(S.p, 0, (size_t)n * ld * sizeof(double), st));
   }
-  // Transposed panels (the GEMM's K x N operand), two so that panel k + 1 can
-  // be transposed while panel k's update still reads its own.
   const size_t ldt = pad4c((size_t)n);
-  if (n > CHW) {
-    LA_TRY(T0.alloc((size_t)CHW * ldt * sizeof(double)));
-    LA_TRY(T1.alloc((size_t)CHW * ldt * sizeof(double)));
-  }
-  double* Tbuf[2] = {T0.d(), T1.d()};
+  if (n > CHW) LA_TRY(T.alloc((size_t)CHW * ldt * sizeof(double)));
   const size_t dsm = (exact ? 2 : 1) * CHW * CHP * sizeof(double);
-  const bool look = ctx->lookahead != 0 && ctx->side_stream != nullptr;
-  cudaStream_t ss = look ? ctx->side_stream : st;
-
-  // Diagonal block, rows below and transpose of panel [j0, j0 + jb) on stream s.
-  auto panel = [&](int j0, int jb, double* T, cudaStream_t s) -> la_status {
-    const int j1 = j0 + jb;
+  for (int j0 = 0; j0 < n; j0 += CHW) {
+    const int jb = std::min(CHW, n - j0), j1 = j0 + jb;
     if (exact)
-      chol_diag_kernel<true><<<1, 256, dsm, s>>>(L, S.d(), ld, j0, jb, d_flags);
+      chol_diag_kernel<true><<<1, 256, dsm, st>>>(L, S.d(), ld, j0, jb, d_flags);
     else
-      chol_diag_kernel<false><<<1, 256, dsm, s>>>(L, nullptr, ld, j0, jb, d_flags);
+      chol_diag_kernel<false><<<1, 256, dsm, st>>>(L, nullptr, ld, j0, jb, d_flags);
     ctx->launches++;
     LA_TRY(la_check_launch(ctx, "chol_diag_kernel"));
-    if (j1 >= n) return LA_OK;
+    if (j1 >= n) break;
     const int rows = n - j1;
     const int pg = (rows + PANEL_T - 1) / PANEL_T;
     if (exact)
-      chol_panel_kernel<true><<<pg, PANEL_T, 0, s>>>(L, S.d(), ld, j0, j1, n);
+      chol_panel_kernel<true><<<pg, PANEL_T, 0, st>>>(L, S.d(), ld, j0, j1, n);
     else
-      chol_panel_kernel<false><<<pg, PANEL_T, 0, s>>>(L, nullptr, ld, j0, j1, n);
+      chol_panel_kernel<false><<<pg, PANEL_T, 0, st>>>(L, nullptr, ld, j0, j1, n);
     ctx->launches++;
     LA_TRY(la_check_launch(ctx, "chol_panel_kernel"));
-    chol_transpose_kernel<<<dim3((rows + 31) / 32, (jb + 31) / 32), dim3(32, 8), 0, s>>>(
-        L, ld, j0, jb, j1, rows, T, ldt);
+    chol_transpose_kernel<<<dim3((rows + 31) / 32, (jb + 31) / 32), dim3(32, 8), 0, st>>>(
+        L, ld, j0, jb, j1, rows, T.d(), ldt);
     ctx->launches++;
-    return la_check_launch(ctx, "chol_transpose_kernel");
-  };
-  // A22 -= L21 L21' (EXACT: S22 += ...) of panel [j0, j0 + jb) on the columns
-  // [c0, c1) of rows [c0, n), in row strips [a, b) that each stop at their own
-  // diagonal block (columns [c0, min(b, c1))): about 1/nstrip of the square's
-  // flops are spent above the diagonal.
-  auto update = [&](int j0, int jb, const double* T, int c0, int c1, size_t min_smem) -> la_status {
-    const int j1 = j0 + jb, rows = n - c0;
-    if (rows <= 0 || c1 <= c0) return LA_OK;
-    const int nstrip = std::max(1, std::min(16, rows / 512));
+    LA_TRY(la_check_launch(ctx, "chol_transpose_kernel"));
+    // Row strips [a, b) of the trailing matrix, each updated on columns
+    // [j1, b): its own diagonal block and everything left of it.
+    const int nstrip = std::max(1, std::min(8, rows / 512));
     const int hs = ((rows + nstrip - 1) / nstrip + CHW - 1) / CHW * CHW;
-    for (int a = c0; a < n; a += hs) {
+    for (int a = j1; a < n; a += hs) {
       const int b = std::min(n, a + hs);
-      const int ce = std::min(b, c1);
-      double* C = (exact ? S.d() : L) + (size_t)a * ld + c0;
-      LA_TRY(launch_gemm(ctx, exact ? GM_EXACT_ADD : GM_FMA_SUB, b - a, ce - c0, jb,
-                         L + (size_t)a * ld + j0, ld, T + (c0 - j1), ldt, C, ld, min_smem));
-    }
-    return LA_OK;
-  };
-
-  // Lookahead, as in the LU: panel k's update of panel k + 1's columns first,
-  // then panel k + 1 on the high-priority side stream while the rest of panel
-  // k's update runs. They touch disjoint data: panel k + 1 owns columns
-  // [j1, j2) of rows >= j1; the rest of the update writes columns >= j2 and
-  // reads panel k's (finished) columns and its transposed copy.
-  LA_TRY(panel(0, std::min(CHW, n), Tbuf[0], st));
-  for (int j0 = 0, k = 0; j0 < n; j0 += CHW, k++) {
-    const int jb = std::min(CHW, n - j0), j1 = j0 + jb;
-    if (j1 >= n) break;
-    const int jbn = std::min(CHW, n - j1), j2 = j1 + jbn;
-    double* Tk = Tbuf[k & 1];
-    double* Tn = Tbuf[(k + 1) & 1];
-    if (look) {
-      LA_TRY(update(j0, jb, Tk, j1, j2, 0));
-      LA_CUDA(ctx, cudaEventRecord(ctx->ev_fork, st));
-      LA_CUDA(ctx, cudaStreamWaitEvent(ss, ctx->ev_fork, 0));
-      LA_TRY(panel(j1, jbn, Tn, ss));
-      LA_CUDA(ctx, cudaEventRecord(ctx->ev_join, ss));
-      LA_TRY(update(j0, jb, Tk, j2, n, CHOL_GEMM_SMEM_WITH_PANEL));
-      LA_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_join, 0));
-    } else {
-      LA_TRY(update(j0, jb, Tk, j1, n, 0));
-      LA_TRY(panel(j1, jbn, Tn, st));
+      double* C = (exact ? S.d() : L) + (size_t)a * ld + j1;
+      LA_TRY(launch_gemm(ctx, exact ? GM_EXACT_ADD : GM_FMA_SUB, b - a, b - j1, jb,
+                         L + (size_t)a * ld + j0, ld, T.d(), ldt, C, ld));
     }
   }
   chol_zero_upper_kernel<<<dim3(nt, nt), dim3(32, 8), 0, st>>>(L, ld, n);

@@ -549,13 +549,15 @@ __device__ void mlp_fwd(const float* __restrict__ P, const float* x, float* h1, 
 
 // One thread per sample: normalise, forward, keep activations; with labels,
 // also the per-sample output delta and loss.
-// Gate of the class output (inference): a system whose FP32-class probability
-// is at least p_min and whose raw feature `feat` is at least feat_min gets
-// class 3 (no mixed attempt, straight to the FP64 pass); feat < 0: no gate.
+// Gate of the class output (inference): a linear score of the raw features
+// and the class probabilities, w[0..15] . x + w[16..18] . p + b; a system
+// whose score is >= 0 gets class 3 (no mixed attempt, straight to the FP64
+// pass). on = 0: no gate.
+constexpr int GATE_NCOEF = NF + NC;
 struct Gate {
-  float p_min;
-  int feat;
-  float feat_min;
+  float w[GATE_NCOEF];
+  float b;
+  int on;
 };
 
 __global__ void mlp_forward_kernel(const float* __restrict__ P, const float* __restrict__ mean,
@@ -584,8 +586,12 @@ __global__ void mlp_forward_kernel(const float* __restrict__ P, const float* __r
     int best = 0;
     for (int k = 1; k < NC; k++)
       if (pr[k] > pr[best]) best = k;
-    if (gate.feat >= 0 && pr[NC - 1] >= gate.p_min && X[(size_t)s * NF + gate.feat] >= gate.feat_min)
-      best = NC;  // straight to the FP64 pass
+    if (gate.on) {
+      float g = gate.b;
+      for (int k = 0; k < NF; k++) g = fmaf(gate.w[k], X[(size_t)s * NF + k], g);
+      for (int k = 0; k < NC; k++) g = fmaf(gate.w[NF + k], pr[k], g);
+      if (g >= 0.f) best = NC;  // straight to the FP64 pass
+    }
     cls[s] = best;
   }
   if (loss && y) loss[s] = -logf(fmaxf(pr[y[s]], 1e-30f));
@@ -665,8 +671,7 @@ struct la_mlp_s {
   float* am() { return d_params + NPARAM + 2 * NF; }
   float* av() { return am() + NPARAM; }
   float* grad() { return av() + NPARAM; }
-  float gate_p = 1.f, gate_min = 0.f;  // la_mlp_set_gate
-  int gate_feat = -1;
+  Gate gate{};  // la_mlp_set_gate (off)
 };
 
 extern "C" {
@@ -735,7 +740,7 @@ static la_status mlp_backprop(la_mlp m, const float* d_x, const int* d_y, int co
   if (s == LA_OK) {
     const int g = (count + 127) / 128;
     mlp_forward_kernel<<<g, 128, 0, ctx->stream>>>(m->P(), m->mean(), m->stdv(), d_x, count, act,
-                                                   nullptr, nullptr, d_y, dl, Gate{0.f, -1, 0.f});
+                                                   nullptr, nullptr, d_y, dl, Gate{});
     mlp_delta_kernel<<<g, 128, 0, ctx->stream>>>(m->P(), act, count, delta);
     mlp_grad_kernel<<<(NPARAM + 127) / 128, 128, 0, ctx->stream>>>(act, delta, count, m->grad());
     ctx->launches += 3;
@@ -780,12 +785,19 @@ la_status la_mlp_train_step(la_mlp m, const float* d_x, const int* d_y, int coun
   return la_check_launch(m->ctx, "adam");
 }
 
-la_status la_mlp_set_gate(la_mlp m, float p_min, int feature, float feature_min) {
-  if (!m || feature >= NF || !(p_min >= 0.f && p_min <= 1.f) || std::isnan(feature_min))
-    return LA_INVALID;
-  m->gate_p = p_min;
-  m->gate_feat = feature < 0 ? -1 : feature;
-  m->gate_min = feature_min;
+la_status la_mlp_set_gate(la_mlp m, const float* coef, float bias) {
+  if (!m) return LA_INVALID;
+  Gate g{};
+  if (coef) {
+    for (int k = 0; k < GATE_NCOEF; k++) {
+      if (!std::isfinite(coef[k])) return LA_INVALID;
+      g.w[k] = coef[k];
+    }
+    if (!std::isfinite(bias)) return LA_INVALID;
+    g.b = bias;
+    g.on = 1;
+  }
+  m->gate = g;
   return LA_OK;
 }
 
@@ -794,7 +806,7 @@ la_status la_mlp_predict(la_mlp m, const float* d_x, int count, float* d_probs, 
   LA_CUDA(m->ctx, cudaSetDevice(m->ctx->device));
   mlp_forward_kernel<<<(count + 127) / 128, 128, 0, m->ctx->stream>>>(
       m->P(), m->mean(), m->stdv(), d_x, count, nullptr, d_probs, d_class, nullptr, nullptr,
-      Gate{m->gate_p, m->gate_feat, m->gate_min});
+      m->gate);
   m->ctx->launches++;
   return la_check_launch(m->ctx, "mlp predict");
 }

@@ -2,7 +2,7 @@
 
     python rust-la_gb300/examples/train_selector.py [--train 200000] [--test 50000]
         [--out rust-la_gb300/selector_weights.npy] [--summary path.json] [--gate-only]
-        [--dump path.npz]
+        [--dump path.npz] [--gate-from path.npz]
 
 Training data: --train Householder-conditioned systems (n uniform in [16, 512],
 1-4 right-hand sides, log10 kappa_2 uniform in [1, 12]) generated on the GPU
@@ -13,10 +13,12 @@ system is the class with the fewest SM cycles spent on it, redo included. The
 MLP (16 -> 64 -> 64 -> 3) is then trained on the GPU by the library's own
 forward, backward and Adam kernels. Each chunk also runs the plain FP64 plan,
 whose per-system cycles are the cost of sending a system straight to the FP64
-pass; the gate (FP32-class probability and one feature above thresholds ->
-FP64 directly) is fitted on them and written beside the weights
+pass; the gate (straight to the FP64 pass where a linear score of the features
+and the class probabilities is >= 0, fitted by logistic regression) is fitted on
+them and written beside the weights
 (<out>.gate.json). --gate-only keeps the weights in --out and fits the gate
-alone; --dump writes the labelled training arrays.
+alone; --dump writes the labelled training arrays, and --gate-from fits the
+gate from such a dump without running the GPU labelling again.
 
 Evaluation: a separately seeded batch of --test systems. Reports the label
 accuracy, the summed per-system cycles of the selector's choices against
@@ -75,7 +77,16 @@ def main():
     ap.add_argument("--summary", default=None)
     ap.add_argument("--gate-only", action="store_true")
     ap.add_argument("--dump", default=None)
+    ap.add_argument("--gate-from", default=None)
     args = ap.parse_args()
+    if args.gate_from:  # the gate alone, from a dump of labelled data (no GPU)
+        d = np.load(args.gate_from)
+        coef, bias, gratio = S.fit_gate(d["probs"], d["feats"], d["cycles"], d["cycles64"])
+        with open(os.path.splitext(args.out)[0] + ".gate.json", "w") as fh:
+            json.dump({"coef": [float(v) for v in coef], "bias": bias}, fh, indent=1)
+        print("gate fitted: cycles x%.4f of the ungated choice on %d systems"
+              % (gratio, len(d["probs"])))
+        return
     ctx = la_gpu.Context(0)
     t_start = time.perf_counter()
 
@@ -121,10 +132,10 @@ def main():
     print("fit %.1f s, loss %s, train accuracy %.3f" % (t_fit, log, train_acc), flush=True)
     probs = sel.probs(X).cpu().numpy()
     fx = X.cpu().numpy()
-    gate = S.fit_gate(probs, fx, cyc_all, cyc64_all)
-    print("gate p_min %.2f feature %d threshold %.4g: cycles x%.3f of the ungated choice"
-          % gate, flush=True)
-    sel.set_gate(gate[0], gate[1], gate[2])
+    coef, bias, gratio = S.fit_gate(probs, fx, cyc_all, cyc64_all)
+    print("gate fitted: cycles x%.3f of the ungated choice on the training set" % gratio,
+          flush=True)
+    sel.set_gate(coef, bias)
     sel.save_gate(os.path.splitext(args.out)[0] + ".gate.json")
     if args.dump:
         np.savez_compressed(args.dump, feats=fx, labels=y, cycles=cyc_all, cycles64=cyc64_all,
@@ -186,7 +197,7 @@ def main():
         "train_accuracy": train_acc, "test_accuracy": test_acc,
         "test_label_counts": np.bincount(lab, minlength=3).tolist(),
         "test_pred_counts": np.bincount(pred, minlength=4).tolist(),
-        "gate": list(gate), "test_all_classes_fail": int((~conv.any(axis=1)).sum()),
+        "gate_train_cycle_ratio": gratio, "test_all_classes_fail": int((~conv.any(axis=1)).sum()),
         "cycles_selector_over_fp32": c_sel / c_f32, "cycles_best_over_fp32": c_best / c_f32,
         "ms_fixed_fp32": t_fixed, "ms_best_labels": t_best, "ms_features_inference": t_feat,
         "ms_selector_total": t_sel, "ms_fp64_plan": t_64, "fp64_plan": [c64, w64],

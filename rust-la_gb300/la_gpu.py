@@ -130,7 +130,7 @@ SIGNATURES = {
     "la_mlp_gradients": ([_P, _P, _P, _I, _P, _P], _I),
     "la_mlp_train_step": ([_P, _P, _P, _I, ctypes.c_float, _P], _I),
     "la_mlp_predict": ([_P, _P, _I, _P, _P], _I),
-    "la_mlp_set_gate": ([_P, ctypes.c_float, _I, ctypes.c_float], _I),
+    "la_mlp_set_gate": ([_P, _P, ctypes.c_float], _I),
 }
 
 BATCH_FP64, BATCH_MIXED = 0, 1
@@ -884,11 +884,17 @@ class Mlp:
                                                  ctypes.byref(loss) if want_loss else None))
         return loss.value if want_loss else None
 
-    def set_gate(self, p_min, feature, feature_min):
-        """Class 3 (straight to the FP64 pass) where P(FP32) >= p_min and raw
-        feature `feature` >= feature_min; feature < 0 turns the gate off."""
-        _check(self.ctx, lib().la_mlp_set_gate(self.h, ctypes.c_float(p_min), int(feature),
-                                               ctypes.c_float(feature_min)))
+    def set_gate(self, coef, bias=0.0):
+        """Class 3 (straight to the FP64 pass) where coef[:16] . x + coef[16:] . p
+        + bias >= 0 (x raw features, p class probabilities); coef None turns
+        the gate off."""
+        if coef is None:
+            _check(self.ctx, lib().la_mlp_set_gate(self.h, None, ctypes.c_float(0.0)))
+            return
+        c = np.ascontiguousarray(coef, dtype=np.float32)
+        if c.size != 19:
+            raise ValueError("the gate has 19 coefficients")
+        _check(self.ctx, lib().la_mlp_set_gate(self.h, _ptr(c), ctypes.c_float(bias)))
 
     def predict(self, x_ptr, count, probs_ptr=None, class_ptr=None):
         _check(self.ctx, lib().la_mlp_predict(self.h, ctypes.c_void_p(x_ptr), count,

@@ -12,11 +12,12 @@ systems: the best class depends on n and on the conditioning.
 (la_mlp_*). Labels come from running the batch once per class and taking, per
 system, the class with the fewest measured SM cycles including the FP64 redo
 (``measure_costs``). A gate on top of the network (``fit_gate``, applied on the
-device by la_mlp_set_gate) sends the systems that the FP32-class probability
-and one feature mark as beyond what refinement of low-precision factors can
+device by la_mlp_set_gate) sends the systems that the network's outputs and the
+features mark as beyond what refinement of low-precision factors can
 reach straight to the plan's FP64 pass, so that they do not pay for a mixed
-attempt first; it is fitted on the same labelled data, against the cycles of
-the plain FP64 plan. Everything runs through the C ABI of liblagpu.so; torch
+attempt first: a linear score of the raw features and the class
+probabilities, fitted by logistic regression on the same labelled data against
+the cycles of the plain FP64 plan. Everything runs through the C ABI of liblagpu.so; torch
 only provides device memory.
 """
 import json
@@ -103,30 +104,40 @@ def fp64_costs(ctx, systems, da, db, dx, ctas_per_sm=1, warps_per_system=8):
         plan.free()
 
 
-def fit_gate(probs, feats, cycles, cycles64, features=None, p_grid=(0.0, 0.2, 0.35, 0.5, 0.65, 0.8,
-                                                                     0.9)):
-    """Grid search of the gate (P(FP32) >= p_min and feature f >= t -> FP64
-    directly) that minimises the summed cycles on labelled data: a gated system
-    costs its FP64-plan cycles, the others the cycles of the network's class.
-    probs [m,3], feats [m,16] raw, cycles [m,3], cycles64 [m]. Returns
-    (p_min, feature, threshold, cost ratio to the ungated choice); feature -1
-    when no gate helps."""
+def fit_gate(probs, feats, cycles, cycles64, steps=3000, lr=0.5, seed=0):
+    """Fits the gate that sends a system straight to the FP64 pass: a linear
+    score of the 16 raw features and the network's 3 class probabilities,
+    learned by logistic regression (gradient descent on standardised inputs)
+    on whether the FP64 plan costs fewer cycles than the network's class, each
+    system weighted by the cycles at stake; the bias is then shifted to the
+    value that minimises the summed cycles. probs [m,3], feats [m,16] raw,
+    cycles [m,3], cycles64 [m]. Returns (coef[19] in raw units, bias, cost
+    ratio to the ungated choice)."""
     pred = np.argmax(probs, axis=1)
     base = cycles[np.arange(len(pred)), pred].astype(np.float64)
+    gain = base - cycles64.astype(np.float64)  # cycles saved by gating each system
+    X = np.concatenate([feats, probs], axis=1).astype(np.float64)
+    mu, sd = X.mean(0), X.std(0) + 1e-9
+    Z = (X - mu) / sd
+    y = (gain > 0).astype(np.float64)
+    w = np.abs(gain) / max(np.abs(gain).mean(), 1e-30)
+    W = np.zeros(Z.shape[1])
+    b = 0.0
+    for _ in range(steps):
+        p = 1.0 / (1.0 + np.exp(-(Z @ W + b)))
+        g = (p - y) * w
+        W -= lr * (Z.T @ g) / len(Z)
+        b -= lr * g.mean()
+    score = Z @ W + b
     total0 = base.sum()
-    gain = base - cycles64  # cycles saved by gating each system
-    best = (1.0, -1, 0.0, 1.0)
-    for f in (range(feats.shape[1]) if features is None else features):
-        col = feats[:, f]
-        qs = np.unique(np.quantile(col, np.linspace(0.0, 1.0, 201)))
-        for p_min in p_grid:
-            ok = probs[:, 2] >= p_min
-            for t in qs:
-                g = ok & (col >= t)
-                ratio = (total0 - gain[g].sum()) / total0
-                if ratio < best[3]:
-                    best = (float(p_min), int(f), float(t), float(ratio))
-    return best
+    best_t, best_ratio = 0.0, 1.0
+    for t in np.quantile(score, np.linspace(0.0, 1.0, 401)):
+        ratio = (total0 - gain[score >= t].sum()) / total0
+        if ratio < best_ratio:
+            best_t, best_ratio = float(t), float(ratio)
+    coef = W / sd
+    bias = b - float((W * mu / sd).sum()) - best_t
+    return coef.astype(np.float32), float(bias), best_ratio
 
 
 def labels_from_costs(cycles):
@@ -140,7 +151,7 @@ class PrecisionSelector:
     def __init__(self, ctx, seed=0):
         self.ctx = ctx
         self.mlp = la_gpu.Mlp(ctx, seed)
-        self.gate = (1.0, -1, 0.0)
+        self.gate = None
 
     def fit(self, feats, labels, steps=1500, lr=3e-3, batch=4096, seed=0, log_every=0):
         """Adam on minibatches of (feats [m,16] FP32 device, labels [m] int32).
@@ -176,11 +187,11 @@ class PrecisionSelector:
         self.ctx.synchronize()
         return log
 
-    def set_gate(self, p_min, feature, threshold):
-        """Class 3 (straight to the FP64 pass) where P(FP32) >= p_min and raw
-        feature `feature` >= threshold; feature < 0 turns the gate off."""
-        self.gate = (float(p_min), int(feature), float(threshold))
-        self.mlp.set_gate(p_min, feature, threshold)
+    def set_gate(self, coef, bias=0.0):
+        """Class 3 (straight to the FP64 pass) where the gate's score
+        coef[:16] . x + coef[16:] . p + bias >= 0; coef None: no gate."""
+        self.gate = None if coef is None else (np.asarray(coef, dtype=np.float32), float(bias))
+        self.mlp.set_gate(coef, bias)
 
     def probs(self, feats):
         """[m, 3] class probabilities (device FP32 tensor)."""
@@ -216,8 +227,8 @@ class PrecisionSelector:
 
     def save_gate(self, path):
         with open(path, "w") as f:
-            json.dump({"p_min": self.gate[0], "feature": self.gate[1],
-                       "threshold": self.gate[2]}, f, indent=1)
+            json.dump({"coef": [float(v) for v in self.gate[0]], "bias": self.gate[1]}, f,
+                      indent=1)
 
     @classmethod
     def from_file(cls, ctx, path, gate=True):
@@ -228,5 +239,5 @@ class PrecisionSelector:
         gpath = os.path.splitext(path)[0] + ".gate.json"
         if gate and os.path.exists(gpath):
             g = json.load(open(gpath))
-            s.set_gate(g["p_min"], g["feature"], g["threshold"])
+            s.set_gate(g["coef"], g["bias"])
         return s

@@ -144,15 +144,97 @@ WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "rust-l
                        "selector_weights.npy")
 
 
+def test_gate_sends_scored_systems_to_fp64_pass(lagpu, ctx_fast, torch, sel_mod):
+    # la_mlp_set_gate: class 3 exactly where coef . [x, p] + bias >= 0, on the
+    # raw features x and the class probabilities p; None turns it off.
+    systems, da, db, dx, kappa = sel_mod.conditioned_batch(ctx_fast, 300, seed=31)
+    f = sel_mod.features(ctx_fast, systems, da)
+    s = sel_mod.PrecisionSelector.from_file(ctx_fast, WEIGHTS, gate=False)
+    probs = s.probs(f).cpu().numpy().astype(np.float64)
+    plain = s.predict(f).cpu().numpy()
+    coef = np.zeros(19, dtype=np.float32)
+    coef[15] = 1.0   # log10 of the Lanczos condition estimate
+    coef[18] = 0.5   # and the FP32-class probability
+    bias = -2.0
+    s.set_gate(coef, bias)
+    gated = s.predict(f).cpu().numpy()
+    x = f.cpu().numpy().astype(np.float64)
+    score = x @ coef[:16] + probs @ coef[16:] + bias
+    clear = np.abs(score) > 1e-4  # away from the threshold's rounding
+    assert np.array_equal(gated[clear & (score >= 0)], np.full((clear & (score >= 0)).sum(), 3))
+    assert np.array_equal(gated[clear & (score < 0)], plain[clear & (score < 0)])
+    assert 0 < (gated == 3).sum() < len(gated)
+    s.set_gate(None)
+    assert np.array_equal(s.predict(f).cpu().numpy(), plain)
+    with pytest.raises(lagpu.LaError):
+        s.set_gate(np.full(19, np.nan, dtype=np.float32), 0.0)
+
+
+def test_selector_wall_clock_gain_over_fp32_factors(lagpu, ctx_fast, torch, sel_mod):
+    """The committed network and gate on a freshly seeded batch of 20,000
+    systems: features + inference + the plan with the chosen classes takes
+    less device time than the same plan with FP32 factors for every system
+    (the method without the selector), medians of 5 runs, and every answer
+    ends at eta <= 1e-14."""
+    tol = 5e-15
+    s = sel_mod.PrecisionSelector.from_file(ctx_fast, WEIGHTS)
+    systems, da, db, dx, kappa = sel_mod.conditioned_batch(ctx_fast, 20000, seed=202)
+    count = len(systems)
+    plan = lagpu.BatchPlan(ctx_fast, da.data_ptr(), db.data_ptr(), dx.data_ptr(), systems, 1,
+                           ctas_per_sm=2, warps_per_system=8, tol=tol)
+    fp32 = torch.full((count,), 2, dtype=torch.int32, device="cuda")
+    cls = torch.empty(count, dtype=torch.int32, device="cuda")
+    fbuf = torch.empty((count, 16), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.Stream()
+    ctx_fast.set_stream(stream.cuda_stream)
+
+    def timed(fn, reps=5):
+        fn()
+        out = []
+        for _ in range(reps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            out.append(e0.elapsed_time(e1))
+        return float(np.median(out))
+
+    def fixed():
+        plan.select_device(fp32.data_ptr())
+        plan.run()
+
+    def selected():
+        lagpu.batch_features_device(ctx_fast, da.data_ptr(), systems, fbuf.data_ptr())
+        s.predict(fbuf, out=cls, sync=False)
+        plan.select_device(cls.data_ptr())
+        plan.run()
+
+    try:
+        t32 = timed(fixed)
+        ts = timed(selected)
+        eta = torch.empty(count, dtype=torch.float64, device="cuda")
+        worst = lagpu.batch_backward_error_device(ctx_fast, da.data_ptr(), db.data_ptr(),
+                                                  dx.data_ptr(), systems, eta.data_ptr())
+    finally:
+        plan.free()
+        ctx_fast.set_stream(None)
+    print("selector path %.1f ms, FP32 factors everywhere %.1f ms (x%.3f)" % (ts, t32, t32 / ts))
+    assert worst <= 1e-14
+    assert ts < t32
+
+
 def test_selector_gain_over_fp32_factors(lagpu, ctx_fast, torch, sel_mod):
     """The trained network (selector_weights.npy: 200,000 labelled systems,
-    rust-la_gb300/examples/train_selector.py) chooses factor precisions for a
-    freshly seeded batch: its choices spend fewer SM cycles than FP32 factors
-    for every system (the method without the selector), measured system by
-    system, and every answer ends at eta <= 1e-14 (refinement or the FP64
-    pass)."""
+    rust-la_gb300/examples/train_selector.py), without its gate, chooses factor
+    precisions for a freshly seeded batch: its choices spend fewer SM cycles
+    than FP32 factors for every system (the method without the selector),
+    measured system by system, and every answer ends at eta <= 1e-14
+    (refinement or the FP64 pass)."""
     tol = 1e-14
-    s = sel_mod.PrecisionSelector.from_file(ctx_fast, WEIGHTS)
+    s = sel_mod.PrecisionSelector.from_file(ctx_fast, WEIGHTS, gate=False)
     systems, da, db, dx, kappa = sel_mod.conditioned_batch(ctx_fast, 6000, seed=202)
     cyc, conv = sel_mod.measure_costs(ctx_fast, systems, da, db, dx, tol=tol)
     f = sel_mod.features(ctx_fast, systems, da)
