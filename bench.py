@@ -269,11 +269,12 @@ def guarded(section, *args, **kwargs):
         return {"error": "%s: %s" % (type(e).__name__, e)}
 
 
-def run_qr(la_gpu, torch, ctx, n=2048, nrhs=4, cpu=True):
-    """QRDecomposition::new + solve (src/decomp/qr.rs:26-238), FAST arithmetic,
-    on an n x n N(0,1) matrix (seed 6): nominal flops 4/3 n^3 + 4 n^2 nrhs
-    (the reference's unblocked Householder form). The CPU line is the oracle
-    (the reference's order, one thread) on n = 1024."""
+def run_qr(la_gpu, torch, ctx, n=2048, nrhs=4, cpu=True, fp64_peak=None):
+    """QRDecomposition::new, get_q and solve (src/decomp/qr.rs:26-238), FAST
+    arithmetic (blocks of 64 reflections in compact WY form), on an n x n
+    N(0,1) matrix (seed 6): nominal flops 4/3 n^3 for the factorization and for
+    Q (the reference's Householder form). The CPU line is the oracle (the
+    reference's order, one thread) on n = 1024."""
     try:
         rng = np.random.default_rng(6)
         a_np = rng.standard_normal((n, n))
@@ -292,11 +293,16 @@ def run_qr(la_gpu, torch, ctx, n=2048, nrhs=4, cpu=True):
         t1 = time.perf_counter()
         qr.solve(la_gpu.Matrix(b_np, ctx))
         ts = time.perf_counter() - t1
+        t1 = time.perf_counter()
+        qr.get_q()  # includes the m x m copy to the host
+        tq = time.perf_counter() - t1
         qr.free()
         flops = 4.0 / 3.0 * n ** 3
-        out = {"workload": "QR factor (Householder, reference order) n=%d, then solve %d RHS" % (n, nrhs),
-               "factor_ms": tf * 1e3, "solve_ms": ts * 1e3,
+        out = {"workload": "QR factor n=%d (Householder reflections, FAST: blocks of 64 in "
+                           "compact WY form), then solve %d RHS and get_q" % (n, nrhs),
+               "factor_ms": tf * 1e3, "solve_ms": ts * 1e3, "get_q_ms": tq * 1e3,
                "factor_gflops": flops / tf / 1e9, "flops_basis": "nominal 4/3 n^3",
+               "factor_frac_of_fp64_peak": (flops / tf / 1e12 / fp64_peak) if fp64_peak else None,
                "cpu_oracle": None}
         if cpu:
             import oracle
@@ -930,7 +936,7 @@ def run_ours(args):
 
     qrs = None
     if not args.no_qr and rank == 0:
-        qrs = run_qr(la_gpu, torch, ctx, cpu=not args.no_cpu)
+        qrs = run_qr(la_gpu, torch, ctx, cpu=not args.no_cpu, fp64_peak=fp64_peak)
 
     csv = None
     if not args.no_csv and rank == 0:

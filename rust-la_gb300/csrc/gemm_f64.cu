@@ -86,7 +86,8 @@ __device__ __forceinline__ void load_slab(T* As, T* Bs, const T* A, size_t lda, 
 template <typename T, int MODE, int BN>
 __global__ void __launch_bounds__(THREADS)
 gemm_f64_kernel(int M, int N, int K, const T* __restrict__ A, size_t lda,
-                const T* __restrict__ B, size_t ldb, T* __restrict__ C, size_t ldc) {
+                const T* __restrict__ B, size_t ldb, T* __restrict__ C, size_t ldc, int kper,
+                size_t czs) {
   constexpr int TN = BN / 16;
   extern __shared__ __align__(16) double smem_raw[];
   T* smem = reinterpret_cast<T*>(smem_raw);
@@ -95,6 +96,9 @@ gemm_f64_kernel(int M, int N, int K, const T* __restrict__ A, size_t lda,
 
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  // split K: this CTA's k range [kb, ke) and its own output slice
+  const int kb = blockIdx.z * kper, ke = min(K, kb + kper);
+  C += blockIdx.z * czs;
 
   T acc[4][TN];
   constexpr bool ZERO = (MODE == GM_FMA_ZERO || MODE == GM_EXACT_ZERO);
@@ -107,18 +111,18 @@ gemm_f64_kernel(int M, int N, int K, const T* __restrict__ A, size_t lda,
       acc[i][j] = (!ZERO && r < M && c < N) ? C[(size_t)r * ldc + c] : T(0);
     }
 
-  const int nslab = (K + BK - 1) / BK;
+  const int nslab = (ke - kb + BK - 1) / BK;
   // Slab order: ascending, or descending for back substitution.
-  auto slab_k0 = [&](int s) { return DESC ? (nslab - 1 - s) * BK : s * BK; };
+  auto slab_k0 = [&](int s) { return kb + (DESC ? (nslab - 1 - s) * BK : s * BK); };
 
-  load_slab<T, BN>(As, Bs, A, lda, B, ldb, M, N, K, m0, n0, slab_k0(0));
+  load_slab<T, BN>(As, Bs, A, lda, B, ldb, M, N, ke, m0, n0, slab_k0(0));
   cp_async_commit();
 
   for (int s = 0; s < nslab; s++) {
     const int buf = s & 1;
     if (s + 1 < nslab) {
       load_slab<T, BN>(As + (buf ^ 1) * BM * BK, Bs + (buf ^ 1) * BK * BN, A, lda, B, ldb, M, N,
-                       K, m0, n0, slab_k0(s + 1));
+                       ke, m0, n0, slab_k0(s + 1));
       cp_async_commit();
       cp_async_wait_1();
     } else {
@@ -128,7 +132,7 @@ gemm_f64_kernel(int M, int N, int K, const T* __restrict__ A, size_t lda,
     const T* as = As + buf * BM * BK;
     const T* bs = Bs + buf * BK * BN;
     const int k0 = slab_k0(s);
-    const int kn = min(BK, K - k0);
+    const int kn = min(BK, ke - k0);
     if (kn == BK) {
 #pragma unroll 8
       for (int kk = 0; kk < BK; kk++) {
@@ -203,7 +207,8 @@ constexpr size_t TMA_SMEM = 2 * (size_t)TMA_STAGE_BYTES + 1024;  // + alignment 
 template <int MODE>
 __global__ void __launch_bounds__(THREADS)
 gemm_f64_tma_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
-                    int M, int N, int K, double* __restrict__ C, size_t ldc, int* err) {
+                    int M, int N, int K, double* __restrict__ C, size_t ldc, int* err, int kper,
+                    size_t czs) {
   extern __shared__ __align__(1024) unsigned char tma_raw[];
   __shared__ __align__(8) uint64_t full[2];
   double* smem = reinterpret_cast<double*>(
@@ -211,6 +216,8 @@ gemm_f64_tma_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constan
   const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * TMA_BN;
   constexpr bool ZERO = MODE == GM_FMA_ZERO;
+  const int kb = blockIdx.z * kper, ke = min(K, kb + kper);  // split K
+  C += blockIdx.z * czs;
 
   double acc[4][4];
 #pragma unroll
@@ -221,7 +228,7 @@ gemm_f64_tma_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constan
       acc[i][j] = (!ZERO && r < M && c < N) ? C[(size_t)r * ldc + c] : 0.0;
     }
 
-  const int nslab = (K + BK - 1) / BK;
+  const int nslab = (ke - kb + BK - 1) / BK;
   if (tid == 0) {
     la_tma::mbar_init(&full[0], 1);
     la_tma::mbar_init(&full[1], 1);
@@ -231,9 +238,9 @@ gemm_f64_tma_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constan
   auto issue = [&](int stage, int s) {
     double* st = smem + stage * TMA_STAGE_D;
     la_tma::mbar_expect_tx(&full[stage], TMA_STAGE_BYTES);
-    la_tma::tma_load_2d(st, &ta, s * BK, m0, &full[stage]);
-    la_tma::tma_load_2d(st + BM * BK, &tb, n0, s * BK, &full[stage]);
-    la_tma::tma_load_2d(st + BM * BK + BK * 32, &tb, n0 + 32, s * BK, &full[stage]);
+    la_tma::tma_load_2d(st, &ta, kb + s * BK, m0, &full[stage]);
+    la_tma::tma_load_2d(st + BM * BK, &tb, n0, kb + s * BK, &full[stage]);
+    la_tma::tma_load_2d(st + BM * BK + BK * 32, &tb, n0 + 32, kb + s * BK, &full[stage]);
   };
   if (tid == 0 && nslab > 0) issue(0, 0);
 
@@ -244,7 +251,7 @@ gemm_f64_tma_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constan
         la_tma::mbar_wait(&full[buf], (uint32_t)((s >> 1) & 1), err, (int)DERR_GEMM_TIMEOUT);
     const double* as = smem + buf * TMA_STAGE_D;
     const double* bs = as + BM * BK;
-    const int kn = min(BK, K - s * BK);
+    const int kn = min(BK, ke - kb - s * BK);
     if (ok) {
 #pragma unroll 8
       for (int k = 0; k < BK; k++) {
@@ -288,7 +295,8 @@ constexpr size_t GEMM_SMEM_CAP = 96 * 1024;
 // units) so that the caller uses the cp.async form.
 template <int MODE>
 la_status launch_tma(la_ctx ctx, int M, int N, int K, const double* A, size_t lda,
-                     const double* B, size_t ldb, double* C, size_t ldc, size_t min_smem) {
+                     const double* B, size_t ldb, double* C, size_t ldc, size_t min_smem,
+                     int splits = 1, int kper = 0, size_t czs = 0) {
   if (K <= 0 || (reinterpret_cast<uintptr_t>(A) % 16) || (reinterpret_cast<uintptr_t>(B) % 16) ||
       (lda % 2) || (ldb % 2))
     return LA_UNSUPPORTED;
@@ -305,16 +313,17 @@ la_status launch_tma(la_ctx ctx, int M, int N, int K, const double* A, size_t ld
   });
   if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaFuncSetAttribute(gemm_tma)");
   const size_t smem = std::min(GEMM_SMEM_CAP, std::max(TMA_SMEM, min_smem));
-  dim3 grid((N + TMA_BN - 1) / TMA_BN, (M + BM - 1) / BM);
-  gemm_f64_tma_kernel<MODE><<<grid, THREADS, smem, ctx->stream>>>(ta, tb, M, N, K, C, ldc,
-                                                                 ctx->d_err);
+  dim3 grid((N + TMA_BN - 1) / TMA_BN, (M + BM - 1) / BM, splits);
+  gemm_f64_tma_kernel<MODE><<<grid, THREADS, smem, ctx->stream>>>(
+      ta, tb, M, N, K, C, ldc, ctx->d_err, splits > 1 ? kper : K, czs);
   ctx->launches++;
   return la_check_launch(ctx, "gemm_f64_tma_kernel");
 }
 
 template <int MODE, int BN, typename T = double>
 la_status launch_mode(la_ctx ctx, int M, int N, int K, const T* A, size_t lda, const T* B,
-                      size_t ldb, T* C, size_t ldc, size_t min_smem) {
+                      size_t ldb, T* C, size_t ldc, size_t min_smem, int splits = 1,
+                      int kper = 0, size_t czs = 0) {
   const size_t smem =
       std::min(GEMM_SMEM_CAP, std::max((size_t)2 * (BM * BK + BK * BN) * sizeof(T), min_smem));
   static la_device_once configured;  // one attribute call per instantiation and device
@@ -323,9 +332,9 @@ la_status launch_mode(la_ctx ctx, int M, int N, int K, const T* A, size_t lda, c
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GEMM_SMEM_CAP);
   });
   if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaFuncSetAttribute(gemm)");
-  dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
-  gemm_f64_kernel<T, MODE, BN><<<grid, THREADS, smem, ctx->stream>>>(M, N, K, A, lda, B, ldb, C,
-                                                                     ldc);
+  dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, splits);
+  gemm_f64_kernel<T, MODE, BN><<<grid, THREADS, smem, ctx->stream>>>(
+      M, N, K, A, lda, B, ldb, C, ldc, splits > 1 ? kper : K, czs);
   ctx->launches++;
   return la_check_launch(ctx, "gemm_f64_kernel");
 }
@@ -364,6 +373,27 @@ la_status launch_gemm(la_ctx ctx, int mode, int M, int N, int K, const double* A
     if (s != LA_UNSUPPORTED) return s;
   }
   return launch_bn<64>(ctx, mode, M, N, K, A, lda, B, ldb, C, ldc, min_smem);
+}
+
+// Split-K product for tall-skinny inner products (C = A B with K >> M): the
+// K range is cut into `splits` pieces of kper (a multiple of the 32-deep slab),
+// and piece z writes its own partial product C + z * czs (z < splits), which
+// the caller sums. Fused arithmetic from zero, as GM_FMA_ZERO.
+la_status launch_gemm_splitk(la_ctx ctx, int M, int N, int K, const double* A, size_t lda,
+                             const double* B, size_t ldb, double* C, size_t ldc, size_t czs,
+                             int splits, int kper) {
+  if (M <= 0 || N <= 0) return LA_OK;
+  if (splits < 1 || kper % BK != 0 || (size_t)(splits - 1) * kper >= (size_t)std::max(K, 1) ||
+      (size_t)splits * kper < (size_t)K)
+    return LA_INVALID;
+  if (N > 16) {
+    const la_status s =
+        launch_tma<GM_FMA_ZERO>(ctx, M, N, K, A, lda, B, ldb, C, ldc, 0, splits, kper, czs);
+    if (s != LA_UNSUPPORTED) return s;
+    return launch_mode<GM_FMA_ZERO, 64>(ctx, M, N, K, A, lda, B, ldb, C, ldc, 0, splits, kper,
+                                        czs);
+  }
+  return launch_mode<GM_FMA_ZERO, 16>(ctx, M, N, K, A, lda, B, ldb, C, ldc, 0, splits, kper, czs);
 }
 
 // FP32 form (FAST arithmetic only) for the panels and triangular updates of the

@@ -179,6 +179,25 @@ la_status launch_tc_update(la_ctx ctx, cudaStream_t stream, int fmt, int M, int 
 // SM (room for a concurrent panel CTA).
 la_status launch_gemm(la_ctx ctx, int mode, int M, int N, int K, const double* A, size_t lda,
                       const double* B, size_t ldb, double* C, size_t ldc, size_t min_smem = 0);
+// C + z * czs = A[:, z kper : (z + 1) kper] B[z kper : (z + 1) kper, :] for z < splits
+// (fused, from zero); kper a multiple of 32, splits * kper >= K > (splits - 1) kper.
+la_status launch_gemm_splitk(la_ctx ctx, int M, int N, int K, const double* A, size_t lda,
+                             const double* B, size_t ldb, double* C, size_t ldc, size_t czs,
+                             int splits, int kper);
+// Blocked FAST QR (qr_blocked.cu): blocks of QR_BLOCK columns in compact WY
+// form. qr_blocked_factor factors A (m x n, pitch ld) in place, writes rdiag
+// and each block's Gram matrix V'V (QR_BLOCK x QR_BLOCK, one after another) to
+// gram; LA_UNSUPPORTED (nothing launched) when the rows exceed one cluster's
+// shared memory. qr_blocked_apply applies the factored reflections to T:
+// mode 1 (get_q) Q[j:, j:] block by block in reverse, mode 2 (solve) X[j:, :]
+// in order; cols = T's columns.
+constexpr int QR_BLOCK = 64;
+bool qr_blocked_supported(la_ctx ctx, int m, int n);
+la_status qr_blocked_factor(la_ctx ctx, double* A, size_t ld, int m, int n, double* rdiag,
+                            double* gram);
+la_status qr_blocked_apply(la_ctx ctx, const double* A, size_t ld, int m, int dc,
+                           const double* rdiag, const double* gram, int mode, double* T,
+                           size_t ldt, int cols);
 la_status launch_panel(la_ctx ctx, cudaStream_t stream, bool exact, double* A, double* S,
                        size_t ld, int m, int j0, int jb, int* d_ipiv, unsigned* bar_base);
 la_status launch_laswp(la_ctx ctx, bool exact, double* A, double* S, size_t ld, int n, int j0,
@@ -194,12 +213,6 @@ la_status launch_panel_cluster_f32(la_ctx ctx, float* A, size_t ld, int m, int j
                                    int* d_ipiv);
 la_status launch_trsm_rowpanel_f32(la_ctx ctx, float* A, size_t ld, int j0, int jb, int c_begin,
                                    int c_end);
-// After an inner panel [i0, i0 + ib): U12 = L11^-1 A12 and A22 -= L21 U12 on the
-// columns [i0 + ib, j1o) (at most 224 of them; LA_UNSUPPORTED beyond). d_count:
-// a device word that is zero at the first launch (the kernel leaves it zero);
-// launches that share it must not overlap.
-la_status launch_panel_update_f32(la_ctx ctx, float* A, size_t ld, int m, int i0, int ib,
-                                  int j1o, unsigned* d_count);
 // X = L11^-1 X for rows [j0, j0 + jbo) (jbo <= 256) of columns [c_begin, c_end).
 la_status launch_trsm_block_f32(la_ctx ctx, float* A, size_t ld, int j0, int jbo, int c_begin,
                                 int c_end);

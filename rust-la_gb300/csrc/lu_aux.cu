@@ -227,80 +227,6 @@ trsm_block_kernel(float* A, size_t ld, int j0, int jbo, int c_begin, int c_end) 
   }
 }
 
-// ---- the mixed LU's inner-panel update ---------------------------------------
-// After an inner panel [i0, i0 + ib) (ib <= 32) of an outer panel ending at
-// j1o: U12 = L11^-1 A[i0 : i1, i1 : j1o] and A[i1 : m, i1 : j1o] -= L21 U12,
-// in one launch. Every CTA solves the small triangle (w = j1o - i1 <= 224
-// columns) in shared memory, one thread per column with its values in
-// registers (the FMAs of trsm_rowpanel_reg_kernel, in the same order); the
-// last CTA to have read A12 (counted on `count`, which starts at zero and
-// which that CTA resets) writes U12 back, when no CTA reads A12 any more; then
-// each CTA updates its 64-row block, a warp per row and a lane per column,
-// with ib-deep dot products in ascending k (the FMAs of the FP32 GEMM). The
-// results are those of the two launches it replaces, one launch less per
-// inner panel on the factorization's critical path.
-constexpr int PU_K = 32, PU_W = 224, PU_R = 64;
-__global__ void __launch_bounds__(256)
-panel_update_kernel(float* A, size_t ld, int m, int i0, int ib, int j1o, unsigned* count) {
-  __shared__ float L11[PU_K][PU_K + 1];
-  __shared__ float U[PU_K][PU_W + 1];
-  __shared__ float L21[PU_R][PU_K + 1];
-  __shared__ int s_last;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int i1 = i0 + ib, w = j1o - i1;
-  for (int idx = tid; idx < ib * ib; idx += 256) {
-    const int i = idx / ib, k = idx % ib;
-    L11[i][k] = A[(size_t)(i0 + i) * ld + i0 + k];
-  }
-  for (int idx = tid; idx < ib * w; idx += 256) {
-    const int i = idx / w, c = idx % w;
-    U[i][c] = A[(size_t)(i0 + i) * ld + i1 + c];
-  }
-  __syncthreads();
-  if (tid == 0) {
-    __threadfence();  // this CTA's reads of A12 are done before it is counted
-    s_last = atomicAdd(count, 1u) == gridDim.x - 1;
-  }
-  if (tid < w) {
-    float x[PU_K];
-#pragma unroll
-    for (int i = 0; i < PU_K; i++) x[i] = i < ib ? U[i][tid] : 0.f;
-#pragma unroll
-    for (int k = 0; k < PU_K; k++) {
-      if (k >= ib) break;
-      const float xk = x[k];
-#pragma unroll
-      for (int i = k + 1; i < PU_K; i++)
-        if (i < ib) x[i] = fmaf(-L11[i][k], xk, x[i]);
-    }
-#pragma unroll
-    for (int i = 0; i < PU_K; i++)
-      if (i < ib) U[i][tid] = x[i];
-  }
-  const int r0 = i1 + blockIdx.x * PU_R;
-  const int nr = min(PU_R, m - r0);
-  for (int idx = tid; idx < nr * PU_K; idx += 256) {
-    const int r = idx / PU_K, k = idx % PU_K;
-    L21[r][k] = k < ib ? A[(size_t)(r0 + r) * ld + i0 + k] : 0.f;
-  }
-  __syncthreads();
-  if (s_last) {  // every other CTA has read A12: U12 replaces it
-    for (int idx = tid; idx < ib * w; idx += 256) {
-      const int i = idx / w, c = idx % w;
-      A[(size_t)(i0 + i) * ld + i1 + c] = U[i][c];
-    }
-    if (tid == 0) atomicExch(count, 0u);  // ready for the next launch
-  }
-  for (int r = warp; r < nr; r += 8) {
-    float* crow = A + (size_t)(r0 + r) * ld + i1;
-    for (int c = lane; c < w; c += 32) {
-      float acc = crow[c];
-      for (int k = 0; k < ib; k++) acc = fmaf(-L21[r][k], U[k][c], acc);
-      crow[c] = acc;
-    }
-  }
-}
-
 // ---- after the factorization: permutation vector, sign, zero diagonal ------
 // The swap list (LAPACK ipiv form) is replayed in order on a permutation
 // vector (lu.rs:147-149), the sign flips once per real swap (lu.rs:151), and
@@ -463,17 +389,6 @@ la_status launch_laswp(la_ctx ctx, bool exact, double* A, double* S, size_t ld, 
 la_status launch_laswp_f32(la_ctx ctx, float* A, size_t ld, int n, int j0, int jb) {
   return launch_laswp_t<float>(ctx, ctx->stream, false, A, nullptr, ld, n, j0, jb);
 }
-la_status launch_panel_update_f32(la_ctx ctx, float* A, size_t ld, int m, int i0, int ib,
-                                  int j1o, unsigned* d_count) {
-  const int i1 = i0 + ib;
-  if (j1o <= i1) return LA_OK;
-  if (ib > PU_K || j1o - i1 > PU_W || !d_count) return LA_UNSUPPORTED;
-  const int grid = std::max(1, (m - i1 + PU_R - 1) / PU_R);
-  panel_update_kernel<<<grid, 256, 0, ctx->stream>>>(A, ld, m, i0, ib, j1o, d_count);
-  ctx->launches++;
-  return la_check_launch(ctx, "panel_update_kernel");
-}
-
 la_status launch_trsm_block_f32(la_ctx ctx, float* A, size_t ld, int j0, int jbo, int c_begin,
                                 int c_end) {
   if (c_end <= c_begin || jbo <= 0) return LA_OK;

@@ -406,8 +406,7 @@ la_status mixed_factor(la_ctx ctx, la_lu h, int prec) {
   }
   LA_TRY(stat.alloc(256));
   float* d_stat = stat.as<float>();
-  // [0] max |U12|, [1] alpha of the current update, [32] the inner-panel
-  // update's arrival count (zero between launches)
+  // [0] max |U12|, [1] alpha of the current update
   LA_CUDA(ctx, cudaMemsetAsync(d_stat, 0, 256, ms));
 
   // Inner panels of the outer panel [j0, j1o) on stream s; row swaps on the
@@ -426,14 +425,13 @@ la_status mixed_factor(la_ctx ctx, la_lu h, int prec) {
       if (st == LA_UNSUPPORTED) st = launch_panel_f32(ctx, s, A, ld, m, i0, ib, h->d_ipiv, &bar_base);
       if (st == LA_OK) st = launch_laswp_f32(ctx, A, ld, climit, i0, ib);
       if (st == LA_OK && i1 < j1o) {
-        st = launch_panel_update_f32(ctx, A, ld, m, i0, ib, j1o,
-                                     reinterpret_cast<unsigned*>(d_stat + 32));
-        if (st == LA_UNSUPPORTED) {
-          st = launch_trsm_rowpanel_f32(ctx, A, ld, i0, ib, i1, j1o);
-          if (st == LA_OK && i1 < m)
-            st = launch_gemm_f32(ctx, GM_FMA_SUB, m - i1, j1o - i1, ib, A + (size_t)i1 * ld + i0,
-                                 ld, A + (size_t)i0 * ld + i1, ld, A + (size_t)i1 * ld + i1, ld);
-        }
+        // Two launches: fusing them into one (every CTA solving the small
+        // triangle, then updating its rows from shared memory) measured 12.6 ms
+        // slower at n = 16384, its update far below the GEMM tile's rate.
+        st = launch_trsm_rowpanel_f32(ctx, A, ld, i0, ib, i1, j1o);
+        if (st == LA_OK && i1 < m)
+          st = launch_gemm_f32(ctx, GM_FMA_SUB, m - i1, j1o - i1, ib, A + (size_t)i1 * ld + i0,
+                               ld, A + (size_t)i0 * ld + i1, ld, A + (size_t)i1 * ld + i1, ld);
       }
     }
     ctx->stream = saved;

@@ -33,6 +33,7 @@ struct la_qr_handle {
   double* d_rdiag = nullptr;  // min(m, n)
   std::vector<double> rdiag;  // host copy (is_full_rank)
   int arith = LA_ARITH_FAST;
+  double* d_gram = nullptr;   // blocked FAST factorization: V'V of each block (else null)
 };
 
 namespace {
@@ -298,6 +299,22 @@ la_status reflect(la_ctx ctx, bool exact, const double* U, size_t ldu, int ucol,
 la_status qr_factor(la_ctx ctx, la_qr h) {
   const int m = (int)h->m, n = (int)h->n, dc = std::min(m, n);
   const bool exact = h->arith == LA_ARITH_EXACT;
+  if (!exact && qr_blocked_supported(ctx, m, n)) {
+    void* g = nullptr;
+    const size_t nblocks = (size_t)(dc + QR_BLOCK - 1) / QR_BLOCK;
+    LA_TRY(la_device_alloc(ctx, &g, nblocks * QR_BLOCK * QR_BLOCK * sizeof(double)));
+    h->d_gram = static_cast<double*>(g);
+    const la_status s = qr_blocked_factor(ctx, h->d_qr, h->ld, m, n, h->d_rdiag, h->d_gram);
+    if (s != LA_UNSUPPORTED) {
+      LA_TRY(s);
+      h->rdiag.assign((size_t)dc, 0.0);
+      LA_CUDA(ctx, cudaMemcpyAsync(h->rdiag.data(), h->d_rdiag, (size_t)dc * sizeof(double),
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+      return la_sync_and_check(ctx, "qr factorization (blocked)");
+    }
+    la_device_free(ctx, h->d_gram);
+    h->d_gram = nullptr;
+  }
   if (!exact) {
     qr_norm_kernel<false><<<1, 32, 0, ctx->stream>>>(h->d_qr, h->ld, m, 0, h->d_rdiag);
     ctx->launches++;
@@ -419,6 +436,7 @@ void la_qr_free(la_qr h) {
   cudaSetDevice(h->ctx->device);
   la_device_free(h->ctx, h->d_qr);
   la_device_free(h->ctx, h->d_rdiag);
+  la_device_free(h->ctx, h->d_gram);
   delete h;
 }
 
@@ -449,8 +467,11 @@ la_status la_qr_get_q(la_qr h, double* out) {
   qr_q_init_kernel<<<blocks_for(h->m * h->m, 256), 256, 0, ctx->stream>>>(Qm.d(), ldq, m, dc);
   ctx->launches++;
   LA_TRY(la_check_launch(ctx, "qr_q_init_kernel"));
-  for (int k = dc - 1; k >= 0; k--)  // qr.rs:163-191
-    LA_TRY(reflect(ctx, exact, h->d_qr, h->ld, k, k, m, h->d_rdiag, Qm.d(), ldq, k, m, 1));
+  if (h->d_gram)  // blocked FAST factorization: the reflections block by block
+    LA_TRY(qr_blocked_apply(ctx, h->d_qr, h->ld, m, dc, h->d_rdiag, h->d_gram, 1, Qm.d(), ldq, m));
+  else
+    for (int k = dc - 1; k >= 0; k--)  // qr.rs:163-191
+      LA_TRY(reflect(ctx, exact, h->d_qr, h->ld, k, k, m, h->d_rdiag, Qm.d(), ldq, k, m, 1));
   LA_CUDA(ctx, cudaMemcpy2DAsync(out, h->m * sizeof(double), Qm.p, ldq * sizeof(double),
                                  h->m * sizeof(double), h->m, cudaMemcpyDeviceToHost,
                                  ctx->stream));
@@ -475,8 +496,11 @@ la_status la_qr_solve(la_qr h, const double* b, size_t brows, size_t nrhs, doubl
   LA_CUDA(ctx, cudaMemcpy2DAsync(X.p, ldw * sizeof(double), b, nrhs * sizeof(double),
                                  nrhs * sizeof(double), h->n, cudaMemcpyHostToDevice,
                                  ctx->stream));
-  for (int k = 0; k < n; k++)  // Y = Q' B (qr.rs:211-223)
-    LA_TRY(reflect(ctx, exact, h->d_qr, h->ld, k, k, n, h->d_rdiag, X.d(), ldw, 0, nx, 2));
+  if (h->d_gram)  // Y = Q' B (qr.rs:211-223), block by block
+    LA_TRY(qr_blocked_apply(ctx, h->d_qr, h->ld, n, n, h->d_rdiag, h->d_gram, 2, X.d(), ldw, nx));
+  else
+    for (int k = 0; k < n; k++)  // Y = Q' B (qr.rs:211-223)
+      LA_TRY(reflect(ctx, exact, h->d_qr, h->ld, k, k, n, h->d_rdiag, X.d(), ldw, 0, nx, 2));
   qr_extract_kernel<<<blocks_for(h->n * h->n, 256), 256, 0, ctx->stream>>>(
       h->d_qr, h->ld, h->d_rdiag, n, n, R.d(), ldr, 0);
   ctx->launches++;
