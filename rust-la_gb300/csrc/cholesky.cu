@@ -40,7 +40,7 @@ namespace {
 
 constexpr int CHW = 64;   // panel width
 constexpr int CHP = CHW + 1;
-constexpr int PANEL_T = 128;
+constexpr int PANEL_T = 64;  // two warps per CTA: rows spread over more SMs
 
 size_t pad4c(size_t x) { return (x + 3) & ~size_t(3); }
 
@@ -108,6 +108,44 @@ chol_diag_kernel(double* L, double* S, size_t ld, int j0, int jb, int* flags) {
       if (c > r) continue;
       if (EXACT) s[r][c] = __dadd_rn(s[r][c], __dmul_rn(a[r][k], a[c][k]));  // :78, :86
       else a[r][c] = fma(-a[r][k], a[c][k], a[r][c]);
+    }
+    __syncthreads();
+  }
+  for (int idx = tid; idx < jb * jb; idx += 256) {
+    const int r = idx / jb, c = idx % jb;
+    if (c <= r) L[(size_t)(j0 + r) * ld + j0 + c] = a[r][c];
+  }
+}
+
+// FAST form of the diagonal block: warp 0 takes the square root and scales
+// the column by its reciprocal, then all threads apply the rank-1 update to
+// the lower triangle still open (rows and columns from a 16 x 16 thread
+// grid, no index division); two barriers per column.
+__global__ void __launch_bounds__(256)
+chol_diag_fast_kernel(double* L, size_t ld, int j0, int jb, int* flags) {
+  extern __shared__ __align__(16) double chd_raw[];
+  double(*a)[CHP] = reinterpret_cast<double(*)[CHP]>(chd_raw);
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  for (int idx = tid; idx < jb * jb; idx += 256) {
+    const int r = idx / jb, c = idx % jb;
+    if (c <= r) a[r][c] = L[(size_t)(j0 + r) * ld + j0 + c];
+  }
+  __syncthreads();
+  for (int k = 0; k < jb; k++) {
+    if (tid < 32) {
+      const double d = a[k][k];
+      const double q = sqrt(d);
+      const double rq = 1.0 / q;
+      if (tid == 0) {
+        if (d <= 0.0) atomicOr(flags + 1, 1);  // cholesky.rs:97-100
+        a[k][k] = q;
+      }
+      for (int r = k + 1 + tid; r < jb; r += 32) a[r][k] *= rq;
+    }
+    __syncthreads();
+    for (int r = k + 1 + ty; r < jb; r += 16) {
+      const double lr = a[r][k];
+      for (int c = k + 1 + tx; c <= r; c += 16) a[r][c] = fma(-lr, a[c][k], a[r][c]);
     }
     __syncthreads();
   }
@@ -200,8 +238,7 @@ cudaError_t configure_chol() {
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)(2 * CHW * CHP * sizeof(double)));
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(chol_diag_kernel<false>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+      e = cudaFuncSetAttribute(chol_diag_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)(CHW * CHP * sizeof(double)));
     return e;
   });
@@ -229,49 +266,99 @@ la_status chol_factor(la_ctx ctx, la_chol h, int* none) {
   ctx->launches++;
   LA_TRY(la_check_launch(ctx, "chol_sym_check_kernel"));
 
-  // Panels and the trailing update run one after the other. A lookahead like
-  // the LU's (next panel on the side stream, the update's CTAs limited to two
-  // per SM to leave it room) measured slower at n = 8192 (253 ms against 227
-  // ms with 8 row strips; 274 against 233 ms with 16): the update loses more
-  // than the 64-column panels hide.
-  Buf S(ctx), T(ctx);
+  Buf S(ctx), T0(ctx), T1(ctx);
   if (exact) {
     LA_TRY(S.alloc((size_t)n * ld * sizeof(double)));
     LA_CUDA(ctx, cudaMemsetAsync(S.p, 0, (size_t)n * ld * sizeof(double), st));
   }
+  // Transposed panels (the GEMM's K x N operand), two so that panel k + 1 can
+  // be transposed while panel k's update still reads its own.
   const size_t ldt = pad4c((size_t)n);
-  if (n > CHW) LA_TRY(T.alloc((size_t)CHW * ldt * sizeof(double)));
+  if (n > CHW) {
+    LA_TRY(T0.alloc((size_t)CHW * ldt * sizeof(double)));
+    LA_TRY(T1.alloc((size_t)CHW * ldt * sizeof(double)));
+  }
+  double* Tbuf[2] = {T0.d(), T1.d()};
   const size_t dsm = (exact ? 2 : 1) * CHW * CHP * sizeof(double);
-  for (int j0 = 0; j0 < n; j0 += CHW) {
-    const int jb = std::min(CHW, n - j0), j1 = j0 + jb;
+  const bool look = ctx->lookahead != 0 && ctx->side_stream != nullptr;
+
+  // Diagonal block, rows below and transpose of panel [j0, j0 + jb) on stream s.
+  auto panel = [&](int j0, int jb, double* T, cudaStream_t s) -> la_status {
+    const int j1 = j0 + jb;
     if (exact)
-      chol_diag_kernel<true><<<1, 256, dsm, st>>>(L, S.d(), ld, j0, jb, d_flags);
+      chol_diag_kernel<true><<<1, 256, dsm, s>>>(L, S.d(), ld, j0, jb, d_flags);
     else
-      chol_diag_kernel<false><<<1, 256, dsm, st>>>(L, nullptr, ld, j0, jb, d_flags);
+      chol_diag_fast_kernel<<<1, 256, dsm, s>>>(L, ld, j0, jb, d_flags);
     ctx->launches++;
     LA_TRY(la_check_launch(ctx, "chol_diag_kernel"));
-    if (j1 >= n) break;
+    if (j1 >= n) return LA_OK;
     const int rows = n - j1;
     const int pg = (rows + PANEL_T - 1) / PANEL_T;
     if (exact)
-      chol_panel_kernel<true><<<pg, PANEL_T, 0, st>>>(L, S.d(), ld, j0, j1, n);
+      chol_panel_kernel<true><<<pg, PANEL_T, 0, s>>>(L, S.d(), ld, j0, j1, n);
     else
-      chol_panel_kernel<false><<<pg, PANEL_T, 0, st>>>(L, nullptr, ld, j0, j1, n);
+      chol_panel_kernel<false><<<pg, PANEL_T, 0, s>>>(L, nullptr, ld, j0, j1, n);
     ctx->launches++;
     LA_TRY(la_check_launch(ctx, "chol_panel_kernel"));
-    chol_transpose_kernel<<<dim3((rows + 31) / 32, (jb + 31) / 32), dim3(32, 8), 0, st>>>(
-        L, ld, j0, jb, j1, rows, T.d(), ldt);
+    chol_transpose_kernel<<<dim3((rows + 31) / 32, (jb + 31) / 32), dim3(32, 8), 0, s>>>(
+        L, ld, j0, jb, j1, rows, T, ldt);
     ctx->launches++;
-    LA_TRY(la_check_launch(ctx, "chol_transpose_kernel"));
-    // Row strips [a, b) of the trailing matrix, each updated on columns
-    // [j1, b): its own diagonal block and everything left of it.
+    return la_check_launch(ctx, "chol_transpose_kernel");
+  };
+  // A22 -= L21 L21' (EXACT: S22 += ...) of panel [j0, j0 + jb) on rows and
+  // columns >= c0 (lower part): FAST as one launch over the tiles at or below
+  // the diagonal; EXACT (and FAST where TMA cannot take the operands) in up
+  // to 8 row strips [a, b) that each stop at their own diagonal block.
+  auto update = [&](int j0, int jb, const double* T, int c0) -> la_status {
+    const int j1 = j0 + jb, rows = n - c0;
+    if (rows <= 0) return LA_OK;
+    if (!exact) {
+      const la_status r = launch_gemm_lower(ctx, rows, jb, L + (size_t)c0 * ld + j0, ld,
+                                            T + (c0 - j1), ldt, L + (size_t)c0 * ld + c0, ld);
+      if (r != LA_UNSUPPORTED) return r;
+    }
     const int nstrip = std::max(1, std::min(8, rows / 512));
     const int hs = ((rows + nstrip - 1) / nstrip + CHW - 1) / CHW * CHW;
-    for (int a = j1; a < n; a += hs) {
+    for (int a = c0; a < n; a += hs) {
       const int b = std::min(n, a + hs);
-      double* C = (exact ? S.d() : L) + (size_t)a * ld + j1;
-      LA_TRY(launch_gemm(ctx, exact ? GM_EXACT_ADD : GM_FMA_SUB, b - a, b - j1, jb,
-                         L + (size_t)a * ld + j0, ld, T.d(), ldt, C, ld));
+      double* C = (exact ? S.d() : L) + (size_t)a * ld + c0;
+      LA_TRY(launch_gemm(ctx, exact ? GM_EXACT_ADD : GM_FMA_SUB, b - a, b - c0, jb,
+                         L + (size_t)a * ld + j0, ld, T + (c0 - j1), ldt, C, ld));
+    }
+    return LA_OK;
+  };
+  // The next panel's columns [j1, j2) of rows >= j1 (a plain GEMM).
+  auto update_next = [&](int j0, int jb, const double* T, int j1, int j2) -> la_status {
+    double* C = (exact ? S.d() : L) + (size_t)j1 * ld + j1;
+    return launch_gemm(ctx, exact ? GM_EXACT_ADD : GM_FMA_SUB, n - j1, j2 - j1, jb,
+                       L + (size_t)j1 * ld + j0, ld, T, ldt, C, ld);
+  };
+
+  // Lookahead, as in the LU: panel k's update of panel k + 1's columns first,
+  // then panel k + 1 on the high-priority side stream while the rest of panel
+  // k's update runs (rows and columns >= j2). They touch disjoint data: panel
+  // k + 1 owns columns [j1, j2) of rows >= j1, and the rest of the update reads
+  // panel k's finished columns and its transposed copy. The update keeps its
+  // full occupancy (an earlier form that capped it at two CTAs per SM to leave
+  // the panel room measured slower than no lookahead at all).
+  LA_TRY(panel(0, std::min(CHW, n), Tbuf[0], st));
+  for (int j0 = 0, k = 0; j0 < n; j0 += CHW, k++) {
+    const int jb = std::min(CHW, n - j0), j1 = j0 + jb;
+    if (j1 >= n) break;
+    const int jbn = std::min(CHW, n - j1), j2 = j1 + jbn;
+    double* Tk = Tbuf[k & 1];
+    double* Tn = Tbuf[(k + 1) & 1];
+    if (look && j2 < n) {
+      LA_TRY(update_next(j0, jb, Tk, j1, j2));
+      LA_CUDA(ctx, cudaEventRecord(ctx->ev_fork, st));
+      LA_CUDA(ctx, cudaStreamWaitEvent(ctx->side_stream, ctx->ev_fork, 0));
+      LA_TRY(panel(j1, jbn, Tn, ctx->side_stream));
+      LA_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->side_stream));
+      LA_TRY(update(j0, jb, Tk, j2));
+      LA_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_join, 0));
+    } else {
+      LA_TRY(update(j0, jb, Tk, j1));
+      LA_TRY(panel(j1, jbn, Tn, st));
     }
   }
   chol_zero_upper_kernel<<<dim3(nt, nt), dim3(32, 8), 0, st>>>(L, ld, n);

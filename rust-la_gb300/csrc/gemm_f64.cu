@@ -208,13 +208,22 @@ template <int MODE>
 __global__ void __launch_bounds__(THREADS)
 gemm_f64_tma_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
                     int M, int N, int K, double* __restrict__ C, size_t ldc, int* err, int kper,
-                    size_t czs) {
+                    size_t czs, int tri) {
   extern __shared__ __align__(1024) unsigned char tma_raw[];
   __shared__ __align__(8) uint64_t full[2];
   double* smem = reinterpret_cast<double*>(
       (reinterpret_cast<uintptr_t>(tma_raw) + 1023) & ~uintptr_t(1023));
   const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
-  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * TMA_BN;
+  int by = blockIdx.y, bx = blockIdx.x;
+  if (tri) {  // lower-triangular tile grid: blockIdx.x enumerates (by, bx), bx <= by, row-major
+    const int t = blockIdx.x;
+    int r = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
+    while ((r + 1) * (r + 2) / 2 <= t) r++;
+    while (r * (r + 1) / 2 > t) r--;
+    by = r;
+    bx = t - r * (r + 1) / 2;
+  }
+  const int m0 = by * BM, n0 = bx * TMA_BN;
   constexpr bool ZERO = MODE == GM_FMA_ZERO;
   const int kb = blockIdx.z * kper, ke = min(K, kb + kper);  // split K
   C += blockIdx.z * czs;
@@ -296,7 +305,7 @@ constexpr size_t GEMM_SMEM_CAP = 96 * 1024;
 template <int MODE>
 la_status launch_tma(la_ctx ctx, int M, int N, int K, const double* A, size_t lda,
                      const double* B, size_t ldb, double* C, size_t ldc, size_t min_smem,
-                     int splits = 1, int kper = 0, size_t czs = 0) {
+                     int splits = 1, int kper = 0, size_t czs = 0, bool tri = false) {
   if (K <= 0 || (reinterpret_cast<uintptr_t>(A) % 16) || (reinterpret_cast<uintptr_t>(B) % 16) ||
       (lda % 2) || (ldb % 2))
     return LA_UNSUPPORTED;
@@ -313,9 +322,10 @@ la_status launch_tma(la_ctx ctx, int M, int N, int K, const double* A, size_t ld
   });
   if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaFuncSetAttribute(gemm_tma)");
   const size_t smem = std::min(GEMM_SMEM_CAP, std::max(TMA_SMEM, min_smem));
-  dim3 grid((N + TMA_BN - 1) / TMA_BN, (M + BM - 1) / BM, splits);
+  const int tm = (M + BM - 1) / BM;
+  dim3 grid(tri ? tm * (tm + 1) / 2 : (N + TMA_BN - 1) / TMA_BN, tri ? 1 : tm, splits);
   gemm_f64_tma_kernel<MODE><<<grid, THREADS, smem, ctx->stream>>>(
-      ta, tb, M, N, K, C, ldc, ctx->d_err, splits > 1 ? kper : K, czs);
+      ta, tb, M, N, K, C, ldc, ctx->d_err, splits > 1 ? kper : K, czs, tri ? 1 : 0);
   ctx->launches++;
   return la_check_launch(ctx, "gemm_f64_tma_kernel");
 }
@@ -394,6 +404,16 @@ la_status launch_gemm_splitk(la_ctx ctx, int M, int N, int K, const double* A, s
                                         czs);
   }
   return launch_mode<GM_FMA_ZERO, 16>(ctx, M, N, K, A, lda, B, ldb, C, ldc, 0, splits, kper, czs);
+}
+
+// C -= A B on the output tiles at or below the diagonal of the square C
+// (M x M; 64 x 64 tiles, a diagonal tile in full): the symmetric trailing
+// update of the Cholesky factorization. LA_UNSUPPORTED (nothing launched)
+// where the TMA form cannot take the operands.
+la_status launch_gemm_lower(la_ctx ctx, int M, int K, const double* A, size_t lda,
+                            const double* B, size_t ldb, double* C, size_t ldc) {
+  if (M <= 0 || K <= 0) return LA_OK;
+  return launch_tma<GM_FMA_SUB>(ctx, M, M, K, A, lda, B, ldb, C, ldc, 0, 1, 0, 0, true);
 }
 
 // FP32 form (FAST arithmetic only) for the panels and triangular updates of the

@@ -13,7 +13,7 @@
 // which hold for tau_i = 0 too (a skipped reflection: row and column i of T
 // are zero). tau per caller:
 //   factorization (qr.rs:60-103): -1/(a u0), 0 where a == 0;
-//   get_q (qr.rs:167-189): -1/(rdiag u0), 0 where u0 == 0; blocks in reverse,
+//   get_q (qr.rs:163-189): -1/(rdiag u0), 0 where u0 == 0; blocks in reverse,
 //       Q[j:, j:] -= V (T (V' Q[j:, j:]));
 //   solve (qr.rs:211-223): 1/u0 (the reference's factor -(dot / u0)); blocks
 //       in order, X[j:] -= V (T' (V' X[j:])).
@@ -47,7 +47,6 @@ namespace {
 
 constexpr int QB = QR_BLOCK;      // block width
 constexpr int QPT = 256;          // panel threads
-constexpr int QPW = QPT / 32;     // panel warps
 constexpr int QNBP = QB + 1;      // shared row pitch (odd: column reads without bank conflicts)
 constexpr int QMAXCL = 16;        // largest cluster
 constexpr int QTS_W = 8;          // warps (columns) per substitution CTA
@@ -85,9 +84,9 @@ __global__ void __launch_bounds__(QPT, 1) qr_panel_kernel(QrPanelArgs p) {
   extern __shared__ __align__(16) double P[];  // [rpc][QNBP]
   __shared__ double xch[2][QMAXCL][QB];        // partial sums, one slot per source CTA
   __shared__ double own[2][QB];                // the diagonal row: q, then t_c
-  __shared__ double red[QPW][QB];
+  __shared__ double red[QPT];
   __shared__ double mine[QB], tot[QB], fac[QB];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x;
   const uint32_t rank = cta_rank();
   const int CL = (int)gridDim.x;  // one cluster per launch
   const int nb = p.nb;
@@ -103,24 +102,26 @@ __global__ void __launch_bounds__(QPT, 1) qr_panel_kernel(QrPanelArgs p) {
   for (int k = 0; k < nb; k++) {
     const int par = k & 1, jc = p.j + k, w = nb - k;
     const int lr0 = max(0, jc - r0);  // first local row at or below the diagonal
-    // x (column k) against columns k..nb-1; the first is x.x
-    double s0 = 0.0, s1 = 0.0;
-    const int c0 = k + lane, c1 = k + 32 + lane;
-    for (int lr = lr0 + warp; lr < nr; lr += QPW) {
-      const double x = P[lr * QNBP + k];
-      if (c0 < nb) s0 = fma(x, P[lr * QNBP + c0], s0);
-      if (c1 < nb) s1 = fma(x, P[lr * QNBP + c1], s1);
+    // x (column k) against columns k..nb-1 (the first is x.x). Thread t takes
+    // column k + t % w of the rows lr0 + t / w + G i: every lane of an FP64
+    // instruction does useful work whatever w is.
+    {
+      const int G = QPT / w;
+      double sacc = 0.0;
+      if (tid < G * w) {
+        const int c = k + tid % w;
+        for (int lr = lr0 + tid / w; lr < nr; lr += G)
+          sacc = fma(P[lr * QNBP + k], P[lr * QNBP + c], sacc);
+      }
+      red[tid] = sacc;
+      __syncthreads();
+      if (tid < w) {
+        double t = 0.0;
+        for (int g = 0; g < G; g++) t += red[g * w + tid];
+        mine[tid] = t;
+      }
+      __syncthreads();
     }
-    red[warp][lane] = s0;
-    red[warp][lane + 32] = s1;
-    __syncthreads();
-    if (tid < w) {
-      double t = 0.0;
-#pragma unroll
-      for (int q = 0; q < QPW; q++) t += red[q][tid];
-      mine[tid] = t;
-    }
-    __syncthreads();
     for (int idx = tid; idx < w * CL; idx += QPT) {
       const int c = idx % w, dst = idx / w;
       st_remote_f64(remote_addr(&xch[par][rank][c], (uint32_t)dst), mine[c]);
@@ -148,15 +149,18 @@ __global__ void __launch_bounds__(QPT, 1) qr_panel_kernel(QrPanelArgs p) {
       p.tau[k] = a != 0.0 ? -1.0 / (a * u0) : 0.0;
     }
     __syncthreads();
-    if (a != 0.0) {
-      const int d0 = k + 1 + lane, d1 = k + 33 + lane;
-      for (int lr = lr0 + warp; lr < nr; lr += QPW) {
-        const double u = (r0 + lr == jc) ? u0 : P[lr * QNBP + k];
-        if (d0 < nb) P[lr * QNBP + d0] = fma(fac[d0 - k], u, P[lr * QNBP + d0]);
-        if (d1 < nb) P[lr * QNBP + d1] = fma(fac[d1 - k], u, P[lr * QNBP + d1]);
+    if (a != 0.0 && w > 1) {  // columns k+1..nb-1, the same mapping
+      const int w1 = w - 1, G = QPT / w1;
+      if (tid < G * w1) {
+        const int c = k + 1 + tid % w1;
+        const double f = fac[c - k];
+        for (int lr = lr0 + tid / w1; lr < nr; lr += G) {
+          const double u = (r0 + lr == jc) ? u0 : P[lr * QNBP + k];
+          P[lr * QNBP + c] = fma(f, u, P[lr * QNBP + c]);
+        }
       }
-      if (owner && tid == 0) P[(jc - r0) * QNBP + k] = u0;
     }
+    if (a != 0.0 && owner && tid == 0) P[(jc - r0) * QNBP + k] = u0;
     __syncthreads();
   }
   // No remote access follows the last cluster barrier.
