@@ -79,12 +79,8 @@ typedef enum la_option {
   /* 1 (default): factor the next panel on a second stream while the rest of
    * the trailing update runs; 0: strictly one phase after the other. */
   LA_OPT_LOOKAHEAD = 5,
-  /* FP32 panels of the mixed LU. 1 (default): one thread-block cluster with
-   * partial pivoting (one exchange per column); 2: one cluster with
-   * tournament pivoting (each CTA picks candidate rows from its own rows,
-   * then the candidates are factored; two cluster barriers per panel);
-   * 0: the cooperative multi-CTA kernel, partial pivoting. The factors serve
-   * the refinement; 1 and 0 pivot on the FP32 values, 2 differently again. */
+  /* 1 (default): the FP32 panels of the mixed LU run on one thread-block
+   * cluster (distributed shared memory); 0: the cooperative multi-CTA kernel. */
   LA_OPT_CLUSTER_PANEL = 6,
   /* Batch plans (read when a plan is built): largest Krylov basis (0-20) of
    * the GMRES-IR stage that a LA_BATCH_MIXED plan runs on a system whose

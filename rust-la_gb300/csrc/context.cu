@@ -237,8 +237,7 @@ la_status la_ctx_set_option(la_ctx ctx, int option, int64_t value) {
       ctx->lookahead = value ? 1 : 0;
       return LA_OK;
     case LA_OPT_CLUSTER_PANEL:
-      if (value < 0 || value > 2) return LA_INVALID;
-      ctx->cluster_panels = (int)value;
+      ctx->cluster_panels = value ? 1 : 0;
       return LA_OK;
     case LA_OPT_BATCH_GMRES:
       if (value < 0 || value > 20) return LA_INVALID;

@@ -97,7 +97,7 @@ struct la_context {
   cudaStream_t side_stream = nullptr;    // high priority: lookahead panels
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int lookahead = 1;
-  int cluster_panels = 1;                // FP32 panels: 2 cluster + tournament, 1 cluster, 0 cooperative
+  int cluster_panels = 1;                // FP32 panels on one thread-block cluster
   int batch_gmres = 0;                   // Krylov steps per GMRES correction in batch plans (0: off)
   int solve_wave = 2;                    // CTAs per SM of the wavefront solve (0: block steps)
   int inject_alloc_at = 0;               // the n-th device allocation from now fails (0: none)
@@ -179,13 +179,13 @@ la_status launch_tc_update(la_ctx ctx, cudaStream_t stream, int fmt, int M, int 
 // SM (room for a concurrent panel CTA).
 la_status launch_gemm(la_ctx ctx, int mode, int M, int N, int K, const double* A, size_t lda,
                       const double* B, size_t ldb, double* C, size_t ldc, size_t min_smem = 0);
-// C + z * czs = A[:, z kper : (z + 1) kper] B[z kper : (z + 1) kper, :] for z < splits
-// (fused, from zero); kper a multiple of 32, splits * kper >= K > (splits - 1) kper.
 // C -= A B on the 64 x 64 output tiles at or below the diagonal of the square
 // C (M x M, FMA); LA_UNSUPPORTED (nothing launched) where TMA cannot take the
 // operands.
 la_status launch_gemm_lower(la_ctx ctx, int M, int K, const double* A, size_t lda,
                             const double* B, size_t ldb, double* C, size_t ldc);
+// C + z * czs = A[:, z kper : (z + 1) kper] B[z kper : (z + 1) kper, :] for z < splits
+// (fused, from zero); kper a multiple of 32, splits * kper >= K > (splits - 1) kper.
 la_status launch_gemm_splitk(la_ctx ctx, int M, int N, int K, const double* A, size_t lda,
                              const double* B, size_t ldb, double* C, size_t ldc, size_t czs,
                              int splits, int kper);
@@ -214,10 +214,8 @@ la_status launch_panel_f32(la_ctx ctx, cudaStream_t stream, float* A, size_t ld,
 la_status launch_laswp_f32(la_ctx ctx, float* A, size_t ld, int n, int j0, int jb);
 la_status launch_laswp_seq_f32(la_ctx ctx, float* A, size_t ld, const int* ipiv, int k0, int k1,
                                int c0, int c1);
-// tournament: the tournament-pivoting kernel (rows in registers) instead of
-// partial pivoting where the rows fit it.
 la_status launch_panel_cluster_f32(la_ctx ctx, float* A, size_t ld, int m, int j0, int jb,
-                                   int* d_ipiv, bool tournament);
+                                   int* d_ipiv);
 la_status launch_trsm_rowpanel_f32(la_ctx ctx, float* A, size_t ld, int j0, int jb, int c_begin,
                                    int c_end);
 // X = L11^-1 X for rows [j0, j0 + jbo) (jbo <= 256) of columns [c_begin, c_end).

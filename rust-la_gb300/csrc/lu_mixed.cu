@@ -140,27 +140,14 @@ struct SplitF16 {
   }
 };
 
-// Power-of-two scale of L21 for the split packings: 2^L_EXP while max |L21|
-// (stat[2]) is at most 1, as under partial pivoting; below that otherwise
-// (tournament pivoting), so that the scaled maximum stays below 2^L_EXP.
-template <typename SP>
-__device__ __forceinline__ float l_scale(const float* stat) {
-  const float mx = stat[2];
-  if (!(mx > 1.f) || !(mx < INFINITY)) return ldexpf(1.f, SP::L_EXP);
-  int e = 0;
-  frexpf(mx, &e);  // mx = f 2^e, 0.5 <= f < 1
-  return ldexpf(1.f, SP::L_EXP - e);
-}
-
-// L21 (rows x k FP32, pitch lds) * l_scale -> split rows of ldd elements:
+// L21 (rows x k FP32, pitch lds) * 2^L_EXP -> split rows of ldd elements:
 // high parts in columns [0, k), low parts in [ldd / 2, ldd / 2 + k), zeros
 // elsewhere.
 template <typename SP>
 __global__ void pack_l_split_kernel(const float* __restrict__ src, size_t lds,
-                                    typename SP::T* __restrict__ dst, size_t ldd, int rows, int k,
-                                    const float* stat) {
+                                    typename SP::T* __restrict__ dst, size_t ldd, int rows, int k) {
   const size_t half = ldd / 2;
-  const float sl = l_scale<SP>(stat);
+  const float sl = ldexpf(1.f, SP::L_EXP);
   size_t total = (size_t)rows * half;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
        i += (size_t)gridDim.x * blockDim.x) {
@@ -174,7 +161,7 @@ __global__ void pack_l_split_kernel(const float* __restrict__ src, size_t lds,
 
 // U12 (k x cols, pitch lds) -> U^T split (cols rows of ldd elements, as
 // pack_l_split_kernel) times a power of two that takes max |U12| (stat[0])
-// just below 2^U_EXP; stat[1] receives alpha = 1 / (l_scale * scale). 32x32
+// just below 2^U_EXP; stat[1] receives alpha = 1 / (2^L_EXP * scale). 32x32
 // tiles through shared memory.
 template <typename SP>
 __global__ void pack_ut_split_kernel(const float* __restrict__ src, size_t lds,
@@ -189,7 +176,7 @@ __global__ void pack_ut_split_kernel(const float* __restrict__ src, size_t lds,
     scale = ldexpf(1.f, SP::U_EXP - e);
   }
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0)
-    stat[1] = 1.f / (l_scale<SP>(stat) * scale);
+    stat[1] = 1.f / (ldexpf(1.f, SP::L_EXP) * scale);
   const size_t half = ldd / 2;
   const int c0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
   for (int i = threadIdx.y; i < 32; i += blockDim.y) {
@@ -419,8 +406,7 @@ la_status mixed_factor(la_ctx ctx, la_lu h, int prec) {
   }
   LA_TRY(stat.alloc(256));
   float* d_stat = stat.as<float>();
-  // [0] max |U12|, [1] alpha of the current update, [2] max |L21| of the
-  // current outer panel (split formats)
+  // [0] max |U12|, [1] alpha of the current update
   LA_CUDA(ctx, cudaMemsetAsync(d_stat, 0, 256, ms));
 
   // Inner panels of the outer panel [j0, j1o) on stream s; row swaps on the
@@ -434,8 +420,7 @@ la_status mixed_factor(la_ctx ctx, la_lu h, int prec) {
       const int i1 = i0 + ib;
       // One thread-block cluster holds the panel when it fits; else the
       // cooperative multi-CTA kernel.
-      st = ctx->cluster_panels ? launch_panel_cluster_f32(ctx, A, ld, m, i0, ib, h->d_ipiv,
-                                                          ctx->cluster_panels == 2)
+      st = ctx->cluster_panels ? launch_panel_cluster_f32(ctx, A, ld, m, i0, ib, h->d_ipiv)
                                : LA_UNSUPPORTED;
       if (st == LA_UNSUPPORTED) st = launch_panel_f32(ctx, s, A, ld, m, i0, ib, h->d_ipiv, &bar_base);
       if (st == LA_OK) st = launch_laswp_f32(ctx, A, ld, climit, i0, ib);
@@ -485,12 +470,6 @@ la_status mixed_factor(la_ctx ctx, la_lu h, int prec) {
     const float* L21 = A + (size_t)j1o * ld + j0;
     const float* U12 = A + (size_t)j0 * ld + c0;
     if (prec == LA_PREC_FP8 || prec == LA_PREC_FP16X3) {
-      if (pack_l) {  // max |L21| (stat[2]) once per outer panel, for the L scale
-        LA_CUDA(ctx, cudaMemsetAsync(d_stat + 2, 0, sizeof(float), ms));
-        absmax_kernel<<<grid_for(ctx, (size_t)M * jbo), 256, 0, ms>>>(L21, ld, M, jbo, d_stat + 2);
-        ctx->launches++;
-        LA_TRY(la_check_launch(ctx, "absmax_kernel"));
-      }
       LA_CUDA(ctx, cudaMemsetAsync(d_stat, 0, 2 * sizeof(float), ms));
       absmax_kernel<<<grid_for(ctx, (size_t)jbo * N), 256, 0, ms>>>(U12, ld, jbo, N, d_stat);
       ctx->launches++;
@@ -503,7 +482,7 @@ la_status mixed_factor(la_ctx ctx, la_lu h, int prec) {
         ub = u8;
         if (pack_l)
           pack_l_split_kernel<SplitE4M3><<<lg, 256, 0, ms>>>(L21, ld, lh.as<uint8_t>(), ldks, M,
-                                                             jbo, d_stat);
+                                                             jbo);
         pack_ut_split_kernel<SplitE4M3><<<pgs, dim3(32, 8), 0, ms>>>(U12, ld, u8, ldks, jbo, N,
                                                                      d_stat);
       } else {
@@ -511,7 +490,7 @@ la_status mixed_factor(la_ctx ctx, la_lu h, int prec) {
         ub = u16;
         if (pack_l)
           pack_l_split_kernel<SplitF16><<<lg, 256, 0, ms>>>(L21, ld, lh.as<uint16_t>(), ldks, M,
-                                                            jbo, d_stat);
+                                                            jbo);
         pack_ut_split_kernel<SplitF16><<<pgs, dim3(32, 8), 0, ms>>>(U12, ld, u16, ldks, jbo, N,
                                                                     d_stat);
       }

@@ -500,305 +500,21 @@ __global__ void __launch_bounds__(CT, 1) panel_cluster_reg_kernel(ClusterPanelAr
 }
 
 
-// ---- tournament pivoting ------------------------------------------------------
-// panel_tslu_kernel factors the same panel by tournament pivoting (TSLU;
-// Grigori, Demmel and Xiang, SIAM J. Matrix Anal. Appl. 32 (2011)) with a flat
-// reduction tree, in three phases:
-//   1. each CTA factors its own rows (in registers, as above) with partial
-//      pivoting inside the CTA: one CTA barrier per column and no cluster
-//      traffic. The jb rows it picks are its candidates;
-//   2. every CTA receives all candidates (at most 16 jb original rows, by
-//      distributed shared memory and one cluster barrier), loads their
-//      original values from global memory and factors them with partial
-//      pivoting, every CTA identically: the jb rows picked are the panel's
-//      pivots in order, and their factored values are the panel's first jb
-//      rows (L11 and U11);
-//   3. every other row r becomes a_r U11^-1 (its row of L21), from its
-//      original values, and after one more cluster barrier (no CTA writes
-//      before every CTA has read the original rows it needs) each row goes to
-//      its final position; the interchanges are composed as for the kernels
-//      above (ipiv and the row moves of the row-swap kernel).
-// Two cluster barriers per panel instead of one exchange per column. The
-// pivots are not partial pivoting's: the factors serve the mixed LU's
-// refinement, and their entries below the diagonal can exceed 1 in magnitude
-// (the split packings scale L21 by its maximum).
-
-// Pivot key of a candidate value: larger |v| wins; NaN ranks lowest but
-// still above "no row".
-__device__ __forceinline__ unsigned tkey(float v) {
-  const unsigned a = __float_as_uint(v) & 0x7fffffffu;
-  return a > 0x7f800000u ? 1u : a + 2u;
-}
-
-__device__ __forceinline__ void st_remote_s32(uint32_t addr, int v) {
-  asm volatile("st.shared::cluster.s32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
-}
-
-// Loads the original panel row `row` (columns j0 .. j0 + jb) into x; zeros
-// beyond jb, and everywhere for row < 0.
-__device__ __forceinline__ void load_panel_row(float (&x)[CW], const ClusterPanelArgs& p, int row,
-                                               bool vec) {
-  const float* src = p.A + (size_t)(row >= 0 ? row : 0) * p.ld + p.j0;
-  if (row >= 0 && vec && p.jb == CW) {
-#pragma unroll
-    for (int c4 = 0; c4 < CW / 4; c4++) {
-      const float4 t = reinterpret_cast<const float4*>(src)[c4];
-      x[4 * c4] = t.x;
-      x[4 * c4 + 1] = t.y;
-      x[4 * c4 + 2] = t.z;
-      x[4 * c4 + 3] = t.w;
-    }
-  } else {
-#pragma unroll
-    for (int c = 0; c < CW; c++) x[c] = (row >= 0 && c < p.jb) ? src[c] : 0.f;
-  }
-}
-
-// Column c of a CTA-local partial-pivoting LU of the rows this CTA's threads
-// hold (R per thread, rotating register windows as in panel_column): the row
-// with the largest |v| among those not yet picked (ties: the lower original
-// row) is picked (at[q] = c) and keeps its values; the others are scaled and
-// updated. Returns the original row picked, or -1 when none is left. Every
-// thread takes part.
-template <int R>
-__device__ __forceinline__ int local_column(int c, float (&v)[R][CW], const int (&oid)[R],
-                                            int (&at)[R], float (*wrow)[PNW][CW],
-                                            unsigned long long (*wkey)[PNW], int lane, int warp) {
-  const int par = c & 1;
-  unsigned long long best = 0ull;
-  int bq = 0;
-#pragma unroll
-  for (int q = 0; q < R; q++)
-    if (oid[q] >= 0 && at[q] < 0) {
-      const unsigned long long pk =
-          ((unsigned long long)tkey(v[q][0]) << 32) | (unsigned)(~oid[q]);
-      if (pk > best) { best = pk; bq = q; }
-    }
-  unsigned long long wb = best;
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    const unsigned long long o = __shfl_xor_sync(0xffffffffu, wb, off);
-    wb = o > wb ? o : wb;
-  }
-  const unsigned wmask = __ballot_sync(0xffffffffu, wb != 0ull && best == wb);
-  if (wmask && lane == __ffs(wmask) - 1) {
-    float* dst = wrow[par][warp];
-#pragma unroll
-    for (int q = 0; q < R; q++)
-      if (q == bq) {
-#pragma unroll
-        for (int k = 0; k < CW; k++) dst[k] = k < CW - c ? v[q][k] : 0.f;
-      }
-  }
-  if (lane == 0) wkey[par][warp] = wb;
-  __syncthreads();
-  unsigned long long gm = 0ull;
-  int gw = 0;
-#pragma unroll
-  for (int w = 0; w < PNW; w++) {
-    const unsigned long long k = wkey[par][w];
-    if (k > gm) { gm = k; gw = w; }
-  }
-  const int win = gm != 0ull ? (int)(~(unsigned)(gm & 0xffffffffull)) : -1;
-  const float* urow = wrow[par][gw];
-  const float d = win >= 0 ? urow[0] : 0.f;
-  const float sc = d != 0.f ? 1.f / d : 1.f;
-  float lq[R];
-  bool act[R];
-#pragma unroll
-  for (int q = 0; q < R; q++) {
-    act[q] = false;
-    if (win >= 0 && oid[q] >= 0 && at[q] < 0) {
-      if (oid[q] == win) at[q] = c;
-      else act[q] = true;
-    }
-    lq[q] = d != 0.f ? v[q][0] * sc : v[q][0];
-    if (act[q]) v[q][0] = lq[q];
-  }
-  if (win >= 0) {
-#pragma unroll
-    for (int k4 = 0; k4 < CW / 4; k4++) {
-      const float4 u4 = reinterpret_cast<const float4*>(urow)[k4];
-      const float uk[4] = {u4.x, u4.y, u4.z, u4.w};
-#pragma unroll
-      for (int i = 0; i < 4; i++) {
-        const int k = 4 * k4 + i;
-        if (k == 0) continue;
-#pragma unroll
-        for (int q = 0; q < R; q++)
-          if (act[q]) v[q][k] = fmaf(-lq[q], uk[i], v[q][k]);
-      }
-    }
-  }
-#pragma unroll
-  for (int q = 0; q < R; q++) {
-    const float t = v[q][0];
-#pragma unroll
-    for (int k = 0; k < CW - 1; k++) v[q][k] = v[q][k + 1];
-    v[q][CW - 1] = t;
-  }
-  return win;
-}
-
-template <int RPT>
-__global__ void __launch_bounds__(CT, 1) panel_tslu_kernel(ClusterPanelArgs p) {
-  __shared__ __align__(16) float wrow[2][PNW][CW];
-  __shared__ unsigned long long wkey[2][PNW];
-  __shared__ int s_loc[CW];                       // this CTA's candidates
-  __shared__ int s_cand[16 * CW];                 // every CTA's, slot g * CW + c
-  __shared__ __align__(16) float s_prow[CW][CW];  // the pivot rows' factored values
-  __shared__ float s_rd[CW];                      // 1 / U11[k][k] (1 where it is 0)
-  __shared__ int s_fin[CW];                       // the pivots' original rows, in order
-  __shared__ int s_atp[SWAP_SLOTS], s_atr[SWAP_SLOTS];
-  __shared__ int s_swaps[1 + 4 * MAX_PANEL_W];    // row moves (CTA 0 writes p.swaps)
-  __shared__ int s_na;
-
-  const int g = (int)cta_rank();
-  const int C = (int)gridDim.x;  // one cluster per launch, C <= 16
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int rpc = p.rpc, jb = p.jb;
-  const int row0 = p.j0 + g * rpc;
-  const int nrows = max(0, min(rpc, p.m - row0));
-  const bool vec = (p.ld % 4 == 0) && (p.j0 % 4 == 0) &&
-                   (reinterpret_cast<uintptr_t>(p.A) % 16 == 0);
-
-  // 1. partial pivoting over this CTA's rows
-  float v[RPT][CW];
-  int oid[RPT], at[RPT];
-#pragma unroll
-  for (int q = 0; q < RPT; q++) {
-    const int lr = q * CT + tid;
-    oid[q] = lr < nrows ? row0 + lr : -1;
-    at[q] = -1;
-    load_panel_row(v[q], p, oid[q], vec);
-  }
-  for (int c = 0; c < jb; c++) {
-    const int w = local_column<RPT>(c, v, oid, at, wrow, wkey, lane, warp);
-    if (tid == 0) s_loc[c] = w;
-  }
-  __syncthreads();
-
-  // 2. the candidates of every CTA, factored by every CTA alike
-  for (int i = tid; i < C * CW; i += CT) {
-    const int dst = i / CW, c = i % CW;
-    st_remote_s32(remote_addr(&s_cand[g * CW + c], (uint32_t)dst), c < jb ? s_loc[c] : -1);
-  }
-  cluster_sync();
-  constexpr int RC = 16 * CW / CT;  // candidate rows per thread
-  float cv[RC][CW];
-  int coid[RC], cat[RC];
-#pragma unroll
-  for (int q = 0; q < RC; q++) {
-    const int slot = q * CT + tid;
-    coid[q] = slot < C * CW ? s_cand[slot] : -1;
-    cat[q] = -1;
-    load_panel_row(cv[q], p, coid[q], vec);
-  }
-  for (int c = 0; c < jb; c++) {
-    const int w = local_column<RC>(c, cv, coid, cat, wrow, wkey, lane, warp);
-    if (tid == 0) s_fin[c] = w;
-  }
-  for (int r = jb; r < CW; r++)  // CW rotations in all: natural column order again
-#pragma unroll
-    for (int q = 0; q < RC; q++) {
-      const float t = cv[q][0];
-#pragma unroll
-      for (int k = 0; k < CW - 1; k++) cv[q][k] = cv[q][k + 1];
-      cv[q][CW - 1] = t;
-    }
-#pragma unroll
-  for (int q = 0; q < RC; q++)
-    if (cat[q] >= 0)
-#pragma unroll
-      for (int k = 0; k < CW; k++) s_prow[cat[q]][k] = cv[q][k];
-  __syncthreads();
-  if (tid < jb) {
-    const float d = s_prow[tid][tid];
-    s_rd[tid] = d != 0.f ? 1.f / d : 1.f;
-  }
-  if (warp == 0) {
-    const int na = compose_swaps_warp(s_fin, jb, p.j0, true, g == 0 ? p.ipiv : nullptr,
-                                      g == 0 ? p.swaps : s_swaps, s_atp, s_atr, lane);
-    if (lane == 0) s_na = na;
-  }
-  __syncthreads();
-
-  // 3. this CTA's rows: the pivot rows from phase 2, the others a U11^-1
-  int fpos[RPT];
-  bool sub[RPT];
-#pragma unroll
-  for (int q = 0; q < RPT; q++) {
-    int pc = -1;
-    fpos[q] = oid[q];
-    if (oid[q] >= 0) {
-      for (int c = 0; c < jb; c++)
-        if (s_fin[c] == oid[q]) pc = c;
-      for (int t = 0; t < s_na; t++)
-        if (s_atr[t] == oid[q]) fpos[q] = s_atp[t];
-    }
-    sub[q] = oid[q] >= 0 && pc < 0;
-    if (pc >= 0) {
-#pragma unroll
-      for (int k = 0; k < CW; k++) v[q][k] = s_prow[pc][k];
-    } else {
-      load_panel_row(v[q], p, oid[q], vec);
-    }
-  }
-  // Columns >= jb are zero in every row and in s_prow (rows and columns
-  // beyond jb stay 0, s_rd beyond jb is unused): the full CW-step loop leaves
-  // them zero, and its register indices stay compile-time constants.
-#pragma unroll
-  for (int k = 0; k < CW; k++) {
-    const float rd = k < jb ? s_rd[k] : 1.f;
-    float l[RPT];
-#pragma unroll
-    for (int q = 0; q < RPT; q++) {
-      l[q] = v[q][k] * rd;
-      if (sub[q]) v[q][k] = l[q];
-    }
-#pragma unroll
-    for (int c = k + 1; c < CW; c++) {
-      const float u = k < jb ? s_prow[k][c] : 0.f;
-#pragma unroll
-      for (int q = 0; q < RPT; q++)
-        if (sub[q]) v[q][c] = fmaf(-l[q], u, v[q][c]);
-    }
-  }
-  cluster_sync();  // every CTA has read the original rows it needs
-#pragma unroll
-  for (int q = 0; q < RPT; q++)
-    if (oid[q] >= 0) {
-      float* dst = p.A + (size_t)fpos[q] * p.ld + p.j0;
-      if (vec && jb == CW) {
-#pragma unroll
-        for (int c4 = 0; c4 < CW / 4; c4++)
-          reinterpret_cast<float4*>(dst)[c4] =
-              make_float4(v[q][4 * c4], v[q][4 * c4 + 1], v[q][4 * c4 + 2], v[q][4 * c4 + 3]);
-      } else {
-#pragma unroll
-        for (int c = 0; c < CW; c++)
-          if (c < jb) dst[c] = v[q][c];
-      }
-    }
-}
-
 }  // namespace
 
-// Launches panel_cluster_reg_kernel<RPT> (TSLU: panel_tslu_kernel<RPT>) as one
-// cluster of `cluster` CTAs; LA_UNSUPPORTED (nothing launched) when such a
-// cluster cannot be resident.
-template <int RPT, bool TSLU>
+// Launches panel_cluster_reg_kernel<RPT> as one cluster of `cluster` CTAs;
+// LA_UNSUPPORTED (nothing launched) when such a cluster cannot be resident.
+template <int RPT>
 la_status launch_reg(la_ctx ctx, float* A, size_t ld, int m, int j0, int jb, int* d_ipiv,
                      int cluster, int rpc) {
-  void (*kern)(ClusterPanelArgs) = TSLU ? panel_tslu_kernel<RPT> : panel_cluster_reg_kernel<RPT>;
   // Cluster size checked once per instantiation and device (0: none).
   static int ok_for[LA_MAX_DEVICES];
   static la_device_once once;
   const int dev = la_current_device();
   if (dev < 0 || dev >= LA_MAX_DEVICES) return LA_UNSUPPORTED;
-  once.run([cluster, kern](int d) {
+  once.run([cluster](int d) {
     ok_for[d] = 0;
-    if (cudaFuncSetAttribute(kern,
+    if (cudaFuncSetAttribute(panel_cluster_reg_kernel<RPT>,
                              cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(cluster);
@@ -811,7 +527,7 @@ la_status launch_reg(la_ctx ctx, float* A, size_t ld, int m, int j0, int jb, int
       cfg.attrs = at;
       cfg.numAttrs = 1;
       int nclusters = 0;
-      if (cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg) ==
+      if (cudaOccupancyMaxActiveClusters(&nclusters, panel_cluster_reg_kernel<RPT>, &cfg) ==
               cudaSuccess &&
           nclusters >= 1)
         ok_for[d] = cluster;
@@ -842,7 +558,7 @@ la_status launch_reg(la_ctx ctx, float* A, size_t ld, int m, int j0, int jb, int
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  cudaError_t e = cudaLaunchKernelEx(&cfg, kern, a);
+  cudaError_t e = cudaLaunchKernelEx(&cfg, panel_cluster_reg_kernel<RPT>, a);
   if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaLaunchKernelEx(panel_cluster_reg)");
   ctx->launches++;
   return LA_OK;
@@ -852,7 +568,7 @@ la_status launch_reg(la_ctx ctx, float* A, size_t ld, int m, int j0, int jb, int
 // Returns LA_UNSUPPORTED (without launching) when the panel does not fit one
 // cluster; the caller then uses the cooperative kernel.
 la_status launch_panel_cluster_f32(la_ctx ctx, float* A, size_t ld, int m, int j0, int jb,
-                                   int* d_ipiv, bool tournament) {
+                                   int* d_ipiv) {
   const int R = m - j0;
   if (R <= 0 || jb <= 0) return LA_OK;
   if (jb > CW) return LA_UNSUPPORTED;
@@ -907,15 +623,9 @@ la_status launch_panel_cluster_f32(la_ctx ctx, float* A, size_t ld, int m, int j
     // Register rows: at most 4 rows per thread.
     const int rpt = (rpc + CT - 1) / CT;
     la_status rs = LA_UNSUPPORTED;
-    if (tournament) {
-      if (rpt <= 1) rs = launch_reg<1, true>(ctx, A, ld, m, j0, jb, d_ipiv, cluster, rpc);
-      else if (rpt <= 2) rs = launch_reg<2, true>(ctx, A, ld, m, j0, jb, d_ipiv, cluster, rpc);
-      else if (rpt <= 4) rs = launch_reg<4, true>(ctx, A, ld, m, j0, jb, d_ipiv, cluster, rpc);
-    } else {
-      if (rpt <= 1) rs = launch_reg<1, false>(ctx, A, ld, m, j0, jb, d_ipiv, cluster, rpc);
-      else if (rpt <= 2) rs = launch_reg<2, false>(ctx, A, ld, m, j0, jb, d_ipiv, cluster, rpc);
-      else if (rpt <= 4) rs = launch_reg<4, false>(ctx, A, ld, m, j0, jb, d_ipiv, cluster, rpc);
-    }
+    if (rpt <= 1) rs = launch_reg<1>(ctx, A, ld, m, j0, jb, d_ipiv, cluster, rpc);
+    else if (rpt <= 2) rs = launch_reg<2>(ctx, A, ld, m, j0, jb, d_ipiv, cluster, rpc);
+    else if (rpt <= 4) rs = launch_reg<4>(ctx, A, ld, m, j0, jb, d_ipiv, cluster, rpc);
     if (rs != LA_UNSUPPORTED) return rs;
   }
   const size_t smem = (size_t)rpc * (CP + 1) * sizeof(float);

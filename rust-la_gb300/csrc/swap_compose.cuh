@@ -34,11 +34,9 @@ __device__ __forceinline__ int swap_find(const int* arr, int na, int val, int la
 // must end at position j0 + c; x_c is its position at step c, written to
 // ipiv[j0 + c] when ipiv is non-null. Writes the moves to swaps: swaps[0] =
 // count, swaps[1 + i] = dst, swaps[1 + 2 MAX_PANEL_W + i] = src.
-// Returns the number of slots used (the positions whose row changed at some
-// step); at_pos[t] holds original row at_row[t] at the end.
-__device__ __forceinline__ int compose_swaps_warp(const int* fin, int jb, int j0, bool by_row,
-                                                  int* ipiv, int* swaps, int* at_pos,
-                                                  int* at_row, int lane) {
+__device__ __forceinline__ void compose_swaps_warp(const int* fin, int jb, int j0, bool by_row,
+                                                   int* ipiv, int* swaps, int* at_pos,
+                                                   int* at_row, int lane) {
   int na = 0;
   for (int c = 0; c < jb; c++) {
     const int a = j0 + c;
@@ -80,5 +78,4 @@ __device__ __forceinline__ int compose_swaps_warp(const int* fin, int jb, int j0
     k += __popc(b);
   }
   if (lane == 0) swaps[0] = k;
-  return na;
 }

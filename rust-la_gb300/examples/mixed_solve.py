@@ -4,8 +4,8 @@
 
 precision: 1 = BF16, 2 = FP16 (default), 3 = FP32, 4 = split FP8 (e4m3 high and
 low parts), 6 = split FP16 trailing updates. panel: the FP32 panel kernel
-(LA_OPT_CLUSTER_PANEL: 1 = cluster with partial pivoting, the default;
-2 = cluster with tournament pivoting; 0 = cooperative). A is N(0,1) + 2 sqrt(n) I
+(LA_OPT_CLUSTER_PANEL: 1 = one thread-block cluster, the default;
+0 = cooperative). A is N(0,1) + 2 sqrt(n) I
 (seed 3), four right-hand sides; prints the factor and refinement times of the
 second of two runs (the first pays the one-time kernel set-up) and the final
 backward error.
