@@ -378,6 +378,15 @@ la_status la_mlp_gradients(la_mlp mlp, const float* d_x, const int* d_y, int cou
  * loss (host, may be NULL) is taken before the step and synchronizes. */
 la_status la_mlp_train_step(la_mlp mlp, const float* d_x, const int* d_y, int count, float lr,
                             float* loss);
+/* The same two calls for the expected cost instead of the cross-entropy:
+ * d_cost [count][3] (device) holds each sample's cost of the three classes
+ * (e.g. measured cycles, scaled), and the loss is the mean over the samples
+ * of sum_c p_c cost_c, so that training weighs each system by what a wrong
+ * class costs it rather than counting mistakes. */
+la_status la_mlp_gradients_cost(la_mlp mlp, const float* d_x, const float* d_cost, int count,
+                                float* grad, float* loss);
+la_status la_mlp_train_step_cost(la_mlp mlp, const float* d_x, const float* d_cost, int count,
+                                 float lr, float* loss);
 /* Class probabilities (d_probs [count][3], may be NULL) and argmax classes
  * (d_class, may be NULL; 3 where the gate below sends the system straight to
  * the FP64 pass); asynchronous on the context's stream. */

@@ -73,7 +73,24 @@ def mlp_loss_grad(p, X, y):
     return loss, np.concatenate([g[name].ravel() for name, _ in SHAPES])
 
 
-def numeric_grad(p, X, y, idx, h=1e-6):
+def mlp_cost_grad(p, X, cost):
+    """Mean expected cost sum_c p_c cost_c (cost [m, 3]) and its gradient
+    w.r.t. the NPARAM weights (logit delta p_c (cost_c - sum_j p_j cost_j))."""
+    P = unpack(p)
+    x, h1, h2, pr = _forward(P, X)
+    m = x.shape[0]
+    cost = np.asarray(cost, dtype=np.float64)
+    ec = (pr * cost).sum(1)
+    loss = float(ec.mean())
+    d3 = pr * (cost - ec[:, None])
+    d2 = (d3 @ P["W3"]) * (h2 > 0)
+    d1 = (d2 @ P["W2"]) * (h1 > 0)
+    g = {"W3": d3.T @ h2 / m, "b3": d3.sum(0) / m, "W2": d2.T @ h1 / m, "b2": d2.sum(0) / m,
+         "W1": d1.T @ x / m, "b1": d1.sum(0) / m}
+    return loss, np.concatenate([g[name].ravel() for name, _ in SHAPES])
+
+
+def numeric_grad(p, X, y, idx, h=1e-6, loss_fn=None):
     """Central-difference derivative of the loss for the parameters in idx."""
     p = np.asarray(p, dtype=np.float64)
     out = []
@@ -81,7 +98,8 @@ def numeric_grad(p, X, y, idx, h=1e-6):
         a, b = p.copy(), p.copy()
         a[i] += h
         b[i] -= h
-        out.append((mlp_loss_grad(a, X, y)[0] - mlp_loss_grad(b, X, y)[0]) / (2 * h))
+        f = loss_fn or mlp_loss_grad
+        out.append((f(a, X, y)[0] - f(b, X, y)[0]) / (2 * h))
     return np.array(out)
 
 

@@ -548,7 +548,10 @@ __device__ void mlp_fwd(const float* __restrict__ P, const float* x, float* h1, 
 }
 
 // One thread per sample: normalise, forward, keep activations; with labels,
-// also the per-sample output delta and loss.
+// also the per-sample output delta and loss: the softmax cross-entropy, or,
+// with per-sample class costs (cost, NC per sample), the expected cost
+// sum_c p_c cost_c, whose gradient with respect to the logits is
+// p_c (cost_c - sum_j p_j cost_j).
 // Gate of the class output (inference): a linear score of the raw features
 // and the class probabilities, w[0..15] . x + w[16..18] . p + b; a system
 // whose score is >= 0 gets class 3 (no mixed attempt, straight to the FP64
@@ -564,7 +567,8 @@ __global__ void mlp_forward_kernel(const float* __restrict__ P, const float* __r
                                    const float* __restrict__ stdv, const float* __restrict__ X,
                                    int count, float* __restrict__ act, float* __restrict__ probs,
                                    int* __restrict__ cls, const int* __restrict__ y,
-                                   float* __restrict__ loss, Gate gate) {
+                                   const float* __restrict__ cost, float* __restrict__ loss,
+                                   Gate gate) {
   __shared__ float Ps[NPARAM];
   for (int i = threadIdx.x; i < NPARAM; i += blockDim.x) Ps[i] = P[i];
   __syncthreads();
@@ -578,7 +582,13 @@ __global__ void mlp_forward_kernel(const float* __restrict__ P, const float* __r
     for (int k = 0; k < NF; k++) a[k] = x[k];
     for (int k = 0; k < H1; k++) a[NF + k] = h1[k];
     for (int k = 0; k < H2; k++) a[NF + H1 + k] = h2[k];
-    for (int k = 0; k < NC; k++) a[NF + H1 + H2 + k] = pr[k] - ((y && y[s] == k) ? 1.f : 0.f);
+    if (cost) {
+      float ec = 0.f;
+      for (int k = 0; k < NC; k++) ec = fmaf(pr[k], cost[(size_t)s * NC + k], ec);
+      for (int k = 0; k < NC; k++) a[NF + H1 + H2 + k] = pr[k] * (cost[(size_t)s * NC + k] - ec);
+    } else {
+      for (int k = 0; k < NC; k++) a[NF + H1 + H2 + k] = pr[k] - ((y && y[s] == k) ? 1.f : 0.f);
+    }
   }
   if (probs)
     for (int k = 0; k < NC; k++) probs[(size_t)s * NC + k] = pr[k];
@@ -594,7 +604,13 @@ __global__ void mlp_forward_kernel(const float* __restrict__ P, const float* __r
     }
     cls[s] = best;
   }
-  if (loss && y) loss[s] = -logf(fmaxf(pr[y[s]], 1e-30f));
+  if (loss && cost) {
+    float ec = 0.f;
+    for (int k = 0; k < NC; k++) ec = fmaf(pr[k], cost[(size_t)s * NC + k], ec);
+    loss[s] = ec;
+  } else if (loss && y) {
+    loss[s] = -logf(fmaxf(pr[y[s]], 1e-30f));
+  }
 }
 
 // Hidden-layer deltas per sample: d2 = (W3^T d3) . [h2 > 0], d1 = (W2^T d2) . [h1 > 0].
@@ -624,8 +640,8 @@ __global__ void mlp_delta_kernel(const float* __restrict__ P, const float* __res
   }
 }
 
-// Mean gradient of the cross-entropy: one thread per parameter, samples summed
-// in index order (deterministic).
+// Mean gradient of the loss: one thread per parameter, samples summed in index
+// order (deterministic).
 __global__ void mlp_grad_kernel(const float* __restrict__ act, const float* __restrict__ delta,
                                 int count, float* __restrict__ G) {
   const int pidx = blockIdx.x * blockDim.x + threadIdx.x;
@@ -729,9 +745,11 @@ la_status la_mlp_set_params(la_mlp m, const float* params) {
   return la_sync_and_check(m->ctx, "mlp params");
 }
 
-// Mean cross-entropy gradient for labels y over count samples (device X, y),
-// without updating; grad (host, NPARAM) may be NULL.
-static la_status mlp_backprop(la_mlp m, const float* d_x, const int* d_y, int count, float* loss) {
+// Mean gradient over count samples (device X) of the cross-entropy for labels
+// y, or of the expected cost for per-sample class costs (d_cost non-null),
+// into m->grad(), without updating.
+static la_status mlp_backprop(la_mlp m, const float* d_x, const int* d_y, const float* d_cost,
+                              int count, float* loss) {
   la_ctx ctx = m->ctx;
   float *act = nullptr, *delta = nullptr, *dl = nullptr;
   la_status s = la_device_alloc(ctx, reinterpret_cast<void**>(&act), (size_t)count * ACT * 4);
@@ -740,7 +758,7 @@ static la_status mlp_backprop(la_mlp m, const float* d_x, const int* d_y, int co
   if (s == LA_OK) {
     const int g = (count + 127) / 128;
     mlp_forward_kernel<<<g, 128, 0, ctx->stream>>>(m->P(), m->mean(), m->stdv(), d_x, count, act,
-                                                   nullptr, nullptr, d_y, dl, Gate{});
+                                                   nullptr, nullptr, d_y, d_cost, dl, Gate{});
     mlp_delta_kernel<<<g, 128, 0, ctx->stream>>>(m->P(), act, count, delta);
     mlp_grad_kernel<<<(NPARAM + 127) / 128, 128, 0, ctx->stream>>>(act, delta, count, m->grad());
     ctx->launches += 3;
@@ -765,7 +783,7 @@ la_status la_mlp_gradients(la_mlp m, const float* d_x, const int* d_y, int count
                            float* loss) {
   if (!m || !d_x || !d_y || count <= 0) return LA_INVALID;
   LA_CUDA(m->ctx, cudaSetDevice(m->ctx->device));
-  LA_TRY(mlp_backprop(m, d_x, d_y, count, loss));
+  LA_TRY(mlp_backprop(m, d_x, d_y, nullptr, count, loss));
   if (grad) {
     LA_CUDA(m->ctx, cudaMemcpyAsync(grad, m->grad(), NPARAM * sizeof(float),
                                     cudaMemcpyDeviceToHost, m->ctx->stream));
@@ -777,7 +795,31 @@ la_status la_mlp_train_step(la_mlp m, const float* d_x, const int* d_y, int coun
                             float* loss) {
   if (!m || !d_x || !d_y || count <= 0) return LA_INVALID;
   LA_CUDA(m->ctx, cudaSetDevice(m->ctx->device));
-  LA_TRY(mlp_backprop(m, d_x, d_y, count, loss));
+  LA_TRY(mlp_backprop(m, d_x, d_y, nullptr, count, loss));
+  m->step++;
+  adam_kernel<<<(NPARAM + 127) / 128, 128, 0, m->ctx->stream>>>(m->P(), m->grad(), m->am(),
+                                                                 m->av(), lr, m->step);
+  m->ctx->launches++;
+  return la_check_launch(m->ctx, "adam");
+}
+
+la_status la_mlp_gradients_cost(la_mlp m, const float* d_x, const float* d_cost, int count,
+                                float* grad, float* loss) {
+  if (!m || !d_x || !d_cost || count <= 0) return LA_INVALID;
+  LA_CUDA(m->ctx, cudaSetDevice(m->ctx->device));
+  LA_TRY(mlp_backprop(m, d_x, nullptr, d_cost, count, loss));
+  if (grad) {
+    LA_CUDA(m->ctx, cudaMemcpyAsync(grad, m->grad(), NPARAM * sizeof(float),
+                                    cudaMemcpyDeviceToHost, m->ctx->stream));
+  }
+  return la_sync_and_check(m->ctx, "mlp gradients (cost)");
+}
+
+la_status la_mlp_train_step_cost(la_mlp m, const float* d_x, const float* d_cost, int count,
+                                 float lr, float* loss) {
+  if (!m || !d_x || !d_cost || count <= 0) return LA_INVALID;
+  LA_CUDA(m->ctx, cudaSetDevice(m->ctx->device));
+  LA_TRY(mlp_backprop(m, d_x, nullptr, d_cost, count, loss));
   m->step++;
   adam_kernel<<<(NPARAM + 127) / 128, 128, 0, m->ctx->stream>>>(m->P(), m->grad(), m->am(),
                                                                  m->av(), lr, m->step);
@@ -806,7 +848,7 @@ la_status la_mlp_predict(la_mlp m, const float* d_x, int count, float* d_probs, 
   LA_CUDA(m->ctx, cudaSetDevice(m->ctx->device));
   mlp_forward_kernel<<<(count + 127) / 128, 128, 0, m->ctx->stream>>>(
       m->P(), m->mean(), m->stdv(), d_x, count, nullptr, d_probs, d_class, nullptr, nullptr,
-      m->gate);
+      nullptr, m->gate);
   m->ctx->launches++;
   return la_check_launch(m->ctx, "mlp predict");
 }

@@ -2,7 +2,7 @@
 
     python rust-la_gb300/examples/train_selector.py [--train 200000] [--test 50000]
         [--out rust-la_gb300/selector_weights.npy] [--summary path.json] [--gate-only]
-        [--dump path.npz] [--gate-from path.npz]
+        [--dump path.npz] [--gate-from path.npz] [--loss cost|xent]
 
 Training data: --train Householder-conditioned systems (n uniform in [16, 512],
 1-4 right-hand sides, log10 kappa_2 uniform in [1, 12]) generated on the GPU
@@ -25,6 +25,12 @@ accuracy, the summed per-system cycles of the selector's choices against
 always-FP32 factors and against the best class per system, and wall-clock
 batch times of (features + inference + solve) against always-FP32 factors and
 against the plain FP64 plan.
+
+--loss cost (the default) trains the MLP on the expected cycles (each system's
+measured cycles of the three classes, scaled by their overall mean) instead of
+the cross-entropy of the cheapest class (--loss xent): a system whose classes
+cost about the same weighs little, one where a wrong class is expensive
+weighs much.
 """
 import argparse
 import json
@@ -78,6 +84,7 @@ def main():
     ap.add_argument("--gate-only", action="store_true")
     ap.add_argument("--dump", default=None)
     ap.add_argument("--gate-from", default=None)
+    ap.add_argument("--loss", default="cost", choices=["cost", "xent"])
     args = ap.parse_args()
     if args.gate_from:  # the gate alone, from a dump of labelled data (no GPU)
         d = np.load(args.gate_from)
@@ -125,7 +132,11 @@ def main():
     else:
         sel = S.PrecisionSelector(ctx, seed=1)
         t0 = time.perf_counter()
-        log = sel.fit(X, y, steps=args.steps, lr=args.lr, batch=4096, log_every=500)
+        costs = None
+        if args.loss == "cost":
+            c = cyc_all.astype(np.float64)
+            costs = torch.from_numpy((c / c.mean()).astype(np.float32)).cuda()
+        log = sel.fit(X, y, steps=args.steps, lr=args.lr, batch=4096, log_every=500, costs=costs)
         t_fit = time.perf_counter() - t0
         sel.save(args.out)
     train_acc = float((sel.predict(X).cpu().numpy() == y).mean())
@@ -194,6 +205,7 @@ def main():
     p64.free()
     summary = {
         "train_systems": args.train, "test_systems": count, "plan": [ctas, warps],
+        "loss": args.loss,
         "train_accuracy": train_acc, "test_accuracy": test_acc,
         "test_label_counts": np.bincount(lab, minlength=3).tolist(),
         "test_pred_counts": np.bincount(pred, minlength=4).tolist(),

@@ -129,6 +129,8 @@ SIGNATURES = {
     "la_mlp_set_params": ([_P, _P], _I),
     "la_mlp_gradients": ([_P, _P, _P, _I, _P, _P], _I),
     "la_mlp_train_step": ([_P, _P, _P, _I, ctypes.c_float, _P], _I),
+    "la_mlp_gradients_cost": ([_P, _P, _P, _I, _P, _P], _I),
+    "la_mlp_train_step_cost": ([_P, _P, _P, _I, ctypes.c_float, _P], _I),
     "la_mlp_predict": ([_P, _P, _I, _P, _P], _I),
     "la_mlp_set_gate": ([_P, _P, ctypes.c_float], _I),
 }
@@ -882,6 +884,23 @@ class Mlp:
         _check(self.ctx, lib().la_mlp_train_step(self.h, ctypes.c_void_p(x_ptr),
                                                  ctypes.c_void_p(y_ptr), count, ctypes.c_float(lr),
                                                  ctypes.byref(loss) if want_loss else None))
+        return loss.value if want_loss else None
+
+    def gradients_cost(self, x_ptr, cost_ptr, count):
+        """Mean expected cost (cost [count, 3] device FP32) and its gradient."""
+        g = np.empty(self.nparam, dtype=np.float32)
+        loss = ctypes.c_float()
+        _check(self.ctx, lib().la_mlp_gradients_cost(self.h, ctypes.c_void_p(x_ptr),
+                                                     ctypes.c_void_p(cost_ptr), count, _ptr(g),
+                                                     ctypes.byref(loss)))
+        return g, loss.value
+
+    def train_step_cost(self, x_ptr, cost_ptr, count, lr, want_loss=False):
+        loss = ctypes.c_float()
+        _check(self.ctx, lib().la_mlp_train_step_cost(self.h, ctypes.c_void_p(x_ptr),
+                                                      ctypes.c_void_p(cost_ptr), count,
+                                                      ctypes.c_float(lr),
+                                                      ctypes.byref(loss) if want_loss else None))
         return loss.value if want_loss else None
 
     def set_gate(self, coef, bias=0.0):

@@ -153,11 +153,17 @@ class PrecisionSelector:
         self.mlp = la_gpu.Mlp(ctx, seed)
         self.gate = None
 
-    def fit(self, feats, labels, steps=1500, lr=3e-3, batch=4096, seed=0, log_every=0):
-        """Adam on minibatches of (feats [m,16] FP32 device, labels [m] int32).
-        Sets the input normalisation from feats. Returns the loss log."""
+    def fit(self, feats, labels, steps=1500, lr=3e-3, batch=4096, seed=0, log_every=0,
+            costs=None):
+        """Adam on minibatches of (feats [m,16] FP32 device, labels [m] int32):
+        the cross-entropy of the labels, or, with costs ([m, 3], each system's
+        cost of each class, e.g. measured cycles scaled to a mean near 1), the
+        expected cost. Sets the input normalisation from feats. Returns the
+        loss log."""
         feats = feats.contiguous()
         labels = torch.as_tensor(labels, dtype=torch.int32, device="cuda").contiguous()
+        if costs is not None:
+            costs = torch.as_tensor(costs, dtype=torch.float32, device="cuda").contiguous()
         m = feats.shape[0]
         p = self.mlp.get_params()
         npar = self.mlp.nparam
@@ -179,9 +185,15 @@ class PrecisionSelector:
             pos += batch
             xb = feats.index_select(0, idx).contiguous()
             yb = labels.index_select(0, idx).contiguous()
+            cb = costs.index_select(0, idx).contiguous() if costs is not None else None
             torch.cuda.synchronize()
             want = bool(log_every) and (step % log_every == 0 or step == steps - 1)
-            loss = self.mlp.train_step(xb.data_ptr(), yb.data_ptr(), batch, lr, want_loss=want)
+            if cb is not None:
+                loss = self.mlp.train_step_cost(xb.data_ptr(), cb.data_ptr(), batch, lr,
+                                                want_loss=want)
+            else:
+                loss = self.mlp.train_step(xb.data_ptr(), yb.data_ptr(), batch, lr,
+                                           want_loss=want)
             if want:
                 log.append((step, loss))
         self.ctx.synchronize()

@@ -91,6 +91,20 @@ def test_mlp_gradients_match_oracle(lagpu, ctx_fast, torch):
     mlp.free()
 
 
+def test_mlp_expected_cost_gradients_match_oracle(lagpu, ctx_fast, torch):
+    mlp = lagpu.Mlp(ctx_fast, seed=3)
+    p = _set_random_params(lagpu, mlp, 4)
+    X, y, dX, dy = _random_mlp_data(torch, 777, 5)
+    cost = np.random.default_rng(6).random((777, 3)).astype(np.float32) * 2.0
+    dc = torch.from_numpy(cost).cuda()
+    torch.cuda.synchronize()
+    g, loss = mlp.gradients_cost(dX.data_ptr(), dc.data_ptr(), len(y))
+    want_loss, want = sr.mlp_cost_grad(p.astype(np.float64), X, cost.astype(np.float64))
+    assert abs(loss - want_loss) <= 1e-5 * max(1.0, abs(want_loss))
+    assert np.allclose(g, want, rtol=2e-4, atol=2e-6)
+    mlp.free()
+
+
 def test_mlp_predict_matches_oracle(lagpu, ctx_fast, torch):
     mlp = lagpu.Mlp(ctx_fast, seed=5)
     p = _set_random_params(lagpu, mlp, 6)

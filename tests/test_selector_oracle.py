@@ -27,6 +27,22 @@ def test_mlp_analytic_gradient_matches_central_differences():
     assert np.allclose(g[idx], num, rtol=1e-5, atol=1e-8)
 
 
+def test_mlp_expected_cost_gradient_matches_central_differences():
+    rng = np.random.default_rng(11)
+    p = _params(12)
+    X = rng.standard_normal((40, 16))
+    cost = rng.random((40, 3)) * 3.0
+    loss, g = sr.mlp_cost_grad(p, X, cost)
+    assert g.shape == (sr.NPARAM,) and np.isfinite(loss)
+    idx = np.concatenate([rng.choice(sr.NPARAM, 60, replace=False),
+                          np.arange(sr.NPARAM - 3, sr.NPARAM)])
+    num = sr.numeric_grad(p, X, cost, idx, loss_fn=sr.mlp_cost_grad)
+    assert np.allclose(g[idx], num, rtol=1e-5, atol=1e-8)
+    # a cost vector that is the same for every class has no gradient
+    flat = np.repeat(cost[:, :1], 3, axis=1)
+    assert np.allclose(sr.mlp_cost_grad(p, X, flat)[1], 0.0, atol=1e-12)
+
+
 def test_mlp_forward_is_a_distribution():
     rng = np.random.default_rng(3)
     pr = sr.mlp_forward(_params(4), rng.standard_normal((25, 16)))
