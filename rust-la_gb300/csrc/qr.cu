@@ -14,14 +14,15 @@
 // target column, each walking the rows in the reference's order with unfused
 // products and sums, so the factors, Q and the solution are bit-identical to
 // the reference; the column norm is one thread's ascending sum.
-// FAST: qr_reflect_fast_kernel, 4 target columns per CTA and 64 row slots
-// (many CTAs per SM, short dependent chains), the dot products reduced by warp
-// shuffles and across warps, then the update with FMA; in the factorization
-// the CTA that holds the next column also takes that column's norm and
-// diagonal once its update is done, so each column costs one launch. The back-substitution of solve is the wavefront
-// upper solve on R (the reference's descending term order, then the division
-// by rdiag). The reflections are sequential by nature (each depends on the
-// last); the work per step is spread over the columns.
+// FAST, from 128 columns while the rows fit one cluster: blocks of 64
+// reflections in compact WY form (qr_blocked.cu), and get_q and solve block by
+// block. FAST otherwise: qr_reflect_fast_kernel, 4 target columns per CTA and
+// 64 row slots (many CTAs per SM, short dependent chains), the dot products
+// reduced by warp shuffles and across warps, then the update with FMA; in the
+// factorization the CTA that holds the next column also takes that column's
+// norm and diagonal once its update is done, so each column costs one launch.
+// The back-substitution of solve is the wavefront upper solve on R (the
+// reference's descending term order, then the division by rdiag).
 #include <cstring>
 
 #include "la_internal.cuh"
