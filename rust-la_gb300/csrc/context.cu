@@ -263,6 +263,9 @@ la_status la_ctx_set_option(la_ctx ctx, int option, int64_t value) {
       if (value < 0 || value > (1 << 20)) return LA_INVALID;
       ctx->inject_panel_stall = (int)value;
       return LA_OK;
+    case LA_OPT_PDL:
+      ctx->pdl = value ? 1 : 0;
+      return LA_OK;
   }
   return LA_INVALID;
 }
@@ -282,6 +285,7 @@ la_status la_ctx_get_option(la_ctx ctx, int option, int64_t* value) {
     case LA_OPT_INJECT_IR_STALL: *value = ctx->inject_ir_stall; return LA_OK;
     case LA_OPT_WAIT_LIMIT_US: *value = ctx->wait_limit_us; return LA_OK;
     case LA_OPT_INJECT_PANEL_STALL: *value = ctx->inject_panel_stall; return LA_OK;
+    case LA_OPT_PDL: *value = ctx->pdl; return LA_OK;
   }
   return LA_INVALID;
 }

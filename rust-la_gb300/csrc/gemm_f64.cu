@@ -88,6 +88,8 @@ __global__ void __launch_bounds__(THREADS)
 gemm_f64_kernel(int M, int N, int K, const T* __restrict__ A, size_t lda,
                 const T* __restrict__ B, size_t ldb, T* __restrict__ C, size_t ldc, int kper,
                 size_t czs) {
+  la_pdl_wait();
+  la_pdl_trigger();
   constexpr int TN = BN / 16;
   extern __shared__ __align__(16) double smem_raw[];
   T* smem = reinterpret_cast<T*>(smem_raw);
@@ -343,8 +345,9 @@ la_status launch_mode(la_ctx ctx, int M, int N, int K, const T* A, size_t lda, c
   });
   if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaFuncSetAttribute(gemm)");
   dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, splits);
-  gemm_f64_kernel<T, MODE, BN><<<grid, THREADS, smem, ctx->stream>>>(
-      M, N, K, A, lda, B, ldb, C, ldc, splits > 1 ? kper : K, czs);
+  e = la_launch(ctx, gemm_f64_kernel<T, MODE, BN>, grid, dim3(THREADS), smem, ctx->stream, M, N, K,
+                A, lda, B, ldb, C, ldc, splits > 1 ? kper : K, czs);
+  if (e != cudaSuccess) return la_cuda_fail(ctx, e, "gemm_f64_kernel launch");
   ctx->launches++;
   return la_check_launch(ctx, "gemm_f64_kernel");
 }

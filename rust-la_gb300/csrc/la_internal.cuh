@@ -110,6 +110,8 @@ struct la_context {
   int panel_width = 64;
   int panel_ctas = 0;
   int profile = 0;
+  int pdl = 1;                           // LA_OPT_PDL: dependent launches in the mixed LU's panel chain
+  bool pdl_now = false;                  // set while that chain is being enqueued
   std::string last_error;
   uint64_t launches = 0;
   double phase_ms[5] = {0, 0, 0, 0, 0};
@@ -151,6 +153,41 @@ struct la_lu_handle {
   int lowp = 0;                  // LA_PREC_* of the trailing update
 };
 
+
+// Programmatic dependent launch. A kernel launched with
+// cudaLaunchAttributeProgrammaticStreamSerialization (la_launch with
+// ctx->pdl_now set) may be scheduled while the kernel before it on the stream
+// still runs; la_pdl_wait blocks until that kernel has completed and its
+// writes are visible, so every such kernel calls it before touching global
+// memory. la_pdl_trigger lets the next kernel be scheduled once every CTA of
+// this one has passed it. Both return at once in a kernel launched without
+// the attribute.
+__device__ __forceinline__ void la_pdl_wait() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+__device__ __forceinline__ void la_pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Launches kernel k on stream s, as a programmatic dependent launch when
+// ctx->pdl_now is set.
+template <typename... KArgs, typename... Args>
+cudaError_t la_launch(la_ctx ctx, void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                      cudaStream_t s, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  if (ctx->pdl_now) {
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+  }
+  return cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
+}
 
 // Host helpers (context.cu).
 la_status la_cuda_fail(la_ctx ctx, cudaError_t e, const char* what);

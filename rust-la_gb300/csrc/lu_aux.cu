@@ -20,6 +20,8 @@ template <typename T>
 __global__ void __launch_bounds__(256)
 laswp_kernel(T* M0, T* M1, T* M2, size_t ld, int b0, int e0, int b1, int e1,
              int b2, int e2, const int* __restrict__ swaps, const int* err) {
+  la_pdl_wait();
+  la_pdl_trigger();
   __shared__ T tmp[2 * MAX_PANEL_W][SW_COLS];
   __shared__ int s_abort;
   if (threadIdx.x == 0) s_abort = aborted(err);
@@ -132,6 +134,8 @@ constexpr int TRR_W = 32;
 constexpr int TRR_T = 128;
 __global__ void __launch_bounds__(TRR_T)
 trsm_rowpanel_reg_kernel(float* A, size_t ld, int j0, int jb, int c_begin, int c_end) {
+  la_pdl_wait();
+  la_pdl_trigger();
   __shared__ float L[TRR_W][TRR_W + 1];
   for (int idx = threadIdx.x; idx < jb * jb; idx += TRR_T) {
     const int i = idx / jb, k = idx % jb;
@@ -376,8 +380,10 @@ la_status launch_laswp_t(la_ctx ctx, cudaStream_t stream, bool exact, T* A, T* S
   const int gx = std::max((left + SW_COLS - 1) / SW_COLS, (right + SW_COLS - 1) / SW_COLS);
   if (gx == 0) return LA_OK;
   dim3 grid(gx, exact ? 3 : 2);
-  laswp_kernel<T><<<grid, 256, 0, stream>>>(A, A, exact ? S : nullptr, ld, 0, j0, j1, n, j1, n,
-                                            ctx->d_swaps, ctx->d_err);
+  const cudaError_t e = la_launch(ctx, laswp_kernel<T>, grid, dim3(256), 0, stream, A, A,
+                                  exact ? S : nullptr, ld, 0, j0, j1, n, j1, n,
+                                  (const int*)ctx->d_swaps, (const int*)ctx->d_err);
+  if (e != cudaSuccess) return la_cuda_fail(ctx, e, "laswp_kernel launch");
   ctx->launches++;
   return la_check_launch(ctx, "laswp_kernel");
 }
@@ -439,7 +445,9 @@ la_status launch_trsm_rowpanel_f32(la_ctx ctx, float* A, size_t ld, int j0, int 
   if (jb > TRR_W) return launch_trsm_t<float>(ctx, false, A, nullptr, ld, j0, jb, c_begin, c_end);
   if (c_end <= c_begin) return LA_OK;
   const int grid = (c_end - c_begin + TRR_T - 1) / TRR_T;
-  trsm_rowpanel_reg_kernel<<<grid, TRR_T, 0, ctx->stream>>>(A, ld, j0, jb, c_begin, c_end);
+  const cudaError_t e = la_launch(ctx, trsm_rowpanel_reg_kernel, dim3(grid), dim3(TRR_T), 0,
+                                  ctx->stream, A, ld, j0, jb, c_begin, c_end);
+  if (e != cudaSuccess) return la_cuda_fail(ctx, e, "trsm_rowpanel_reg_kernel launch");
   ctx->launches++;
   return la_check_launch(ctx, "trsm_rowpanel_reg_kernel");
 }

@@ -414,6 +414,9 @@ la_status mixed_factor(la_ctx ctx, la_lu h, int prec) {
   auto inner = [&](int j0, int j1o, int climit, cudaStream_t s) -> la_status {
     cudaStream_t saved = ctx->stream;
     ctx->stream = s;
+    // panel, row swaps, triangular solve and rank-32 update follow one
+    // another on s: each may be scheduled while the one before it finishes
+    ctx->pdl_now = ctx->pdl != 0;
     la_status st = LA_OK;
     for (int i0 = j0; i0 < j1o && st == LA_OK; i0 += WI) {
       const int ib = std::min(WI, j1o - i0);
@@ -434,6 +437,7 @@ la_status mixed_factor(la_ctx ctx, la_lu h, int prec) {
                                ld, A + (size_t)i0 * ld + i1, ld, A + (size_t)i1 * ld + i1, ld);
       }
     }
+    ctx->pdl_now = false;
     ctx->stream = saved;
     return st;
   };

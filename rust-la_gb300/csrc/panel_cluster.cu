@@ -409,6 +409,8 @@ __device__ __forceinline__ bool panel_column(int c, const ClusterPanelArgs& p, i
 
 template <int RPT>
 __global__ void __launch_bounds__(CT, 1) panel_cluster_reg_kernel(ClusterPanelArgs p) {
+  la_pdl_wait();
+  la_pdl_trigger();
   __shared__ __align__(16) float wrow[2][PNW][CW];
   __shared__ unsigned long long wkey[2][PNW];
   __shared__ __align__(16) uint32_t recv[2][16][PSLOT];
@@ -551,13 +553,15 @@ la_status launch_reg(la_ctx ctx, float* A, size_t ld, int m, int j0, int jb, int
   cfg.blockDim = dim3(CT);
   cfg.dynamicSmemBytes = 0;
   cfg.stream = ctx->stream;
-  cudaLaunchAttribute at[1];
+  cudaLaunchAttribute at[2];
   at[0].id = cudaLaunchAttributeClusterDimension;
   at[0].val.clusterDim.x = cluster;
   at[0].val.clusterDim.y = 1;
   at[0].val.clusterDim.z = 1;
+  at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[1].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = at;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = ctx->pdl_now ? 2 : 1;
   cudaError_t e = cudaLaunchKernelEx(&cfg, panel_cluster_reg_kernel<RPT>, a);
   if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaLaunchKernelEx(panel_cluster_reg)");
   ctx->launches++;

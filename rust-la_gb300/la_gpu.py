@@ -31,6 +31,7 @@ OPT_BATCH_GMRES = 7
 OPT_SOLVE_WAVE = 8
 OPT_INJECT_ALLOC_FAIL, OPT_INJECT_IR_STALL = 10, 11
 OPT_WAIT_LIMIT_US, OPT_INJECT_PANEL_STALL = 12, 13
+OPT_PDL = 14
 ARITH_FAST, ARITH_EXACT = 0, 1
 
 
