@@ -14,6 +14,8 @@ the oracle (the CPU restatement of src/decomp/lu.rs:104-278).
   oracle on a sample, and the FP64 pass's row order against the oracle's
   pivots system by system.
 """
+import hashlib
+import json
 import os
 
 import numpy as np
@@ -30,21 +32,58 @@ def torch():
     return pytest.importorskip("torch")
 
 
+GOLDEN2 = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "config2_n8192.json")
+
+
+def _digest(x):
+    return hashlib.sha256(np.ascontiguousarray(x).tobytes()).hexdigest()
+
+
+class _Config2Ref:
+    """The oracle's answer on the benchmark's inputs as SHA-256 digests of its
+    exact bytes: from tests/golden/config2_n8192.json (made by
+    tests/golden/make_golden_config2.py) when this machine's generator gives
+    the same inputs, else from the oracle run here (minutes)."""
+
+    def __init__(self, a, b):
+        rec = None
+        if os.path.exists(GOLDEN2):
+            with open(GOLDEN2) as f:
+                rec = json.load(f)
+            if rec["sha256_a"] != _digest(a) or rec["sha256_b"] != _digest(b):
+                rec = None
+        if rec is None:
+            threads = os.cpu_count() or 4
+            ref = oracle.lu_factor(a, threads=threads)
+            rec = {"sha256_lu": _digest(ref.lu), "sha256_piv": _digest(ref.piv.astype(np.uint64)),
+                   "sha256_x": _digest(oracle.solve_mt(ref, b, threads)),
+                   "pospivsign": int(ref.pospivsign)}
+        self.rec = rec
+
+    def piv_matches(self, piv):
+        return _digest(np.asarray(piv, dtype=np.uint64)) == self.rec["sha256_piv"]
+
+    def lu_matches(self, lu):
+        return _digest(np.asarray(lu, dtype=np.float64)) == self.rec["sha256_lu"]
+
+    def x_matches(self, x):
+        return _digest(np.asarray(x, dtype=np.float64)) == self.rec["sha256_x"]
+
+
 @pytest.fixture(scope="module")
 def config2():
     n, nrhs = 8192, 16
     rng = np.random.default_rng(2)  # the benchmark's inputs
     a = rng.standard_normal((n, n))
     b = rng.standard_normal((n, nrhs))
-    ref = oracle.lu_factor(a, threads=os.cpu_count() or 4)
-    return a, b, ref
+    return a, b, _Config2Ref(a, b)
 
 
 def test_config2_fast_pivots_and_eta(lagpu, ctx_fast, config2):
     a, b, ref = config2
     lu = lagpu.LUDecomposition.new(a, ctx_fast)
-    assert np.array_equal(lu.get_piv(), ref.piv)
-    assert lu.pospivsign() == bool(ref.pospivsign)
+    assert ref.piv_matches(lu.get_piv())
+    assert lu.pospivsign() == bool(ref.rec["pospivsign"])
     x = lu.solve(lagpu.Matrix(b, ctx_fast)).data
     lu.free()
     assert oracle.backward_error(a, x, b) <= ETA_MAX
@@ -53,12 +92,12 @@ def test_config2_fast_pivots_and_eta(lagpu, ctx_fast, config2):
 def test_config2_exact_bit_identical(lagpu, ctx_exact, config2):
     a, b, ref = config2
     lu = lagpu.LUDecomposition.new(a, ctx_exact)
-    assert np.array_equal(lu.get_piv(), ref.piv)
-    assert lu.pospivsign() == bool(ref.pospivsign)
-    assert np.array_equal(lu.get_packed().data, ref.lu)
+    assert ref.piv_matches(lu.get_piv())
+    assert lu.pospivsign() == bool(ref.rec["pospivsign"])
+    assert ref.lu_matches(lu.get_packed().data)
     x = lu.solve(lagpu.Matrix(b, ctx_exact)).data
     lu.free()
-    assert np.array_equal(x, oracle.solve_mt(ref, b, os.cpu_count() or 4))
+    assert ref.x_matches(x)
 
 
 @pytest.fixture(scope="module")

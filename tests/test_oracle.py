@@ -158,3 +158,19 @@ def test_backward_error_small():
     eta = oracle.backward_error(a, x, b)
     assert 0 <= eta < 1e-15
     assert oracle.backward_error(a, x + 1e-3, b) > 1e-6
+
+
+def test_benchmark_workload_fixture_matches_this_generator():
+    # tests/golden/config2_n8192.json holds the oracle's answer on the
+    # benchmark's n = 8192 inputs as digests; the GPU parity test relies on
+    # this machine's generator giving the same inputs.
+    import hashlib
+    with open(os.path.join(HERE, "golden", "config2_n8192.json")) as f:
+        rec = json.load(f)
+    rng = np.random.default_rng(rec["seed"])
+    a = rng.standard_normal((rec["n"], rec["n"]))
+    b = rng.standard_normal((rec["n"], rec["nrhs"]))
+    assert hashlib.sha256(a.tobytes()).hexdigest() == rec["sha256_a"]
+    assert hashlib.sha256(b.tobytes()).hexdigest() == rec["sha256_b"]
+    assert rec["backward_error"] <= 1e-14
+    assert len(rec["sha256_lu"]) == len(rec["sha256_piv"]) == len(rec["sha256_x"]) == 64
