@@ -84,6 +84,8 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tmap_a,
                  const __grid_constant__ CUtensorMap tmap_b,
                  const __grid_constant__ CUtensorMap tmap_c, int N, int K, int lo,
                  const float* __restrict__ alpha_ptr, uint32_t idesc, int* err) {
+  la_pdl_wait();
+  la_pdl_trigger();
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], done;
   __shared__ uint32_t tmem_holder;
@@ -306,15 +308,17 @@ la_status launch_tc_update(la_ctx ctx, cudaStream_t stream, int fmt, int M, int 
   });
   if (e != cudaSuccess) return la_cuda_fail(ctx, e, "cudaFuncSetAttribute(tc_update)");
   dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM);
+  const float* alpha = d_alpha;
   if (f8)
-    tc_update_kernel<true, true><<<grid, TC_THREADS, TC_SMEM, stream>>>(
-        ta, tb, tc, N, K, lo, d_alpha, idesc_mma(0u), ctx->d_err);
+    e = la_launch(ctx, tc_update_kernel<true, true>, grid, dim3(TC_THREADS), TC_SMEM, stream, ta,
+                  tb, tc, N, K, lo, alpha, idesc_mma(0u), ctx->d_err);
   else if (split)
-    tc_update_kernel<false, true><<<grid, TC_THREADS, TC_SMEM, stream>>>(
-        ta, tb, tc, N, K, lo, d_alpha, idesc_mma(0u), ctx->d_err);
+    e = la_launch(ctx, tc_update_kernel<false, true>, grid, dim3(TC_THREADS), TC_SMEM, stream, ta,
+                  tb, tc, N, K, lo, alpha, idesc_mma(0u), ctx->d_err);
   else
-    tc_update_kernel<false, false><<<grid, TC_THREADS, TC_SMEM, stream>>>(
-        ta, tb, tc, N, K, 0, d_alpha, idesc_mma(fmt == LA_LOWP_BF16 ? 1u : 0u), ctx->d_err);
+    e = la_launch(ctx, tc_update_kernel<false, false>, grid, dim3(TC_THREADS), TC_SMEM, stream, ta,
+                  tb, tc, N, K, 0, alpha, idesc_mma(fmt == LA_LOWP_BF16 ? 1u : 0u), ctx->d_err);
+  if (e != cudaSuccess) return la_cuda_fail(ctx, e, "tc_update_kernel launch");
   ctx->launches++;
   return la_check_launch(ctx, "tc_update_kernel");
 }

@@ -56,6 +56,8 @@ laswp_kernel(T* M0, T* M1, T* M2, size_t ld, int b0, int e0, int b1, int e1,
 template <typename T>
 __global__ void laswp_seq_kernel(T* A, size_t ld, const int* __restrict__ ipiv, int k0, int k1,
                                  int c0, int c1, const int* err) {
+  la_pdl_wait();
+  la_pdl_trigger();
   const int c = c0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= c1 || aborted(err)) return;  // no barrier in this kernel
   for (int k = k0; k < k1; k++) {
@@ -174,6 +176,8 @@ constexpr int TB_R = 256, TB_C = 32;
 constexpr size_t TB_SMEM = (size_t)2 * TB_R * (TB_C + 1) * sizeof(float);
 __global__ void __launch_bounds__(256)
 trsm_block_kernel(float* A, size_t ld, int j0, int jbo, int c_begin, int c_end) {
+  la_pdl_wait();
+  la_pdl_trigger();
   extern __shared__ __align__(16) float tb_sm[];
   float(*X)[TB_C + 1] = reinterpret_cast<float(*)[TB_C + 1]>(tb_sm);
   float(*Lb)[TB_C + 1] = reinterpret_cast<float(*)[TB_C + 1]>(tb_sm + TB_R * (TB_C + 1));
@@ -405,8 +409,9 @@ la_status launch_trsm_block_f32(la_ctx ctx, float* A, size_t ld, int j0, int jbo
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)TB_SMEM);
           }));
-  trsm_block_kernel<<<(c_end - c_begin + TB_C - 1) / TB_C, 256, TB_SMEM, ctx->stream>>>(
-      A, ld, j0, jbo, c_begin, c_end);
+  const cudaError_t e = la_launch(ctx, trsm_block_kernel, dim3((c_end - c_begin + TB_C - 1) / TB_C),
+                                  dim3(256), TB_SMEM, ctx->stream, A, ld, j0, jbo, c_begin, c_end);
+  if (e != cudaSuccess) return la_cuda_fail(ctx, e, "trsm_block_kernel launch");
   ctx->launches++;
   return la_check_launch(ctx, "trsm_block_kernel");
 }
@@ -414,8 +419,10 @@ la_status launch_trsm_block_f32(la_ctx ctx, float* A, size_t ld, int j0, int jbo
 la_status launch_laswp_seq_f32(la_ctx ctx, float* A, size_t ld, const int* ipiv, int k0, int k1,
                                int c0, int c1) {
   if (k1 <= k0 || c1 <= c0) return LA_OK;
-  laswp_seq_kernel<float><<<(c1 - c0 + 255) / 256, 256, 0, ctx->stream>>>(A, ld, ipiv, k0, k1, c0,
-                                                                          c1, ctx->d_err);
+  const cudaError_t e = la_launch(ctx, laswp_seq_kernel<float>, dim3((c1 - c0 + 255) / 256),
+                                  dim3(256), 0, ctx->stream, A, ld, ipiv, k0, k1, c0, c1,
+                                  (const int*)ctx->d_err);
+  if (e != cudaSuccess) return la_cuda_fail(ctx, e, "laswp_seq_kernel launch");
   ctx->launches++;
   return la_check_launch(ctx, "laswp_seq_kernel");
 }

@@ -54,6 +54,8 @@ __device__ __forceinline__ uint16_t to16(float v) {
 template <int FMT>
 __global__ void pack_l_kernel(const float* __restrict__ src, size_t lds, uint16_t* __restrict__ dst,
                               size_t ldd, int rows, int k) {
+  la_pdl_wait();
+  la_pdl_trigger();
   size_t total = (size_t)rows * ldd;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
        i += (size_t)gridDim.x * blockDim.x) {
@@ -69,6 +71,8 @@ __device__ __forceinline__ void atomic_max_nonneg_f(float* a, float v) {
 // max |U12| for the FP16 scale (stat[0] must start at 0).
 __global__ void absmax_kernel(const float* __restrict__ src, size_t lds, int rows, int cols,
                               float* stat) {
+  la_pdl_wait();
+  la_pdl_trigger();
   float m = 0.f;
   size_t total = (size_t)rows * cols;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
@@ -86,6 +90,8 @@ __global__ void absmax_kernel(const float* __restrict__ src, size_t lds, int row
 template <int FMT>
 __global__ void pack_ut_kernel(const float* __restrict__ src, size_t lds, uint16_t* __restrict__ dst,
                                size_t ldd, int k, int cols, float* stat) {
+  la_pdl_wait();
+  la_pdl_trigger();
   __shared__ float t[32][33];
   float scale = 1.f;
   if (FMT == LA_LOWP_FP16) {
@@ -112,7 +118,12 @@ __global__ void pack_ut_kernel(const float* __restrict__ src, size_t lds, uint16
   }
 }
 
-__global__ void set_alpha_one(float* stat) { stat[0] = 0.f; stat[1] = 1.f; }
+__global__ void set_alpha_one(float* stat) {
+  la_pdl_wait();
+  la_pdl_trigger();
+  stat[0] = 0.f;
+  stat[1] = 1.f;
+}
 
 // Split storage: v (already scaled) ~ hi + lo with hi = rn(v), lo = rn(v - hi)
 // in the storage format (FP8 e4m3 saturating at its largest finite value, or
@@ -146,6 +157,8 @@ struct SplitF16 {
 template <typename SP>
 __global__ void pack_l_split_kernel(const float* __restrict__ src, size_t lds,
                                     typename SP::T* __restrict__ dst, size_t ldd, int rows, int k) {
+  la_pdl_wait();
+  la_pdl_trigger();
   const size_t half = ldd / 2;
   const float sl = ldexpf(1.f, SP::L_EXP);
   size_t total = (size_t)rows * half;
@@ -167,6 +180,8 @@ template <typename SP>
 __global__ void pack_ut_split_kernel(const float* __restrict__ src, size_t lds,
                                      typename SP::T* __restrict__ dst, size_t ldd, int k, int cols,
                                      float* stat) {
+  la_pdl_wait();
+  la_pdl_trigger();
   __shared__ float t[32][33];
   float scale = 1.f;
   const float mx = stat[0];
@@ -475,9 +490,9 @@ la_status mixed_factor(la_ctx ctx, la_lu h, int prec) {
     const float* U12 = A + (size_t)j0 * ld + c0;
     if (prec == LA_PREC_FP8 || prec == LA_PREC_FP16X3) {
       LA_CUDA(ctx, cudaMemsetAsync(d_stat, 0, 2 * sizeof(float), ms));
-      absmax_kernel<<<grid_for(ctx, (size_t)jbo * N), 256, 0, ms>>>(U12, ld, jbo, N, d_stat);
+      LA_CUDA(ctx, la_launch(ctx, absmax_kernel, dim3(grid_for(ctx, (size_t)jbo * N)), dim3(256), 0,
+                             ms, U12, ld, jbo, N, d_stat));
       ctx->launches++;
-      LA_TRY(la_check_launch(ctx, "absmax_kernel"));
       const dim3 pgs((N + 31) / 32, (WO + 31) / 32);
       const size_t lg = grid_for(ctx, (size_t)M * WO);
       void* ub;
@@ -485,18 +500,18 @@ la_status mixed_factor(la_ctx ctx, la_lu h, int prec) {
         uint8_t* u8 = uh.as<uint8_t>() + (size_t)(c0 - j1o) * ldks;
         ub = u8;
         if (pack_l)
-          pack_l_split_kernel<SplitE4M3><<<lg, 256, 0, ms>>>(L21, ld, lh.as<uint8_t>(), ldks, M,
-                                                             jbo);
-        pack_ut_split_kernel<SplitE4M3><<<pgs, dim3(32, 8), 0, ms>>>(U12, ld, u8, ldks, jbo, N,
-                                                                     d_stat);
+          LA_CUDA(ctx, la_launch(ctx, pack_l_split_kernel<SplitE4M3>, dim3(lg), dim3(256), 0, ms,
+                                 L21, ld, lh.as<uint8_t>(), ldks, M, jbo));
+        LA_CUDA(ctx, la_launch(ctx, pack_ut_split_kernel<SplitE4M3>, pgs, dim3(32, 8), 0, ms, U12,
+                               ld, u8, ldks, jbo, N, d_stat));
       } else {
         uint16_t* u16 = uh.as<uint16_t>() + (size_t)(c0 - j1o) * ldks;
         ub = u16;
         if (pack_l)
-          pack_l_split_kernel<SplitF16><<<lg, 256, 0, ms>>>(L21, ld, lh.as<uint16_t>(), ldks, M,
-                                                            jbo);
-        pack_ut_split_kernel<SplitF16><<<pgs, dim3(32, 8), 0, ms>>>(U12, ld, u16, ldks, jbo, N,
-                                                                    d_stat);
+          LA_CUDA(ctx, la_launch(ctx, pack_l_split_kernel<SplitF16>, dim3(lg), dim3(256), 0, ms,
+                                 L21, ld, lh.as<uint16_t>(), ldks, M, jbo));
+        LA_CUDA(ctx, la_launch(ctx, pack_ut_split_kernel<SplitF16>, pgs, dim3(32, 8), 0, ms, U12,
+                               ld, u16, ldks, jbo, N, d_stat));
       }
       ctx->launches += pack_l ? 2 : 1;
       LA_TRY(la_check_launch(ctx, "pack_split_kernel"));
@@ -507,44 +522,54 @@ la_status mixed_factor(la_ctx ctx, la_lu h, int prec) {
     uint16_t* ub = uh.as<uint16_t>() + (size_t)(c0 - j1o) * ldk;
     if (fmt == LA_LOWP_FP16) {
       LA_CUDA(ctx, cudaMemsetAsync(d_stat, 0, 2 * sizeof(float), ms));
-      absmax_kernel<<<grid_for(ctx, (size_t)jbo * N), 256, 0, ms>>>(U12, ld, jbo, N, d_stat);
+      LA_CUDA(ctx, la_launch(ctx, absmax_kernel, dim3(grid_for(ctx, (size_t)jbo * N)), dim3(256), 0,
+                             ms, U12, ld, jbo, N, d_stat));
       ctx->launches++;
-      LA_TRY(la_check_launch(ctx, "absmax_kernel"));
     } else {
-      set_alpha_one<<<1, 1, 0, ms>>>(d_stat);
+      LA_CUDA(ctx, la_launch(ctx, set_alpha_one, dim3(1), dim3(1), 0, ms, d_stat));
       ctx->launches++;
-      LA_TRY(la_check_launch(ctx, "set_alpha_one"));
     }
     if (pack_l) {
+      const dim3 lg(grid_for(ctx, (size_t)M * ldk));
       if (fmt == LA_LOWP_BF16)
-        pack_l_kernel<LA_LOWP_BF16><<<grid_for(ctx, (size_t)M * ldk), 256, 0, ms>>>(
-            L21, ld, lh.as<uint16_t>(), ldk, M, jbo);
+        LA_CUDA(ctx, la_launch(ctx, pack_l_kernel<LA_LOWP_BF16>, lg, dim3(256), 0, ms, L21, ld,
+                               lh.as<uint16_t>(), ldk, M, jbo));
       else
-        pack_l_kernel<LA_LOWP_FP16><<<grid_for(ctx, (size_t)M * ldk), 256, 0, ms>>>(
-            L21, ld, lh.as<uint16_t>(), ldk, M, jbo);
+        LA_CUDA(ctx, la_launch(ctx, pack_l_kernel<LA_LOWP_FP16>, lg, dim3(256), 0, ms, L21, ld,
+                               lh.as<uint16_t>(), ldk, M, jbo));
       ctx->launches++;
-      LA_TRY(la_check_launch(ctx, "pack_l_kernel"));
     }
     dim3 pg((N + 31) / 32, ((int)ldk + 31) / 32);
     if (fmt == LA_LOWP_BF16)
-      pack_ut_kernel<LA_LOWP_BF16><<<pg, dim3(32, 8), 0, ms>>>(U12, ld, ub, ldk, jbo, N, d_stat);
+      LA_CUDA(ctx, la_launch(ctx, pack_ut_kernel<LA_LOWP_BF16>, pg, dim3(32, 8), 0, ms, U12, ld, ub,
+                             ldk, jbo, N, d_stat));
     else
-      pack_ut_kernel<LA_LOWP_FP16><<<pg, dim3(32, 8), 0, ms>>>(U12, ld, ub, ldk, jbo, N, d_stat);
+      LA_CUDA(ctx, la_launch(ctx, pack_ut_kernel<LA_LOWP_FP16>, pg, dim3(32, 8), 0, ms, U12, ld, ub,
+                             ldk, jbo, N, d_stat));
     ctx->launches++;
-    LA_TRY(la_check_launch(ctx, "pack_ut_kernel"));
     return launch_tc_update(ctx, ms, fmt, M, N, jbo, lh.p, ldk, ub, ldk, C, ld, d_stat + 1);
   };
 
+  // No launch after this function keeps the dependent-launch attribute, also
+  // on an early return.
+  struct PdlReset {
+    la_ctx c;
+    ~PdlReset() { c->pdl_now = false; }
+  } pdl_reset{ctx};
   // The first outer panel on the main stream.
   LA_TRY(inner(0, std::min(WO, kmin), std::min(WO, kmin), ms));
   for (int j0 = 0; j0 < kmin; j0 += WO) {
     const int j1o = std::min(j0 + WO, kmin);
     if (j1o >= n) break;
     const int j2o = std::min(j1o + WO, kmin);  // the next outer panel [j1o, j2o)
-    // this panel's swaps on the columns its inner panels left out
+    // This panel's swaps on the columns its inner panels left out, then the
+    // next panel's columns: the serial part between the two chains, as
+    // dependent launches (the rest of the update, after the fork, is not).
+    ctx->pdl_now = ctx->pdl != 0;
     LA_TRY(launch_laswp_seq_f32(ctx, A, ld, h->d_ipiv, j0, j1o, j1o, n));
     LA_TRY(outer_trsm(j0, j1o, j1o, j2o));
     LA_TRY(update(j0, j1o, j1o, j2o, true));
+    ctx->pdl_now = false;
     bool forked = false;
     if (j1o < kmin) {
       if (look) {
