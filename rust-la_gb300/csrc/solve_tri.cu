@@ -30,8 +30,8 @@
 //
 // Order of the terms of row i (both schedules): forward (unit L, lu.rs:257-263)
 // ascending k; backward (U, lu.rs:266-275) descending k, then the division by
-// u_ii. EXACT applies each term as x_i = x_i - x_k * l_ik without fusion; FAST
-// uses FMA.
+// u_ii. EXACT applies each term as x_i = x_i - x_k * l_ik without fusion and
+// divides; FAST uses FMA and multiplies by the reciprocal of u_ii (quot).
 #include "la_internal.cuh"
 
 namespace {
@@ -45,6 +45,19 @@ template <bool EXACT, typename T>
 __device__ __forceinline__ T apply(T x, T xk, T l) {
   if constexpr (EXACT) return __dsub_rn(x, __dmul_rn(xk, l));
   else return fma(-xk, l, x);
+}
+
+// A row's value over its diagonal entry d once its terms are in. EXACT: the
+// division of the reference (lu.rs:272, cholesky.rs:127-139). FAST: the
+// product with r = RN(1/d), taken before the row's turn, so no division sits
+// on the solve's sequential chain (FP64 division is a long instruction
+// sequence on this GPU's FP64 pipe); one extra rounding per row, far inside
+// the FAST mode's backward-error bound. Both schedules use it, so their
+// results stay bit-identical.
+template <bool EXACT, typename T>
+__device__ __forceinline__ T quot(T v, T d, T r) {
+  if constexpr (EXACT) return v / d;
+  else return v * r;
 }
 
 // UPPER = false: forward with unit L; UPPER = true: backward with U.
@@ -121,7 +134,7 @@ solve_step_kernel(const T* __restrict__ LU, size_t ld, T* __restrict__ X, size_t
       }
     } else {
       for (int k = rn - 1; k >= 0; k--) {
-        if (ty == (k % (ST / CT))) xt[k][tx] = xt[k][tx] / dg[k][k];
+        if (ty == (k % (ST / CT))) xt[k][tx] = quot<EXACT>(xt[k][tx], dg[k][k], T(1) / dg[k][k]);
         __syncthreads();
         const T v = xt[k][tx];
         for (int i = ty; i < k; i += ST / CT) xt[i][tx] = apply<EXACT, T>(xt[i][tx], v, dg[i][k]);
@@ -324,21 +337,26 @@ solve_wave_kernel(const T* __restrict__ LU, size_t ld, T* X, size_t ldx, int n, 
           const T xk = __shfl_sync(full, x, k);
           if (lane > k) x = apply<EXACT, T>(x, xk, tile[lane][k]);
         }
-      } else if (!UPPER) {
-        // as in the backward case: every lane divides row k's value in lockstep
-        for (int k = 0; k < sb; k++) {
-          const T xk = __shfl_sync(full, x, k) / tile[k][k];
-          if (lane == k) x = xk;
-          else if (lane > k) x = apply<EXACT, T>(x, xk, tile[lane][k]);
-        }
       } else {
-        // Every lane takes row k's undivided value and divides it by u_kk in
-        // lockstep (the same operands give the same quotient in every lane), so
-        // the division is not a divergent branch on the chain.
-        for (int k = sb - 1; k >= 0; k--) {
-          const T xk = __shfl_sync(full, x, k) / tile[k][k];
-          if (lane == k) x = xk;
-          else if (lane < k) x = apply<EXACT, T>(x, xk, tile[lane][k]);
+        // FAST: lane l takes the reciprocal of its row's diagonal entry once,
+        // off the chain; EXACT divides on the chain as the reference does.
+        const T rcp = (!EXACT && lane < sb) ? T(1) / tile[lane][lane] : T(1);
+        if (!UPPER) {
+          // as in the backward case: every lane divides row k's value in lockstep
+          for (int k = 0; k < sb; k++) {
+            const T xk = quot<EXACT>(__shfl_sync(full, x, k), tile[k][k], __shfl_sync(full, rcp, k));
+            if (lane == k) x = xk;
+            else if (lane > k) x = apply<EXACT, T>(x, xk, tile[lane][k]);
+          }
+        } else {
+          // Every lane takes row k's undivided value and divides it by u_kk in
+          // lockstep (the same operands give the same quotient in every lane),
+          // so the division is not a divergent branch on the chain.
+          for (int k = sb - 1; k >= 0; k--) {
+            const T xk = quot<EXACT>(__shfl_sync(full, x, k), tile[k][k], __shfl_sync(full, rcp, k));
+            if (lane == k) x = xk;
+            else if (lane < k) x = apply<EXACT, T>(x, xk, tile[lane][k]);
+          }
         }
       }
     }
