@@ -691,8 +691,9 @@ def lu_solve_refined_device(lu, b_ptr, ldb, nrhs, x_ptr, ldx, max_iters=50, tol=
 
 
 def lu_solve_auto_device(ctx, a_ptr, lda, n, b_ptr, ldb, nrhs, x_ptr, ldx, tol=1e-14):
-    """Automatic precision (la_lu_solve_auto_device): FP16 factors, then FP32,
-    then the plain FP64 LU. Returns (status, RefineStats)."""
+    """Automatic precision (la_lu_solve_auto_device): split-FP16 factors with
+    refinement and then GMRES-IR, then the plain FP64 LU for whatever they
+    could not answer. Returns (status, RefineStats)."""
     stats = RefineStats()
     st = lib().la_lu_solve_auto_device(ctx.h, ctypes.c_void_p(a_ptr), lda, n,
                                        ctypes.c_void_p(b_ptr), ldb, nrhs, ctypes.c_void_p(x_ptr),
