@@ -271,6 +271,17 @@ __device__ __forceinline__ void st_async_v4(uint32_t dst, uint32_t bar, uint32_t
       : "memory");
 }
 
+// Largest 64-bit value over the full warp (every lane gets it), as two 32-bit
+// warp reductions (redux.sync): the high words, then the low words of the
+// lanes whose high word is the largest; shorter than five rounds of 64-bit
+// shuffles on the column's critical path.
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long x) {
+  const unsigned hi = (unsigned)(x >> 32), lo = (unsigned)x;
+  const unsigned mh = __reduce_max_sync(0xffffffffu, hi);
+  const unsigned ml = __reduce_max_sync(0xffffffffu, hi == mh ? lo : 0u);
+  return ((unsigned long long)mh << 32) | ml;
+}
+
 // One column of panel_cluster_reg_kernel (see there); false when a wait gave
 // up. The rows' register windows rotate: the current column is slot 0.
 template <int RPT>
@@ -294,12 +305,7 @@ __device__ __forceinline__ bool panel_column(int c, const ClusterPanelArgs& p, i
             (unsigned)(~pos[q]);
         if (pk > best) { best = pk; bq = q; }
       }
-    unsigned long long wb = best;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      const unsigned long long o = __shfl_xor_sync(0xffffffffu, wb, off);
-      wb = o > wb ? o : wb;
-    }
+    const unsigned long long wb = warp_max_u64(best);
     const unsigned wmask = __ballot_sync(0xffffffffu, wb != 0ull && best == wb);
     if (wmask && lane == __ffs(wmask) - 1) {
       // published without its finished slots (zeros: the update leaves the
@@ -318,12 +324,7 @@ __device__ __forceinline__ bool panel_column(int c, const ClusterPanelArgs& p, i
     //    CTA's receive buffer (the slots alternate by column parity).
     if (warp == 0) {
       const unsigned long long k = lane < NW ? wkey[par][lane] : 0ull;
-      unsigned long long km = k;
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        const unsigned long long o = __shfl_xor_sync(0xffffffffu, km, off);
-        km = o > km ? o : km;
-      }
+      const unsigned long long km = warp_max_u64(k);
       const unsigned cm = __ballot_sync(0xffffffffu, km != 0ull && k == km);
       const float* crow = wrow[par][cm ? __ffs(cm) - 1 : 0];
       if (lane < C) {
@@ -349,12 +350,7 @@ __device__ __forceinline__ bool panel_column(int c, const ClusterPanelArgs& p, i
     // 4. the winner and its row, from local shared memory
     const unsigned long long gk =
         lane < C ? *reinterpret_cast<const unsigned long long*>(&recv[par][lane][0]) : 0ull;
-    unsigned long long gm = gk;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      const unsigned long long o = __shfl_xor_sync(0xffffffffu, gm, off);
-      gm = o > gm ? o : gm;
-    }
+    const unsigned long long gm = warp_max_u64(gk);
     const unsigned gmask = __ballot_sync(0xffffffffu, lane < C && gk == gm);
     const int gsrc = __ffs(gmask) - 1;  // the row at position j is a candidate: gm != 0
     const int piv = (int)(~(unsigned)(gm & 0xffffffffull));
