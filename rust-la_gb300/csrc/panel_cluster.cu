@@ -283,8 +283,14 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long x)
 }
 
 // One column of panel_cluster_reg_kernel (see there); false when a wait gave
-// up. The rows' register windows rotate: the current column is slot 0.
-template <int RPT>
+// up. The rows' register windows rotate: columns are taken in pairs, the
+// first at slot S = 0 and the second at slot S = 1, and each window moves by
+// two slots after the pair (ROT = 2); a lone last column uses S = 0, ROT = 1.
+// So the window stays put within a pair and moves by two instead of twice by
+// one. Slot k of the window at S = 1 is slot k - 1 of the window the pair's
+// first column would have left after a one-slot move, so every column meets
+// the same values in the same operations.
+template <int RPT, int S, int ROT>
 __device__ __forceinline__ bool panel_column(int c, const ClusterPanelArgs& p, int g, int C,
                                              int tid, int lane, int warp, float (&v)[RPT][CW],
                                              int (&pos)[RPT], float (*wrow)[PNW][CW],
@@ -301,7 +307,7 @@ __device__ __forceinline__ bool panel_column(int c, const ClusterPanelArgs& p, i
     for (int q = 0; q < RPT; q++)
       if (pos[q] >= j) {
         const unsigned long long pk =
-            ((unsigned long long)ckey(v[q][0], pos[q], j) << 32) |
+            ((unsigned long long)ckey(v[q][S], pos[q], j) << 32) |
             (unsigned)(~pos[q]);
         if (pk > best) { best = pk; bq = q; }
       }
@@ -315,7 +321,7 @@ __device__ __forceinline__ bool panel_column(int c, const ClusterPanelArgs& p, i
       for (int q = 0; q < RPT; q++)
         if (q == bq) {
 #pragma unroll
-          for (int k = 0; k < CW; k++) dst[k] = k < CW - c ? v[q][k] : 0.f;
+          for (int k = 0; k < CW; k++) dst[k] = (k >= S && k < S + CW - c) ? v[q][k] : 0.f;
         }
     }
     if (lane == 0) wkey[par][warp] = wb;
@@ -358,7 +364,7 @@ __device__ __forceinline__ bool panel_column(int c, const ClusterPanelArgs& p, i
     {
       // The pivot row streams from shared memory in float4 chunks, each chunk
       // applied to all of this thread's rows (4 registers for it, not 32).
-      const float d = urow[0];
+      const float d = urow[S];
       const float sc = d != 0.f ? 1.f / d : 1.f;
       float lq[RPT];
       bool act[RPT];
@@ -371,8 +377,8 @@ __device__ __forceinline__ bool panel_column(int c, const ClusterPanelArgs& p, i
           if (pos[q] == j) pos[q] = piv;  // the displaced row takes the pivot's place
           act[q] = pos[q] > j;
         }
-        lq[q] = d != 0.f ? v[q][0] * sc : v[q][0];
-        if (act[q]) v[q][0] = lq[q];
+        lq[q] = d != 0.f ? v[q][S] * sc : v[q][S];
+        if (act[q]) v[q][S] = lq[q];
       }
 #pragma unroll
       for (int k4 = 0; k4 < CW / 4; k4++) {
@@ -381,7 +387,7 @@ __device__ __forceinline__ bool panel_column(int c, const ClusterPanelArgs& p, i
 #pragma unroll
         for (int i = 0; i < 4; i++) {
           const int k = 4 * k4 + i;
-          if (k == 0) continue;
+          if (k == S) continue;
 #pragma unroll
           for (int q = 0; q < RPT; q++)
             if (act[q]) v[q][k] = fmaf(-lq[q], uk[i], v[q][k]);
@@ -389,11 +395,15 @@ __device__ __forceinline__ bool panel_column(int c, const ClusterPanelArgs& p, i
       }
 #pragma unroll
       for (int q = 0; q < RPT; q++) {
-        // rotate: the next column comes to slot 0, the finished value to the end
-        const float t = v[q][0];
+        // rotate by ROT: the next column comes to slot 0, the finished values
+        // to the end
+        float t[ROT > 0 ? ROT : 1];
 #pragma unroll
-        for (int k = 0; k < CW - 1; k++) v[q][k] = v[q][k + 1];
-        v[q][CW - 1] = t;
+        for (int r = 0; r < ROT; r++) t[r] = v[q][r];
+#pragma unroll
+        for (int k = 0; k < CW - ROT; k++) v[q][k] = v[q][k + ROT];
+#pragma unroll
+        for (int r = 0; r < ROT; r++) v[q][CW - ROT + r] = t[r];
       }
       if (g == 0 && tid == 0) {
         p.ipiv[j] = piv;
@@ -459,12 +469,17 @@ __global__ void __launch_bounds__(CT, 1) panel_cluster_reg_kernel(ClusterPanelAr
   // instruction cache and stalled on instruction fetch; the rotating loop
   // stays in cache even where it spills a little at 4 rows per thread.
   bool ok = true;
-  for (int c = 0; c < jb; c++)
-    if (!panel_column<RPT>(c, p, g, C, tid, lane, warp, v, pos, wrow, wkey, recv, rbar,
-                           s_pivs)) {
-      ok = false;
-      break;
+  for (int c = 0; c < jb && ok; c += 2) {
+    if (c + 1 < jb) {
+      ok = panel_column<RPT, 0, 0>(c, p, g, C, tid, lane, warp, v, pos, wrow, wkey, recv, rbar,
+                                   s_pivs) &&
+           panel_column<RPT, 1, 2>(c + 1, p, g, C, tid, lane, warp, v, pos, wrow, wkey, recv,
+                                   rbar, s_pivs);
+    } else {
+      ok = panel_column<RPT, 0, 1>(c, p, g, C, tid, lane, warp, v, pos, wrow, wkey, recv, rbar,
+                                   s_pivs);
     }
+  }
   cluster_sync();  // no CTA leaves while pushes into its shared memory may be in flight
   if (!ok) return;
   // jb rotations so far; 32 in all bring every value back to its column
