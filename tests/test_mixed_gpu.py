@@ -219,3 +219,33 @@ def test_auto_precision_singular_and_limits(lagpu, ctx_fast, torch):
         lagpu.lu_solve_auto_device(ctx_fast, a.data_ptr(), n, n, x.data_ptr(), 17, 17,
                                    x.data_ptr(), 17)
     assert e.value.status == lagpu.UNSUPPORTED
+
+
+@pytest.mark.parametrize("n,prec", [(1500, 3), (4099, 2), (6000, 6), (9000, 1)],
+                         ids=["fp32-1500", "fp16-4099", "fp16x3-6000", "bf16-9000"])
+def test_dependent_launches_change_no_bit(lagpu, torch, n, prec):
+    # LA_OPT_PDL lets each kernel of the panel chain and of the serial part
+    # between outer panels start while the one before it finishes, each
+    # waiting on the device for its predecessor's results; the pivots and the
+    # refined solution must be the same bits as in plain stream order (1, 2
+    # and 4 rows per thread in the cluster panels, odd panel widths at 4099).
+    a_np, b_np = _problem(n, 2, 60 + prec, shift=0.0 if prec == 3 else 2.0 * np.sqrt(n))
+    a = torch.from_numpy(a_np).cuda()
+    b = torch.from_numpy(b_np).cuda()
+    outs = []
+    for pdl in (0, 1):
+        ctx = lagpu.Context(0)
+        ctx.set_option(lagpu.OPT_PDL, pdl)
+        assert ctx.get_option(lagpu.OPT_PDL) == pdl
+        x = torch.zeros((n, 2), dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        lu = lagpu.lu_mixed_new_device(ctx, a.data_ptr(), n, n, prec)
+        piv = lu.get_piv()
+        lagpu.lu_solve_refined_device(lu, b.data_ptr(), 2, 2, x.data_ptr(), 2, max_iters=60,
+                                      tol=1e-14)
+        lu.free()
+        ctx.close()
+        outs.append((piv, x.cpu().numpy()))
+    assert np.array_equal(outs[0][0], outs[1][0])
+    assert np.array_equal(outs[0][1], outs[1][1])
+    assert oracle.backward_error(a_np, outs[1][1], b_np) <= ETA_MAX
