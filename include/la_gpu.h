@@ -114,11 +114,13 @@ typedef enum la_option {
    * one arrival more than there are CTAs, so that the wait runs out (after
    * LA_OPT_WAIT_LIMIT_US) exactly as when a CTA cannot reach the barrier. */
   LA_OPT_INJECT_PANEL_STALL = 13,
-  /* 1 (default): the mixed LU's chain of inner-panel kernels (32-column
-   * panel, row swaps, triangular solve, rank-32 update) is launched with
-   * programmatic stream serialization, so that each kernel is scheduled while
-   * the one before it finishes and waits on the device for its results; 0:
-   * ordinary stream order. Results are bit-identical either way. */
+  /* 1 (default): in the mixed LU, the chain of inner-panel kernels (32-column
+   * panel, row swaps, triangular solve, rank-32 update) and the serial part
+   * between outer panels (row swaps, the next panel's triangular solve, U12
+   * scale and packing, tensor-core update) are launched with programmatic
+   * stream serialization, so that each kernel is scheduled while the one
+   * before it finishes and waits on the device for its results; 0: ordinary
+   * stream order. Results are bit-identical either way. */
   LA_OPT_PDL = 14
 } la_option;
 
