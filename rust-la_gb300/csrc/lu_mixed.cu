@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(256)
 residual_f64_kernel(const double* __restrict__ A, size_t lda, const double* __restrict__ X,
                     size_t ldx, const double* __restrict__ B, size_t ldb, double* __restrict__ Rout,
                     size_t ldr, int n, int nrhs, double* colmax) {
-  constexpr int RPW = R >= 8 ? 1 : 8 / R;
+  constexpr int RPW = R >= 4 ? 1 : 4 / R;
   constexpr int KC = 256;
   __shared__ double xs[KC][R];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -275,7 +275,7 @@ template <int R>
 void launch_residual_r(int n, cudaStream_t st, const double* A, size_t lda, const double* X,
                        size_t ldx, const double* B, size_t ldb, double* Rout, size_t ldr, int nrhs,
                        double* colmax) {
-  constexpr int ROWS = 8 * (R >= 8 ? 1 : 8 / R);
+  constexpr int ROWS = 8 * (R >= 4 ? 1 : 4 / R);
   residual_f64_kernel<R><<<(n + ROWS - 1) / ROWS, 256, 0, st>>>(A, lda, X, ldx, B, ldb, Rout, ldr,
                                                                 n, nrhs, colmax);
 }
